@@ -1,0 +1,189 @@
+/*
+ * gbrt.h -- C ABI of the GB300-native ray-tracing hot path (visionaray_gb300).
+ *
+ * This is the drop-in boundary for visionaray's GPU ray-tracing path.  Every entry
+ * point below names the visionaray interface it replaces (file:line inside the
+ * visionaray source tree).  All types are plain C; no CUDA or C++ type crosses the
+ * boundary except an opaque `void*` CUDA stream.
+ *
+ * Conventions
+ *   - Device pointers unless the name ends in `_host`.  Caller owns input and output
+ *     buffers; the library owns BVH arenas behind opaque handles.
+ *   - Every call returns a gbrt_status.  Nothing aborts, throws or prints.
+ *     gbrt_last_error() gives a one-line description of the last failure on a context.
+ *   - Calls are asynchronous on the context's stream unless documented otherwise,
+ *     like visionaray's cuda_sched::frame (detail/cuda_sched.inl:226-246).
+ *   - A context is used by one host thread at a time (no internal locking).
+ */
+#ifndef VISIONARAY_GB300_GBRT_H
+#define VISIONARAY_GB300_GBRT_H 1
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBRT_ABI_VERSION 1
+
+typedef enum gbrt_status
+{
+    GBRT_OK                 = 0,
+    GBRT_ERR_INVALID_ARG    = 1,  /* null pointer, bad size, bad enum                  */
+    GBRT_ERR_OUT_OF_MEMORY  = 2,  /* device allocation failed                           */
+    GBRT_ERR_CUDA           = 3,  /* a CUDA runtime call or kernel launch failed        */
+    GBRT_ERR_WATCHDOG       = 4,  /* a bounded device-side wait gave up                 */
+    GBRT_ERR_STACK_OVERFLOW = 5,  /* traversal stack exceeded (tree deeper than limit)  */
+    GBRT_ERR_TOO_LARGE      = 6   /* input larger than a documented maximum             */
+} gbrt_status;
+
+/* visionaray basic_triangle<3, float, unsigned> (math/triangle.h:18-36 with the
+ * primitive<unsigned> base of math/primitive.h:15-21): 44 bytes, no padding.      */
+typedef struct gbrt_triangle
+{
+    uint32_t geom_id;
+    uint32_t prim_id;
+    float    v1[3];
+    float    e1[3];
+    float    e2[3];
+} gbrt_triangle;
+
+/* visionaray basic_ray<float> (math/ray.h:16-45): 32 bytes.                        */
+typedef struct gbrt_ray
+{
+    float ori[3];
+    float dir[3];
+    float tmin;
+    float tmax;
+} gbrt_ray;
+
+/* The traced result of one ray: the fields of visionaray's
+ * hit_record<ray, primitive<unsigned>> (math/intersect.h:151-169) that the hot path
+ * consumes.  prim_id is the hit triangle's own prim_id field, or GBRT_NO_HIT.
+ * A miss stores t = FLT_MAX and u = v = 0, as the reference record does.           */
+typedef struct gbrt_hit
+{
+    uint32_t prim_id;
+    float    t;
+    float    u;
+    float    v;
+} gbrt_hit;
+
+#define GBRT_NO_HIT 0xFFFFFFFFu
+
+/* visionaray bvh_node (bvh.h:70-141): 32 bytes.  Inner: num_prims == 0 and
+ * first_child indexes the first of two adjacent children.  Leaf: first_prim indexes
+ * the bvh's index list, num_prims > 0.                                            */
+typedef struct gbrt_bvh_node
+{
+    float    bbox_min[3];
+    float    bbox_max[3];
+    uint32_t first_child_or_prim;
+    uint16_t num_prims;
+    uint8_t  ordered_traversal_axis;
+    uint8_t  ordered_traversal_sign;
+} gbrt_bvh_node;
+
+typedef struct gbrt_context gbrt_context;
+typedef struct gbrt_bvh     gbrt_bvh;
+
+/* ------------------------------------------------------------------------------ */
+/* Context                                                                         */
+
+/* Binds a context to CUDA device `device` and stream `stream` (a cudaStream_t, or
+ * NULL for the legacy default stream).  No visionaray counterpart: visionaray's
+ * builders and schedulers take the stream per call (detail/cuda_sched.h:39,
+ * detail/bvh/lbvh.h:669-679); the context carries it once instead.               */
+gbrt_status gbrt_context_create(int device, void* stream, gbrt_context** out);
+gbrt_status gbrt_context_destroy(gbrt_context* ctx);
+gbrt_status gbrt_context_set_stream(gbrt_context* ctx, void* stream);
+/* Blocks until all work queued on the context's stream is done and reports any
+ * deferred device-side error (watchdog, stack overflow).                          */
+gbrt_status gbrt_context_synchronize(gbrt_context* ctx);
+const char* gbrt_last_error(gbrt_context const* ctx);
+int         gbrt_abi_version(void);
+
+/* ------------------------------------------------------------------------------ */
+/* BVH construction                                                                */
+
+/* GPU LBVH build (Karras 2012) over `n` triangles in device memory.
+ * Replaces lbvh_builder::build(cuda_index_bvh<P>{}, P* prims, size_t n)
+ * (detail/bvh/lbvh.h:681-844): 30-bit Morton codes of centroids quantised exactly as
+ * lbvh.h:253-267, a stable sort by code, Karras hierarchy (lbvh.h:120-185, 281-330)
+ * and a bottom-up refit.  One primitive per leaf, as the reference.  The tree keeps
+ * its own copy of the triangles, so `d_tris` may be freed after the call.
+ * n == 0 yields an empty tree whose traces report misses.                         */
+gbrt_status gbrt_bvh_build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n,
+                                gbrt_bvh** out);
+
+/* Same, with the triangles in host memory (copied in on the context's stream).    */
+gbrt_status gbrt_bvh_build_lbvh_host(gbrt_context* ctx, gbrt_triangle const* h_tris, uint32_t n,
+                                     gbrt_bvh** out);
+
+/* Uploads a BVH2 built elsewhere (e.g. visionaray's binned_sah_builder,
+ * detail/bvh/sah.h:176-807) from host memory: `nodes` in visionaray bvh_node layout,
+ * `indices` the index list (primitive(i) = tris[indices[i]], bvh.h:550-553).
+ * Replaces the host->device copy constructor of cuda_index_bvh (bvh.h:963-1009).
+ * Synchronous.                                                                     */
+gbrt_status gbrt_bvh_upload_bvh2_host(gbrt_context* ctx,
+                                      gbrt_bvh_node const* nodes, uint32_t num_nodes,
+                                      uint32_t const* indices, uint32_t num_indices,
+                                      gbrt_triangle const* tris, uint32_t num_tris,
+                                      gbrt_bvh** out);
+
+gbrt_status gbrt_bvh_destroy(gbrt_bvh* bvh);
+
+/* Sizes of the reference-layout export below: 2n-1 nodes and n indices for an
+ * LBVH of n > 0 triangles.                                                         */
+gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* num_bvh2_nodes,
+                            uint32_t* depth_bound);
+
+/* Writes the tree in visionaray's cuda_index_bvh node layout, exactly as the
+ * reference's lbvh::collapse kernel emits it (detail/bvh/lbvh.h:374-451): root at 0,
+ * the children of Karras inner node i at 1+2i and 2+2i, leaves with one primitive
+ * and first_prim = the primitive's original index; indices = 0,1,2,... (lbvh.h:453).
+ * d_nodes holds num_bvh2_nodes entries, d_indices num_prims entries (device).
+ * Only for trees built by gbrt_bvh_build_lbvh.                                    */
+gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                 gbrt_bvh_node* d_nodes, uint32_t* d_indices);
+
+/* Writes the 30-bit Morton code of every primitive, in input order, exactly as
+ * lbvh::assign_morton_codes computes it (detail/bvh/lbvh.h:242-269).  Only for trees
+ * built by gbrt_bvh_build_lbvh.  d_codes holds num_prims entries.                  */
+gbrt_status gbrt_bvh_morton_codes(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes);
+
+/* ------------------------------------------------------------------------------ */
+/* Traversal                                                                       */
+
+/* closest_hit(ray, refs, refs + 1) over one BVH for `n` rays
+ * (detail/traverse_linear.inl:192-225 -> detail/bvh/intersect.inl:41-357 with the
+ * ray/triangle test of math/intersect.h:176-229).  A hit is accepted iff the
+ * triangle test hits with tmin <= t <= tmax and t strictly below the best t so far
+ * (update_if.h:68-107).                                                            */
+gbrt_status gbrt_trace_closest_hit(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                   gbrt_ray const* d_rays, uint32_t n, gbrt_hit* d_hits);
+
+/* any_hit(ray, refs, refs + 1) (detail/traverse_linear.inl:156-189): stops at the
+ * first accepted hit (detail/exit_traversal.h:49-56).  Which triangle is reported
+ * depends on traversal order; whether a hit exists does not.                       */
+gbrt_status gbrt_trace_any_hit(gbrt_context* ctx, gbrt_bvh const* bvh,
+                               gbrt_ray const* d_rays, uint32_t n, gbrt_hit* d_hits);
+
+/* The same two calls with rays and hits in host memory (pinned memory gives
+ * full copy speed).  Rays are copied in, traced and copied out in chunks that
+ * overlap copies with traversal.  Synchronous: on return, h_hits is complete.      */
+gbrt_status gbrt_trace_closest_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                        gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits);
+gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                    gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits);
+
+/* Number of kernels the library launched on this context since creation (the
+ * count covers every kernel of every call).                                        */
+uint64_t gbrt_kernel_launch_count(gbrt_context const* ctx);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* VISIONARAY_GB300_GBRT_H */

@@ -1,0 +1,213 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
+bench.py, always as the checker or the timed CPU baseline, never as the product.
+`Oracle` wraps oracle/_build/liboracle.so (the restatement, oracle.cpp);
+`Reference` wraps oracle/_ref/libvsnray_ref.so (visionaray's own CPU code compiled
+from its headers), which exists only where the visionaray sources were present.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from visionaray_gb300.types import BVH_NODE, HIT
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")
+LIBREF = os.path.join(HERE, "_ref", "libvsnray_ref.so")
+
+_vp, _u32, _u64, _i32, _f32 = (ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                               ctypes.c_int, ctypes.c_float)
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Tree:
+    """Host BVH in visionaray's index_bvh layout: nodes (BVH_NODE) and indices."""
+
+    def __init__(self, nodes, indices):
+        self.nodes = nodes
+        self.indices = indices
+
+    @property
+    def depth(self):
+        if len(self.nodes) == 0:
+            return 0
+        best, st = 0, [(0, 1)]
+        while st:
+            i, d = st.pop()
+            best = max(best, d)
+            if self.nodes["num_prims"][i] == 0:
+                f = int(self.nodes["first"][i])
+                st += [(f, d + 1), (f + 1, d + 1)]
+        return best
+
+
+class Oracle:
+    def __init__(self, path=LIBORACLE):
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} missing: build the oracle (make -C oracle)")
+        L = ctypes.CDLL(path)
+        for name in ("orc_build_sah", "orc_build_lbvh_cpu"):
+            getattr(L, name).argtypes = [_vp, _u32, _i32]
+            getattr(L, name).restype = _vp
+        L.orc_build_karras.argtypes = [_vp, _u32]
+        L.orc_build_karras.restype = _vp
+        for name in ("orc_bvh_num_nodes", "orc_bvh_num_indices", "orc_bvh_depth"):
+            getattr(L, name).argtypes = [_vp]
+            getattr(L, name).restype = _u32
+        L.orc_bvh_copy.argtypes = [_vp, _vp, _vp]
+        L.orc_bvh_free.argtypes = [_vp]
+        L.orc_morton_codes.argtypes = [_vp, _u32, _vp]
+        L.orc_karras_children.argtypes = [_vp, _u32, _vp, _vp]
+        L.orc_sah_cost.argtypes = [_vp, _u32, _f32, _f32, _f32]
+        L.orc_sah_cost.restype = _f32
+        L.orc_intersect_triangle.argtypes = [_vp, _vp, _vp]
+        L.orc_intersect_triangle.restype = _i32
+        L.orc_trace.argtypes = [_vp, _u32, _vp, _vp, _vp, _u64, _i32, _i32, _vp, _vp]
+        L.orc_trace.restype = _i32
+        L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
+        self.L = L
+
+    def _tree(self, h):
+        if not h:
+            raise ValueError("oracle refused the build")
+        try:
+            nodes = np.zeros(self.L.orc_bvh_num_nodes(h), BVH_NODE)
+            idx = np.zeros(self.L.orc_bvh_num_indices(h), np.uint32)
+            self.L.orc_bvh_copy(h, _p(nodes), _p(idx))
+            return Tree(nodes, idx)
+        finally:
+            self.L.orc_bvh_free(h)
+
+    def build_sah(self, tris, max_leaf=4):
+        tris = np.ascontiguousarray(tris)
+        return self._tree(self.L.orc_build_sah(_p(tris), len(tris), max_leaf))
+
+    def build_lbvh_cpu(self, tris, max_leaf=4):
+        tris = np.ascontiguousarray(tris)
+        return self._tree(self.L.orc_build_lbvh_cpu(_p(tris), len(tris), max_leaf))
+
+    def build_karras(self, tris):
+        tris = np.ascontiguousarray(tris)
+        return self._tree(self.L.orc_build_karras(_p(tris), len(tris)))
+
+    def morton_codes(self, tris):
+        tris = np.ascontiguousarray(tris)
+        out = np.empty(len(tris), np.uint32)
+        self.L.orc_morton_codes(_p(tris), len(tris), _p(out))
+        return out
+
+    def karras_children(self, sorted_codes):
+        c = np.ascontiguousarray(sorted_codes, np.uint32)
+        n = len(c)
+        left = np.empty(max(n - 1, 0), np.int32)
+        right = np.empty(max(n - 1, 0), np.int32)
+        self.L.orc_karras_children(_p(c), n, _p(left), _p(right))
+        return left, right
+
+    def sah_cost(self, tree, ci=1.2, cl=0.0, cp=1.0):
+        return self.L.orc_sah_cost(_p(tree.nodes), len(tree.nodes), ci, cl, cp)
+
+    def trace(self, tree, tris, rays, any_hit=False, nthreads=0, counters=False):
+        tris = np.ascontiguousarray(tris)
+        rays = np.ascontiguousarray(rays)
+        hits = np.empty(len(rays), HIT)
+        cnt = np.zeros(2, np.uint64)
+        rc = self.L.orc_trace(_p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(tris),
+                              _p(rays), len(rays), int(any_hit), nthreads, _p(hits), _p(cnt))
+        if rc != 0:
+            raise RuntimeError("oracle traversal stack (32 entries) overflowed")
+        return (hits, cnt) if counters else hits
+
+    def trace_linear(self, tris, rays, any_hit=False, nthreads=0):
+        tris = np.ascontiguousarray(tris)
+        rays = np.ascontiguousarray(rays)
+        hits = np.empty(len(rays), HIT)
+        self.L.orc_trace_linear(_p(tris), len(tris), _p(rays), len(rays), int(any_hit), nthreads,
+                                _p(hits))
+        return hits
+
+    def intersect(self, ray, tri):
+        ray = np.ascontiguousarray(np.asarray(ray).reshape(1))
+        tri = np.ascontiguousarray(np.asarray(tri).reshape(1))
+        out = np.empty(1, HIT)
+        hit = self.L.orc_intersect_triangle(_p(ray), _p(tri), _p(out))
+        return bool(hit), out[0]
+
+
+class Reference:
+    """visionaray's own CPU code (oracle/_ref); only where it was built."""
+
+    @staticmethod
+    def available():
+        return os.path.exists(LIBREF)
+
+    def __init__(self, path=LIBREF):
+        L = ctypes.CDLL(path)
+        for name in ("ref_build_sah", "ref_build_lbvh_cpu"):
+            getattr(L, name).argtypes = [_vp, _u32, _i32]
+            getattr(L, name).restype = _vp
+        for name in ("ref_num_nodes", "ref_num_indices"):
+            getattr(L, name).argtypes = [_vp]
+            getattr(L, name).restype = _u32
+        L.ref_copy.argtypes = [_vp, _vp, _vp]
+        L.ref_free.argtypes = [_vp]
+        L.ref_sah_cost.argtypes = [_vp]
+        L.ref_sah_cost.restype = _f32
+        L.ref_lbvh_sorted_refs.argtypes = [_vp, _u32, _vp, _vp]
+        L.ref_karras_children.argtypes = [_vp, _u32, _vp, _vp]
+        L.ref_trace.argtypes = [_vp, _vp, _u64, _i32, _i32, _vp, _vp]
+        L.ref_trace.restype = _i32
+        self.L = L
+
+    class Handle:
+        def __init__(self, L, h):
+            self.L, self.h = L, h
+
+        def __del__(self):
+            if self.h:
+                self.L.ref_free(self.h)
+                self.h = None
+
+        def tree(self):
+            nodes = np.zeros(self.L.ref_num_nodes(self.h), BVH_NODE)
+            idx = np.zeros(self.L.ref_num_indices(self.h), np.uint32)
+            self.L.ref_copy(self.h, _p(nodes), _p(idx))
+            return Tree(nodes, idx)
+
+        def sah_cost(self):
+            return self.L.ref_sah_cost(self.h)
+
+        def trace(self, rays, any_hit=False, nthreads=0, counters=False):
+            rays = np.ascontiguousarray(rays)
+            hits = np.empty(len(rays), HIT)
+            cnt = np.zeros(2, np.uint64)
+            self.L.ref_trace(self.h, _p(rays), len(rays), int(any_hit), nthreads, _p(hits), _p(cnt))
+            return (hits, cnt) if counters else hits
+
+    def build_sah(self, tris, max_leaf=4):
+        tris = np.ascontiguousarray(tris)
+        return Reference.Handle(self.L, self.L.ref_build_sah(_p(tris), len(tris), max_leaf))
+
+    def build_lbvh_cpu(self, tris, max_leaf=4):
+        tris = np.ascontiguousarray(tris)
+        return Reference.Handle(self.L, self.L.ref_build_lbvh_cpu(_p(tris), len(tris), max_leaf))
+
+    def lbvh_sorted_refs(self, tris):
+        tris = np.ascontiguousarray(tris)
+        ids = np.empty(len(tris), np.int32)
+        codes = np.empty(len(tris), np.uint32)
+        self.L.ref_lbvh_sorted_refs(_p(tris), len(tris), _p(ids), _p(codes))
+        return ids, codes
+
+    def karras_children(self, sorted_codes):
+        c = np.ascontiguousarray(sorted_codes, np.uint32)
+        n = len(c)
+        left = np.empty(max(n - 1, 0), np.int32)
+        right = np.empty(max(n - 1, 0), np.int32)
+        self.L.ref_karras_children(_p(c), n, _p(left), _p(right))
+        return left, right

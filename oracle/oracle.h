@@ -1,0 +1,79 @@
+/*
+ * oracle.h -- CPU restatement of visionaray's ray-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the CUDA path in
+ * visionaray_gb300: only tests, the smoke check and the CPU-baseline leg of the
+ * benchmark load it.  The product never calls it and has no CPU fallback.
+ *
+ * Every function restates, in its own code, the algorithm of the visionaray file:line
+ * it cites, keeping the exact floating-point operation order (the library is built
+ * with -ffp-contract=off, so no multiply-add is fused) so that its results match the
+ * reference's CPU path bit for bit.  Parity pin: the restatement is checked against
+ * the reference's own CPU code compiled from its headers (oracle/_ref, built by
+ * oracle/Makefile where the visionaray sources are present) and against golden
+ * vectors in tests/golden that were generated from that build.
+ */
+#ifndef VISIONARAY_GB300_ORACLE_H
+#define VISIONARAY_GB300_ORACLE_H 1
+
+#include <stdint.h>
+
+#include "../include/visionaray_gb300/gbrt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_bvh orc_bvh;
+
+/* binned_sah_builder{}.build(index_bvh<P>{}, tris, n, max_leaf) with object splits
+ * only (detail/bvh/sah.h:176-807, detail/bvh/build_top_down.h:27-173).            */
+orc_bvh* orc_build_sah(const gbrt_triangle* tris, uint32_t n, int max_leaf_size);
+
+/* CPU lbvh_builder{}.build(index_bvh<P>{}, tris, n, max_leaf): top-down Morton split
+ * (detail/bvh/lbvh.h:473-656).  max_leaf_size must be >= 2: with 1, equal adjacent
+ * codes make the reference recurse forever (lbvh.h:505-508); NULL is returned.    */
+orc_bvh* orc_build_lbvh_cpu(const gbrt_triangle* tris, uint32_t n, int max_leaf_size);
+
+/* The GPU lbvh_builder's result restated on the CPU (detail/bvh/lbvh.h:215-451):
+ * Morton codes, stable sort, Karras hierarchy, bottom-up bounds and the collapse into
+ * the cuda_index_bvh node layout.                                                  */
+orc_bvh* orc_build_karras(const gbrt_triangle* tris, uint32_t n);
+
+uint32_t orc_bvh_num_nodes(const orc_bvh* b);
+uint32_t orc_bvh_num_indices(const orc_bvh* b);
+uint32_t orc_bvh_depth(const orc_bvh* b);
+void     orc_bvh_copy(const orc_bvh* b, gbrt_bvh_node* nodes, uint32_t* indices);
+void     orc_bvh_free(orc_bvh* b);
+
+/* 30-bit Morton codes in input order (detail/bvh/lbvh.h:242-269 and :577-594).     */
+void orc_morton_codes(const gbrt_triangle* tris, uint32_t n, uint32_t* codes);
+
+/* Karras inner-node children for sorted codes (detail/bvh/lbvh.h:120-185, 281-330):
+ * left[i], right[i] for inner i in [0, n-2]; a value >= n-1 denotes leaf (v-(n-1)). */
+void orc_karras_children(const uint32_t* sorted_codes, uint32_t n, int32_t* left, int32_t* right);
+
+/* sah_cost(bvh, ci, cl, cp) (detail/bvh/statistics.h:34-68).                        */
+float orc_sah_cost(const gbrt_bvh_node* nodes, uint32_t num_nodes, float ci, float cl, float cp);
+
+/* Single ray / triangle test (math/intersect.h:176-229); returns the hit flag.     */
+int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* tri, gbrt_hit* out);
+
+/* closest_hit / any_hit of rays over one index BVH given by its arrays, with the CPU
+ * full-stack traversal (detail/bvh/intersect.inl:51-165).  counters (may be NULL)
+ * receives {box tests, triangle tests} summed over all rays.  nthreads <= 0 uses the
+ * machine's hardware concurrency.  Returns 0, or -1 if a ray's stack overflowed the
+ * reference's 32 entries.                                                          */
+int orc_trace(const gbrt_bvh_node* nodes, uint32_t num_nodes, const uint32_t* indices,
+              const gbrt_triangle* tris, const gbrt_ray* rays, uint64_t nrays, int any_hit,
+              int nthreads, gbrt_hit* hits, uint64_t* counters);
+
+/* Brute force over all triangles (traverse_linear.inl:71-113 over a primitive list). */
+void orc_trace_linear(const gbrt_triangle* tris, uint32_t ntris, const gbrt_ray* rays,
+                      uint64_t nrays, int any_hit, int nthreads, gbrt_hit* hits);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

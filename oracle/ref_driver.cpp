@@ -1,0 +1,191 @@
+// Thin extern "C" driver around visionaray's own CPU code, compiled from the
+// unmodified visionaray headers (see oracle/Makefile).  TEST INFRASTRUCTURE ONLY:
+// it pins the oracle restatement (oracle.cpp) to the reference and generates the
+// golden vectors in tests/golden.  Nothing in the product links it.
+//
+// Calls used: binned_sah_builder / lbvh_builder ::build (detail/bvh/sah.h:197-205,
+// detail/bvh/lbvh.h:534-542), closest_hit / any_hit (detail/traverse_linear.inl:156-225)
+// with a counting basic_intersector (intersector.h:24-87), detail::lbvh::determine_range
+// (detail/bvh/lbvh.h:120-185) and sah_cost (detail/bvh/statistics.h:34-68).
+
+#include <atomic>
+#include <cfloat>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include <visionaray/bvh.h>
+#include <visionaray/math/math.h>
+#include <visionaray/traverse.h>
+#include <visionaray/detail/bvh/statistics.h>
+
+#include "oracle.h"
+
+using namespace visionaray;
+
+using triangle_t = basic_triangle<3, float, unsigned>;
+static_assert(sizeof(triangle_t) == sizeof(gbrt_triangle), "triangle layout");
+static_assert(sizeof(bvh_node) == sizeof(gbrt_bvh_node), "node layout");
+static_assert(sizeof(basic_ray<float>) == sizeof(gbrt_ray), "ray layout");
+
+namespace {
+
+struct counting_intersector : basic_intersector<counting_intersector>
+{
+    using basic_intersector<counting_intersector>::operator();
+
+    uint64_t boxes = 0;
+    uint64_t tris = 0;
+
+    template <typename R, typename T, typename V>
+    hit_record<R, basic_aabb<T>> operator()(R const& ray, basic_aabb<T> const& box, V&& inv_dir)
+    {
+        ++boxes;
+        return intersect(ray, box, inv_dir);
+    }
+
+    template <typename R>
+    hit_record<R, primitive<unsigned>> operator()(R const& ray, triangle_t const& tri)
+    {
+        ++tris;
+        return intersect(ray, tri);
+    }
+};
+
+struct ref_tree
+{
+    std::vector<triangle_t> prims;
+    index_bvh<triangle_t> tree;
+};
+
+std::vector<triangle_t> to_prims(const gbrt_triangle* tris, uint32_t n)
+{
+    std::vector<triangle_t> v(n);
+    if (n) std::memcpy(v.data(), tris, size_t(n) * sizeof(triangle_t));
+    return v;
+}
+
+} // namespace
+
+extern "C" {
+
+void* ref_build_sah(const gbrt_triangle* tris, uint32_t n, int max_leaf)
+{
+    auto* t = new ref_tree;
+    t->prims = to_prims(tris, n);
+    binned_sah_builder builder;
+    t->tree = builder.build(index_bvh<triangle_t>{}, t->prims.data(), t->prims.size(), max_leaf);
+    return t;
+}
+
+void* ref_build_lbvh_cpu(const gbrt_triangle* tris, uint32_t n, int max_leaf)
+{
+    auto* t = new ref_tree;
+    t->prims = to_prims(tris, n);
+    lbvh_builder builder;
+    t->tree = builder.build(index_bvh<triangle_t>{}, t->prims.data(), t->prims.size(), max_leaf);
+    return t;
+}
+
+uint32_t ref_num_nodes(void* h) { return uint32_t(static_cast<ref_tree*>(h)->tree.num_nodes()); }
+uint32_t ref_num_indices(void* h) { return uint32_t(static_cast<ref_tree*>(h)->tree.num_indices()); }
+
+void ref_copy(void* h, gbrt_bvh_node* nodes, uint32_t* indices)
+{
+    auto* t = static_cast<ref_tree*>(h);
+    auto r = t->tree.ref();
+    std::memcpy(nodes, r.nodes(), r.num_nodes() * sizeof(bvh_node));
+    std::memcpy(indices, r.indices(), r.num_indices() * sizeof(unsigned));
+}
+
+void ref_free(void* h) { delete static_cast<ref_tree*>(h); }
+
+float ref_sah_cost(void* h) { return sah_cost(static_cast<ref_tree*>(h)->tree); }
+
+// Sorted (id, code) pairs of the CPU lbvh_builder::init (lbvh.h:544-599).
+void ref_lbvh_sorted_refs(const gbrt_triangle* tris, uint32_t n, int32_t* ids, uint32_t* codes)
+{
+    auto prims = to_prims(tris, n);
+    lbvh_builder builder;
+    builder.init(prims.data(), prims.data() + n);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        ids[i] = builder.prim_refs[i].id;
+        codes[i] = builder.prim_refs[i].morton_code;
+    }
+}
+
+// Karras children through the reference's own determine_range (lbvh.h:120-185) and
+// the child rule of build_hierarchy (lbvh.h:300-328).
+void ref_karras_children(const uint32_t* codes, uint32_t n, int32_t* left, int32_t* right)
+{
+    std::vector<detail::lbvh::prim_ref> refs(n);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        refs[i].id = int(i);
+        refs[i].morton_code = codes[i];
+    }
+    int num_inner = int(n) - 1;
+    for (int i = 0; i < num_inner; ++i)
+    {
+        int split = -1;
+        vec2i range = detail::lbvh::determine_range(refs.data(), int(n), i, split);
+        left[i] = split == range.x ? num_inner + split : split;
+        right[i] = split + 1 == range.y ? num_inner + split + 1 : split + 1;
+    }
+}
+
+int ref_trace(void* h, const gbrt_ray* rays, uint64_t nrays, int any_hit_flag, int nthreads,
+              gbrt_hit* hits, uint64_t* counters)
+{
+    auto* t = static_cast<ref_tree*>(h);
+    auto bref = t->tree.ref();
+    if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<uint64_t> next{ 0 }, nbox{ 0 }, ntri{ 0 };
+    const uint64_t chunk = 4096;
+    auto worker = [&]() {
+        counting_intersector isect;
+        for (;;)
+        {
+            uint64_t b = next.fetch_add(chunk);
+            if (b >= nrays) break;
+            uint64_t e = std::min(nrays, b + chunk);
+            for (uint64_t i = b; i < e; ++i)
+            {
+                basic_ray<float> r;
+                std::memcpy(&r, &rays[i], sizeof(r));
+                auto hr = any_hit_flag ? any_hit(r, &bref, &bref + 1, isect)
+                                       : closest_hit(r, &bref, &bref + 1, isect);
+                hits[i].prim_id = hr.hit ? hr.prim_id : GBRT_NO_HIT;
+                hits[i].t = hr.t;
+                hits[i].u = hr.u;
+                hits[i].v = hr.v;
+            }
+        }
+        nbox += isect.boxes;
+        ntri += isect.tris;
+    };
+    if (t->tree.num_nodes() == 0)
+    {
+        for (uint64_t i = 0; i < nrays; ++i) hits[i] = { GBRT_NO_HIT, FLT_MAX, 0.0f, 0.0f };
+    }
+    else if (nthreads == 1)
+    {
+        worker();
+    }
+    else
+    {
+        std::vector<std::thread> pool;
+        for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
+        for (auto& th : pool) th.join();
+    }
+    if (counters)
+    {
+        counters[0] = nbox.load();
+        counters[1] = ntri.load();
+    }
+    return 0;
+}
+
+} // extern "C"

@@ -1,0 +1,99 @@
+"""In-tree build of the native parts (no cmake, no pip): run `python -m visionaray_gb300.build`.
+
+Products, all git-ignored and rebuilt on every machine (x86-64 here, AArch64 on the
+GPU host):
+  visionaray_gb300/_lib/libgbrt.so         CUDA kernels + C ABI (sm_103a only)
+  visionaray_gb300/_lib/libgbrt_scenes.so  deterministic synthetic workloads (host)
+  oracle/_build/liboracle.so               CPU oracle (test infrastructure)
+  oracle/_ref/libvsnray_ref.so             visionaray's own CPU code, only where its
+                                           headers are present (test infrastructure)
+Translation units compile in parallel; an up-to-date output is not rebuilt.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "_lib")
+ORACLE = os.path.join(ROOT, "oracle")
+REFERENCE_INCLUDE = os.environ.get("VSNRAY_INCLUDE", "/root/reference/include")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CU_SOURCES = ["api.cu", "lbvh.cu", "radix_sort.cu", "traverse.cu"]
+CU_HEADERS = ["common.cuh", "device_math.cuh", "bvh_layout.cuh", "api_internal.h"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+              "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")] + ARCH
+
+LIBGBRT = os.path.join(LIB, "libgbrt.so")
+LIBSCENES = os.path.join(LIB, "libgbrt_scenes.so")
+LIBORACLE = os.path.join(ORACLE, "_build", "liboracle.so")
+LIBREF = os.path.join(ORACLE, "_ref", "libvsnray_ref.so")
+
+
+def _stale(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _run_all(jobs):
+    procs = [(name, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT))
+             for name, cmd in jobs]
+    failed = []
+    for name, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            failed.append((name, out.decode(errors="replace")))
+    if failed:
+        msg = "\n".join(f"--- {n} ---\n{o}" for n, o in failed)
+        raise RuntimeError(f"native build failed:\n{msg}")
+
+
+def build(verbose=False, with_reference=True):
+    os.makedirs(LIB, exist_ok=True)
+    os.makedirs(os.path.join(LIB, "obj"), exist_ok=True)
+    headers = [os.path.join(CSRC, h) for h in CU_HEADERS] + [
+        os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h")]
+
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(LIB, "obj", src.replace(".cu", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append((src, [NVCC] + NVCC_FLAGS + ["-c", s, "-o", o]))
+    scenes_src = os.path.join(CSRC, "scenes.cpp")
+    if _stale(LIBSCENES, [scenes_src, os.path.join(CSRC, "scenes.h")]):
+        jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+                                "-ffp-contract=off", "-Wall", scenes_src, "-o", LIBSCENES]))
+    oracle_deps = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "oracle.h", "Makefile")]
+    if _stale(LIBORACLE, oracle_deps):
+        jobs.append(("oracle", ["make", "-s", "-C", ORACLE, "all"]))
+    have_ref = with_reference and os.path.isdir(os.path.join(REFERENCE_INCLUDE, "visionaray"))
+    if have_ref and _stale(LIBREF, oracle_deps + [os.path.join(ORACLE, "ref_driver.cpp")]):
+        jobs.append(("reference", ["make", "-s", "-C", ORACLE, "ref",
+                                   "VSNRAY_INCLUDE=" + REFERENCE_INCLUDE]))
+    if verbose:
+        for n, c in jobs:
+            print(n, " ".join(c))
+    _run_all(jobs)
+
+    if _stale(LIBGBRT, objs):
+        _run_all([("link", [NVCC] + ARCH + ["-shared", "-o", LIBGBRT] + objs)])
+    return LIBGBRT
+
+
+def clean():
+    shutil.rmtree(LIB, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print("built", LIBGBRT)

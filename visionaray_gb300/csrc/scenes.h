@@ -1,0 +1,59 @@
+/*
+ * scenes.h -- deterministic synthetic workloads for the ray-tracing hot path.
+ *
+ * These generators have no counterpart in visionaray's library: they stand in for
+ * the scenes the benchmarks are defined on (random triangle soups, a procedural
+ * heightfield, pinhole primary rays, surface-sampled secondary rays).  Every value
+ * comes from a counter-based hash of (seed, stream, index) and from IEEE-754 basic
+ * operations only (+ - * / sqrt, no fused multiply-add, no libm transcendental), so
+ * x86-64 and AArch64 hosts produce bit-identical triangles and rays.  The library is
+ * compiled with -ffp-contract=off for that reason.
+ */
+#ifndef VISIONARAY_GB300_SCENES_H
+#define VISIONARAY_GB300_SCENES_H 1
+
+#include <stdint.h>
+
+#include "../../include/visionaray_gb300/gbrt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Random triangle soup: triangle i has its centre uniform in [0,1]^3 and three vertex
+ * offsets uniform in [-offset, offset]^3; v1 = c + o0, e1 = o1 - o0 style edges
+ * computed from the float vertices.  prim_id = i, geom_id = 0.                     */
+void gbrt_scene_soup(uint32_t n, uint64_t seed, float offset, gbrt_triangle* out);
+
+/* Heightfield over [0,1]^2 (z up): grid x grid cells, two triangles per cell, heights
+ * a sum of `octaves` sines along seeded random directions with seeded phases,
+ * amplitude halving and frequency doubling per octave.  2*grid*grid triangles;
+ * triangle 2c is (P00,P10,P11) and 2c+1 is (P00,P11,P01) of cell c = j*grid + i.
+ * prim_id = triangle index, geom_id = 0.                                           */
+void gbrt_scene_heightfield(uint32_t grid, uint64_t seed, double base_amplitude,
+                            double base_frequency, int octaves, gbrt_triangle* out);
+
+/* Pinhole primary rays, one per pixel centre, in the semantics of visionaray's
+ * pinhole_camera (look_at + perspective, detail/pinhole_camera.inl:87-120):
+ * ray index y*w + x, tmin = 0, tmax = FLT_MAX.                                     */
+void gbrt_rays_pinhole(const float eye[3], const float center[3], const float up[3],
+                       float fovy_degrees, uint32_t w, uint32_t h, gbrt_ray* out);
+
+/* Secondary rays from surface points: origin o picks a triangle uniformly, a uniform
+ * point on it, and offsets it by `offset` along the normal (the normal flipped to
+ * +z).  closest_out[o] gets one cosine-weighted direction with tmax = FLT_MAX;
+ * ao_out[o*ao_per_origin + k] gets ao_per_origin further cosine-weighted directions
+ * with tmax = ao_tmax.  Either output may be NULL.                                  */
+void gbrt_rays_surface(const gbrt_triangle* tris, uint32_t ntris, uint32_t n_origins,
+                       uint64_t seed, float offset, uint32_t ao_per_origin, float ao_tmax,
+                       gbrt_ray* closest_out, gbrt_ray* ao_out);
+
+/* Uniform float in [0,1) of the counter-based generator used above (exposed so that
+ * tests can reproduce any value).                                                  */
+float gbrt_scene_u01(uint64_t seed, uint64_t stream, uint64_t index);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

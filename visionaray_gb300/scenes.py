@@ -1,0 +1,75 @@
+"""Deterministic synthetic workloads (ctypes over libgbrt_scenes.so, see csrc/scenes.h).
+
+The scenes stand in for the benchmark inputs: a random triangle soup (65,536
+triangles for the soup case), a 2048x2048 sine heightfield (8,388,608 triangles),
+pinhole primary rays and surface-sampled secondary / ambient-occlusion rays.  All
+values are bit-identical on x86-64 and AArch64 hosts.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .types import RAY, TRIANGLE
+
+_LIB = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt_scenes.so")
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            raise RuntimeError(f"{_LIB} is missing: run visionaray_gb300.build.build() first")
+        lib = ctypes.CDLL(_LIB)
+        vp, u32, u64, f32, f64 = (ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                                  ctypes.c_float, ctypes.c_double)
+        lib.gbrt_scene_soup.argtypes = [u32, u64, f32, vp]
+        lib.gbrt_scene_heightfield.argtypes = [u32, u64, f64, f64, ctypes.c_int, vp]
+        lib.gbrt_rays_pinhole.argtypes = [vp, vp, vp, f32, u32, u32, vp]
+        lib.gbrt_rays_surface.argtypes = [vp, u32, u32, u64, f32, u32, f32, vp, vp]
+        lib.gbrt_scene_u01.argtypes = [u64, u64, u64]
+        lib.gbrt_scene_u01.restype = f32
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def soup(n, seed=1, offset=0.02):
+    """Random soup: centres U[0,1]^3, vertex offsets U[-offset, offset]^3."""
+    out = np.empty(n, TRIANGLE)
+    _load().gbrt_scene_soup(n, seed, offset, _ptr(out))
+    return out
+
+
+def heightfield(grid=2048, seed=1, base_amplitude=0.05, base_frequency=2.0, octaves=6):
+    """2*grid^2 triangles over [0,1]^2, z = sum of `octaves` sines."""
+    out = np.empty(2 * grid * grid, TRIANGLE)
+    _load().gbrt_scene_heightfield(grid, seed, base_amplitude, base_frequency, octaves, _ptr(out))
+    return out
+
+
+def pinhole_rays(width, height, eye=(0.5, 0.5, -1.5), center=(0.5, 0.5, 0.0), up=(0.0, 1.0, 0.0),
+                 fovy_degrees=45.0):
+    out = np.empty(width * height, RAY)
+    e, c, u = (np.asarray(v, np.float32) for v in (eye, center, up))
+    _load().gbrt_rays_pinhole(_ptr(e), _ptr(c), _ptr(u), fovy_degrees, width, height, _ptr(out))
+    return out
+
+
+def surface_rays(tris, n_origins, seed=7, offset=1e-4, ao_per_origin=8, ao_tmax=0.05,
+                 closest=True, ao=True):
+    """(closest_rays, ao_rays) from uniformly sampled surface points."""
+    tris = np.ascontiguousarray(tris)
+    c = np.empty(n_origins, RAY) if closest else None
+    a = np.empty(n_origins * ao_per_origin, RAY) if ao else None
+    _load().gbrt_rays_surface(_ptr(tris), len(tris), n_origins, seed, offset, ao_per_origin,
+                              ao_tmax, _ptr(c), _ptr(a))
+    return c, a
+
+
+def u01(seed, stream, index):
+    return _load().gbrt_scene_u01(seed, stream, index)

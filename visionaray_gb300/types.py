@@ -1,0 +1,23 @@
+"""numpy views of the C-ABI structs in include/visionaray_gb300/gbrt.h.
+
+The layouts are visionaray's own: basic_triangle<3, float, unsigned>
+(math/triangle.h:18-36, 44 bytes), basic_ray<float> (math/ray.h:16-45, 32 bytes),
+bvh_node (bvh.h:70-141, 32 bytes) and the (prim_id, t, u, v) part of
+hit_record<ray, primitive<unsigned>> (math/intersect.h:151-169).
+"""
+import numpy as np
+
+TRIANGLE = np.dtype([("geom_id", "<u4"), ("prim_id", "<u4"),
+                     ("v1", "<f4", (3,)), ("e1", "<f4", (3,)), ("e2", "<f4", (3,))])
+RAY = np.dtype([("ori", "<f4", (3,)), ("dir", "<f4", (3,)),
+                ("tmin", "<f4"), ("tmax", "<f4")])
+HIT = np.dtype([("prim_id", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+BVH_NODE = np.dtype([("bbox_min", "<f4", (3,)), ("bbox_max", "<f4", (3,)),
+                     ("first", "<u4"), ("num_prims", "<u2"),
+                     ("axis", "u1"), ("sign", "u1")])
+
+NO_HIT = 0xFFFFFFFF
+FLT_MAX = float(np.finfo(np.float32).max)
+
+assert TRIANGLE.itemsize == 44 and RAY.itemsize == 32
+assert HIT.itemsize == 16 and BVH_NODE.itemsize == 32
