@@ -1,0 +1,345 @@
+"""Benchmark of the ray-tracing hot path: LBVH build + incoherent traversal on the
+2048x2048 sine heightfield (8,388,608 triangles), 4,194,304 secondary closest-hit rays
+from surface points plus 8 ambient-occlusion any-hit rays per origin (tmax 0.05),
+33,554,432 of them.  One step = closest_hit over the 4M rays + any_hit over the 32M
+rays; the metric is rays traced per second over both kinds (Mrays/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times visionaray's own CPU path for the same workload (the
+oracle's restatement, pinned to the reference's CPU code; its binned-SAH tree; all
+host threads) on a bounded sample of each step.  For N > 1 (torchrun) every rank
+traces its own replica (replicas only: the path has no exchange step) and the value is
+the whole job's rays / the slowest rank's time.  Data are synthetic (seeded generators
+of visionaray_gb300.scenes); inputs (1.2 GB of rays, 0.9 GB of BVH) exceed the 129 MB L2.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "incoherent closest-hit Mrays/s; PT Msamples/s batched vs plain; bwd/fwd time"
+UNIT = "Mrays/s"
+GRID, SCENE_SEED = 2048, 1
+ORIGINS, RAY_SEED, AO_PER_ORIGIN, AO_TMAX, OFFSET = 1 << 22, 7, 8, 0.05, 1e-4
+WORKLOAD = ("heightfield 2048x2048 (8,388,608 tris, 6 sine octaves) LBVH; 4,194,304 closest-hit "
+            "secondary rays + 33,554,432 any-hit AO rays (tmax 0.05) per step")
+
+# Algorithmic bytes per ray, B_ray = 32 (ray) + 16 (hit) + N_node*32 + N_tri*48, with
+# N_node / N_tri the mean box / triangle tests per ray of visionaray's CPU traversal on
+# its binned-SAH BVH2 of this heightfield, counted over all 4,194,304 closest rays and
+# all 33,554,432 AO rays of this workload (oracle counters, equal to the reference's).
+N_NODE_CLOSEST, N_TRI_CLOSEST = 76.92786217, 7.44575715   # B_ray = 2867.1 bytes
+N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
+
+
+def b_ray(n_node, n_tri):
+    return 32 + 16 + n_node * 32 + n_tri * 48
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(rank_print=print):
+    from visionaray_gb300 import scenes
+    t0 = time.time()
+    tris = scenes.heightfield(grid=GRID, seed=SCENE_SEED)
+    closest, ao = scenes.surface_rays(tris, ORIGINS, seed=RAY_SEED, offset=OFFSET,
+                                      ao_per_origin=AO_PER_ORIGIN, ao_tmax=AO_TMAX)
+    rank_print(f"# workload generated in {time.time() - t0:.1f} s", file=sys.stderr)
+    return tris, closest, ao
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=8, repeats=1):
+    """The reference's CPU path (oracle restatement, binned-SAH tree, all host threads)
+    on every `sample_every`-th origin's closest ray and its AO rays."""
+    from oracle import Oracle, Reference
+    kind = "reference" if Reference.available() else "port"
+    nthreads = os.cpu_count() or 1
+    t0 = time.time()
+    if kind == "reference":
+        ref = Reference()
+        handle = ref.build_sah(tris)
+        trace = lambda r, a: handle.trace(r, any_hit=a, nthreads=nthreads)  # noqa: E731
+    else:
+        o = Oracle()
+        tree = o.build_sah(tris)
+        trace = lambda r, a: o.trace(tree, tris, r, any_hit=a, nthreads=nthreads)  # noqa: E731
+    build_s = time.time() - t0
+    sel = np.arange(0, len(closest), sample_every)
+    c_s = closest[sel]
+    a_s = ao.reshape(len(closest), AO_PER_ORIGIN)[sel].reshape(-1)
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        trace(c_s, False)
+        trace(a_s, True)
+        times.append(time.perf_counter() - t0)
+    rays = len(c_s) + len(a_s)
+    return {"kind": kind, "cores": nthreads, "build_s": build_s, "rays": rays, "times": times,
+            "sample": f"every {sample_every}th origin: {len(c_s)} closest + {len(a_s)} AO rays "
+                      f"(1/{sample_every} of a step); binned-SAH tree built in {build_s:.1f} s (not timed)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    tris, closest, ao = workload()
+    res = cpu_baseline(tris, closest, ao, sample_every=8, repeats=args.warmup + args.steps)
+    t = res["times"][args.warmup:]
+    ms = 1e3 * statistics.mean(t)
+    value = res["rays"] / statistics.mean(t) / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " (each step a bounded sample, see cpu_baseline.sample)",
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": res["cores"], "kind": res["kind"],
+                             "sample": res["sample"]},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import visionaray_gb300 as vg
+    from visionaray_gb300.types import HIT
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+
+    def rprint(*a, **k):
+        if rank == 0:
+            print(*a, **k)
+
+    tris, closest, ao = workload(rprint)
+    n_c, n_a = len(closest), len(ao)
+    rays_per_step = n_c + n_a
+
+    ctx = vg.Context(local)
+    stream = ctx.stream
+
+    # LBVH build, timed separately (build is not part of the traversal metric)
+    d_tris = vg.as_device_bytes(tris, local)
+    torch.cuda.synchronize()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    builder = vg.lbvh_builder(ctx)
+    bvh = builder.build(d_tris)   # warm (allocates the context scratch)
+    del bvh
+    b0.record(stream)
+    bvh = builder.build(d_tris)
+    b1.record(stream)
+    torch.cuda.synchronize()
+    build_ms = b0.elapsed_time(b1)
+
+    d_closest = vg.device_rays(closest, local)
+    d_ao = vg.device_rays(ao, local)
+    h_closest = torch.empty((n_c, 4), dtype=torch.float32, device=dev)
+    h_ao = torch.empty((n_a, 4), dtype=torch.float32, device=dev)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        vg.closest_hit(d_closest, bvh, out=h_closest)
+        if ev:
+            ev[1].record(stream)
+        vg.any_hit(d_ao, bvh, out=h_ao)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launches
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for k in range(args.steps):
+            step(events[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    gpu_launches = ctx.launches - launches0
+    ctx.synchronize()   # raises on a flagged stack overflow / bad index
+    total_ms = start.elapsed_time(stop)
+    t_closest = [e[0].elapsed_time(e[1]) for e in events]
+    t_any = [e[1].elapsed_time(e[2]) for e in events]
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * rays_per_step * args.steps / (total_ms * 1e-3) / 1e6
+
+    # end to end through the host-buffer C ABI: pinned host rays in, hits out, per step
+    pin_c = torch.from_numpy(closest.view(np.float32).reshape(-1, 8)).pin_memory()
+    pin_a = torch.from_numpy(ao.view(np.float32).reshape(-1, 8)).pin_memory()
+    out_c = torch.empty((n_c, 4), dtype=torch.float32).pin_memory()
+    out_a = torch.empty((n_a, 4), dtype=torch.float32).pin_memory()
+    np_c, np_a = pin_c.numpy().view(closest.dtype).reshape(-1), pin_a.numpy().view(ao.dtype).reshape(-1)
+    np_oc, np_oa = out_c.numpy().view(HIT).reshape(-1), out_a.numpy().view(HIT).reshape(-1)
+    e2e_steps = max(1, min(args.steps, 5))
+    vg.closest_hit(np_c, bvh, out=np_oc)
+    vg.any_hit(np_a, bvh, out=np_oa)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        vg.closest_hit(np_c, bvh, out=np_oc)
+        vg.any_hit(np_a, bvh, out=np_oa)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * rays_per_step / e2e_s / 1e6
+    # the host path must give the device path's answers
+    same = bool((np_oc.view(np.uint8) == h_closest.cpu().numpy().view(np.uint8).reshape(-1)).all())
+
+    # roofline of the dominant kernel (per launch)
+    peak, peak_kind = measured_hbm_peak()
+    per = {}
+    for name, ts, n, nn, nt in (("closest", t_closest, n_c, N_NODE_CLOSEST, N_TRI_CLOSEST),
+                                ("any", t_any, n_a, N_NODE_AO, N_TRI_AO)):
+        ms = statistics.mean(ts)
+        rec = {"ms_per_launch": round(ms, 4), "rays": n, "mrays_s": round(n / (ms * 1e-3) / 1e6, 2)}
+        if nn is not None:
+            algo = n * b_ray(nn, nt)
+            rec["algorithmic_bytes"] = int(algo)
+            rec["achieved_gbs"] = round(algo / (ms * 1e-3) / 1e9, 1)
+        per[name] = rec
+    dom = max(per, key=lambda k: per[k]["ms_per_launch"] * 1)
+    d = per[dom]
+    roofline = {"bound": "hbm", "kernel": f"trace_rays<{'true' if dom == 'any' else 'false'}>",
+                "achieved": d.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
+                "frac": round(d["achieved_gbs"] / peak, 4) if d.get("achieved_gbs") else None,
+                "traffic": None, "peak_source": f"{peak_kind} hbm_gbs"}
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        res = cpu_baseline(tris, closest, ao, rank_print=rprint, sample_every=8, repeats=2)
+        tb = min(res["times"])
+        base = {"value": round(res["rays"] / tb / 1e6, 3), "unit": UNIT, "cores": res["cores"],
+                "kind": res["kind"], "sample": res["sample"]}
+
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
+                       "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3)},
+            "kernels": per, "roofline": roofline,
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
+                    "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
+            "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3:
+        print("# warmup raised to 3 (timing rule)", file=sys.stderr)
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    from visionaray_gb300 import build
+    build.build()
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

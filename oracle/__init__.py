@@ -67,6 +67,8 @@ class Oracle:
         L.orc_sah_cost.restype = _f32
         L.orc_intersect_triangle.argtypes = [_vp, _vp, _vp]
         L.orc_intersect_triangle.restype = _i32
+        L.orc_intersect_box.argtypes = [_vp, _vp, _vp, _vp, _vp]
+        L.orc_intersect_box.restype = _i32
         L.orc_trace.argtypes = [_vp, _u32, _vp, _vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.orc_trace.restype = _i32
         L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
@@ -130,6 +132,14 @@ class Oracle:
         self.L.orc_trace_linear(_p(tris), len(tris), _p(rays), len(rays), int(any_hit), nthreads,
                                 _p(hits))
         return hits
+
+    def intersect_box(self, ray, bmin, bmax):
+        ray = np.ascontiguousarray(np.asarray(ray).reshape(1))
+        lo = np.ascontiguousarray(bmin, np.float32)
+        hi = np.ascontiguousarray(bmax, np.float32)
+        tn, tf = ctypes.c_float(), ctypes.c_float()
+        hit = self.L.orc_intersect_box(_p(ray), _p(lo), _p(hi), ctypes.byref(tn), ctypes.byref(tf))
+        return bool(hit), tn.value, tf.value
 
     def intersect(self, ray, tri):
         ray = np.ascontiguousarray(np.asarray(ray).reshape(1))

@@ -923,6 +923,16 @@ extern "C" int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* 
     return h.hit ? 1 : 0;
 }
 
+extern "C" int orc_intersect_box(const gbrt_ray* ray, const float bmin[3], const float bmax[3], float* tnear,
+                                 float* tfar)
+{
+    box b{ load3(bmin), load3(bmax) };
+    box_rec r = intersect_box(load3(ray->ori), inverse_dir(load3(ray->dir)), b);
+    if (tnear) *tnear = r.tnear;
+    if (tfar) *tfar = r.tfar;
+    return r.hit ? 1 : 0;
+}
+
 extern "C" int orc_trace(const gbrt_bvh_node* nodes, uint32_t num_nodes, const uint32_t* indices,
                          const gbrt_triangle* tris, const gbrt_ray* rays, uint64_t nrays, int any_hit,
                          int nthreads, gbrt_hit* hits, uint64_t* counters)

@@ -59,6 +59,11 @@ float orc_sah_cost(const gbrt_bvh_node* nodes, uint32_t num_nodes, float ci, flo
 /* Single ray / triangle test (math/intersect.h:176-229); returns the hit flag.     */
 int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* tri, gbrt_hit* out);
 
+/* Scalar ray / box slab test (math/intersect.h:44-62, no tmin/tmax clamp); returns
+ * the hit flag and writes tnear, tfar.                                             */
+int orc_intersect_box(const gbrt_ray* ray, const float bmin[3], const float bmax[3], float* tnear,
+                      float* tfar);
+
 /* closest_hit / any_hit of rays over one index BVH given by its arrays, with the CPU
  * full-stack traversal (detail/bvh/intersect.inl:51-165).  counters (may be NULL)
  * receives {box tests, triangle tests} summed over all rays.  nthreads <= 0 uses the

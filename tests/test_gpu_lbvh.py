@@ -1,0 +1,87 @@
+"""GPU LBVH build against the oracle's restatement of visionaray's GPU builder.
+
+Topology (children, leaf primitive ids) must be bit-exact and boxes equal, given
+identical Morton codes -- which are compared first."""
+import numpy as np
+import pytest
+
+import visionaray_gb300 as vg
+from visionaray_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_build(tris):
+    return vg.lbvh_builder().build(vg.as_device_bytes(tris))
+
+
+def assert_same_tree(got_nodes, got_idx, ref_tree):
+    assert len(got_nodes) == len(ref_tree.nodes)
+    for f in ("first", "num_prims"):
+        assert np.array_equal(got_nodes[f], ref_tree.nodes[f]), f
+    for f in ("bbox_min", "bbox_max"):
+        assert (got_nodes[f] == ref_tree.nodes[f]).all(), f   # float ==: +0 equals -0
+    assert np.array_equal(got_idx, ref_tree.indices)
+
+
+CASES = [("soup", 2, 11), ("soup", 3, 12), ("soup", 17, 13), ("soup", 1000, 14), ("soup", 65536, 1),
+         ("soup", 100003, 15), ("heightfield", 64, 1), ("heightfield", 256, 2)]
+
+
+@pytest.mark.parametrize("kind,size,seed", CASES)
+def test_lbvh_matches_restated_reference_builder(oracle, kind, size, seed):
+    tris = scenes.soup(size, seed=seed) if kind == "soup" else scenes.heightfield(grid=size, seed=seed)
+    bvh = gpu_build(tris)
+    assert np.array_equal(bvh.morton_codes(), oracle.morton_codes(tris))
+    nodes, idx = bvh.export_bvh2()
+    ref = oracle.build_karras(tris)
+    assert_same_tree(nodes, idx, ref)
+    n, nn, height = bvh.counts
+    assert n == len(tris) and nn == 2 * len(tris) - 1
+    assert height + 1 == ref.depth   # inner levels on the longest path = depth - 1
+
+
+def test_duplicate_centroids_order_by_index(oracle):
+    base = scenes.soup(1, seed=1)
+    tris = np.repeat(base, 300)
+    tris["prim_id"] = np.arange(300)
+    bvh = gpu_build(tris)
+    nodes, idx = bvh.export_bvh2()
+    assert_same_tree(nodes, idx, oracle.build_karras(tris))
+
+
+def test_flat_scene_degenerate_axis(oracle):
+    # all centroids on z = 0.5: size.z = 0 makes the quantised z NaN -> 1023 (lbvh.h:256-263)
+    tris = scenes.soup(5000, seed=9)
+    tris["v1"][:, 2] = 0.5
+    tris["e1"][:, 2] = 0.0
+    tris["e2"][:, 2] = 0.0
+    bvh = gpu_build(tris)
+    assert np.array_equal(bvh.morton_codes(), oracle.morton_codes(tris))
+    nodes, idx = bvh.export_bvh2()
+    assert_same_tree(nodes, idx, oracle.build_karras(tris))
+
+
+def test_single_and_empty():
+    one = scenes.soup(1, seed=2)
+    bvh = gpu_build(one)
+    nodes, idx = bvh.export_bvh2()
+    assert len(nodes) == 1 and nodes["num_prims"][0] == 1 and nodes["first"][0] == 0
+    empty = vg.lbvh_builder().build(np.zeros(0, vg.TRIANGLE))
+    assert empty.counts == (0, 0, 0)
+
+
+def test_host_and_device_builds_agree():
+    tris = scenes.soup(4096, seed=21)
+    a = vg.lbvh_builder().build(tris).export_bvh2()
+    b = gpu_build(tris).export_bvh2()
+    assert a[0].tobytes() == b[0].tobytes() and np.array_equal(a[1], b[1])
+
+
+def test_rebuild_reuses_context_scratch():
+    ctx = vg.default_context()
+    before = ctx.launches
+    for seed in (1, 2):
+        gpu_build(scenes.soup(30000, seed=seed))
+    assert ctx.launches > before
+    ctx.synchronize()

@@ -1,0 +1,10 @@
+"""GB300-native (sm_103a) ray-tracing hot path of visionaray: GPU LBVH build and
+closest_hit / any_hit traversal behind the C ABI of include/visionaray_gb300/gbrt.h.
+
+The Python layer is a thin host-side mirror of the reference's interface
+(runtime.py); all work runs in the CUDA kernels of libgbrt.so.
+"""
+from .types import BVH_NODE, FLT_MAX, HIT, NO_HIT, RAY, TRIANGLE  # noqa: F401
+from .runtime import (Context, GbrtError, IndexBVH, any_hit, closest_hit,  # noqa: F401
+                      default_context, device_rays, as_device_bytes, hits_to_numpy,
+                      lbvh_builder, load_library)

@@ -73,13 +73,18 @@ def build(verbose=False, with_reference=True):
     if _stale(LIBSCENES, [scenes_src, os.path.join(CSRC, "scenes.h")]):
         jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
                                 "-ffp-contract=off", "-Wall", scenes_src, "-o", LIBSCENES]))
-    oracle_deps = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "oracle.h", "Makefile")]
+    # the oracle flags are those of oracle/Makefile (kept for manual builds)
+    oracle_flags = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"]
+    oracle_deps = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "oracle.h")]
     if _stale(LIBORACLE, oracle_deps):
-        jobs.append(("oracle", ["make", "-s", "-C", ORACLE, "all"]))
+        os.makedirs(os.path.dirname(LIBORACLE), exist_ok=True)
+        jobs.append(("oracle", oracle_flags + ["-o", LIBORACLE, os.path.join(ORACLE, "oracle.cpp"), "-lpthread"]))
     have_ref = with_reference and os.path.isdir(os.path.join(REFERENCE_INCLUDE, "visionaray"))
-    if have_ref and _stale(LIBREF, oracle_deps + [os.path.join(ORACLE, "ref_driver.cpp")]):
-        jobs.append(("reference", ["make", "-s", "-C", ORACLE, "ref",
-                                   "VSNRAY_INCLUDE=" + REFERENCE_INCLUDE]))
+    ref_src = os.path.join(ORACLE, "ref_driver.cpp")
+    if have_ref and _stale(LIBREF, oracle_deps + [ref_src]):
+        os.makedirs(os.path.dirname(LIBREF), exist_ok=True)
+        jobs.append(("reference", oracle_flags + ["-w", "-DNDEBUG", "-I" + REFERENCE_INCLUDE, "-o", LIBREF,
+                                                  ref_src, "-lpthread"]))
     if verbose:
         for n, c in jobs:
             print(n, " ".join(c))

@@ -1,0 +1,374 @@
+// C ABI of include/visionaray_gb300/gbrt.h: argument checks, ownership, streams.
+
+#include "api_internal.h"
+
+#include <algorithm>
+#include <new>
+
+namespace gbrt {
+
+constexpr uint32_t kMaxPrims = 1u << 29;   // keeps every Karras index computation in int range
+
+gbrt_status fail(gbrt_context* ctx, gbrt_status st, std::string const& what)
+{
+    if (ctx) ctx->last_error = what;
+    return st;
+}
+
+gbrt_status check_cuda(gbrt_context* ctx, cudaError_t err, const char* where)
+{
+    std::string msg = std::string(where) + ": " + cudaGetErrorName(err) + " (" + cudaGetErrorString(err) + ")";
+    return fail(ctx, err == cudaErrorMemoryAllocation ? GBRT_ERR_OUT_OF_MEMORY : GBRT_ERR_CUDA, msg);
+}
+
+gbrt_status ensure_scratch(gbrt_context* ctx, size_t bytes)
+{
+    if (ctx->scratch_bytes >= bytes) return GBRT_OK;
+    if (ctx->scratch)
+    {
+        // the old scratch may still be read by queued work
+        GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        GBRT_CUDA(ctx, cudaFree(ctx->scratch));
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    size_t grow = std::max(bytes, size_t(1) << 20);
+    GBRT_CUDA(ctx, cudaMalloc(&ctx->scratch, grow));
+    ctx->scratch_bytes = grow;
+    return GBRT_OK;
+}
+
+namespace {
+
+struct device_guard
+{
+    int prev = -1;
+    explicit device_guard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~device_guard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+void free_bvh_arrays(gbrt_bvh* b)
+{
+    cudaFree(b->nodes);
+    cudaFree(b->tris);
+    cudaFree(b->sorted_codes);
+    cudaFree(b->sorted_ids);
+    b->nodes = nullptr;
+    b->tris = nullptr;
+    b->sorted_codes = nullptr;
+    b->sorted_ids = nullptr;
+}
+
+gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
+{
+    if (ctx->slot_capacity >= rays_per_slot) return GBRT_OK;
+    for (int k = 0; k < gbrt_context::kSlots; ++k)
+    {
+        if (ctx->slot_stream[k]) GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->slot_stream[k]));
+        cudaFree(ctx->slot_rays[k]);
+        cudaFree(ctx->slot_hits[k]);
+        ctx->slot_rays[k] = ctx->slot_hits[k] = nullptr;
+    }
+    ctx->slot_capacity = 0;
+    for (int k = 0; k < gbrt_context::kSlots; ++k)
+    {
+        if (!ctx->slot_stream[k]) GBRT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->slot_stream[k], cudaStreamNonBlocking));
+        if (!ctx->slot_done[k]) GBRT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->slot_done[k], cudaEventDisableTiming));
+        GBRT_CUDA(ctx, cudaMalloc(&ctx->slot_rays[k], rays_per_slot * sizeof(gbrt_ray)));
+        GBRT_CUDA(ctx, cudaMalloc(&ctx->slot_hits[k], rays_per_slot * sizeof(gbrt_hit)));
+    }
+    ctx->slot_capacity = rays_per_slot;
+    return GBRT_OK;
+}
+
+// Host-buffer trace: chunks alternate between two slots, each on its own stream, so
+// the copy-in of one chunk overlaps the traversal and copy-out of the other.
+gbrt_status trace_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits,
+                       bool any_hit)
+{
+    if (n == 0) return GBRT_OK;
+    const size_t chunk = std::min<size_t>(n, size_t(1) << 22);   // 4M rays (128 MB) per slot
+    gbrt_status st = ensure_slots(ctx, chunk);
+    if (st != GBRT_OK) return st;
+    // work queued on the context stream (e.g. the build) must finish first
+    cudaEvent_t ready;
+    GBRT_CUDA(ctx, cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    GBRT_CUDA(ctx, cudaEventRecord(ready, ctx->stream));
+    for (int k = 0; k < gbrt_context::kSlots; ++k) GBRT_CUDA(ctx, cudaStreamWaitEvent(ctx->slot_stream[k], ready, 0));
+    int c = 0;
+    for (size_t b = 0; b < n; b += chunk, ++c)
+    {
+        int k = c % gbrt_context::kSlots;
+        cudaStream_t s = ctx->slot_stream[k];
+        uint32_t m = uint32_t(std::min<size_t>(chunk, n - b));
+        GBRT_CUDA(ctx, cudaMemcpyAsync(ctx->slot_rays[k], h_rays + b, size_t(m) * sizeof(gbrt_ray),
+                                       cudaMemcpyHostToDevice, s));
+        st = trace(ctx, bvh, static_cast<gbrt_ray*>(ctx->slot_rays[k]), m, static_cast<gbrt_hit*>(ctx->slot_hits[k]),
+                   any_hit, s);
+        if (st != GBRT_OK) return st;
+        GBRT_CUDA(ctx, cudaMemcpyAsync(h_hits + b, ctx->slot_hits[k], size_t(m) * sizeof(gbrt_hit),
+                                       cudaMemcpyDeviceToHost, s));
+    }
+    for (int k = 0; k < gbrt_context::kSlots; ++k) GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->slot_stream[k]));
+    cudaEventDestroy(ready);
+    return GBRT_OK;
+}
+
+gbrt_status check_trace_args(gbrt_context* ctx, gbrt_bvh const* bvh, const void* rays, uint32_t n, const void* hits)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!bvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "trace: null bvh");
+    if (n > 0 && (!rays || !hits)) return fail(ctx, GBRT_ERR_INVALID_ARG, "trace: null ray or hit buffer");
+    return GBRT_OK;
+}
+
+} // namespace
+} // namespace gbrt
+
+using namespace gbrt;
+
+extern "C" {
+
+int gbrt_abi_version(void) { return GBRT_ABI_VERSION; }
+
+gbrt_status gbrt_context_create(int device, void* stream, gbrt_context** out)
+{
+    if (!out) return GBRT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return GBRT_ERR_INVALID_ARG;
+    auto* ctx = new (std::nothrow) gbrt_context;
+    if (!ctx) return GBRT_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    device_guard g(device);
+    if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaMalloc(&ctx->d_status, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->d_status, 0, sizeof(uint32_t)) != cudaSuccess)
+    {
+        cudaFree(ctx->d_status);
+        delete ctx;
+        return GBRT_ERR_CUDA;
+    }
+    *out = ctx;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_destroy(gbrt_context* ctx)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    {
+        device_guard g(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        for (int k = 0; k < gbrt_context::kSlots; ++k)
+        {
+            if (ctx->slot_stream[k])
+            {
+                cudaStreamSynchronize(ctx->slot_stream[k]);
+                cudaStreamDestroy(ctx->slot_stream[k]);
+            }
+            if (ctx->slot_done[k]) cudaEventDestroy(ctx->slot_done[k]);
+            cudaFree(ctx->slot_rays[k]);
+            cudaFree(ctx->slot_hits[k]);
+        }
+        cudaFree(ctx->scratch);
+        cudaFree(ctx->d_status);
+    }
+    delete ctx;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_set_stream(gbrt_context* ctx, void* stream)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_synchronize(gbrt_context* ctx)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    device_guard g(ctx->device);
+    uint32_t status = 0;
+    GBRT_CUDA(ctx, cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (status != 0)
+    {
+        GBRT_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
+        GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (status & kStatusStackOverflow)
+            return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "a traversal stack overflowed; results are incomplete");
+        if (status & kStatusBadIndex)
+            return fail(ctx, GBRT_ERR_CUDA, "a kernel met an out-of-range node or triangle index and skipped it");
+        return fail(ctx, GBRT_ERR_WATCHDOG, "a bounded device-side wait gave up");
+    }
+    return GBRT_OK;
+}
+
+const char* gbrt_last_error(gbrt_context const* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+uint64_t gbrt_kernel_launch_count(gbrt_context const* ctx) { return ctx ? ctx->launches : 0; }
+
+gbrt_status gbrt_bvh_build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_lbvh: null output");
+    *out = nullptr;
+    if (n > 0 && !d_tris) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_lbvh: null triangles");
+    if (n > kMaxPrims) return fail(ctx, GBRT_ERR_TOO_LARGE, "build_lbvh: more than 2^29 triangles");
+    if ((reinterpret_cast<uintptr_t>(d_tris) & 3u) != 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "build_lbvh: triangles not 4-byte aligned");
+    device_guard g(ctx->device);
+    auto* bvh = new (std::nothrow) gbrt_bvh;
+    if (!bvh) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "build_lbvh: host allocation");
+    bvh->device = ctx->device;
+    gbrt_status st = build_lbvh(ctx, d_tris, n, bvh);
+    if (st != GBRT_OK)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        free_bvh_arrays(bvh);
+        delete bvh;
+        return st;
+    }
+    *out = bvh;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_bvh_build_lbvh_host(gbrt_context* ctx, gbrt_triangle const* h_tris, uint32_t n, gbrt_bvh** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_lbvh_host: null output");
+    if (n > 0 && !h_tris) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_lbvh_host: null triangles");
+    if (n > kMaxPrims) return fail(ctx, GBRT_ERR_TOO_LARGE, "build_lbvh_host: more than 2^29 triangles");
+    device_guard g(ctx->device);
+    gbrt_triangle* d = nullptr;
+    if (n > 0)
+    {
+        GBRT_CUDA(ctx, cudaMalloc(&d, size_t(n) * sizeof(gbrt_triangle)));
+        cudaError_t e = cudaMemcpyAsync(d, h_tris, size_t(n) * sizeof(gbrt_triangle), cudaMemcpyHostToDevice,
+                                        ctx->stream);
+        if (e != cudaSuccess)
+        {
+            cudaFree(d);
+            return check_cuda(ctx, e, "build_lbvh_host: copy");
+        }
+    }
+    gbrt_status st = gbrt_bvh_build_lbvh(ctx, d, n, out);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    return st;
+}
+
+gbrt_status gbrt_bvh_upload_bvh2_host(gbrt_context* ctx, gbrt_bvh_node const* nodes, uint32_t num_nodes,
+                                      uint32_t const* indices, uint32_t num_indices, gbrt_triangle const* tris,
+                                      uint32_t num_tris, gbrt_bvh** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: null output");
+    *out = nullptr;
+    if ((num_nodes && !nodes) || (num_indices && !indices) || (num_tris && !tris))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: null array");
+    if (num_tris > kMaxPrims || num_indices > kMaxPrims)
+        return fail(ctx, GBRT_ERR_TOO_LARGE, "upload_bvh2: more than 2^29 primitives");
+    device_guard g(ctx->device);
+    auto* bvh = new (std::nothrow) gbrt_bvh;
+    if (!bvh) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "upload_bvh2: host allocation");
+    bvh->device = ctx->device;
+    gbrt_status st = upload_bvh2(ctx, nodes, num_nodes, indices, num_indices, tris, num_tris, bvh);
+    if (st != GBRT_OK)
+    {
+        free_bvh_arrays(bvh);
+        delete bvh;
+        return st;
+    }
+    *out = bvh;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_bvh_destroy(gbrt_bvh* bvh)
+{
+    if (!bvh) return GBRT_ERR_INVALID_ARG;
+    device_guard g(bvh->device);
+    free_bvh_arrays(bvh);
+    delete bvh;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* num_bvh2_nodes, uint32_t* depth_bound)
+{
+    if (!bvh) return GBRT_ERR_INVALID_ARG;
+    if (num_prims) *num_prims = bvh->num_prims;
+    if (num_bvh2_nodes) *num_bvh2_nodes = bvh->num_prims > 0 ? 2 * bvh->num_prims - 1 : 0;
+    if (depth_bound) *depth_bound = bvh->height;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes, uint32_t* d_indices)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!bvh || (bvh->num_prims > 0 && (!d_nodes || !d_indices)))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "export_bvh2: null argument");
+    if (!aligned16(d_nodes)) return fail(ctx, GBRT_ERR_INVALID_ARG, "export_bvh2: nodes not 16-byte aligned");
+    device_guard g(ctx->device);
+    return export_bvh2(ctx, bvh, d_nodes, d_indices);
+}
+
+gbrt_status gbrt_bvh_morton_codes(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!bvh || (bvh->num_prims > 0 && !d_codes)) return fail(ctx, GBRT_ERR_INVALID_ARG, "morton_codes: null argument");
+    device_guard g(ctx->device);
+    return morton_codes_input_order(ctx, bvh, d_codes);
+}
+
+static gbrt_status trace_device(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
+                                gbrt_hit* d_hits, bool any_hit)
+{
+    gbrt_status st = check_trace_args(ctx, bvh, d_rays, n, d_hits);
+    if (st != GBRT_OK) return st;
+    if (!aligned16(d_rays) || !aligned16(d_hits))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "trace: ray and hit buffers must be 16-byte aligned");
+    device_guard g(ctx->device);
+    return trace(ctx, bvh, d_rays, n, d_hits, any_hit, ctx->stream);
+}
+
+gbrt_status gbrt_trace_closest_hit(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
+                                   gbrt_hit* d_hits)
+{
+    return trace_device(ctx, bvh, d_rays, n, d_hits, false);
+}
+
+gbrt_status gbrt_trace_any_hit(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
+                               gbrt_hit* d_hits)
+{
+    return trace_device(ctx, bvh, d_rays, n, d_hits, true);
+}
+
+gbrt_status gbrt_trace_closest_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h_rays, uint32_t n,
+                                        gbrt_hit* h_hits)
+{
+    gbrt_status st = check_trace_args(ctx, bvh, h_rays, n, h_hits);
+    if (st != GBRT_OK) return st;
+    device_guard g(ctx->device);
+    return trace_host(ctx, bvh, h_rays, n, h_hits, false);
+}
+
+gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h_rays, uint32_t n,
+                                    gbrt_hit* h_hits)
+{
+    gbrt_status st = check_trace_args(ctx, bvh, h_rays, n, h_hits);
+    if (st != GBRT_OK) return st;
+    device_guard g(ctx->device);
+    return trace_host(ctx, bvh, h_rays, n, h_hits, true);
+}
+
+} // extern "C"

@@ -1,0 +1,110 @@
+// Internal state behind the opaque handles of gbrt.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/visionaray_gb300/gbrt.h"
+#include "bvh_layout.cuh"
+
+// Device status bits, OR-ed by kernels into gbrt_context::d_status and reported by
+// gbrt_context_synchronize.
+enum : uint32_t
+{
+    kStatusStackOverflow = 1u << 0,
+    kStatusWatchdog      = 1u << 1,
+    kStatusBadIndex      = 1u << 2,   // a node/triangle index outside its array was skipped
+};
+
+struct gbrt_context
+{
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    uint64_t launches = 0;
+
+    uint32_t* d_status = nullptr;     // one word of status bits
+
+    // Reusable scratch for builds (grown on demand, freed with the context).
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+
+    // Host-buffer trace path: two staging slots, each on its own stream.
+    static constexpr int kSlots = 2;
+    cudaStream_t slot_stream[kSlots] = { nullptr, nullptr };
+    cudaEvent_t slot_done[kSlots] = { nullptr, nullptr };
+    void* slot_rays[kSlots] = { nullptr, nullptr };
+    void* slot_hits[kSlots] = { nullptr, nullptr };
+    size_t slot_capacity = 0;   // rays per slot
+};
+
+enum class bvh_kind
+{
+    lbvh,
+    uploaded,
+};
+
+struct gbrt_bvh
+{
+    bvh_kind kind = bvh_kind::lbvh;
+    int device = 0;
+    uint32_t num_prims = 0;
+    uint32_t num_inner = 0;      // inner nodes (records in `nodes`)
+    int32_t root = 0;            // >= 0 inner node, < 0 leaf (~first triangle)
+    uint32_t height = 0;         // levels of inner nodes on the longest root-leaf path
+    gbrt::bvh2_node* nodes = nullptr;
+    gbrt::tri48* tris = nullptr; // leaf order
+    // LBVH only: sorted Morton codes and, per sorted position, the input index.
+    uint32_t* sorted_codes = nullptr;
+    uint32_t* sorted_ids = nullptr;
+};
+
+namespace gbrt {
+
+// Sets ctx->last_error and returns `st`.
+gbrt_status fail(gbrt_context* ctx, gbrt_status st, std::string const& what);
+// Maps a CUDA error to a status, recording `where`.
+gbrt_status check_cuda(gbrt_context* ctx, cudaError_t err, const char* where);
+// Grows the context scratch to at least `bytes`.
+gbrt_status ensure_scratch(gbrt_context* ctx, size_t bytes);
+
+// lbvh.cu
+gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh);
+gbrt_status export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes,
+                        uint32_t* d_indices);
+gbrt_status morton_codes_input_order(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes);
+gbrt_status upload_bvh2(gbrt_context* ctx, gbrt_bvh_node const* nodes, uint32_t num_nodes,
+                        uint32_t const* indices, uint32_t num_indices, gbrt_triangle const* tris,
+                        uint32_t num_tris, gbrt_bvh* bvh);
+
+// radix_sort.cu: stable LSD sort of (key, value) pairs by the low `key_bits` bits.
+// Result lands in (keys, values); keys_alt/values_alt are same-sized scratch.
+size_t radix_sort_scratch_bytes(uint32_t n);
+gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values,
+                             uint32_t* keys_alt, uint32_t* values_alt, uint32_t n, int key_bits,
+                             void* scratch);
+
+// traverse.cu
+gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
+                  gbrt_hit* d_hits, bool any_hit, cudaStream_t stream);
+
+} // namespace gbrt
+
+// Launch bookkeeping: counts the kernel and checks the launch.
+#define GBRT_LAUNCH_CHECK(ctx, name)                                                       \
+    do                                                                                     \
+    {                                                                                      \
+        (ctx)->launches++;                                                                 \
+        cudaError_t e_ = cudaGetLastError();                                               \
+        if (e_ != cudaSuccess) return gbrt::check_cuda((ctx), e_, name);                   \
+    } while (0)
+
+#define GBRT_CUDA(ctx, call)                                                               \
+    do                                                                                     \
+    {                                                                                      \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) return gbrt::check_cuda((ctx), e_, #call);                  \
+    } while (0)

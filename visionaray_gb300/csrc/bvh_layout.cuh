@@ -1,0 +1,46 @@
+// HBM layout of a traversal BVH.
+//
+// Nodes: one 64-byte record per inner node holding BOTH children's boxes, so a
+// traversal step is four coalesced 128-bit loads and two slab tests (the node-pair
+// layout of Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
+// HPG 2009):
+//     xy0  = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//     xy1  = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//     z01  = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//     link = (child0, child1, height, parent)
+// child >= 0 is an inner node index; child < 0 is a leaf whose first triangle is
+// ~child.  height is the subtree height (leaves 0); parent is the parent inner
+// node (-1 for the root) -- both are build-time fields, unused by traversal.
+//
+// Triangles: 48 bytes, three float4, stored in leaf order so that a leaf is a
+// contiguous run; the last triangle of a leaf carries kLastInLeaf.
+//     t0 = (v1.x, v1.y, v1.z, prim_id bits)
+//     t1 = (e1.x, e1.y, e1.z, geom_id bits)
+//     t2 = (e2.x, e2.y, e2.z, flags bits)
+#pragma once
+
+#include <cstdint>
+
+namespace gbrt {
+
+struct __align__(16) bvh2_node
+{
+    float4 xy0;
+    float4 xy1;
+    float4 z01;
+    int4 link;
+};
+static_assert(sizeof(bvh2_node) == 64, "node is one 64-byte record");
+
+struct __align__(16) tri48
+{
+    float4 t0;
+    float4 t1;
+    float4 t2;
+};
+static_assert(sizeof(tri48) == 48, "triangle is 48 bytes");
+
+constexpr uint32_t kLastInLeaf = 1u;
+constexpr int kStackSize = 64;   // traversal stack entries (tree height must stay below)
+
+} // namespace gbrt

@@ -1,0 +1,640 @@
+// GPU LBVH construction (Karras, "Maximizing Parallelism in the Construction of BVHs,
+// Octrees, and k-d Trees", HPG 2012) -- replaces lbvh_builder::build(cuda_index_bvh<P>{},
+// prims, n) of visionaray detail/bvh/lbvh.h:681-844.
+//
+// Pipeline (all on the context stream, one synchronisation at the end):
+//   1. centroid_bounds  : per-triangle bounds and centroid (lbvh.h:215-240), block
+//                         min/max reduction, 6 atomics per block on order-preserving
+//                         ints (the reference does 6 CAS loops per triangle on one
+//                         address).
+//   2. morton_codes     : centroid quantised op-for-op as lbvh.h:253-267.
+//   3. radix sort       : stable, by the 30-bit code (radix_sort.cu).
+//   4. build_hierarchy  : Karras split per inner node (lbvh.h:120-185, 281-330).
+//   5. refit_and_emit   : one thread per leaf writes the triangle in leaf order and its
+//                         box into the parent's child slot, then climbs; at each node
+//                         the SECOND arriving thread continues (an atomic counter per
+//                         node) so every node is combined once -- the reference walks
+//                         every leaf to the root with 6 CAS loops per level
+//                         (lbvh.h:332-372).
+// Topology and boxes equal the reference's for identical Morton codes; the node-pair
+// layout is gbrt::bvh2_node (bvh_layout.cuh).
+
+#include "api_internal.h"
+#include "device_math.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace gbrt {
+namespace {
+
+constexpr int kBlock = 256;
+
+struct tri_in
+{
+    f3 v1, e1, e2;
+    uint32_t prim_id, geom_id;
+};
+
+__device__ __forceinline__ tri_in load_tri(gbrt_triangle const* __restrict__ tris, uint64_t i)
+{
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(tris + i);
+    uint32_t g = __ldg(w + 0), p = __ldg(w + 1);
+    tri_in t;
+    t.geom_id = g;
+    t.prim_id = p;
+    t.v1 = { __uint_as_float(__ldg(w + 2)), __uint_as_float(__ldg(w + 3)), __uint_as_float(__ldg(w + 4)) };
+    t.e1 = { __uint_as_float(__ldg(w + 5)), __uint_as_float(__ldg(w + 6)), __uint_as_float(__ldg(w + 7)) };
+    t.e2 = { __uint_as_float(__ldg(w + 8)), __uint_as_float(__ldg(w + 9)), __uint_as_float(__ldg(w + 10)) };
+    return t;
+}
+
+struct box3
+{
+    f3 lo, hi;
+};
+
+// get_bounds(triangle) (math/detail/triangle.inl:43-52): insert v1, v1+e1, v1+e2 into
+// an invalid box with the reference's min/max forms.
+__device__ __forceinline__ box3 tri_box(tri_in const& t)
+{
+    f3 p1 = { __fadd_rn(t.v1.x, t.e1.x), __fadd_rn(t.v1.y, t.e1.y), __fadd_rn(t.v1.z, t.e1.z) };
+    f3 p2 = { __fadd_rn(t.v1.x, t.e2.x), __fadd_rn(t.v1.y, t.e2.y), __fadd_rn(t.v1.z, t.e2.z) };
+    box3 b;
+    b.lo = { ref_min(FLT_MAX, t.v1.x), ref_min(FLT_MAX, t.v1.y), ref_min(FLT_MAX, t.v1.z) };
+    b.hi = { ref_max(-FLT_MAX, t.v1.x), ref_max(-FLT_MAX, t.v1.y), ref_max(-FLT_MAX, t.v1.z) };
+    b.lo = { ref_min(b.lo.x, p1.x), ref_min(b.lo.y, p1.y), ref_min(b.lo.z, p1.z) };
+    b.hi = { ref_max(b.hi.x, p1.x), ref_max(b.hi.y, p1.y), ref_max(b.hi.z, p1.z) };
+    b.lo = { ref_min(b.lo.x, p2.x), ref_min(b.lo.y, p2.y), ref_min(b.lo.z, p2.z) };
+    b.hi = { ref_max(b.hi.x, p2.x), ref_max(b.hi.y, p2.y), ref_max(b.hi.z, p2.z) };
+    return b;
+}
+
+__device__ __forceinline__ f3 box_center(box3 const& b)
+{
+    return { __fmul_rn(__fadd_rn(b.hi.x, b.lo.x), 0.5f), __fmul_rn(__fadd_rn(b.hi.y, b.lo.y), 0.5f),
+             __fmul_rn(__fadd_rn(b.hi.z, b.lo.z), 0.5f) };
+}
+
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ref_min(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ref_max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+// cb_ordered: {min.x, min.y, min.z, max.x, max.y, max.z} as order-preserving ints,
+// initialised to (+FLT_MAX, -FLT_MAX).
+__global__ void __launch_bounds__(kBlock) centroid_bounds(gbrt_triangle const* __restrict__ tris, uint32_t n,
+                                                          float4* __restrict__ centroids,
+                                                          int* __restrict__ cb_ordered)
+{
+    float mn[3] = { FLT_MAX, FLT_MAX, FLT_MAX };
+    float mx[3] = { -FLT_MAX, -FLT_MAX, -FLT_MAX };
+    for (uint64_t i = uint64_t(blockIdx.x) * kBlock + threadIdx.x; i < n; i += uint64_t(gridDim.x) * kBlock)
+    {
+        box3 b = tri_box(load_tri(tris, i));
+        f3 c = box_center(b);
+        centroids[i] = make_float4(c.x, c.y, c.z, 0.0f);
+        mn[0] = ref_min(mn[0], c.x);
+        mn[1] = ref_min(mn[1], c.y);
+        mn[2] = ref_min(mn[2], c.z);
+        mx[0] = ref_max(mx[0], c.x);
+        mx[1] = ref_max(mx[1], c.y);
+        mx[2] = ref_max(mx[2], c.z);
+    }
+    __shared__ float red[kBlock / 32][6];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int a = 0; a < 3; ++a)
+    {
+        mn[a] = warp_min(mn[a]);
+        mx[a] = warp_max(mx[a]);
+    }
+    if (lane == 0)
+    {
+        for (int a = 0; a < 3; ++a)
+        {
+            red[warp][a] = mn[a];
+            red[warp][3 + a] = mx[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6)
+    {
+        int a = threadIdx.x;
+        float v = red[0][a];
+        for (int w = 1; w < kBlock / 32; ++w) v = a < 3 ? ref_min(v, red[w][a]) : ref_max(v, red[w][a]);
+        if (a < 3)
+            atomicMin(&cb_ordered[a], float_to_ordered(v));
+        else
+            atomicMax(&cb_ordered[a], float_to_ordered(v));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) morton_codes(const float4* __restrict__ centroids, uint32_t n,
+                                                       const int* __restrict__ cb_ordered,
+                                                       uint32_t* __restrict__ keys,
+                                                       uint32_t* __restrict__ values)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    box3 cb;
+    cb.lo = { ordered_to_float(cb_ordered[0]), ordered_to_float(cb_ordered[1]), ordered_to_float(cb_ordered[2]) };
+    cb.hi = { ordered_to_float(cb_ordered[3]), ordered_to_float(cb_ordered[4]), ordered_to_float(cb_ordered[5]) };
+    f3 center = box_center(cb);
+    f3 size = { __fsub_rn(cb.hi.x, cb.lo.x), __fsub_rn(cb.hi.y, cb.lo.y), __fsub_rn(cb.hi.z, cb.lo.z) };
+    float4 c4 = centroids[i];
+    float c[3] = { c4.x, c4.y, c4.z };
+    float cc[3] = { center.x, center.y, center.z };
+    float cs[3] = { size.x, size.y, size.z };
+    uint32_t q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        // centroid -= center; centroid = (centroid + size * 0.5) / size;
+        // centroid = min(max(centroid * 1024, 0), 1023)       (lbvh.h:256-263)
+        float v = __fsub_rn(c[a], cc[a]);
+        v = __fdiv_rn(__fadd_rn(v, __fmul_rn(cs[a], 0.5f)), cs[a]);
+        v = __fmul_rn(v, 1024.0f);
+        v = ref_min(ref_max(v, 0.0f), 1023.0f);
+        q[a] = static_cast<uint32_t>(v);
+    }
+    keys[i] = morton3(q[0], q[1], q[2]);
+    values[i] = i;
+}
+
+// Karras delta: common-prefix length of sorted keys i and j, with the index as a
+// tie-break for equal keys, -1 outside [0, n).
+__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ codes, int n, int i, uint32_t ci, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    uint32_t x = ci ^ __ldg(&codes[j]);
+    return x == 0 ? 32 + __clz(uint32_t(i) ^ uint32_t(j)) : __clz(x);
+}
+
+// Inner node i of n-1: children into nodes[i].link.{x,y} (inner index, or ~leaf for a
+// leaf), parent links for inner children in nodes[c].link.w = (i << 1) | side, for
+// leaves in leaf_parent[j].
+__global__ void __launch_bounds__(kBlock) build_hierarchy(const uint32_t* __restrict__ codes, int n,
+                                                          bvh2_node* __restrict__ nodes,
+                                                          int* __restrict__ leaf_parent)
+{
+    int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n - 1) return;
+    uint32_t ci = __ldg(&codes[i]);
+    int d = kdelta(codes, n, i, ci, i + 1) >= kdelta(codes, n, i, ci, i - 1) ? 1 : -1;
+    int dmin = kdelta(codes, n, i, ci, i - d);
+    int lmax = 2;
+    while (kdelta(codes, n, i, ci, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(codes, n, i, ci, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(codes, n, i, ci, j);
+    int s = 0;
+    int t = l;
+    do
+    {
+        t = (t + 1) >> 1;
+        if (kdelta(codes, n, i, ci, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int split = i + s * d + min(d, 0);
+    int first = min(i, j), last = max(i, j);
+
+    int left = split, right = split + 1;
+    int cl, cr;
+    if (left == first)
+    {
+        cl = ~left;
+        leaf_parent[left] = (i << 1) | 0;
+    }
+    else
+    {
+        cl = left;
+        nodes[left].link.w = (i << 1) | 0;
+    }
+    if (right == last)
+    {
+        cr = ~right;
+        leaf_parent[right] = (i << 1) | 1;
+    }
+    else
+    {
+        cr = right;
+        nodes[right].link.w = (i << 1) | 1;
+    }
+    nodes[i].link.x = cl;
+    nodes[i].link.y = cr;
+    if (i == 0) nodes[0].link.w = -1;
+}
+
+__device__ __forceinline__ void store_child_box(bvh2_node* node, int side, box3 const& b)
+{
+    float4 xy = make_float4(b.lo.x, b.hi.x, b.lo.y, b.hi.y);
+    if (side == 0)
+    {
+        node->xy0 = xy;
+        node->z01.x = b.lo.z;
+        node->z01.y = b.hi.z;
+    }
+    else
+    {
+        node->xy1 = xy;
+        node->z01.z = b.lo.z;
+        node->z01.w = b.hi.z;
+    }
+}
+
+// Loads through L2 (bypassing L1): the sibling's box was written by another SM.
+__device__ __forceinline__ box3 load_union_cg(bvh2_node* node)
+{
+    float4 a = __ldcg(&node->xy0);
+    float4 b = __ldcg(&node->xy1);
+    float4 z = __ldcg(&node->z01);
+    box3 r;
+    r.lo = { ref_min(a.x, b.x), ref_min(a.z, b.z), ref_min(z.x, z.z) };
+    r.hi = { ref_max(a.y, b.y), ref_max(a.w, b.w), ref_max(z.y, z.w) };
+    return r;
+}
+
+__global__ void __launch_bounds__(kBlock) refit_and_emit(gbrt_triangle const* __restrict__ tris_in,
+                                                         const uint32_t* __restrict__ sorted_ids, int n,
+                                                         const int* __restrict__ leaf_parent,
+                                                         bvh2_node* __restrict__ nodes,
+                                                         uint32_t* __restrict__ arrivals,
+                                                         tri48* __restrict__ tris_out,
+                                                         uint32_t* __restrict__ root_height,
+                                                         uint32_t* __restrict__ status)
+{
+    int j = blockIdx.x * kBlock + threadIdx.x;
+    if (j >= n) return;
+    tri_in t = load_tri(tris_in, __ldg(&sorted_ids[j]));
+    tri48 o;
+    o.t0 = make_float4(t.v1.x, t.v1.y, t.v1.z, __uint_as_float(t.prim_id));
+    o.t1 = make_float4(t.e1.x, t.e1.y, t.e1.z, __uint_as_float(t.geom_id));
+    o.t2 = make_float4(t.e2.x, t.e2.y, t.e2.z, __uint_as_float(kLastInLeaf));
+    tris_out[j] = o;
+
+    box3 b = tri_box(t);
+    int link = leaf_parent[j];
+    int height = 0;   // height of the subtree whose box is `b`
+    // a valid tree has at most n-1 levels; the bound only guards against a corrupt link
+    for (int step = 0; step < n; ++step)
+    {
+        if (link < 0 || (link >> 1) >= n - 1)
+        {
+            atomicOr(status, kStatusBadIndex);
+            return;
+        }
+        int node = link >> 1, side = link & 1;
+        bvh2_node* nd = &nodes[node];
+        store_child_box(nd, side, b);
+        // the subtree height travels in the node's link.z as max over arrivals
+        atomicMax(&nd->link.z, height + 1);
+        __threadfence();
+        if (atomicAdd(&arrivals[node], 1u) == 0) return;   // first arrival stops
+        __threadfence();
+        b = load_union_cg(nd);
+        height = __ldcg(&nd->link.z);
+        int up = __ldcg(&nd->link.w);
+        if (up < 0)
+        {
+            *root_height = uint32_t(height);
+            return;
+        }
+        link = up;
+    }
+    atomicOr(status, kStatusBadIndex);
+}
+
+// lbvh::collapse (lbvh.h:374-451): nodes of the cuda_index_bvh layout -- root at 0, the
+// children of inner node i at 1+2i and 2+2i, one primitive per leaf with first_prim =
+// the original index.
+__global__ void __launch_bounds__(kBlock) export_collapse(const bvh2_node* __restrict__ nodes, int num_inner,
+                                                          const uint32_t* __restrict__ sorted_ids,
+                                                          gbrt_bvh_node* __restrict__ out)
+{
+    int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= num_inner) return;
+    bvh2_node nd = nodes[i];
+    box3 cbox[2];
+    cbox[0].lo = { nd.xy0.x, nd.xy0.z, nd.z01.x };
+    cbox[0].hi = { nd.xy0.y, nd.xy0.w, nd.z01.y };
+    cbox[1].lo = { nd.xy1.x, nd.xy1.z, nd.z01.z };
+    cbox[1].hi = { nd.xy1.y, nd.xy1.w, nd.z01.w };
+    int child[2] = { nd.link.x, nd.link.y };
+    auto put = [&](gbrt_bvh_node& d, box3 const& b, uint32_t first, uint16_t count) {
+        d.bbox_min[0] = b.lo.x;
+        d.bbox_min[1] = b.lo.y;
+        d.bbox_min[2] = b.lo.z;
+        d.bbox_max[0] = b.hi.x;
+        d.bbox_max[1] = b.hi.y;
+        d.bbox_max[2] = b.hi.z;
+        d.first_child_or_prim = first;
+        d.num_prims = count;
+        d.ordered_traversal_axis = 0;
+        d.ordered_traversal_sign = 0;
+    };
+    for (int s = 0; s < 2; ++s)
+    {
+        gbrt_bvh_node& d = out[1 + 2 * i + s];
+        if (child[s] < 0)
+            put(d, cbox[s], __ldg(&sorted_ids[~child[s]]), 1);
+        else
+            put(d, cbox[s], uint32_t(1 + 2 * child[s]), 0);
+    }
+    if (i == 0)
+    {
+        box3 r;
+        r.lo = { ref_min(cbox[0].lo.x, cbox[1].lo.x), ref_min(cbox[0].lo.y, cbox[1].lo.y),
+                 ref_min(cbox[0].lo.z, cbox[1].lo.z) };
+        r.hi = { ref_max(cbox[0].hi.x, cbox[1].hi.x), ref_max(cbox[0].hi.y, cbox[1].hi.y),
+                 ref_max(cbox[0].hi.z, cbox[1].hi.z) };
+        put(out[0], r, 1u, 0);
+    }
+}
+
+// Single-triangle tree: the root is the leaf (lbvh.h:428-433).
+__global__ void export_single_leaf(const tri48* __restrict__ tris, const uint32_t* __restrict__ sorted_ids,
+                                   gbrt_bvh_node* __restrict__ out, uint32_t* __restrict__ indices)
+{
+    tri48 t = tris[0];
+    tri_in ti;
+    ti.v1 = { t.t0.x, t.t0.y, t.t0.z };
+    ti.e1 = { t.t1.x, t.t1.y, t.t1.z };
+    ti.e2 = { t.t2.x, t.t2.y, t.t2.z };
+    box3 b = tri_box(ti);
+    gbrt_bvh_node& d = out[0];
+    d.bbox_min[0] = b.lo.x;
+    d.bbox_min[1] = b.lo.y;
+    d.bbox_min[2] = b.lo.z;
+    d.bbox_max[0] = b.hi.x;
+    d.bbox_max[1] = b.hi.y;
+    d.bbox_max[2] = b.hi.z;
+    d.first_child_or_prim = sorted_ids[0];
+    d.num_prims = 1;
+    d.ordered_traversal_axis = 0;
+    d.ordered_traversal_sign = 0;
+    indices[0] = 0;
+}
+
+__global__ void emit_single(gbrt_triangle const* __restrict__ tris_in, tri48* __restrict__ tris_out)
+{
+    tri_in t = load_tri(tris_in, 0);
+    tri48 o;
+    o.t0 = make_float4(t.v1.x, t.v1.y, t.v1.z, __uint_as_float(t.prim_id));
+    o.t1 = make_float4(t.e1.x, t.e1.y, t.e1.z, __uint_as_float(t.geom_id));
+    o.t2 = make_float4(t.e2.x, t.e2.y, t.e2.z, __uint_as_float(kLastInLeaf));
+    tris_out[0] = o;
+}
+
+__global__ void __launch_bounds__(kBlock) iota(uint32_t* __restrict__ out, uint32_t n)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < n) out[i] = i;
+}
+
+__global__ void __launch_bounds__(kBlock) scatter_codes(const uint32_t* __restrict__ sorted_codes,
+                                                        const uint32_t* __restrict__ sorted_ids, uint32_t n,
+                                                        uint32_t* __restrict__ out)
+{
+    uint32_t j = blockIdx.x * kBlock + threadIdx.x;
+    if (j < n) out[sorted_ids[j]] = sorted_codes[j];
+}
+
+inline uint32_t blocks_for(uint64_t n) { return uint32_t((n + kBlock - 1) / kBlock); }
+
+inline size_t align_up(size_t v) { return (v + 255) & ~size_t(255); }
+
+} // namespace
+
+gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh)
+{
+    bvh->kind = bvh_kind::lbvh;
+    bvh->num_prims = n;
+    bvh->num_inner = n > 0 ? n - 1 : 0;
+    bvh->root = n > 1 ? 0 : ~0;
+    bvh->height = n > 1 ? 1 : 0;
+    if (n == 0) return GBRT_OK;
+
+    cudaStream_t s = ctx->stream;
+    GBRT_CUDA(ctx, cudaMalloc(&bvh->tris, size_t(n) * sizeof(tri48)));
+    GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_codes, size_t(n) * 4));
+    GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_ids, size_t(n) * 4));
+    if (bvh->num_inner > 0) GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes, size_t(bvh->num_inner) * sizeof(bvh2_node)));
+
+    // scratch: centroids | keys_alt | vals_alt | leaf_parent | arrivals | cb(6) | height | sort
+    size_t off_centroids = 0;
+    size_t off_keys_alt = align_up(off_centroids + size_t(n) * 16);
+    size_t off_vals_alt = align_up(off_keys_alt + size_t(n) * 4);
+    size_t off_parent = align_up(off_vals_alt + size_t(n) * 4);
+    size_t off_arrivals = align_up(off_parent + size_t(n) * 4);
+    size_t off_cb = align_up(off_arrivals + size_t(n) * 4);
+    size_t off_sort = align_up(off_cb + 8 * 4);
+    size_t total = off_sort + radix_sort_scratch_bytes(n);
+    gbrt_status st = ensure_scratch(ctx, total);
+    if (st != GBRT_OK) return st;
+    char* base = static_cast<char*>(ctx->scratch);
+    float4* centroids = reinterpret_cast<float4*>(base + off_centroids);
+    uint32_t* keys_alt = reinterpret_cast<uint32_t*>(base + off_keys_alt);
+    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(base + off_vals_alt);
+    int* leaf_parent = reinterpret_cast<int*>(base + off_parent);
+    uint32_t* arrivals = reinterpret_cast<uint32_t*>(base + off_arrivals);
+    int* cb = reinterpret_cast<int*>(base + off_cb);
+    uint32_t* root_height = reinterpret_cast<uint32_t*>(cb + 6);
+
+    // cb = (+FLT_MAX x3, -FLT_MAX x3) as ordered ints; root height 1 by default
+    int init[8];
+    {
+        float lo = FLT_MAX, hi = -FLT_MAX;
+        int li, hi_i;
+        memcpy(&li, &lo, 4);
+        memcpy(&hi_i, &hi, 4);
+        hi_i = hi_i ^ 0x7FFFFFFF;   // negative float -> ordered int
+        for (int a = 0; a < 3; ++a)
+        {
+            init[a] = li;
+            init[3 + a] = hi_i;
+        }
+        init[6] = 1;
+        init[7] = 0;
+    }
+    GBRT_CUDA(ctx, cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, s));
+
+    uint32_t grid = std::min<uint32_t>(blocks_for(n), uint32_t(ctx->num_sms) * 8);
+    centroid_bounds<<<grid, kBlock, 0, s>>>(d_tris, n, centroids, cb);
+    GBRT_LAUNCH_CHECK(ctx, "centroid_bounds");
+    morton_codes<<<blocks_for(n), kBlock, 0, s>>>(centroids, n, cb, bvh->sorted_codes, bvh->sorted_ids);
+    GBRT_LAUNCH_CHECK(ctx, "morton_codes");
+    st = radix_sort_pairs(ctx, bvh->sorted_codes, bvh->sorted_ids, keys_alt, vals_alt, n, 30,
+                          base + off_sort);
+    if (st != GBRT_OK) return st;
+
+    if (n > 1)
+    {
+        GBRT_CUDA(ctx, cudaMemsetAsync(bvh->nodes, 0, size_t(bvh->num_inner) * sizeof(bvh2_node), s));
+        GBRT_CUDA(ctx, cudaMemsetAsync(arrivals, 0, size_t(n) * 4, s));
+        GBRT_CUDA(ctx, cudaMemsetAsync(leaf_parent, 0xFF, size_t(n) * 4, s));
+        build_hierarchy<<<blocks_for(n - 1), kBlock, 0, s>>>(bvh->sorted_codes, int(n), bvh->nodes, leaf_parent);
+        GBRT_LAUNCH_CHECK(ctx, "build_hierarchy");
+        refit_and_emit<<<blocks_for(n), kBlock, 0, s>>>(d_tris, bvh->sorted_ids, int(n), leaf_parent, bvh->nodes,
+                                                        arrivals, bvh->tris, root_height, ctx->d_status);
+        GBRT_LAUNCH_CHECK(ctx, "refit_and_emit");
+        uint32_t h = 0;
+        GBRT_CUDA(ctx, cudaMemcpyAsync(&h, root_height, 4, cudaMemcpyDeviceToHost, s));
+        GBRT_CUDA(ctx, cudaStreamSynchronize(s));
+        bvh->height = h;
+    }
+    else
+    {
+        // one triangle: it is the root leaf (lbvh.h:428-433)
+        emit_single<<<1, 1, 0, s>>>(d_tris, bvh->tris);
+        GBRT_LAUNCH_CHECK(ctx, "emit_single");
+    }
+    if (bvh->height + 1 > uint32_t(kStackSize))
+        return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "LBVH height exceeds the traversal stack");
+    return GBRT_OK;
+}
+
+gbrt_status export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes, uint32_t* d_indices)
+{
+    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "export_bvh2: not an LBVH");
+    uint32_t n = bvh->num_prims;
+    if (n == 0) return GBRT_OK;
+    cudaStream_t s = ctx->stream;
+    if (n == 1)
+    {
+        export_single_leaf<<<1, 1, 0, s>>>(bvh->tris, bvh->sorted_ids, d_nodes, d_indices);
+        GBRT_LAUNCH_CHECK(ctx, "export_single_leaf");
+        return GBRT_OK;
+    }
+    export_collapse<<<blocks_for(bvh->num_inner), kBlock, 0, s>>>(bvh->nodes, int(bvh->num_inner), bvh->sorted_ids,
+                                                                  d_nodes);
+    GBRT_LAUNCH_CHECK(ctx, "export_collapse");
+    iota<<<blocks_for(n), kBlock, 0, s>>>(d_indices, n);
+    GBRT_LAUNCH_CHECK(ctx, "iota");
+    return GBRT_OK;
+}
+
+gbrt_status morton_codes_input_order(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes)
+{
+    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "morton_codes: not an LBVH");
+    if (bvh->num_prims == 0) return GBRT_OK;
+    scatter_codes<<<blocks_for(bvh->num_prims), kBlock, 0, ctx->stream>>>(bvh->sorted_codes, bvh->sorted_ids,
+                                                                           bvh->num_prims, d_codes);
+    GBRT_LAUNCH_CHECK(ctx, "scatter_codes");
+    return GBRT_OK;
+}
+
+// Host conversion of a visionaray index BVH (bvh_node + indices) into the node-pair
+// layout: inner nodes renumbered in depth-first order, each leaf's primitives copied
+// contiguously in leaf order with the last one flagged.
+gbrt_status upload_bvh2(gbrt_context* ctx, gbrt_bvh_node const* nodes, uint32_t num_nodes,
+                        uint32_t const* indices, uint32_t num_indices, gbrt_triangle const* tris,
+                        uint32_t num_tris, gbrt_bvh* bvh)
+{
+    bvh->kind = bvh_kind::uploaded;
+    bvh->num_prims = num_tris;
+    if (num_nodes == 0 || num_tris == 0)
+    {
+        bvh->num_inner = 0;
+        bvh->root = ~0;
+        bvh->num_prims = 0;
+        return GBRT_OK;
+    }
+    std::vector<int32_t> inner_id(num_nodes, -1);
+    std::vector<uint32_t> order;   // reference inner nodes in DFS order
+    std::vector<tri48> out_tris;
+    std::vector<int32_t> leaf_ref(num_nodes, 0);
+    out_tris.reserve(num_indices);
+
+    auto emit_leaf = [&](uint32_t r) -> gbrt_status {
+        gbrt_bvh_node const& nd = nodes[r];
+        if (nd.num_prims == 0) return GBRT_OK;
+        if (uint64_t(nd.first_child_or_prim) + nd.num_prims > num_indices)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: leaf range outside the index list");
+        leaf_ref[r] = ~int32_t(out_tris.size());
+        for (uint32_t k = 0; k < nd.num_prims; ++k)
+        {
+            uint32_t pi = indices[nd.first_child_or_prim + k];
+            if (pi >= num_tris) return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: index outside triangles");
+            gbrt_triangle const& t = tris[pi];
+            tri48 o;
+            uint32_t flags = k + 1 == nd.num_prims ? kLastInLeaf : 0u;
+            o.t0 = make_float4(t.v1[0], t.v1[1], t.v1[2], 0.0f);
+            o.t1 = make_float4(t.e1[0], t.e1[1], t.e1[2], 0.0f);
+            o.t2 = make_float4(t.e2[0], t.e2[1], t.e2[2], 0.0f);
+            memcpy(&o.t0.w, &t.prim_id, 4);
+            memcpy(&o.t1.w, &t.geom_id, 4);
+            memcpy(&o.t2.w, &flags, 4);
+            out_tris.push_back(o);
+        }
+        return GBRT_OK;
+    };
+
+    // depth-first numbering of inner nodes, leaves emitted in visiting order
+    std::vector<std::pair<uint32_t, uint32_t>> st{ { 0u, 1u } };
+    uint32_t height = 0;
+    while (!st.empty())
+    {
+        auto [r, depth] = st.back();
+        st.pop_back();
+        if (r >= num_nodes) return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: child outside the node list");
+        gbrt_bvh_node const& nd = nodes[r];
+        if (nd.num_prims != 0)
+        {
+            gbrt_status e = emit_leaf(r);
+            if (e != GBRT_OK) return e;
+            continue;
+        }
+        if (inner_id[r] >= 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "upload_bvh2: node reached twice");
+        inner_id[r] = int32_t(order.size());
+        order.push_back(r);
+        height = std::max(height, depth);
+        st.push_back({ nd.first_child_or_prim + 1, depth + 1 });
+        st.push_back({ nd.first_child_or_prim + 0, depth + 1 });
+    }
+
+    std::vector<bvh2_node> out_nodes(order.size());
+    for (size_t k = 0; k < order.size(); ++k)
+    {
+        gbrt_bvh_node const& nd = nodes[order[k]];
+        int32_t ch[2];
+        gbrt_bvh_node const* cn[2];
+        for (int s = 0; s < 2; ++s)
+        {
+            uint32_t c = nd.first_child_or_prim + uint32_t(s);
+            cn[s] = &nodes[c];
+            ch[s] = cn[s]->num_prims != 0 ? leaf_ref[c] : inner_id[c];
+        }
+        bvh2_node& o = out_nodes[k];
+        o.xy0 = make_float4(cn[0]->bbox_min[0], cn[0]->bbox_max[0], cn[0]->bbox_min[1], cn[0]->bbox_max[1]);
+        o.xy1 = make_float4(cn[1]->bbox_min[0], cn[1]->bbox_max[0], cn[1]->bbox_min[1], cn[1]->bbox_max[1]);
+        o.z01 = make_float4(cn[0]->bbox_min[2], cn[0]->bbox_max[2], cn[1]->bbox_min[2], cn[1]->bbox_max[2]);
+        o.link = make_int4(ch[0], ch[1], 0, -1);
+    }
+
+    bvh->num_inner = uint32_t(out_nodes.size());
+    bvh->root = nodes[0].num_prims != 0 ? leaf_ref[0] : 0;
+    bvh->height = height;
+    bvh->num_prims = uint32_t(out_tris.size());
+    if (height + 1 > uint32_t(kStackSize))
+        return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "uploaded BVH deeper than the traversal stack");
+    if (!out_nodes.empty())
+    {
+        GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes, out_nodes.size() * sizeof(bvh2_node)));
+        GBRT_CUDA(ctx, cudaMemcpy(bvh->nodes, out_nodes.data(), out_nodes.size() * sizeof(bvh2_node),
+                                  cudaMemcpyHostToDevice));
+    }
+    GBRT_CUDA(ctx, cudaMalloc(&bvh->tris, out_tris.size() * sizeof(tri48)));
+    GBRT_CUDA(ctx, cudaMemcpy(bvh->tris, out_tris.data(), out_tris.size() * sizeof(tri48), cudaMemcpyHostToDevice));
+    return GBRT_OK;
+}
+
+} // namespace gbrt

@@ -1,0 +1,253 @@
+"""Python host side over the C ABI (include/visionaray_gb300/gbrt.h).
+
+Mirrors the reference's interface for the hot path:
+  visionaray                                      here
+  lbvh_builder{}.build(cuda_index_bvh<P>{}, p, n)  lbvh_builder().build(tris)        -> IndexBVH
+  (cuda_index_bvh from a host index_bvh)           IndexBVH.upload(nodes, indices, tris)
+  closest_hit(ray, refs, refs + 1)                 closest_hit(rays, bvh)            -> hits
+  any_hit(ray, refs, refs + 1)                     any_hit(rays, bvh)                -> hits
+Rays/hits are batched (a C ABI cannot take per-ray device functors).  Device buffers
+are torch CUDA tensors used as plain memory; host buffers are numpy arrays.  There is
+no CPU fallback: without libgbrt.so or a GPU every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .types import BVH_NODE, HIT, RAY, TRIANGLE
+
+LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
+
+STATUS = {0: "GBRT_OK", 1: "GBRT_ERR_INVALID_ARG", 2: "GBRT_ERR_OUT_OF_MEMORY", 3: "GBRT_ERR_CUDA",
+          4: "GBRT_ERR_WATCHDOG", 5: "GBRT_ERR_STACK_OVERFLOW", 6: "GBRT_ERR_TOO_LARGE"}
+
+# Every function the C ABI exports, with its ctypes signature (restype, argtypes).
+_vp, _u32, _u64, _i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+_pp = ctypes.POINTER(ctypes.c_void_p)
+SIGNATURES = {
+    "gbrt_abi_version": (_i32, []),
+    "gbrt_context_create": (_i32, [_i32, _vp, _pp]),
+    "gbrt_context_destroy": (_i32, [_vp]),
+    "gbrt_context_set_stream": (_i32, [_vp, _vp]),
+    "gbrt_context_synchronize": (_i32, [_vp]),
+    "gbrt_last_error": (ctypes.c_char_p, [_vp]),
+    "gbrt_kernel_launch_count": (_u64, [_vp]),
+    "gbrt_bvh_build_lbvh": (_i32, [_vp, _vp, _u32, _pp]),
+    "gbrt_bvh_build_lbvh_host": (_i32, [_vp, _vp, _u32, _pp]),
+    "gbrt_bvh_upload_bvh2_host": (_i32, [_vp, _vp, _u32, _vp, _u32, _vp, _u32, _pp]),
+    "gbrt_bvh_destroy": (_i32, [_vp]),
+    "gbrt_bvh_counts": (_i32, [_vp, _vp, _vp, _vp]),
+    "gbrt_bvh_export_bvh2": (_i32, [_vp, _vp, _vp, _vp]),
+    "gbrt_bvh_morton_codes": (_i32, [_vp, _vp, _vp]),
+    "gbrt_trace_closest_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+    "gbrt_trace_any_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+    "gbrt_trace_closest_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+    "gbrt_trace_any_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+}
+
+_lib = None
+
+
+class GbrtError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+def load_library(path=LIBGBRT):
+    """Loads libgbrt.so (no GPU needed to load).  Raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run visionaray_gb300.build.build() "
+                               "(the CUDA path has no fallback)")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype, fn.argtypes = res, args
+        _lib = lib
+    return _lib
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("visionaray_gb300 needs a CUDA GPU (there is no CPU path)")
+    return torch
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _hptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """A gbrt_context bound to one device and (by default) torch's current stream."""
+
+    def __init__(self, device=0, stream=None):
+        torch = _torch()
+        self.lib = load_library()
+        self.device = device
+        if stream is None:
+            stream = torch.cuda.current_stream(device)
+        self.stream = stream
+        h = ctypes.c_void_p()
+        st = self.lib.gbrt_context_create(device, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h))
+        if st != 0:
+            raise GbrtError(st, "gbrt_context_create failed")
+        self.h = h
+
+    def check(self, st):
+        if st != 0:
+            raise GbrtError(st, self.lib.gbrt_last_error(self.h).decode())
+
+    def synchronize(self):
+        self.check(self.lib.gbrt_context_synchronize(self.h))
+
+    @property
+    def launches(self):
+        return int(self.lib.gbrt_kernel_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbrt_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = {}
+
+
+def default_context(device=0):
+    if device not in _default:
+        _default[device] = Context(device)
+    return _default[device]
+
+
+def as_device_bytes(arr, device=0):
+    """numpy structured array -> torch uint8 CUDA tensor holding the same bytes."""
+    torch = _torch()
+    a = np.ascontiguousarray(arr)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1)).to(f"cuda:{device}")
+
+
+def device_rays(rays, device=0):
+    """Rays as an (n, 8) float32 CUDA tensor (16-byte aligned, 32 bytes per ray)."""
+    torch = _torch()
+    a = np.ascontiguousarray(rays)
+    return torch.from_numpy(a.view(np.float32).reshape(-1, 8)).to(f"cuda:{device}")
+
+
+def hits_to_numpy(t):
+    return t.detach().cpu().numpy().reshape(-1).view(HIT)
+
+
+class IndexBVH:
+    """cuda_index_bvh<basic_triangle<3, float>> counterpart: an opaque device BVH."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.h = ctx, handle
+
+    @property
+    def counts(self):
+        p, nn, d = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.gbrt_bvh_counts(self.h, ctypes.byref(p), ctypes.byref(nn), ctypes.byref(d)))
+        return p.value, nn.value, d.value
+
+    @classmethod
+    def upload(cls, nodes, indices, tris, ctx=None):
+        """Host visionaray index_bvh (BVH_NODE nodes, uint32 indices, TRIANGLE prims)."""
+        ctx = ctx or default_context()
+        nodes = np.ascontiguousarray(nodes, BVH_NODE)
+        indices = np.ascontiguousarray(indices, np.uint32)
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.gbrt_bvh_upload_bvh2_host(ctx.h, _hptr(nodes), len(nodes), _hptr(indices), len(indices),
+                                                    _hptr(tris), len(tris), ctypes.byref(h)))
+        return cls(ctx, h)
+
+    def export_bvh2(self):
+        """(nodes, indices) in the reference GPU builder's cuda_index_bvh layout."""
+        torch = _torch()
+        n, nn, _ = self.counts
+        nodes = torch.empty(max(nn, 1) * 32, dtype=torch.uint8, device=f"cuda:{self.ctx.device}")
+        idx = torch.empty(max(n, 1), dtype=torch.int32, device=f"cuda:{self.ctx.device}")
+        self.ctx.check(self.ctx.lib.gbrt_bvh_export_bvh2(self.ctx.h, self.h, _dptr(nodes), _dptr(idx)))
+        self.ctx.synchronize()
+        return (nodes.cpu().numpy()[: nn * 32].view(BVH_NODE),
+                idx.cpu().numpy()[:n].view(np.uint32))
+
+    def morton_codes(self):
+        torch = _torch()
+        n, _, _ = self.counts
+        out = torch.empty(max(n, 1), dtype=torch.int32, device=f"cuda:{self.ctx.device}")
+        self.ctx.check(self.ctx.lib.gbrt_bvh_morton_codes(self.ctx.h, self.h, _dptr(out)))
+        self.ctx.synchronize()
+        return out.cpu().numpy()[:n].view(np.uint32)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbrt_bvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class lbvh_builder:
+    """lbvh_builder (detail/bvh/lbvh.h:473-851), GPU build only."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+
+    def build(self, tris):
+        """tris: torch uint8 CUDA tensor of n*44 bytes (device path) or a numpy
+        TRIANGLE array (host path, copied in)."""
+        ctx = self.ctx
+        h = ctypes.c_void_p()
+        if isinstance(tris, np.ndarray):
+            tris = np.ascontiguousarray(tris, TRIANGLE)
+            ctx.check(ctx.lib.gbrt_bvh_build_lbvh_host(ctx.h, _hptr(tris), len(tris), ctypes.byref(h)))
+        else:
+            n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
+            ctx.check(ctx.lib.gbrt_bvh_build_lbvh(ctx.h, _dptr(tris), n, ctypes.byref(h)))
+        return IndexBVH(ctx, h)
+
+
+def _trace(rays, bvh, out, any_hit):
+    ctx = bvh.ctx
+    lib = ctx.lib
+    if isinstance(rays, np.ndarray):
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = out if out is not None else np.empty(len(rays), HIT)
+        fn = lib.gbrt_trace_any_hit_host if any_hit else lib.gbrt_trace_closest_hit_host
+        ctx.check(fn(ctx.h, bvh.h, _hptr(rays), len(rays), _hptr(hits)))
+        return hits
+    torch = _torch()
+    n = rays.numel() * rays.element_size() // RAY.itemsize
+    hits = out if out is not None else torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+    fn = lib.gbrt_trace_any_hit if any_hit else lib.gbrt_trace_closest_hit
+    ctx.check(fn(ctx.h, bvh.h, _dptr(rays), n, _dptr(hits)))
+    return hits
+
+
+def closest_hit(rays, bvh, out=None):
+    """closest_hit over one BVH for a batch of rays (device tensor or host array)."""
+    return _trace(rays, bvh, out, False)
+
+
+def any_hit(rays, bvh, out=None):
+    """any_hit over one BVH for a batch of rays (device tensor or host array)."""
+    return _trace(rays, bvh, out, True)
