@@ -1,0 +1,165 @@
+// visionaray_gb300.hpp -- header-only C++ shim over the C ABI (gbrt.h) that keeps the
+// shape of visionaray's API for the GPU ray-tracing path, so a visionaray caller
+// changes a namespace and a few types, not its control flow:
+//
+//   visionaray                                          visionaray_gb300
+//   lbvh_builder builder;                               visionaray_gb300::lbvh_builder builder(ctx);
+//   auto bvh = builder.build(cuda_index_bvh<P>{},       auto bvh = builder.build(visionaray_gb300::cuda_index_bvh{},
+//                            d_prims, n);                                        d_prims, n);
+//   (lbvh.h:681-844)
+//   closest_hit(ray, refs, refs + 1)  (per ray,         visionaray_gb300::closest_hit(ctx, bvh, d_rays, n, d_hits)
+//   traverse_linear.inl:192-225)                        (batched: a device functor cannot cross a C ABI)
+//   any_hit(ray, refs, refs + 1)  (:156-189)            visionaray_gb300::any_hit(ctx, bvh, d_rays, n, d_hits)
+//
+// Errors: the reference prints through CUDA_SAFE_CALL (cuda/safe_call.h:18-23) and
+// carries on; the shim throws visionaray_gb300::error carrying the gbrt_status.
+#pragma once
+
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbrt.h"
+
+namespace visionaray_gb300 {
+
+struct error : std::runtime_error
+{
+    gbrt_status status;
+    error(gbrt_status st, std::string const& what) : std::runtime_error(what), status(st) {}
+};
+
+inline void check(gbrt_status st, gbrt_context const* ctx, const char* where)
+{
+    if (st != GBRT_OK)
+        throw error(st, std::string(where) + ": " + (ctx ? gbrt_last_error(ctx) : "invalid argument"));
+}
+
+// One device + one CUDA stream (the stream argument of cuda_sched::frame and the
+// copy stream of lbvh_builder, detail/cuda_sched.h:39, detail/bvh/lbvh.h:669-679).
+class context
+{
+public:
+    explicit context(int device = 0, void* stream = nullptr)
+    {
+        check(gbrt_context_create(device, stream, &h_), nullptr, "gbrt_context_create");
+    }
+    ~context()
+    {
+        if (h_) gbrt_context_destroy(h_);
+    }
+    context(context const&) = delete;
+    context& operator=(context const&) = delete;
+
+    gbrt_context* get() const { return h_; }
+    void synchronize() { check(gbrt_context_synchronize(h_), h_, "gbrt_context_synchronize"); }
+    void set_stream(void* stream) { check(gbrt_context_set_stream(h_, stream), h_, "gbrt_context_set_stream"); }
+    unsigned long long kernel_launches() const { return gbrt_kernel_launch_count(h_); }
+
+private:
+    gbrt_context* h_ = nullptr;
+};
+
+// Owning device BVH over basic_triangle<3, float, unsigned> (bvh.h:1093).  Move-only:
+// the reference's deep copy between host and device trees is the upload below.
+class cuda_index_bvh
+{
+public:
+    cuda_index_bvh() = default;
+    cuda_index_bvh(context& ctx, gbrt_bvh* h) : ctx_(&ctx), h_(h) {}
+    ~cuda_index_bvh() { reset(); }
+    cuda_index_bvh(cuda_index_bvh&& o) noexcept : ctx_(o.ctx_), h_(std::exchange(o.h_, nullptr)) {}
+    cuda_index_bvh& operator=(cuda_index_bvh&& o) noexcept
+    {
+        if (this != &o)
+        {
+            reset();
+            ctx_ = o.ctx_;
+            h_ = std::exchange(o.h_, nullptr);
+        }
+        return *this;
+    }
+    cuda_index_bvh(cuda_index_bvh const&) = delete;
+    cuda_index_bvh& operator=(cuda_index_bvh const&) = delete;
+
+    // Host index_bvh (nodes + index list + primitives) copied to the device
+    // (bvh.h:963-1009).
+    static cuda_index_bvh upload(context& ctx, std::vector<gbrt_bvh_node> const& nodes,
+                                 std::vector<uint32_t> const& indices, gbrt_triangle const* prims, size_t n)
+    {
+        gbrt_bvh* h = nullptr;
+        check(gbrt_bvh_upload_bvh2_host(ctx.get(), nodes.data(), uint32_t(nodes.size()), indices.data(),
+                                        uint32_t(indices.size()), prims, uint32_t(n), &h),
+              ctx.get(), "gbrt_bvh_upload_bvh2_host");
+        return cuda_index_bvh(ctx, h);
+    }
+
+    gbrt_bvh* get() const { return h_; }
+    size_t num_primitives() const
+    {
+        uint32_t n = 0;
+        gbrt_bvh_counts(h_, &n, nullptr, nullptr);
+        return n;
+    }
+    size_t num_nodes() const
+    {
+        uint32_t nn = 0;
+        gbrt_bvh_counts(h_, nullptr, &nn, nullptr);
+        return nn;
+    }
+
+    // The tree in the reference's cuda_index_bvh node layout (device buffers sized
+    // num_nodes() and num_primitives()).
+    void export_nodes(gbrt_bvh_node* d_nodes, uint32_t* d_indices) const
+    {
+        check(gbrt_bvh_export_bvh2(ctx_->get(), h_, d_nodes, d_indices), ctx_->get(), "gbrt_bvh_export_bvh2");
+    }
+
+private:
+    void reset()
+    {
+        if (h_) gbrt_bvh_destroy(h_);
+        h_ = nullptr;
+    }
+    context* ctx_ = nullptr;
+    gbrt_bvh* h_ = nullptr;
+};
+
+// lbvh_builder (detail/bvh/lbvh.h:473-851), GPU build.  P must have the layout of
+// basic_triangle<3, float, unsigned> (44 bytes).
+struct lbvh_builder
+{
+    explicit lbvh_builder(context& ctx) : ctx_(&ctx) {}
+
+    template <typename P>
+    cuda_index_bvh build(cuda_index_bvh /* tag, as the reference's Tree{} */, P const* d_primitives, size_t num_prims)
+    {
+        static_assert(sizeof(P) == sizeof(gbrt_triangle), "P must be laid out as basic_triangle<3, float, unsigned>");
+        if (num_prims > 0xFFFFFFFFu) throw error(GBRT_ERR_TOO_LARGE, "lbvh_builder::build: too many primitives");
+        gbrt_bvh* h = nullptr;
+        check(gbrt_bvh_build_lbvh(ctx_->get(), reinterpret_cast<gbrt_triangle const*>(d_primitives),
+                                  uint32_t(num_prims), &h),
+              ctx_->get(), "gbrt_bvh_build_lbvh");
+        return cuda_index_bvh(*ctx_, h);
+    }
+
+private:
+    context* ctx_;
+};
+
+// Batched closest_hit / any_hit over one BVH (device buffers, asynchronous on the
+// context stream).
+inline void closest_hit(context& ctx, cuda_index_bvh const& bvh, gbrt_ray const* d_rays, size_t n, gbrt_hit* d_hits)
+{
+    check(gbrt_trace_closest_hit(ctx.get(), bvh.get(), d_rays, uint32_t(n), d_hits), ctx.get(),
+          "gbrt_trace_closest_hit");
+}
+
+inline void any_hit(context& ctx, cuda_index_bvh const& bvh, gbrt_ray const* d_rays, size_t n, gbrt_hit* d_hits)
+{
+    check(gbrt_trace_any_hit(ctx.get(), bvh.get(), d_rays, uint32_t(n), d_hits), ctx.get(), "gbrt_trace_any_hit");
+}
+
+} // namespace visionaray_gb300
