@@ -54,11 +54,11 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def workload(rank_print=print):
+def workload(rank_print=print, grid=GRID, origins=ORIGINS):
     from visionaray_gb300 import scenes
     t0 = time.time()
-    tris = scenes.heightfield(grid=GRID, seed=SCENE_SEED)
-    closest, ao = scenes.surface_rays(tris, ORIGINS, seed=RAY_SEED, offset=OFFSET,
+    tris = scenes.heightfield(grid=grid, seed=SCENE_SEED)
+    closest, ao = scenes.surface_rays(tris, origins, seed=RAY_SEED, offset=OFFSET,
                                       ao_per_origin=AO_PER_ORIGIN, ao_tmax=AO_TMAX)
     rank_print(f"# workload generated in {time.time() - t0:.1f} s", file=sys.stderr)
     return tris, closest, ao
@@ -154,7 +154,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    tris, closest, ao = workload()
+    tris, closest, ao = workload(grid=args.grid, origins=args.origins)
     res = cpu_baseline(tris, closest, ao, sample_every=8, repeats=args.warmup + args.steps)
     t = res["times"][args.warmup:]
     ms = 1e3 * statistics.mean(t)
@@ -190,7 +190,7 @@ def run_ours(args):
         if rank == 0:
             print(*a, **k)
 
-    tris, closest, ao = workload(rprint)
+    tris, closest, ao = workload(rprint, grid=args.grid, origins=args.origins)
     n_c, n_a = len(closest), len(ao)
     rays_per_step = n_c + n_a
 
@@ -309,7 +309,9 @@ def run_ours(args):
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
+            "config": {"workload": WORKLOAD if (args.grid, args.origins) == (GRID, ORIGINS) else
+                       f"REDUCED profiling case: heightfield {args.grid}x{args.grid}, {args.origins} origins",
+                       "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
                        "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3)},
             "kernels": per, "roofline": roofline,
@@ -330,6 +332,9 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller cases for profiling captures only; the benchmark is the default size
+    p.add_argument("--grid", type=int, default=GRID)
+    p.add_argument("--origins", type=int, default=ORIGINS)
     args = p.parse_args()
     if args.warmup < 3:
         print("# warmup raised to 3 (timing rule)", file=sys.stderr)
