@@ -148,6 +148,21 @@ gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* 
 gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh,
                                  gbrt_bvh_node* d_nodes, uint32_t* d_indices);
 
+/* LBVH build that allocates no device memory, for callers that cannot allocate:
+ * hosts that own the whole device-memory budget and give a library only its output
+ * buffers, and per-frame rebuild loops where cudaMalloc/cudaFree would synchronise
+ * the device.  No counterpart in visionaray (its builder always allocates,
+ * detail/bvh/lbvh.h:693-834).  Same tree as gbrt_bvh_build_lbvh + gbrt_bvh_export_bvh2:
+ * d_nodes receives 2n-1 nodes, d_indices n indices (device buffers of the caller).
+ * All temporaries live in one fixed device array of this library (about 10 MB, held
+ * by every GPU that loads it until exit), so n is limited to 65,536 triangles
+ * (GBRT_ERR_TOO_LARGE beyond).  Calls share that array: consecutive calls on a stream
+ * are independent, calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address; make it before any stream capture.  Asynchronous on
+ * the context stream.                                                              */
+gbrt_status gbrt_bvh_build_lbvh_noalloc(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n,
+                                        gbrt_bvh_node* d_nodes, uint32_t* d_indices);
+
 /* Writes the 30-bit Morton code of every primitive, in input order, exactly as
  * lbvh::assign_morton_codes computes it (detail/bvh/lbvh.h:242-269).  Only for trees
  * built by gbrt_bvh_build_lbvh.  d_codes holds num_prims entries.                  */

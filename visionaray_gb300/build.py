@@ -24,7 +24,7 @@ REFERENCE_INCLUDE = os.environ.get("VSNRAY_INCLUDE", "/root/reference/include")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "lbvh.cu", "radix_sort.cu", "traverse.cu"]
+CU_SOURCES = ["api.cu", "lbvh.cu", "noalloc.cu", "radix_sort.cu", "traverse.cu"]
 CU_HEADERS = ["common.cuh", "device_math.cuh", "bvh_layout.cuh", "api_internal.h"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")] + ARCH

@@ -80,6 +80,47 @@ gbrt_status upload_bvh2(gbrt_context* ctx, gbrt_bvh_node const* nodes, uint32_t 
                         uint32_t const* indices, uint32_t num_indices, gbrt_triangle const* tris,
                         uint32_t num_tris, gbrt_bvh* bvh);
 
+// Partition of one caller-supplied region holding every buffer of an LBVH build of
+// up to n primitives (offsets in bytes, each 256-byte aligned).  The sort's share
+// mirrors radix_sort_scratch_bytes (4096-key tiles, 256 digits, 4096-entry scan
+// chunks); build_lbvh_in_scratch re-checks it at run time.
+struct lbvh_scratch_layout
+{
+    size_t centroids, keys, vals, keys_alt, vals_alt, leaf_parent, arrivals, nodes, tris, words, sort, total;
+};
+
+constexpr size_t scratch_align(size_t v) { return (v + 255) & ~size_t(255); }
+
+constexpr lbvh_scratch_layout lbvh_scratch_layout_for(uint32_t n)
+{
+    lbvh_scratch_layout l{};
+    size_t o = 0;
+    l.centroids = o;   o = scratch_align(o + size_t(n) * 16);
+    l.keys = o;        o = scratch_align(o + size_t(n) * 4);
+    l.vals = o;        o = scratch_align(o + size_t(n) * 4);
+    l.keys_alt = o;    o = scratch_align(o + size_t(n) * 4);
+    l.vals_alt = o;    o = scratch_align(o + size_t(n) * 4);
+    l.leaf_parent = o; o = scratch_align(o + size_t(n) * 4);
+    l.arrivals = o;    o = scratch_align(o + size_t(n) * 4);
+    l.nodes = o;       o = scratch_align(o + size_t(n) * 64);
+    l.tris = o;        o = scratch_align(o + size_t(n) * 48);
+    l.words = o;       o = scratch_align(o + 8 * 4);
+    l.sort = o;
+    size_t tiles = (size_t(n) + 4095) / 4096;
+    size_t len = 256 * tiles;
+    size_t chunks = (len + 4095) / 4096;
+    o = scratch_align(o + (len + chunks + 64) * 4);
+    l.total = o;
+    return l;
+}
+
+// LBVH build whose every temporary and the node-pair tree live in `scratch`
+// (laid out by lbvh_scratch_layout_for(n)); writes the reference's cuda_index_bvh
+// layout (2n-1 nodes, n indices) to d_nodes / d_indices.  Allocates nothing, does
+// not synchronise; stream-ordered on ctx->stream.
+gbrt_status build_lbvh_in_scratch(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, void* scratch,
+                                  size_t scratch_bytes, gbrt_bvh_node* d_nodes, uint32_t* d_indices);
+
 // radix_sort.cu: stable LSD sort of (key, value) pairs by the low `key_bits` bits.
 // Result lands in (keys, values); keys_alt/values_alt are same-sized scratch.
 size_t radix_sort_scratch_bytes(uint32_t n);

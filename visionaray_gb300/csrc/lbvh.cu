@@ -408,6 +408,16 @@ __global__ void __launch_bounds__(kBlock) scatter_codes(const uint32_t* __restri
     if (j < n) out[sorted_ids[j]] = sorted_codes[j];
 }
 
+// Centroid-bounds words (+FLT_MAX x3, -FLT_MAX x3 as ordered ints) and the root
+// height word, set on the device so a build needs no host-side staging.
+__global__ void init_build_words(int* __restrict__ words)
+{
+    int t = threadIdx.x;
+    if (t < 3) words[t] = float_to_ordered(FLT_MAX);
+    else if (t < 6) words[t] = float_to_ordered(-FLT_MAX);
+    else if (t < 8) words[t] = t == 6 ? 1 : 0;
+}
+
 inline uint32_t blocks_for(uint64_t n) { return uint32_t((n + kBlock - 1) / kBlock); }
 
 inline size_t align_up(size_t v) { return (v + 255) & ~size_t(255); }
@@ -529,6 +539,62 @@ gbrt_status morton_codes_input_order(gbrt_context* ctx, gbrt_bvh const* bvh, uin
     scatter_codes<<<blocks_for(bvh->num_prims), kBlock, 0, ctx->stream>>>(bvh->sorted_codes, bvh->sorted_ids,
                                                                            bvh->num_prims, d_codes);
     GBRT_LAUNCH_CHECK(ctx, "scatter_codes");
+    return GBRT_OK;
+}
+
+gbrt_status build_lbvh_in_scratch(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, void* scratch,
+                                  size_t scratch_bytes, gbrt_bvh_node* d_nodes, uint32_t* d_indices)
+{
+    if (n == 0) return GBRT_OK;
+    const lbvh_scratch_layout l = lbvh_scratch_layout_for(n);
+    if (l.total > scratch_bytes || radix_sort_scratch_bytes(n) > l.total - l.sort)
+        return fail(ctx, GBRT_ERR_TOO_LARGE, "LBVH build: scratch region too small for this many triangles");
+    char* base = static_cast<char*>(scratch);
+    float4* centroids = reinterpret_cast<float4*>(base + l.centroids);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(base + l.keys);
+    uint32_t* vals = reinterpret_cast<uint32_t*>(base + l.vals);
+    uint32_t* keys_alt = reinterpret_cast<uint32_t*>(base + l.keys_alt);
+    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(base + l.vals_alt);
+    int* leaf_parent = reinterpret_cast<int*>(base + l.leaf_parent);
+    uint32_t* arrivals = reinterpret_cast<uint32_t*>(base + l.arrivals);
+    bvh2_node* nodes = reinterpret_cast<bvh2_node*>(base + l.nodes);
+    tri48* tris = reinterpret_cast<tri48*>(base + l.tris);
+    int* words = reinterpret_cast<int*>(base + l.words);
+    uint32_t* root_height = reinterpret_cast<uint32_t*>(words + 6);
+    cudaStream_t s = ctx->stream;
+
+    init_build_words<<<1, 32, 0, s>>>(words);
+    GBRT_LAUNCH_CHECK(ctx, "init_build_words");
+    uint32_t grid = std::min<uint32_t>(blocks_for(n), uint32_t(ctx->num_sms) * 8);
+    centroid_bounds<<<grid, kBlock, 0, s>>>(d_tris, n, centroids, words);
+    GBRT_LAUNCH_CHECK(ctx, "centroid_bounds");
+    morton_codes<<<blocks_for(n), kBlock, 0, s>>>(centroids, n, words, keys, vals);
+    GBRT_LAUNCH_CHECK(ctx, "morton_codes");
+    gbrt_status st = radix_sort_pairs(ctx, keys, vals, keys_alt, vals_alt, n, 30, base + l.sort);
+    if (st != GBRT_OK) return st;
+
+    if (n == 1)
+    {
+        emit_single<<<1, 1, 0, s>>>(d_tris, tris);
+        GBRT_LAUNCH_CHECK(ctx, "emit_single");
+        export_single_leaf<<<1, 1, 0, s>>>(tris, vals, d_nodes, d_indices);
+        GBRT_LAUNCH_CHECK(ctx, "export_single_leaf");
+        return GBRT_OK;
+    }
+    // every call starts from cleared nodes, arrival counters and parent links: the
+    // region keeps whatever the previous build left in it
+    GBRT_CUDA(ctx, cudaMemsetAsync(nodes, 0, size_t(n - 1) * sizeof(bvh2_node), s));
+    GBRT_CUDA(ctx, cudaMemsetAsync(arrivals, 0, size_t(n) * 4, s));
+    GBRT_CUDA(ctx, cudaMemsetAsync(leaf_parent, 0xFF, size_t(n) * 4, s));
+    build_hierarchy<<<blocks_for(n - 1), kBlock, 0, s>>>(keys, int(n), nodes, leaf_parent);
+    GBRT_LAUNCH_CHECK(ctx, "build_hierarchy");
+    refit_and_emit<<<blocks_for(n), kBlock, 0, s>>>(d_tris, vals, int(n), leaf_parent, nodes, arrivals, tris,
+                                                    root_height, ctx->d_status);
+    GBRT_LAUNCH_CHECK(ctx, "refit_and_emit");
+    export_collapse<<<blocks_for(n - 1), kBlock, 0, s>>>(nodes, int(n - 1), vals, d_nodes);
+    GBRT_LAUNCH_CHECK(ctx, "export_collapse");
+    iota<<<blocks_for(n), kBlock, 0, s>>>(d_indices, n);
+    GBRT_LAUNCH_CHECK(ctx, "iota");
     return GBRT_OK;
 }
 

@@ -40,6 +40,7 @@ SIGNATURES = {
     "gbrt_bvh_counts": (_i32, [_vp, _vp, _vp, _vp]),
     "gbrt_bvh_export_bvh2": (_i32, [_vp, _vp, _vp, _vp]),
     "gbrt_bvh_morton_codes": (_i32, [_vp, _vp, _vp]),
+    "gbrt_bvh_build_lbvh_noalloc": (_i32, [_vp, _vp, _u32, _vp, _vp]),
     "gbrt_trace_closest_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_trace_any_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_trace_closest_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
