@@ -193,6 +193,89 @@ gbrt_status gbrt_trace_closest_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
 gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
                                     gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits);
 
+/* ------------------------------------------------------------------------------ */
+/* Path tracing                                                                    */
+
+/* One material per geom_id (materials[geom_id], get_surface.h:158): visionaray's
+ * matte (Lambertian, detail/material/matte.inl; cd = color, kd = scale) or emissive
+ * (detail/material/emissive.inl; ce = color, ls = scale), the two members of the
+ * generic_material the path-tracing configurations use.                           */
+#define GBRT_MATERIAL_MATTE    0u
+#define GBRT_MATERIAL_EMISSIVE 1u
+typedef struct gbrt_material
+{
+    uint32_t kind;
+    float    color[3];
+    float    scale;
+} gbrt_material;
+
+/* area_light<float, basic_triangle<3, float>> (area_light.h, detail/area_light.inl:
+ * 27-53): the emitting triangle and its intensity cl * kl.                         */
+typedef struct gbrt_area_light
+{
+    gbrt_triangle geometry;
+    float         cl[3];
+    float         kl;
+} gbrt_area_light;
+
+/* pinhole_camera after look_at(eye, center, up) and perspective(fovy, w / h, ...)
+ * (pinhole_camera.h, detail/pinhole_camera.inl:87-120).                            */
+typedef struct gbrt_camera
+{
+    float eye[3];
+    float center[3];
+    float up[3];
+    float fovy_degrees;
+} gbrt_camera;
+
+/* One frame of the jittered-blend pixel sampler (pixel_sampler_types.h,
+ * detail/sched_common.h:427-526) around pathtracing::kernel (pathtracing.inl:42-233):
+ * per pixel, spp jittered samples are averaged, then accum = sfactor * average +
+ * dfactor * accum, and color = accum.  Random numbers come from gbrt_rng.h with
+ * (frame_id, pixel = y * width + x, sample).                                      */
+typedef struct gbrt_pt_params
+{
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t num_bounces;    /* kernel_params::num_bounces (kernels.h:66)                */
+    float    epsilon;        /* kernel_params::epsilon: ray-offset distance              */
+    uint32_t frame_id;
+    float    sfactor;
+    float    dfactor;
+    float    background[4];  /* make_kernel_params' bg_color: rgb * w for missed pixels  */
+    float    ambient[3];     /* ambient light seen by rays that leave the scene          */
+    uint32_t flags;          /* GBRT_PT_* bits                                           */
+} gbrt_pt_params;
+
+/* visionaray offsets a shadow ray's origin by epsilon towards the light sample AND ends
+ * it at tmax = distance - epsilon (pathtracing.inl:171-176), so the sampled light
+ * point lies exactly at tmax and the light's own triangle occludes it whenever
+ * rounding lands its hit at or below tmax (about 80% of samples in FP32, 90% in
+ * FP64).  Without this flag the kernel reproduces that behaviour bit for bit; with it
+ * shadow rays end at distance - 2 * epsilon, as the reference evidently intends.     */
+#define GBRT_PT_SHADOW_RANGE_FIX 1u
+
+typedef struct gbrt_pt_scene gbrt_pt_scene;
+
+/* Binds a BVH, its materials (indexed by geom_id) and area lights (host arrays,
+ * copied) into a renderable scene; the BVH must outlive the scene.  Plays the role of
+ * make_kernel_params(prims, materials, lights, ...) (kernels.h:136-188).          */
+gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                 gbrt_material const* h_materials, uint32_t num_materials,
+                                 gbrt_area_light const* h_lights, uint32_t num_lights,
+                                 gbrt_pt_scene** out);
+gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene);
+
+/* Renders one frame: cuda_sched<basic_ray<float>>::frame(pathtracing::kernel{params},
+ * make_sched_params(jittered_blend, cam, rt)) (detail/cuda_sched.inl:226-246) as a
+ * wavefront path tracer.  d_accum and d_color are RGBA32F device images of
+ * width * height pixels (row y at offset y * width); d_color may be NULL.
+ * Asynchronous on the context stream.                                             */
+gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene const* scene,
+                                 gbrt_camera const* camera, gbrt_pt_params const* params,
+                                 float* d_accum, float* d_color);
+
 /* Number of kernels the library launched on this context since creation (the
  * count covers every kernel of every call).                                        */
 uint64_t gbrt_kernel_launch_count(gbrt_context const* ctx);

@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from visionaray_gb300.types import BVH_NODE, HIT
+from visionaray_gb300.types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")
@@ -72,6 +72,7 @@ class Oracle:
         L.orc_trace.argtypes = [_vp, _u32, _vp, _vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.orc_trace.restype = _i32
         L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
+        L.orc_pathtrace.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp, _vp]
         self.L = L
 
     def _tree(self, h):
@@ -133,6 +134,25 @@ class Oracle:
                                 _p(hits))
         return hits
 
+    PT_FLOAT, PT_DOUBLE, PT_FLOAT_TRIG_DOUBLE = 0, 1, 2
+
+    def pathtrace(self, tree, tris, materials, lights, camera, params, mode=1, nthreads=0):
+        """Per-pixel average RGBA (height, width, 4) of one frame, and the counters
+        {closest, shadow, boxes, tris}.  mode: PT_FLOAT (the reference's arithmetic),
+        PT_DOUBLE (the FP64 oracle), PT_FLOAT_TRIG_DOUBLE (the CUDA path's)."""
+        tris = np.ascontiguousarray(tris)
+        materials = np.ascontiguousarray(materials, MATERIAL)
+        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+        params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+        w, h = int(params["width"][0]), int(params["height"][0])
+        out = np.zeros((h, w, 4), np.float64)
+        cnt = np.zeros(4, np.uint64)
+        self.L.orc_pathtrace(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
+                             len(materials), _p(lights), len(lights), _p(camera), _p(params), int(mode), nthreads,
+                             _p(out), _p(cnt))
+        return out, cnt
+
     def intersect_box(self, ray, bmin, bmax):
         ray = np.ascontiguousarray(np.asarray(ray).reshape(1))
         lo = np.ascontiguousarray(bmin, np.float32)
@@ -172,6 +192,7 @@ class Reference:
         L.ref_karras_children.argtypes = [_vp, _u32, _vp, _vp]
         L.ref_trace.argtypes = [_vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.ref_trace.restype = _i32
+        L.ref_pathtrace.argtypes = [_vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _i32]
         self.L = L
 
     class Handle:
@@ -221,3 +242,17 @@ class Reference:
         right = np.empty(max(n - 1, 0), np.int32)
         self.L.ref_karras_children(_p(c), n, _p(left), _p(right))
         return left, right
+
+    def pathtrace(self, tris, materials, lights, camera, params, accum=None, nthreads=0):
+        """visionaray's pathtracing::kernel (its SAH tree), one frame blended into accum
+        (height, width, 4) float32."""
+        tris = np.ascontiguousarray(tris)
+        materials = np.ascontiguousarray(materials, MATERIAL)
+        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+        params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+        w, h = int(params["width"][0]), int(params["height"][0])
+        acc = np.zeros((h, w, 4), np.float32) if accum is None else np.ascontiguousarray(accum, np.float32)
+        self.L.ref_pathtrace(_p(tris), len(tris), _p(materials), len(materials), _p(lights), len(lights),
+                             _p(camera), _p(params), _p(acc), nthreads)
+        return acc

@@ -1,0 +1,424 @@
+// CPU restatement of visionaray's path tracer -- TEST INFRASTRUCTURE ONLY (see
+// oracle.h).  One template, instantiated in float (to pin against the reference's own
+// FP32 kernel at matched random numbers) and in double (the FP64 host oracle the CUDA
+// path is checked against).  Build with -ffp-contract=off.
+//
+// Restates detail/pathtracing.inl:42-233 with, for the materials and lights the
+// configurations use: matte + lambertian (detail/material/matte.inl:40-70,
+// brdf.h:26-84), emissive (detail/material/emissive.inl:20-44), area_light on a
+// triangle (detail/area_light.inl:27-53), sample_random_light (sampling.h:195-213),
+// cosine_sample_hemisphere (sampling.h:117-127), power_heuristic (sampling.h:73-79),
+// sample_surface on a triangle (math/detail/triangle.inl:69-83), get_surface /
+// get_normal / get_area (get_surface.h:129-160, get_normal.h:108-113,
+// get_area.h:92-105), the pinhole camera (detail/pinhole_camera.inl:87-120) and the
+// jittered-blend sampler (detail/sched_common.h:209-233, 427-526).
+
+#include "oracle.h"
+
+#include "../include/visionaray_gb300/gbrt_rng.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+template <typename T>
+struct vec
+{
+    T x, y, z;
+};
+
+template <typename T> inline vec<T> operator+(vec<T> a, vec<T> b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
+template <typename T> inline vec<T> operator-(vec<T> a, vec<T> b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+template <typename T> inline vec<T> operator-(vec<T> a) { return { -a.x, -a.y, -a.z }; }
+template <typename T> inline vec<T> operator*(vec<T> a, vec<T> b) { return { a.x * b.x, a.y * b.y, a.z * b.z }; }
+template <typename T> inline vec<T> operator*(vec<T> a, T s) { return { a.x * s, a.y * s, a.z * s }; }
+template <typename T> inline vec<T> operator*(T s, vec<T> a) { return { s * a.x, s * a.y, s * a.z }; }
+template <typename T> inline vec<T> operator/(vec<T> a, T s) { return { a.x / s, a.y / s, a.z / s }; }
+template <typename T> inline T dot(vec<T> u, vec<T> v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+template <typename T> inline vec<T> cross(vec<T> u, vec<T> v)
+{
+    return { u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x };
+}
+template <typename T> inline T length(vec<T> v) { return std::sqrt(dot(v, v)); }
+// normalize(v) = v * rsqrt(dot(v, v)), rsqrt(x) = 1 / sqrt(x) on the host
+// (math/detail/vector3.inl:332-335, math/detail/math.h:596-599)
+template <typename T> inline vec<T> normalize(vec<T> v) { return v * (T(1.0) / std::sqrt(dot(v, v))); }
+template <typename T> inline vec<T> faceforward(vec<T> n, vec<T> i, vec<T> nref)
+{
+    return dot(nref, i) < T(0.0) ? -n : n;   // math/detail/vector.inl:677-685
+}
+template <typename T> inline T max_element(vec<T> v)
+{
+    T m = v.x < v.y ? v.y : v.x;
+    return m < v.z ? v.z : m;
+}
+template <typename T> inline T power_heuristic(T p1, T p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
+
+template <typename T> inline vec<T> load(const float* p) { return { T(p[0]), T(p[1]), T(p[2]) }; }
+
+template <typename T>
+struct tri_t
+{
+    vec<T> v1, e1, e2;
+    uint32_t prim_id, geom_id;
+};
+
+template <typename T> inline tri_t<T> load_tri(gbrt_triangle const& t)
+{
+    return { load<T>(t.v1), load<T>(t.e1), load<T>(t.e2), t.prim_id, t.geom_id };
+}
+
+template <typename T>
+struct hit_t
+{
+    bool hit = false;
+    T t = T(FLT_MAX);
+    uint32_t index = 0;   // primitive list index (position in the index list)
+};
+
+// math/intersect.h:176-229 in T
+template <typename T>
+inline bool intersect(vec<T> ori, vec<T> dir, tri_t<T> const& tri, T& t_out)
+{
+    vec<T> s1 = cross(dir, tri.e2);
+    T div = dot(s1, tri.e1);
+    if (!(div != T(0.0))) return false;
+    T inv_div = T(1.0) / div;
+    vec<T> d = ori - tri.v1;
+    T b1 = dot(d, s1) * inv_div;
+    if (!(b1 >= T(0.0) && b1 <= T(1.0))) return false;
+    vec<T> s2 = cross(d, tri.e1);
+    T b2 = dot(dir, s2) * inv_div;
+    if (!(b2 >= T(0.0) && b1 + b2 <= T(1.0))) return false;
+    t_out = dot(tri.e2, s2) * inv_div;
+    return true;
+}
+
+template <typename T> inline T tmin_(T a, T b) { return a < b ? a : b; }
+template <typename T> inline T tmax_(T a, T b) { return a < b ? b : a; }
+
+struct scene_arrays
+{
+    const gbrt_triangle* tris;
+    const gbrt_bvh_node* nodes;
+    uint32_t num_nodes;
+    const uint32_t* indices;
+};
+
+// detail/bvh/intersect.inl:51-165 (scalar ray, ordered by split axis and sign) in T.
+template <typename T>
+hit_t<T> traverse(scene_arrays const& s, vec<T> ori, vec<T> dir, T tmin, T tmax, bool any_hit, uint64_t& nbox,
+                  uint64_t& ntri)
+{
+    hit_t<T> best;
+    if (s.num_nodes == 0) return best;
+    vec<T> inv = { dir.x != T(0) ? T(1) / dir.x : T(FLT_MAX), dir.y != T(0) ? T(1) / dir.y : T(FLT_MAX),
+                   dir.z != T(0) ? T(1) / dir.z : T(FLT_MAX) };
+    uint32_t st[64];
+    int sp = 0;
+    st[sp++] = 0;
+    while (sp > 0)
+    {
+        gbrt_bvh_node const* nd = &s.nodes[st[--sp]];
+        bool leaf = false;
+        while (true)
+        {
+            vec<T> lo = load<T>(nd->bbox_min), hi = load<T>(nd->bbox_max);
+            vec<T> t1 = (lo - ori) * inv, t2 = (hi - ori) * inv;
+            T tn = tmax_(tmin_(t1.x, t2.x), tmax_(tmin_(t1.y, t2.y), tmin_(t1.z, t2.z)));
+            T tf = tmin_(tmax_(t1.x, t2.x), tmin_(tmax_(t1.y, t2.y), tmax_(t1.z, t2.z)));
+            ++nbox;
+            if (!(tf >= tn && tn < best.t && tf >= tmin && tn <= tmax)) break;
+            if (nd->num_prims != 0)
+            {
+                leaf = true;
+                break;
+            }
+            T dc = nd->ordered_traversal_axis == 0 ? dir.x : (nd->ordered_traversal_axis == 1 ? dir.y : dir.z);
+            float dcf = float(dc);
+            uint32_t bits;
+            std::memcpy(&bits, &dcf, 4);
+            int32_t sign_rd = int32_t(bits) >> 31;
+            uint32_t near_addr = (int32_t(nd->ordered_traversal_sign) ^ sign_rd) != 0 ? 1u : 0u;
+            if (sp < 64) st[sp++] = nd->first_child_or_prim + (near_addr ? 0u : 1u);
+            nd = &s.nodes[nd->first_child_or_prim + near_addr];
+        }
+        if (!leaf) continue;
+        for (uint32_t i = nd->first_child_or_prim; i != nd->first_child_or_prim + nd->num_prims; ++i)
+        {
+            T t;
+            ++ntri;
+            if (!intersect(ori, dir, load_tri<T>(s.tris[s.indices[i]]), t)) continue;
+            if (!(t < best.t && t >= tmin && t <= tmax)) continue;
+            best.hit = true;
+            best.t = t;
+            best.index = i;
+            if (any_hit) return best;
+        }
+    }
+    return best;
+}
+
+struct pt_counters
+{
+    uint64_t closest = 0, shadow = 0, boxes = 0, tris = 0;
+};
+
+// pathtracing::kernel::operator() (detail/pathtracing.inl:42-233) for one camera ray.
+template <typename T>
+inline T trig_cos(T x, bool via_double) { return via_double ? T(std::cos(double(x))) : std::cos(x); }
+template <typename T>
+inline T trig_sin(T x, bool via_double) { return via_double ? T(std::sin(double(x))) : std::sin(x); }
+
+template <typename T>
+vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+                uint32_t nl, gbrt_pt_params const& p, vec<T> ori, vec<T> dir, T tmin, T tmax,
+                gbrt_sample_generator& gen, bool& first_hit, pt_counters& cnt, bool trig_double)
+{
+    const T inv_pi = T(3.18309886183790691216444201928e-01);
+    const T pi = T(3.14159265358979323846264338328e+00);
+    const T two_pi = T(6.28318530717958623199592693709e+00);
+    const T eps = T(p.epsilon);
+    vec<T> intensity = { 0, 0, 0 };
+    vec<T> throughput = { 1, 1, 1 };
+    bool active = true;
+    bool last_specular = true;
+    const vec<T> ambient = { T(p.ambient[0]), T(p.ambient[1]), T(p.ambient[2]) };
+    first_hit = false;
+
+    for (uint32_t bounce = 0; bounce < p.num_bounces; ++bounce)
+    {
+        hit_t<T> hr = traverse(s, ori, dir, tmin, tmax, false, cnt.boxes, cnt.tris);
+        ++cnt.closest;
+        if (active && !hr.hit) intensity = intensity + ambient * throughput;
+        active = active && hr.hit;
+        if (!active) break;
+        if (bounce == 0) first_hit = true;
+
+        tri_t<T> tri = load_tri<T>(s.tris[s.indices[hr.index]]);
+        vec<T> view_dir = -dir;
+        vec<T> isect = ori + dir * hr.t;
+        vec<T> gn = normalize(cross(tri.e1, tri.e2));
+        vec<T> sn = gn;
+        gbrt_material m = tri.geom_id < nmat ? mats[tri.geom_id] : gbrt_material{ GBRT_MATERIAL_MATTE, { 0, 0, 0 }, 0 };
+        vec<T> mcol = { T(m.color[0]), T(m.color[1]), T(m.color[2]) };
+        bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+
+        // surf.sample(view_dir, refl_dir, brdf_pdf, inter, gen)
+        vec<T> refl = { 0, 0, 0 };
+        T brdf_pdf;
+        vec<T> src;
+        if (!emission)
+        {
+            vec<T> n = faceforward(sn, view_dir, gn);
+            vec<T> w = n;
+            vec<T> v = std::abs(w.x) > std::abs(w.y) ? normalize(vec<T>{ -w.z, T(0), w.x })
+                                                     : normalize(vec<T>{ T(0), w.z, -w.y });
+            vec<T> u = cross(v, w);
+            // cosine_sample_hemisphere(gen.next(), gen.next()): the reference build
+            // evaluates the second argument first
+            T u2 = T(gen.next());
+            T u1 = T(gen.next());
+            T r = std::sqrt(u1);
+            T theta = two_pi * u2;
+            vec<T> sp = { r * trig_cos(theta, trig_double), r * trig_sin(theta, trig_double),
+                          std::sqrt(T(1.0) - u1) };
+            refl = normalize(u * sp.x + v * sp.y + w * sp.z);
+            brdf_pdf = dot(n, refl) * inv_pi;
+            src = (mcol * T(m.scale)) * inv_pi;
+        }
+        else
+        {
+            brdf_pdf = T(1.0);
+            src = mcol * T(m.scale);
+        }
+        bool zero_pdf = brdf_pdf <= T(0.0);
+
+        T light_pdf = T(0.0);
+        if (nl > 0 && emission)
+        {
+            T A = T(0.5) * length(cross(tri.e1, tri.e2));
+            T ld = length(isect - ori);
+            vec<T> L = normalize(isect - ori);
+            T ldotln = std::abs(dot(-L, gn));
+            T solid_angle = (ldotln * A) / (ld * ld);
+            light_pdf = T(1.0) / solid_angle;
+        }
+        T mis = (bounce > 0 && nl > 0 && !last_specular) ? power_heuristic(brdf_pdf, light_pdf / T(float(nl)))
+                                                          : T(1.0);
+        if (active && emission) intensity = intensity + (throughput * mis) * src;
+        active = active && !emission && !zero_pdf;
+
+        vec<T> n = faceforward(sn, view_dir, gn);
+        if (nl > 0)
+        {
+            // sample_random_light + area_light::sample + sample_surface
+            T ul = T(gen.next());
+            int light_id = static_cast<int>(float(ul) * float(nl));
+            if (light_id >= int(nl)) light_id = int(nl) - 1;
+            tri_t<T> lt = load_tri<T>(lights[light_id].geometry);
+            T s1 = T(gen.next());
+            T s2 = T(gen.next());
+            vec<T> lv1 = lt.v1, lv2 = lt.v1 + lt.e1, lv3 = lt.v1 + lt.e2;
+            T sq = std::sqrt(s1);
+            vec<T> pos = lv1 * (T(1.0) - sq) + lv2 * sq * (T(1.0) - s2) + lv3 * sq * s2;
+            vec<T> ldir = pos - isect;
+            T dist = length(ldir);
+            vec<T> lint = { T(lights[light_id].cl[0]) * T(lights[light_id].kl),
+                            T(lights[light_id].cl[1]) * T(lights[light_id].kl),
+                            T(lights[light_id].cl[2]) * T(lights[light_id].kl) };
+            vec<T> lnormal = normalize(cross(lt.e1, lt.e2));
+            T larea = T(0.5) * length(cross(lt.e1, lt.e2));
+            T ldotln0 = std::abs(dot(-normalize(ldir), lnormal));
+            T solid_angle = (ldotln0 * larea) / (dist * dist);
+            T lpdf = T(1.0) / solid_angle;
+
+            vec<T> L = normalize(ldir);
+            vec<T> ln = faceforward(lnormal, -L, lnormal);
+            T ldotn = dot(L, n);
+            T ldotln = std::abs(dot(-L, ln));
+            // shadow ray (pathtracing.inl:171-176); GBRT_PT_SHADOW_RANGE_FIX ends it one
+            // more epsilon before the light sample
+            T shadow_tmax = (p.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - eps - eps : dist - eps;
+            hit_t<T> sh = traverse(s, isect + L * eps, L, eps, shadow_tmax, true, cnt.boxes, cnt.tris);
+            ++cnt.shadow;
+            if (!emission)
+            {
+                vec<T> n2 = faceforward(sn, view_dir, gn);
+                T bpdf = dot(n2, L) * inv_pi;
+                T prob = max_element(throughput);
+                bpdf = bpdf * prob;
+                T ndotl = std::max(T(0.0), dot(n2, L));
+                vec<T> cd = (mcol * T(m.scale)) * inv_pi;
+                vec<T> shade = ((cd * pi) * lint) * ndotl;
+                vec<T> src2 = (shade * inv_pi) / ldotn;
+                T mis2 = power_heuristic(lpdf / T(float(nl)), bpdf);
+                if (active && !sh.hit && ldotn > T(0.0) && ldotln > T(0.0))
+                    intensity = intensity + (((throughput * mis2) * src2) * (ldotn / lpdf)) * T(float(nl));
+            }
+        }
+
+        throughput = throughput * (src * (dot(n, refl) / brdf_pdf));
+        if (zero_pdf) throughput = { 0, 0, 0 };
+
+        if (bounce >= 2)
+        {
+            T prob = max_element(throughput);
+            bool terminate = T(gen.next()) > prob;
+            active = active && !terminate;
+            throughput = throughput / prob;
+            if (!active) break;
+        }
+        if (!active) break;   // emission / zero pdf: nothing further reaches the image
+        ori = isect + refl * eps;
+        dir = refl;
+        last_specular = false;
+    }
+    return intensity;
+}
+
+template <typename T>
+void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+            uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, int nthreads, double* out,
+            pt_counters& total, bool trig_double)
+{
+    // pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) in T
+    vec<T> eye = load<T>(cam.eye), center = load<T>(cam.center), up = load<T>(cam.up);
+    vec<T> f = normalize(eye - center);
+    vec<T> sv = normalize(cross(up, f));
+    vec<T> uv = cross(f, sv);
+    T fovy = T(cam.fovy_degrees) * T(1.74532925199432957692369076849e-02);
+    T aspect = T(p.width) / T(p.height);
+    T th = std::tan(fovy / T(2.0));
+    vec<T> U = sv * th * aspect;
+    vec<T> V = uv * th;
+    vec<T> W = -f;
+
+    uint64_t npix = uint64_t(p.width) * p.height;
+    if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<uint64_t> next{ 0 };
+    std::vector<pt_counters> per(static_cast<size_t>(nthreads));
+    auto worker = [&](int tid) {
+        for (;;)
+        {
+            uint64_t b = next.fetch_add(64);
+            if (b >= npix) break;
+            for (uint64_t pix = b; pix < std::min(npix, b + 64); ++pix)
+            {
+                T x = T(pix % p.width), y = T(pix / p.width);
+                vec<T> sum = { 0, 0, 0 };
+                T alpha = 0;
+                for (uint32_t smp = 0; smp < p.spp; ++smp)
+                {
+                    gbrt_sample_generator gen{ p.frame_id, uint32_t(pix), smp, 0u };
+                    T jx = T(gen.next() - 0.5f);
+                    T jy = T(gen.next() - 0.5f);
+                    // pinhole_camera::primary_ray (detail/pinhole_camera.inl:103-120)
+                    T sx = (x + jx + T(0.5)) / T(p.width);
+                    T sy = (y + jy + T(0.5)) / T(p.height);
+                    T u = T(2.0) * sx - T(1.0);
+                    T v = T(2.0) * sy - T(1.0);
+                    vec<T> d = normalize(U * u + V * v + W);
+                    bool hit = false;
+                    vec<T> c = radiance<T>(s, mats, nmat, lights, nl, p, eye, d, T(0.0), T(FLT_MAX), gen, hit,
+                                           per[size_t(tid)], trig_double);
+                    if (hit)
+                    {
+                        sum = sum + c;
+                        alpha = alpha + T(1.0);
+                    }
+                    else
+                    {
+                        vec<T> bg = { T(p.background[0]) * T(p.background[3]), T(p.background[1]) * T(p.background[3]),
+                                      T(p.background[2]) * T(p.background[3]) };
+                        sum = sum + bg;
+                        alpha = alpha + T(1.0);
+                    }
+                }
+                T inv = T(float(p.spp));
+                out[4 * pix + 0] = double(sum.x / inv);
+                out[4 * pix + 1] = double(sum.y / inv);
+                out[4 * pix + 2] = double(sum.z / inv);
+                out[4 * pix + 3] = double(alpha / inv);
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
+    for (auto& th : pool) th.join();
+    for (auto const& c : per)
+    {
+        total.closest += c.closest;
+        total.shadow += c.shadow;
+        total.boxes += c.boxes;
+        total.tris += c.tris;
+    }
+}
+
+} // namespace
+
+extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
+                              const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
+                              const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                              const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba, uint64_t* counters)
+{
+    scene_arrays s{ tris, nodes, num_nodes, indices };
+    pt_counters c;
+    if (mode == 1)
+        render<double>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, false);
+    else
+        render<float>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, mode == 2);
+    if (counters)
+    {
+        counters[0] = c.closest;
+        counters[1] = c.shadow;
+        counters[2] = c.boxes;
+        counters[3] = c.tris;
+    }
+}

@@ -15,11 +15,17 @@
 #include <thread>
 #include <vector>
 
+#include <visionaray/area_light.h>
 #include <visionaray/bvh.h>
+#include <visionaray/generic_material.h>
+#include <visionaray/kernels.h>
+#include <visionaray/material.h>
 #include <visionaray/math/math.h>
+#include <visionaray/pinhole_camera.h>
 #include <visionaray/traverse.h>
 #include <visionaray/detail/bvh/statistics.h>
 
+#include "../include/visionaray_gb300/gbrt_rng.h"
 #include "oracle.h"
 
 using namespace visionaray;
@@ -186,6 +192,106 @@ int ref_trace(void* h, const gbrt_ray* rays, uint64_t nrays, int any_hit_flag, i
         counters[1] = ntri.load();
     }
     return 0;
+}
+
+// visionaray's pathtracing::kernel (detail/pathtracing.inl:42-233) over a binned-SAH
+// index_bvh, generic_material<matte, emissive> per geom_id and triangle area lights,
+// driven per (pixel, sample) by the gbrt_rng.h stream: the jittered primary ray
+// (sched_common.h:209-233, jitter x drawn before y) through visionaray's own
+// pinhole_camera, samples averaged and blended into accum as sample_pixel_impl does
+// (sched_common.h:427-526).  accum is RGBA32F, read and written.
+void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
+                   const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam, const gbrt_pt_params* p,
+                   float* accum, int nthreads)
+{
+    using mat_t = generic_material<matte<float>, emissive<float>>;
+    using light_t = area_light<float, triangle_t>;
+    auto prims = to_prims(tris, n);
+    binned_sah_builder builder;
+    auto tree = builder.build(index_bvh<triangle_t>{}, prims.data(), prims.size());
+    std::vector<decltype(tree.ref())> refs{ tree.ref() };
+
+    std::vector<mat_t> materials(nmat);
+    for (uint32_t i = 0; i < nmat; ++i)
+    {
+        vec3 c(mats[i].color[0], mats[i].color[1], mats[i].color[2]);
+        if (mats[i].kind == GBRT_MATERIAL_EMISSIVE)
+        {
+            emissive<float> e;
+            e.ce() = from_rgb(c);
+            e.ls() = mats[i].scale;
+            materials[i] = e;
+        }
+        else
+        {
+            matte<float> m;
+            m.ca() = from_rgb(vec3(0.0f));
+            m.ka() = 0.0f;
+            m.cd() = from_rgb(c);
+            m.kd() = mats[i].scale;
+            materials[i] = m;
+        }
+    }
+    std::vector<light_t> al;
+    for (uint32_t i = 0; i < nl; ++i)
+    {
+        triangle_t g;
+        std::memcpy(&g, &lights[i].geometry, sizeof(g));
+        light_t l(g);
+        l.set_cl(vec3(lights[i].cl[0], lights[i].cl[1], lights[i].cl[2]));
+        l.set_kl(lights[i].kl);
+        al.push_back(l);
+    }
+    auto kp = make_kernel_params(refs.data(), refs.data() + 1, materials.data(), al.data(), al.data() + al.size(),
+                                 p->num_bounces, p->epsilon,
+                                 vec4(p->background[0], p->background[1], p->background[2], p->background[3]),
+                                 vec4(p->ambient[0], p->ambient[1], p->ambient[2], 1.0f));
+    pathtracing::kernel<decltype(kp)> kernel;
+    kernel.params = kp;
+
+    pinhole_camera c;
+    float fovy = cam->fovy_degrees * constants::degrees_to_radians<float>();
+    c.perspective(fovy, float(p->width) / float(p->height), 0.001f, 1000.0f);
+    c.look_at(vec3(cam->eye[0], cam->eye[1], cam->eye[2]), vec3(cam->center[0], cam->center[1], cam->center[2]),
+              vec3(cam->up[0], cam->up[1], cam->up[2]));
+    c.begin_frame();
+
+    uint64_t npix = uint64_t(p->width) * p->height;
+    if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<uint64_t> next{ 0 };
+    auto worker = [&]() {
+        for (;;)
+        {
+            uint64_t b = next.fetch_add(64);
+            if (b >= npix) break;
+            for (uint64_t pix = b; pix < std::min(npix, b + 64); ++pix)
+            {
+                int x = int(pix % p->width), y = int(pix / p->width);
+                vec4 sum(0.0f);
+                for (uint32_t s = 0; s < p->spp; ++s)
+                {
+                    gbrt_sample_generator gen{ p->frame_id, uint32_t(pix), s, 0u };
+                    float jx = gen.next() - 0.5f;
+                    float jy = gen.next() - 0.5f;
+                    auto r = c.primary_ray(basic_ray<float>{}, float(x) + jx, float(y) + jy, float(p->width),
+                                           float(p->height));
+                    auto res = kernel(r, gen);
+                    sum += res.color;
+                }
+                sum /= float(p->spp);
+                float* a = accum + 4 * pix;
+                vec4 dst(a[0], a[1], a[2], a[3]);
+                vec4 out = sum * p->sfactor + dst * p->dfactor;
+                a[0] = out.x;
+                a[1] = out.y;
+                a[2] = out.z;
+                a[3] = out.w;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
 }
 
 } // extern "C"

@@ -11,13 +11,29 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include", "visionaray_gb300")
 
 
+def strip_bodies(text):
+    """Drops every {...} block (function bodies, struct bodies, extern "C" braces
+    excepted by keeping their contents) so that only top-level declarations remain."""
+    out, depth, i = [], 0, 0
+    text = text.replace('extern "C" {', "").replace("} /* extern \"C\" */", "")
+    for ch in text:
+        if ch == "{":
+            depth += 1
+        elif ch == "}":
+            depth = max(0, depth - 1)
+        elif depth == 0:
+            out.append(ch)
+    return "".join(out)
+
+
 def declared_functions():
     names = set()
     for fn in os.listdir(INCLUDE):
         if fn.endswith(".h"):
             text = open(os.path.join(INCLUDE, fn)).read()
-            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-            names |= set(re.findall(r"\b(gbrt_[a-z0-9_]+)\s*\(", text))
+            text = strip_bodies(re.sub(r"/\*.*?\*/", "", text, flags=re.S))
+            # prototypes only (a declaration ends in ';'); inline helpers are not exports
+            names |= set(re.findall(r"\b(gbrt_[a-z0-9_]+)\s*\([^;{}]*\)\s*;", text))
     return names
 
 

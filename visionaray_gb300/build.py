@@ -24,10 +24,16 @@ REFERENCE_INCLUDE = os.environ.get("VSNRAY_INCLUDE", "/root/reference/include")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "lbvh.cu", "noalloc.cu", "radix_sort.cu", "traverse.cu"]
-CU_HEADERS = ["common.cuh", "device_math.cuh", "bvh_layout.cuh", "api_internal.h"]
+CU_SOURCES = ["api.cu", "lbvh.cu", "noalloc.cu", "pathtrace.cu", "radix_sort.cu", "traverse.cu"]
+CU_HEADERS = ["device_math.cuh", "bvh_layout.cuh", "api_internal.h", "traverse_core.cuh"]
+# host code of every unit keeps expressions unfused (-ffp-contract=off) so x86-64 and
+# AArch64 hosts compute the same camera bases and copies
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-              "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")] + ARCH
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+              "-I" + os.path.join(ROOT, "include")] + ARCH
+# the path tracer's shading repeats the reference's float expressions operation for
+# operation: no fused multiply-add anywhere in its device code
+PER_FILE_FLAGS = {"pathtrace.cu": ["--fmad=false"]}
 
 LIBGBRT = os.path.join(LIB, "libgbrt.so")
 LIBSCENES = os.path.join(LIB, "libgbrt_scenes.so")
@@ -59,7 +65,7 @@ def build(verbose=False, with_reference=True):
     os.makedirs(LIB, exist_ok=True)
     os.makedirs(os.path.join(LIB, "obj"), exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in CU_HEADERS] + [
-        os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h")]
+        os.path.join(ROOT, "include", "visionaray_gb300", h) for h in ("gbrt.h", "gbrt_rng.h")]
 
     jobs = []
     objs = []
@@ -68,17 +74,20 @@ def build(verbose=False, with_reference=True):
         o = os.path.join(LIB, "obj", src.replace(".cu", ".o"))
         objs.append(o)
         if _stale(o, [s] + headers):
-            jobs.append((src, [NVCC] + NVCC_FLAGS + ["-c", s, "-o", o]))
+            jobs.append((src, [NVCC] + NVCC_FLAGS + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o]))
     scenes_src = os.path.join(CSRC, "scenes.cpp")
     if _stale(LIBSCENES, [scenes_src, os.path.join(CSRC, "scenes.h")]):
         jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
                                 "-ffp-contract=off", "-Wall", scenes_src, "-o", LIBSCENES]))
     # the oracle flags are those of oracle/Makefile (kept for manual builds)
     oracle_flags = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"]
-    oracle_deps = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "oracle.h")]
+    oracle_srcs = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "pathtrace.cpp")]
+    oracle_deps = oracle_srcs + [os.path.join(ORACLE, "oracle.h"),
+                                 os.path.join(ROOT, "include", "visionaray_gb300", "gbrt_rng.h"),
+                                 os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h")]
     if _stale(LIBORACLE, oracle_deps):
         os.makedirs(os.path.dirname(LIBORACLE), exist_ok=True)
-        jobs.append(("oracle", oracle_flags + ["-o", LIBORACLE, os.path.join(ORACLE, "oracle.cpp"), "-lpthread"]))
+        jobs.append(("oracle", oracle_flags + ["-o", LIBORACLE] + oracle_srcs + ["-lpthread"]))
     have_ref = with_reference and os.path.isdir(os.path.join(REFERENCE_INCLUDE, "visionaray"))
     ref_src = os.path.join(ORACLE, "ref_driver.cpp")
     if have_ref and _stale(LIBREF, oracle_deps + [ref_src]):

@@ -40,20 +40,6 @@ gbrt_status ensure_scratch(gbrt_context* ctx, size_t bytes)
 
 namespace {
 
-struct device_guard
-{
-    int prev = -1;
-    explicit device_guard(int dev)
-    {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~device_guard()
-    {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 void free_bvh_arrays(gbrt_bvh* b)
@@ -181,6 +167,7 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
             cudaFree(ctx->slot_hits[k]);
         }
         cudaFree(ctx->scratch);
+        cudaFree(ctx->pt_scratch);
         cudaFree(ctx->d_status);
     }
     delete ctx;

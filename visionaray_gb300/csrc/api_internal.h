@@ -39,6 +39,10 @@ struct gbrt_context
     void* slot_rays[kSlots] = { nullptr, nullptr };
     void* slot_hits[kSlots] = { nullptr, nullptr };
     size_t slot_capacity = 0;   // rays per slot
+
+    // Path-tracer wavefront state (grown on demand, freed with the context).
+    void* pt_scratch = nullptr;
+    size_t pt_scratch_bytes = 0;
 };
 
 enum class bvh_kind
@@ -63,6 +67,21 @@ struct gbrt_bvh
 };
 
 namespace gbrt {
+
+// Makes `dev` current for the guard's lifetime.
+struct device_guard
+{
+    int prev = -1;
+    explicit device_guard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~device_guard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 // Sets ctx->last_error and returns `st`.
 gbrt_status fail(gbrt_context* ctx, gbrt_status st, std::string const& what);

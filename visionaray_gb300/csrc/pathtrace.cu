@@ -1,0 +1,645 @@
+// Wavefront path tracer: cuda_sched<basic_ray<float>>::frame(pathtracing::kernel{params},
+// jittered-blend sampler) of visionaray (detail/cuda_sched.inl:32-69, 226-246,
+// detail/pathtracing.inl:42-233) re-designed for the GPU.
+//
+// visionaray runs the whole path (all bounces, its traversal, shading and shadow
+// ray) in one thread per pixel; threads of a warp diverge as soon as paths end at
+// different bounces or traverse different subtrees.  Here a frame is a sequence of
+// passes, one per sample index; each pass keeps one path per pixel and advances all
+// live paths one bounce at a time through three kernels:
+//   extend : closest-hit traversal of the live rays (queue in, hits out)
+//   shade  : surface sampling, emission with MIS, next-event estimation (light
+//            sample + shadow ray), throughput update, Russian roulette; live paths
+//            and shadow rays are appended to compacted queues with one atomic per
+//            warp (ballot + popc)
+//   shadow : any-hit traversal of the shadow queue, unoccluded contributions added
+// so every traversal launch runs over a dense queue of live rays.  The arithmetic is
+// the reference's, operation for operation (this file is compiled with
+// --fmad=false; divisions and square roots are IEEE), and the random numbers are
+// the gbrt_rng.h stream, so a path can be replayed on the CPU bit for bit; the one
+// deliberate difference is the hemisphere sample's cos/sin, evaluated in double and
+// rounded once (the host's cosf/sinf may differ from that in the last bit).
+
+#include "traverse_core.cuh"
+
+#include "../../include/visionaray_gb300/gbrt_rng.h"
+
+#include <cmath>
+#include <vector>
+
+struct gbrt_pt_scene
+{
+    gbrt_bvh const* bvh = nullptr;
+    int device = 0;
+    gbrt_material* materials = nullptr;
+    uint32_t num_materials = 0;
+    float4* lights = nullptr;   // 4 float4 per light: v1, e1, e2, intensity (cl * kl)
+    uint32_t num_lights = 0;
+};
+
+namespace gbrt {
+namespace {
+
+constexpr int kBlock = 128;
+constexpr uint32_t kLastSpecular = 1u;
+constexpr uint32_t kFirstHit = 2u;
+
+struct v3
+{
+    float x, y, z;
+};
+__device__ __forceinline__ v3 operator+(v3 a, v3 b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
+__device__ __forceinline__ v3 operator-(v3 a, v3 b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+__device__ __forceinline__ v3 operator-(v3 a) { return { -a.x, -a.y, -a.z }; }
+__device__ __forceinline__ v3 operator*(v3 a, v3 b) { return { a.x * b.x, a.y * b.y, a.z * b.z }; }
+__device__ __forceinline__ v3 operator*(v3 a, float s) { return { a.x * s, a.y * s, a.z * s }; }
+__device__ __forceinline__ v3 operator/(v3 a, float s) { return { a.x / s, a.y / s, a.z / s }; }
+__device__ __forceinline__ float dot3(v3 u, v3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+__device__ __forceinline__ v3 cross3(v3 u, v3 v)
+{
+    return { u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x };
+}
+__device__ __forceinline__ float length3(v3 v) { return sqrtf(dot3(v, v)); }
+// normalize(v) = v * (1 / sqrt(dot(v, v))) (math/detail/vector3.inl:332-335)
+__device__ __forceinline__ v3 normalize3(v3 v) { return v * (1.0f / sqrtf(dot3(v, v))); }
+__device__ __forceinline__ v3 faceforward3(v3 n, v3 i, v3 nref) { return dot3(nref, i) < 0.0f ? -n : n; }
+__device__ __forceinline__ float max_elem(v3 v)
+{
+    float m = v.x < v.y ? v.y : v.x;
+    return m < v.z ? v.z : m;
+}
+__device__ __forceinline__ float power_heuristic(float p1, float p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
+__device__ __forceinline__ v3 xyz(float4 a) { return { a.x, a.y, a.z }; }
+
+struct camera_basis
+{
+    float3 eye, U, V, W;
+};
+
+struct frame_buffers
+{
+    gbrt_ray* rays[2];
+    uint32_t* path[2];
+    uint4* hits;
+    gbrt_ray* shadow_rays;
+    uint32_t* shadow_path;
+    float4* shadow_contrib;
+    float4* throughput;
+    float4* radiance;
+    uint2* rng_flags;   // draw counter, flags
+    float4* sum;
+    uint32_t* counts;   // queue 0, queue 1, shadow queue
+};
+
+// Appends the lanes with `take` to a queue: one atomic per warp.  Every lane of the
+// warp must call it.
+__device__ __forceinline__ uint32_t warp_append(bool take, uint32_t* counter)
+{
+    const uint32_t full = 0xFFFFFFFFu;
+    uint32_t mask = __ballot_sync(full, take);
+    if (mask == 0) return 0;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
+    base = __shfl_sync(full, base, leader);
+    return base + uint32_t(__popc(mask & ((1u << lane) - 1u)));
+}
+
+__device__ __forceinline__ void store_ray(gbrt_ray* dst, v3 o, v3 d, float tmin, float tmax)
+{
+    float4* p = reinterpret_cast<float4*>(dst);
+    p[0] = make_float4(o.x, o.y, o.z, d.x);
+    p[1] = make_float4(d.y, d.z, tmin, tmax);
+}
+
+// Jittered primary rays (detail/sched_common.h:209-233: jitter x drawn before y) through
+// the pinhole camera (detail/pinhole_camera.inl:103-120).
+__global__ void __launch_bounds__(kBlock) pt_raygen(frame_buffers fb, uint32_t width, uint32_t height,
+                                                    uint32_t frame, uint32_t sample, camera_basis cam)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t n = width * height;
+    if (i == 0)
+    {
+        fb.counts[0] = n;
+        fb.counts[1] = 0;
+        fb.counts[2] = 0;
+    }
+    if (i >= n) return;
+    float x = float(i % width), y = float(i / width);
+    float jx = gbrt_rng_u01(frame, i, sample, 0) - 0.5f;
+    float jy = gbrt_rng_u01(frame, i, sample, 1) - 0.5f;
+    float sx = ((x + jx) + 0.5f) / float(width);
+    float sy = ((y + jy) + 0.5f) / float(height);
+    float u = 2.0f * sx - 1.0f;
+    float v = 2.0f * sy - 1.0f;
+    v3 U = { cam.U.x, cam.U.y, cam.U.z }, V = { cam.V.x, cam.V.y, cam.V.z }, W = { cam.W.x, cam.W.y, cam.W.z };
+    v3 d = normalize3(U * u + V * v + W);
+    store_ray(&fb.rays[0][i], { cam.eye.x, cam.eye.y, cam.eye.z }, d, 0.0f, FLT_MAX);
+    fb.path[0][i] = i;
+    fb.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    fb.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    fb.rng_flags[i] = make_uint2(2u, kLastSpecular);
+}
+
+__global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, const bvh2_node* __restrict__ nodes,
+                                                    const tri48* __restrict__ tris, int32_t root, int32_t num_inner,
+                                                    int32_t num_tris, uint32_t* __restrict__ status)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i == 0)
+    {
+        fb.counts[q ^ 1] = 0;   // the shade kernel that follows appends to these
+        fb.counts[2] = 0;
+    }
+    uint32_t n = fb.counts[q];
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
+    float4 r0 = rp[0], r1 = rp[1];
+    trace_result h = traverse_bvh<false>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
+                                         { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    fb.hits[i] = make_uint4(uint32_t(h.tri), __float_as_uint(h.t), 0u, 0u);
+}
+
+struct shade_params
+{
+    const gbrt_material* materials;
+    uint32_t num_materials;
+    const float4* lights;
+    uint32_t num_lights;
+    const tri48* tris;
+    int32_t num_tris;
+    float epsilon;
+    float3 ambient;
+    uint32_t frame, sample, bounce, flags;
+};
+
+// One bounce of pathtracing::kernel::operator() (detail/pathtracing.inl:65-221) for every
+// live path.
+__global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shade_params sp,
+                                                   uint32_t* __restrict__ status)
+{
+    const float inv_pi = 3.18309886183790691216444201928e-01f;
+    const float pi = 3.14159265358979323846264338328e+00f;
+    const float two_pi = 6.28318530717958623199592693709e+00f;
+
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t n = fb.counts[q];
+    bool live = i < n;
+
+    bool cont = false, shadow = false;
+    v3 next_o{}, next_d{}, sh_o{}, sh_d{};
+    float next_tmin = 0.0f, next_tmax = 0.0f, sh_tmax = 0.0f;
+    float4 contrib{};
+    uint32_t p = 0;
+
+    if (live)
+    {
+        p = fb.path[q][i];
+        const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
+        float4 r0 = rp[0], r1 = rp[1];
+        v3 ori = { r0.x, r0.y, r0.z }, dir = { r0.w, r1.x, r1.y };
+        uint4 hh = fb.hits[i];
+        int tri = int(hh.x);
+        float t = __uint_as_float(hh.y);
+        uint2 st = fb.rng_flags[p];
+        uint32_t k = st.x, flags = st.y;
+        v3 thr = xyz(fb.throughput[p]);
+        float4 rad4 = fb.radiance[p];
+        v3 rad = xyz(rad4);
+
+        if (tri < 0 || tri >= sp.num_tris)
+        {
+            // the ray left the scene: ambient light (pathtracing.inl:71-79)
+            v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
+            rad = rad + amb * thr;
+        }
+        else
+        {
+            if (sp.bounce == 0) flags |= kFirstHit;
+            float4 t1 = ldg4(&sp.tris[tri].t1);
+            float4 t2 = ldg4(&sp.tris[tri].t2);
+            v3 e1 = xyz(t1), e2 = xyz(t2);
+            uint32_t geom = __float_as_uint(t1.w);
+            v3 view = -dir;
+            v3 isect = ori + dir * t;
+            v3 gn = normalize3(cross3(e1, e2));
+            v3 sn = gn;
+            gbrt_material m;
+            if (geom < sp.num_materials)
+            {
+                m = sp.materials[geom];
+            }
+            else
+            {
+                atomicOr(status, kStatusBadIndex);
+                m = gbrt_material{ GBRT_MATERIAL_MATTE, { 0.0f, 0.0f, 0.0f }, 0.0f };
+            }
+            v3 mcol = { m.color[0], m.color[1], m.color[2] };
+            bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+
+            v3 refl = { 0.0f, 0.0f, 0.0f };
+            float brdf_pdf;
+            v3 src;
+            if (!emission)
+            {
+                // matte::sample -> lambertian::sample_f (matte.inl:40-56, brdf.h:50-76)
+                v3 nn = faceforward3(sn, view, gn);
+                v3 w = nn;
+                v3 v = fabsf(w.x) > fabsf(w.y) ? normalize3(v3{ -w.z, 0.0f, w.x }) : normalize3(v3{ 0.0f, w.z, -w.y });
+                v3 u = cross3(v, w);
+                // cosine_sample_hemisphere(gen.next(), gen.next()), second argument drawn
+                // first as in the reference build (sampling.h:117-127)
+                float u2 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
+                float u1 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
+                float r = sqrtf(u1);
+                float theta = two_pi * u2;
+                // cos and sin evaluated in double and rounded once to float
+                float ct = float(cos(double(theta)));
+                float sth = float(sin(double(theta)));
+                v3 s3 = { r * ct, r * sth, sqrtf(1.0f - u1) };
+                refl = normalize3(u * s3.x + v * s3.y + w * s3.z);
+                brdf_pdf = dot3(nn, refl) * inv_pi;
+                src = (mcol * m.scale) * inv_pi;
+            }
+            else
+            {
+                brdf_pdf = 1.0f;   // emissive::sample (emissive.inl:28-44)
+                src = mcol * m.scale;
+            }
+            bool zero_pdf = brdf_pdf <= 0.0f;
+
+            float light_pdf = 0.0f;
+            if (sp.num_lights > 0 && emission)
+            {
+                float A = 0.5f * length3(cross3(e1, e2));
+                float ld = length3(isect - ori);
+                v3 L = normalize3(isect - ori);
+                float ldotln = fabsf(dot3(-L, gn));
+                float solid_angle = (ldotln * A) / (ld * ld);
+                light_pdf = 1.0f / solid_angle;
+            }
+            float mis = (sp.bounce > 0 && sp.num_lights > 0 && !(flags & kLastSpecular))
+                            ? power_heuristic(brdf_pdf, light_pdf / float(sp.num_lights))
+                            : 1.0f;
+            if (emission)
+            {
+                rad = rad + (thr * mis) * src;
+            }
+            else if (!zero_pdf)
+            {
+                v3 nn = faceforward3(sn, view, gn);
+                if (sp.num_lights > 0)
+                {
+                    // sample_random_light + area_light::sample + sample_surface
+                    // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
+                    float ul = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
+                    int lid = int(ul * float(sp.num_lights));
+                    if (lid >= int(sp.num_lights)) lid = int(sp.num_lights) - 1;
+                    const float4* lp = sp.lights + 4 * lid;
+                    v3 lv1 = xyz(lp[0]), le1 = xyz(lp[1]), le2 = xyz(lp[2]), lint = xyz(lp[3]);
+                    float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
+                    float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
+                    v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
+                    float sq = sqrtf(s1);
+                    v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
+                    v3 ldir = pos - isect;
+                    float dist = length3(ldir);
+                    v3 lnormal = normalize3(cross3(le1, le2));
+                    float larea = 0.5f * length3(cross3(le1, le2));
+                    float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
+                    float lsolid = (ldotln0 * larea) / (dist * dist);
+                    float lpdf = 1.0f / lsolid;
+                    v3 L = normalize3(ldir);
+                    v3 ln = faceforward3(lnormal, -L, lnormal);
+                    float ldotn = dot3(L, nn);
+                    float ldotln = fabsf(dot3(-L, ln));
+                    float bpdf = dot3(nn, L) * inv_pi;
+                    bpdf = bpdf * max_elem(thr);
+                    float ndotl = fmaxf(0.0f, dot3(nn, L));
+                    v3 cd = (mcol * m.scale) * inv_pi;
+                    v3 shade = ((cd * pi) * lint) * ndotl;
+                    v3 src2 = (shade * inv_pi) / ldotn;
+                    float mis2 = power_heuristic(lpdf / float(sp.num_lights), bpdf);
+                    if (ldotn > 0.0f && ldotln > 0.0f)
+                    {
+                        v3 c = (((thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
+                        contrib = make_float4(c.x, c.y, c.z, 0.0f);
+                        shadow = true;
+                        sh_o = isect + L * sp.epsilon;
+                        sh_d = L;
+                        sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon
+                                                                         : dist - sp.epsilon;
+                    }
+                }
+                thr = thr * (src * (dot3(nn, refl) / brdf_pdf));
+                bool terminate = false;
+                if (sp.bounce >= 2)
+                {
+                    // Russian roulette (pathtracing.inl:201-213)
+                    float prob = max_elem(thr);
+                    terminate = gbrt_rng_u01(sp.frame, p, sp.sample, k++) > prob;
+                    thr = thr / prob;
+                }
+                if (!terminate)
+                {
+                    cont = true;
+                    next_o = isect + refl * sp.epsilon;
+                    next_d = refl;
+                    next_tmin = r1.z;
+                    next_tmax = r1.w;
+                    flags &= ~kLastSpecular;
+                }
+            }
+        }
+        fb.throughput[p] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+        fb.radiance[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        fb.rng_flags[p] = make_uint2(k, flags);
+    }
+
+    uint32_t slot = warp_append(cont, &fb.counts[q ^ 1]);
+    if (cont)
+    {
+        store_ray(&fb.rays[q ^ 1][slot], next_o, next_d, next_tmin, next_tmax);
+        fb.path[q ^ 1][slot] = p;
+    }
+    uint32_t sslot = warp_append(shadow, &fb.counts[2]);
+    if (shadow)
+    {
+        store_ray(&fb.shadow_rays[sslot], sh_o, sh_d, sp.epsilon, sh_tmax);
+        fb.shadow_path[sslot] = p;
+        fb.shadow_contrib[sslot] = contrib;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) pt_shadow(frame_buffers fb, const bvh2_node* __restrict__ nodes,
+                                                    const tri48* __restrict__ tris, int32_t root, int32_t num_inner,
+                                                    int32_t num_tris, uint32_t* __restrict__ status)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t n = fb.counts[2];
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(&fb.shadow_rays[i]);
+    float4 r0 = rp[0], r1 = rp[1];
+    trace_result h = traverse_bvh<true>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
+                                        { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    if (h.tri < 0)
+    {
+        uint32_t p = fb.shadow_path[i];
+        float4 c = fb.shadow_contrib[i];
+        float4 r = fb.radiance[p];
+        fb.radiance[p] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+    }
+}
+
+// rr.color += result.color over the samples (sched_common.h:452-470): the path's
+// radiance with alpha 1 if the camera ray hit, else the background.
+__global__ void __launch_bounds__(kBlock) pt_accumulate(frame_buffers fb, uint32_t n, uint32_t sample, float4 bg)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    float4 c = (fb.rng_flags[i].y & kFirstHit) ? make_float4(fb.radiance[i].x, fb.radiance[i].y, fb.radiance[i].z, 1.0f)
+                                               : bg;
+    if (sample == 0)
+    {
+        float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        fb.sum[i] = make_float4(z.x + c.x, z.y + c.y, z.z + c.z, z.w + c.w);
+    }
+    else
+    {
+        float4 s = fb.sum[i];
+        fb.sum[i] = make_float4(s.x + c.x, s.y + c.y, s.z + c.z, s.w + c.w);
+    }
+}
+
+// rr.color /= spp; accum = src * sfactor + dst * dfactor; color = accum
+// (sched_common.h:472-511, pixel_access.h:1040-1043).
+__global__ void __launch_bounds__(kBlock) pt_blend(frame_buffers fb, uint32_t n, float spp, float sfactor,
+                                                   float dfactor, float4* __restrict__ accum,
+                                                   float4* __restrict__ color)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    float4 s = fb.sum[i];
+    float4 a = make_float4(s.x / spp, s.y / spp, s.z / spp, s.w / spp);
+    float4 d = accum[i];
+    float4 o = make_float4(a.x * sfactor + d.x * dfactor, a.y * sfactor + d.y * dfactor, a.z * sfactor + d.z * dfactor,
+                           a.w * sfactor + d.w * dfactor);
+    accum[i] = o;
+    if (color) color[i] = o;
+}
+
+inline size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+gbrt_status frame_buffers_for(gbrt_context* ctx, uint32_t n, frame_buffers& fb)
+{
+    size_t sizes[] = { size_t(n) * 32, size_t(n) * 32, size_t(n) * 4, size_t(n) * 4, size_t(n) * 16,
+                       size_t(n) * 32, size_t(n) * 4,  size_t(n) * 16, size_t(n) * 16, size_t(n) * 16,
+                       size_t(n) * 8,  size_t(n) * 16, 64 };
+    size_t total = 0;
+    for (size_t s : sizes) total += align256(s);
+    if (ctx->pt_scratch_bytes < total)
+    {
+        if (ctx->pt_scratch)
+        {
+            GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            GBRT_CUDA(ctx, cudaFree(ctx->pt_scratch));
+            ctx->pt_scratch = nullptr;
+            ctx->pt_scratch_bytes = 0;
+        }
+        GBRT_CUDA(ctx, cudaMalloc(&ctx->pt_scratch, total));
+        ctx->pt_scratch_bytes = total;
+    }
+    char* base = static_cast<char*>(ctx->pt_scratch);
+    void* ptr[13];
+    size_t off = 0;
+    for (int k = 0; k < 13; ++k)
+    {
+        ptr[k] = base + off;
+        off += align256(sizes[k]);
+    }
+    fb.rays[0] = static_cast<gbrt_ray*>(ptr[0]);
+    fb.rays[1] = static_cast<gbrt_ray*>(ptr[1]);
+    fb.path[0] = static_cast<uint32_t*>(ptr[2]);
+    fb.path[1] = static_cast<uint32_t*>(ptr[3]);
+    fb.hits = static_cast<uint4*>(ptr[4]);
+    fb.shadow_rays = static_cast<gbrt_ray*>(ptr[5]);
+    fb.shadow_path = static_cast<uint32_t*>(ptr[6]);
+    fb.shadow_contrib = static_cast<float4*>(ptr[7]);
+    fb.throughput = static_cast<float4*>(ptr[8]);
+    fb.radiance = static_cast<float4*>(ptr[9]);
+    fb.rng_flags = static_cast<uint2*>(ptr[10]);
+    fb.sum = static_cast<float4*>(ptr[11]);
+    fb.counts = static_cast<uint32_t*>(ptr[12]);
+    return GBRT_OK;
+}
+
+// pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) in float, with
+// perspective()'s fovy in radians and aspect = width / height.
+camera_basis camera_for(gbrt_camera const& c, uint32_t width, uint32_t height)
+{
+    auto sub = [](const float* a, const float* b) { return float3{ a[0] - b[0], a[1] - b[1], a[2] - b[2] }; };
+    auto dot = [](float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+    auto cross = [](float3 u, float3 v) {
+        return float3{ u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x };
+    };
+    auto scale = [](float3 a, float s) { return float3{ a.x * s, a.y * s, a.z * s }; };
+    auto normalize = [&](float3 v) { return scale(v, 1.0f / std::sqrt(dot(v, v))); };
+    float3 f = normalize(sub(c.eye, c.center));
+    float3 up = { c.up[0], c.up[1], c.up[2] };
+    float3 s = normalize(cross(up, f));
+    float3 u = cross(f, s);
+    float fovy = c.fovy_degrees * 1.74532925199432957692369076849e-02f;
+    float aspect = float(width) / float(height);
+    float th = std::tan(fovy / 2.0f);
+    camera_basis b;
+    b.eye = { c.eye[0], c.eye[1], c.eye[2] };
+    b.U = scale(scale(s, th), aspect);
+    b.V = scale(u, th);
+    b.W = { -f.x, -f.y, -f.z };
+    return b;
+}
+
+} // namespace
+} // namespace gbrt
+
+using namespace gbrt;
+
+extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_material const* h_materials,
+                                            uint32_t num_materials, gbrt_area_light const* h_lights,
+                                            uint32_t num_lights, gbrt_pt_scene** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out || !bvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null bvh or output");
+    *out = nullptr;
+    if ((num_materials && !h_materials) || (num_lights && !h_lights))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null material or light array");
+    device_guard g(ctx->device);
+    auto* sc = new (std::nothrow) gbrt_pt_scene;
+    if (!sc) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "pt_scene_create: host allocation");
+    sc->bvh = bvh;
+    sc->device = ctx->device;
+    sc->num_materials = num_materials;
+    sc->num_lights = num_lights;
+    auto cleanup = [&]() {
+        cudaFree(sc->materials);
+        cudaFree(sc->lights);
+        delete sc;
+    };
+    if (num_materials)
+    {
+        cudaError_t e = cudaMalloc(&sc->materials, size_t(num_materials) * sizeof(gbrt_material));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sc->materials, h_materials, size_t(num_materials) * sizeof(gbrt_material),
+                           cudaMemcpyHostToDevice);
+        if (e != cudaSuccess)
+        {
+            cleanup();
+            return check_cuda(ctx, e, "pt_scene_create: materials");
+        }
+    }
+    if (num_lights)
+    {
+        std::vector<float4> l(size_t(num_lights) * 4);
+        for (uint32_t k = 0; k < num_lights; ++k)
+        {
+            gbrt_triangle const& t = h_lights[k].geometry;
+            l[4 * k + 0] = make_float4(t.v1[0], t.v1[1], t.v1[2], 0.0f);
+            l[4 * k + 1] = make_float4(t.e1[0], t.e1[1], t.e1[2], 0.0f);
+            l[4 * k + 2] = make_float4(t.e2[0], t.e2[1], t.e2[2], 0.0f);
+            // area_light::intensity = cl * kl (area_light.inl:22-25)
+            l[4 * k + 3] = make_float4(h_lights[k].cl[0] * h_lights[k].kl, h_lights[k].cl[1] * h_lights[k].kl,
+                                       h_lights[k].cl[2] * h_lights[k].kl, 0.0f);
+        }
+        cudaError_t e = cudaMalloc(&sc->lights, l.size() * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMemcpy(sc->lights, l.data(), l.size() * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess)
+        {
+            cleanup();
+            return check_cuda(ctx, e, "pt_scene_create: lights");
+        }
+    }
+    *out = sc;
+    return GBRT_OK;
+}
+
+extern "C" gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene)
+{
+    if (!scene) return GBRT_ERR_INVALID_ARG;
+    device_guard g(scene->device);
+    cudaFree(scene->materials);
+    cudaFree(scene->lights);
+    delete scene;
+    return GBRT_OK;
+}
+
+extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
+                                            gbrt_pt_params const* params, float* d_accum, float* d_color)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!scene || !camera || !params || !d_accum)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: null argument");
+    gbrt_pt_params const& p = *params;
+    if (p.width == 0 || p.height == 0 || p.spp == 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: empty frame");
+    if (uint64_t(p.width) * p.height > (1ull << 28))
+        return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_frame: more than 2^28 pixels");
+    if ((reinterpret_cast<uintptr_t>(d_accum) & 15u) || (reinterpret_cast<uintptr_t>(d_color) & 15u))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: images must be 16-byte aligned");
+    device_guard g(ctx->device);
+    const uint32_t n = p.width * p.height;
+    frame_buffers fb;
+    gbrt_status st = frame_buffers_for(ctx, n, fb);
+    if (st != GBRT_OK) return st;
+    camera_basis cam = camera_for(*camera, p.width, p.height);
+    gbrt_bvh const* bvh = scene->bvh;
+    shade_params sp;
+    sp.materials = scene->materials;
+    sp.num_materials = scene->num_materials;
+    sp.lights = scene->lights;
+    sp.num_lights = scene->num_lights;
+    sp.tris = bvh->tris;
+    sp.num_tris = int32_t(bvh->num_prims);
+    sp.epsilon = p.epsilon;
+    sp.ambient = make_float3(p.ambient[0], p.ambient[1], p.ambient[2]);
+    sp.frame = p.frame_id;
+    sp.flags = p.flags;
+    // background: ambient_light(bg.xyz, bg.w).intensity with alpha 1 (kernels.h:172-174,
+    // pathtracing.inl:62)
+    float4 bg = make_float4(p.background[0] * p.background[3], p.background[1] * p.background[3],
+                            p.background[2] * p.background[3], 1.0f);
+    const uint32_t blocks = (n + kBlock - 1) / kBlock;
+    cudaStream_t s = ctx->stream;
+    for (uint32_t smp = 0; smp < p.spp; ++smp)
+    {
+        sp.sample = smp;
+        pt_raygen<<<blocks, kBlock, 0, s>>>(fb, p.width, p.height, p.frame_id, smp, cam);
+        GBRT_LAUNCH_CHECK(ctx, "pt_raygen");
+        int q = 0;
+        if (bvh->num_prims > 0)
+        {
+            for (uint32_t b = 0; b < p.num_bounces; ++b)
+            {
+                sp.bounce = b;
+                pt_extend<<<blocks, kBlock, 0, s>>>(fb, q, bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
+                                                    int32_t(bvh->num_prims), ctx->d_status);
+                GBRT_LAUNCH_CHECK(ctx, "pt_extend");
+                pt_shade<<<blocks, kBlock, 0, s>>>(fb, q, sp, ctx->d_status);
+                GBRT_LAUNCH_CHECK(ctx, "pt_shade");
+                if (scene->num_lights > 0)
+                {
+                    pt_shadow<<<blocks, kBlock, 0, s>>>(fb, bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
+                                                        int32_t(bvh->num_prims), ctx->d_status);
+                    GBRT_LAUNCH_CHECK(ctx, "pt_shadow");
+                }
+                q ^= 1;
+            }
+        }
+        pt_accumulate<<<blocks, kBlock, 0, s>>>(fb, n, smp, bg);
+        GBRT_LAUNCH_CHECK(ctx, "pt_accumulate");
+    }
+    pt_blend<<<blocks, kBlock, 0, s>>>(fb, n, float(p.spp), p.sfactor, p.dfactor, reinterpret_cast<float4*>(d_accum),
+                                       reinterpret_cast<float4*>(d_color));
+    GBRT_LAUNCH_CHECK(ctx, "pt_blend");
+    return GBRT_OK;
+}

@@ -316,3 +316,109 @@ extern "C" void gbrt_rays_surface(const gbrt_triangle* tris, uint32_t ntris, uin
         }
     }
 }
+
+namespace {
+
+// Regular icosahedron: 12 vertices (0, +-1, +-phi) cyclic, 20 faces.
+const double kPhi = 1.61803398874989490253;
+const double kIcoVerts[12][3] = {
+    { -1, kPhi, 0 }, { 1, kPhi, 0 }, { -1, -kPhi, 0 }, { 1, -kPhi, 0 },
+    { 0, -1, kPhi }, { 0, 1, kPhi }, { 0, -1, -kPhi }, { 0, 1, -kPhi },
+    { kPhi, 0, -1 }, { kPhi, 0, 1 }, { -kPhi, 0, -1 }, { -kPhi, 0, 1 } };
+const int kIcoFaces[20][3] = {
+    { 0, 11, 5 }, { 0, 5, 1 }, { 0, 1, 7 }, { 0, 7, 10 }, { 0, 10, 11 },
+    { 1, 5, 9 }, { 5, 11, 4 }, { 11, 10, 2 }, { 10, 7, 6 }, { 7, 1, 8 },
+    { 3, 9, 4 }, { 3, 4, 2 }, { 3, 2, 6 }, { 3, 6, 8 }, { 3, 8, 9 },
+    { 4, 9, 5 }, { 2, 4, 11 }, { 6, 2, 10 }, { 8, 6, 7 }, { 9, 8, 1 } };
+
+void box_quad(gbrt_triangle* out, uint32_t first, const float a[3], const float b[3], const float c[3],
+              const float d[3])
+{
+    // quad a-b-c-d as (a, b, c) and (a, c, d)
+    set_tri(out[0], first, first, a, b, c);
+    set_tri(out[1], first + 1, first + 1, a, c, d);
+}
+
+} // namespace
+
+extern "C" uint64_t gbrt_scene_box_count(uint32_t n_blobs, uint32_t subdiv)
+{
+    return 14 + uint64_t(n_blobs) * 20 * subdiv * subdiv;
+}
+
+extern "C" void gbrt_scene_box(uint32_t n_blobs, uint32_t subdiv, uint64_t seed, float light_y,
+                               gbrt_triangle* tris, float* albedo)
+{
+    // the box: 6 faces of [0,1]^3
+    const float P[8][3] = { { 0, 0, 0 }, { 1, 0, 0 }, { 1, 1, 0 }, { 0, 1, 0 },
+                            { 0, 0, 1 }, { 1, 0, 1 }, { 1, 1, 1 }, { 0, 1, 1 } };
+    const int F[6][4] = { { 0, 1, 2, 3 }, { 5, 4, 7, 6 }, { 4, 0, 3, 7 },
+                          { 1, 5, 6, 2 }, { 4, 5, 1, 0 }, { 3, 2, 6, 7 } };
+    for (int f = 0; f < 6; ++f)
+        box_quad(tris + 2 * f, uint32_t(2 * f), P[F[f][0]], P[F[f][1]], P[F[f][2]], P[F[f][3]]);
+    // the light quad just below the ceiling
+    const float L[4][3] = { { 0.375f, light_y, 0.375f }, { 0.625f, light_y, 0.375f },
+                            { 0.625f, light_y, 0.625f }, { 0.375f, light_y, 0.625f } };
+    box_quad(tris + 12, 12u, L[0], L[1], L[2], L[3]);
+
+    const uint64_t per_blob = uint64_t(20) * subdiv * subdiv;
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t b = 0; b < int64_t(n_blobs); ++b)
+    {
+        double radius = 0.03 + 0.05 * u01d(seed, 400, uint64_t(b));
+        double margin = radius * 1.2;
+        d3 c = { margin + (1.0 - 2.0 * margin) * u01d(seed, 401, uint64_t(b)),
+                 margin + (1.0 - 2.0 * margin) * u01d(seed, 402, uint64_t(b)),
+                 margin + (1.0 - 2.0 * margin) * u01d(seed, 403, uint64_t(b)) };
+        double ph[3] = { kTwoPi * u01d(seed, 404, uint64_t(b)), kTwoPi * u01d(seed, 405, uint64_t(b)),
+                         kTwoPi * u01d(seed, 406, uint64_t(b)) };
+        auto vertex = [&](d3 a, d3 bb, d3 cc, uint32_t i, uint32_t j, float out[3]) {
+            double s = double(i) / double(subdiv), t = double(j) / double(subdiv);
+            d3 p = { a.x + (bb.x - a.x) * s + (cc.x - a.x) * t, a.y + (bb.y - a.y) * s + (cc.y - a.y) * t,
+                     a.z + (bb.z - a.z) * s + (cc.z - a.z) * t };
+            d3 d = normalize(p);
+            double noise = det_sin(7.0 * d.x + ph[0]) * det_sin(9.0 * d.y + ph[1]) * det_sin(8.0 * d.z + ph[2]);
+            double r = radius * (1.0 + 0.15 * noise);
+            out[0] = float(c.x + r * d.x);
+            out[1] = float(c.y + r * d.y);
+            out[2] = float(c.z + r * d.z);
+        };
+        uint64_t k = 14 + uint64_t(b) * per_blob;
+        for (int f = 0; f < 20; ++f)
+        {
+            d3 A = normalize({ kIcoVerts[kIcoFaces[f][0]][0], kIcoVerts[kIcoFaces[f][0]][1], kIcoVerts[kIcoFaces[f][0]][2] });
+            d3 B = normalize({ kIcoVerts[kIcoFaces[f][1]][0], kIcoVerts[kIcoFaces[f][1]][1], kIcoVerts[kIcoFaces[f][1]][2] });
+            d3 C = normalize({ kIcoVerts[kIcoFaces[f][2]][0], kIcoVerts[kIcoFaces[f][2]][1], kIcoVerts[kIcoFaces[f][2]][2] });
+            for (uint32_t j = 0; j < subdiv; ++j)
+            {
+                for (uint32_t i = 0; i + j < subdiv; ++i)
+                {
+                    float p00[3], p10[3], p01[3];
+                    vertex(A, B, C, i, j, p00);
+                    vertex(A, B, C, i + 1, j, p10);
+                    vertex(A, B, C, i, j + 1, p01);
+                    set_tri(tris[k], uint32_t(k), uint32_t(k), p00, p10, p01);
+                    ++k;
+                    if (i + j + 1 < subdiv)
+                    {
+                        float p11[3];
+                        vertex(A, B, C, i + 1, j + 1, p11);
+                        set_tri(tris[k], uint32_t(k), uint32_t(k), p10, p11, p01);
+                        ++k;
+                    }
+                }
+            }
+        }
+    }
+    if (albedo)
+    {
+        uint64_t n = gbrt_scene_box_count(n_blobs, subdiv);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < int64_t(n); ++i)
+        {
+            for (int a = 0; a < 3; ++a)
+                albedo[3 * i + a] = (i == 12 || i == 13) ? 0.0f
+                                                          : 0.2f + 0.6f * u01f(seed, 410 + uint64_t(a), uint64_t(i));
+        }
+    }
+}

@@ -48,6 +48,19 @@ void gbrt_rays_surface(const gbrt_triangle* tris, uint32_t ntris, uint32_t n_ori
                        uint64_t seed, float offset, uint32_t ao_per_origin, float ao_tmax,
                        gbrt_ray* closest_out, gbrt_ray* ao_out);
 
+/* Closed unit box with a ceiling quad light and noisy icosphere blobs (the path-
+ * tracing scene).  Layout: triangles 0..11 the box [0,1]^3, 12..13 the light quad
+ * (0.375..0.625 in x and z, at y = light_y), then n_blobs blobs of 20*subdiv^2
+ * triangles each: a geodesic sphere (each icosahedron face cut into subdiv^2
+ * triangles) of radius uniform in [0.03, 0.08], radially displaced by up to 15% with
+ * a smooth seeded noise, centred uniformly inside the box.  geom_id = prim_id =
+ * triangle index.  Writes gbrt_scene_box_count() triangles to `tris`; `albedo` (3
+ * floats per triangle, may be NULL) gets per-triangle albedo uniform in [0.2, 0.8]
+ * (the light quad's entries are 0).                                                */
+uint64_t gbrt_scene_box_count(uint32_t n_blobs, uint32_t subdiv);
+void gbrt_scene_box(uint32_t n_blobs, uint32_t subdiv, uint64_t seed, float light_y,
+                    gbrt_triangle* tris, float* albedo);
+
 /* Uniform float in [0,1) of the counter-based generator used above (exposed so that
  * tests can reproduce any value).                                                  */
 float gbrt_scene_u01(uint64_t seed, uint64_t stream, uint64_t index);

@@ -1,26 +1,12 @@
-// closest_hit / any_hit traversal of the node-pair BVH (bvh_layout.cuh).
-//
-// Replaces the device branch of visionaray's intersect<Traversal>(ray, bvh, isect)
-// (detail/bvh/intersect.inl:166-356), which visits BVH2 nodes one 32-byte box at a
-// time with a 5-entry stack and a restart trail.  Here each step fetches one 64-byte
-// record (four 128-bit read-only loads) that holds both children's boxes, tests both,
-// descends into the nearer hit child and pushes the farther one on a per-thread stack
-// (Aila & Laine 2009 "while-while" form).  Leaves are contiguous runs of 48-byte
-// triangles tested with the reference's exact ray/triangle arithmetic
-// (device_math.cuh), and a hit is accepted exactly as update_if.h:68-107 does:
-// tmin <= t <= tmax and t strictly below the best t so far.  Any-hit returns at the
-// first accepted hit (detail/exit_traversal.h:49-56).
+// closest_hit / any_hit ray queries over the node-pair BVH: one thread per ray over
+// the shared traversal core (traverse_core.cuh), 128-bit ray loads and hit stores.
 
-#include "api_internal.h"
-#include "device_math.cuh"
+#include "traverse_core.cuh"
 
 namespace gbrt {
 namespace {
 
 constexpr int kTraceBlock = 128;
-constexpr int kEmpty = INT32_MIN;   // stack sentinel: neither an inner node nor a leaf
-
-__device__ __forceinline__ float4 ldg4(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
 template <bool AnyHit>
 __global__ void __launch_bounds__(kTraceBlock) trace_rays(const bvh2_node* __restrict__ nodes,
@@ -35,108 +21,11 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays(const bvh2_node* __res
 
     float4 r0 = ldg4(&rays[i]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
-    const f3 o = { r0.x, r0.y, r0.z };
-    const f3 d = { r0.w, r1.x, r1.y };
-    const float tmin = r1.z, tmax = r1.w;
-    const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
-
-    float best_t = FLT_MAX, best_u = 0.0f, best_v = 0.0f;
-    uint32_t best_prim = GBRT_NO_HIT;
-
-    int stack[kStackSize];
-    int sp = 0;
-    int node = root;
-
-    while (node != kEmpty)
-    {
-        // inner nodes
-        while (node >= 0)
-        {
-            if (node >= num_inner)
-            {
-                atomicOr(status, kStatusBadIndex);
-                node = kEmpty;
-                break;
-            }
-            const bvh2_node* np = nodes + node;
-            float4 a = ldg4(&np->xy0);
-            float4 b = ldg4(&np->xy1);
-            float4 z = ldg4(&np->z01);
-            int4 link = __ldg(&np->link);
-
-            // slab test as (box - origin) * inv_dir, like detail/bvh/intersect.inl:257-276
-            float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
-            float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
-            float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;
-            float lx1 = (b.x - o.x) * ix, hx1 = (b.y - o.x) * ix;
-            float ly1 = (b.z - o.y) * iy, hy1 = (b.w - o.y) * iy;
-            float lz1 = (z.z - o.z) * iz, hz1 = (z.w - o.z) * iz;
-            float tn0 = fmaxf(tmin, fmaxf(fminf(lx0, hx0), fmaxf(fminf(ly0, hy0), fminf(lz0, hz0))));
-            float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
-            float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
-            float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
-            bool h0 = tf0 >= tn0 && tn0 < best_t;
-            bool h1 = tf1 >= tn1 && tn1 < best_t;
-
-            if (h0 && h1)
-            {
-                bool first0 = tn0 < tn1;   // ties go to child 1, as intersect.inl:283
-                int near_child = first0 ? link.x : link.y;
-                int far_child = first0 ? link.y : link.x;
-                if (sp < kStackSize)
-                {
-                    stack[sp++] = far_child;
-                }
-                else
-                {
-                    atomicOr(status, kStatusStackOverflow);
-                }
-                node = near_child;
-            }
-            else if (h0 || h1)
-            {
-                node = h0 ? link.x : link.y;
-            }
-            else
-            {
-                node = sp > 0 ? stack[--sp] : kEmpty;
-            }
-        }
-        if (node == kEmpty) break;
-
-        // leaf: contiguous triangles from ~node, the last one flagged
-        for (int t = ~node;; ++t)
-        {
-            if (t >= num_tris)
-            {
-                atomicOr(status, kStatusBadIndex);
-                break;
-            }
-            const tri48* tp = tris + t;
-            float4 t0 = ldg4(&tp->t0);
-            float4 t1 = ldg4(&tp->t1);
-            float4 t2 = ldg4(&tp->t2);
-            tri_hit h = intersect_triangle(o, d, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z }, { t2.x, t2.y, t2.z });
-            if (h.hit && h.t < best_t && h.t >= tmin && h.t <= tmax)
-            {
-                best_t = h.t;
-                best_u = h.u;
-                best_v = h.v;
-                best_prim = __float_as_uint(t0.w);
-                if (AnyHit)
-                {
-                    node = kEmpty;
-                    break;
-                }
-            }
-            if (__float_as_uint(t2.w) & kLastInLeaf) break;
-        }
-        if (AnyHit && node == kEmpty) break;
-        node = sp > 0 ? stack[--sp] : kEmpty;
-    }
-
+    trace_result h = traverse_bvh<AnyHit>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
+                                          { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[i] =
-        make_uint4(best_prim, __float_as_uint(best_t), __float_as_uint(best_u), __float_as_uint(best_v));
+        make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
 }
 
 __global__ void __launch_bounds__(kTraceBlock) write_misses(gbrt_hit* __restrict__ hits, uint32_t n)
@@ -162,8 +51,9 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         trace_rays<true><<<blocks, kTraceBlock, 0, stream>>>(bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
                                                              int32_t(bvh->num_prims), d_rays, n, d_hits, ctx->d_status);
     else
-        trace_rays<false><<<blocks, kTraceBlock, 0, stream>>>(bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
-                                                              int32_t(bvh->num_prims), d_rays, n, d_hits, ctx->d_status);
+        trace_rays<false><<<blocks, kTraceBlock, 0, stream>>>(bvh->nodes, bvh->tris, bvh->root,
+                                                              int32_t(bvh->num_inner), int32_t(bvh->num_prims), d_rays,
+                                                              n, d_hits, ctx->d_status);
     GBRT_LAUNCH_CHECK(ctx, "trace_rays");
     return GBRT_OK;
 }

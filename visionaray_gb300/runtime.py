@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .types import BVH_NODE, HIT, RAY, TRIANGLE
+from .types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS, RAY, TRIANGLE
 
 LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
 
@@ -45,6 +45,9 @@ SIGNATURES = {
     "gbrt_trace_any_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_trace_closest_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_trace_any_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+    "gbrt_pt_scene_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
+    "gbrt_pt_scene_destroy": (_i32, [_vp]),
+    "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -252,3 +255,45 @@ def closest_hit(rays, bvh, out=None):
 def any_hit(rays, bvh, out=None):
     """any_hit over one BVH for a batch of rays (device tensor or host array)."""
     return _trace(rays, bvh, out, True)
+
+
+class PTScene:
+    """make_kernel_params(prims, materials, lights, ...) counterpart: a BVH with its
+    materials (one per geom_id) and area lights, ready for pathtrace_frame."""
+
+    def __init__(self, bvh, materials, lights):
+        self.bvh, self.ctx = bvh, bvh.ctx
+        mats = np.ascontiguousarray(materials, MATERIAL)
+        lts = np.ascontiguousarray(lights, AREA_LIGHT)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbrt_pt_scene_create(self.ctx.h, bvh.h, _hptr(mats), len(mats), _hptr(lts),
+                                                         len(lts), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbrt_pt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pathtrace_frame(scene, camera, params, accum=None, color=None):
+    """One frame of the jittered-blend sampler around the path tracer
+    (cuda_sched::frame(pathtracing::kernel, sparams)).  accum / color are (h, w, 4)
+    float32 CUDA tensors (accum is read and written); returns accum."""
+    torch = _torch()
+    ctx = scene.ctx
+    cam = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+    par = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+    w, h = int(par["width"][0]), int(par["height"][0])
+    dev = f"cuda:{ctx.device}"
+    if accum is None:
+        accum = torch.zeros((h, w, 4), dtype=torch.float32, device=dev)
+    cptr = _dptr(color) if color is not None else None
+    ctx.check(ctx.lib.gbrt_pathtrace_frame(ctx.h, scene.h, _hptr(cam), _hptr(par), _dptr(accum), cptr))
+    return accum

@@ -73,3 +73,50 @@ def surface_rays(tris, n_origins, seed=7, offset=1e-4, ao_per_origin=8, ao_tmax=
 
 def u01(seed, stream, index):
     return _load().gbrt_scene_u01(seed, stream, index)
+
+
+def box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
+    """The path-tracing scene: unit box (12 triangles), a 0.25 x 0.25 ceiling quad light
+    (2 triangles, emission `emission`), `n_blobs` noisy icospheres of 20*subdiv^2
+    triangles.  Returns (triangles, materials per geom_id, area lights)."""
+    from .types import AREA_LIGHT, EMISSIVE, MATERIAL, MATTE
+    lib = _load()
+    if not hasattr(lib.gbrt_scene_box, "_typed"):
+        lib.gbrt_scene_box_count.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+        lib.gbrt_scene_box_count.restype = ctypes.c_uint64
+        lib.gbrt_scene_box.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float,
+                                       ctypes.c_void_p, ctypes.c_void_p]
+        lib.gbrt_scene_box._typed = True
+    n = lib.gbrt_scene_box_count(n_blobs, subdiv)
+    tris = np.empty(n, TRIANGLE)
+    albedo = np.empty((n, 3), np.float32)
+    lib.gbrt_scene_box(n_blobs, subdiv, seed, light_y, _ptr(tris), _ptr(albedo))
+    mats = np.zeros(n, MATERIAL)
+    mats["kind"] = MATTE
+    mats["color"] = albedo
+    mats["scale"] = 1.0
+    mats["kind"][12:14] = EMISSIVE
+    mats["color"][12:14] = emission
+    lights = np.zeros(2, AREA_LIGHT)
+    lights["geometry"] = tris[12:14]
+    lights["cl"] = emission
+    lights["kl"] = 1.0
+    return tris, mats, lights
+
+
+def box_camera(eye=(0.5, 0.5, 0.02), center=(0.5, 0.5, 1.0), up=(0.0, 1.0, 0.0), fovy_degrees=60.0):
+    """Camera inside the closed box, near the front wall, looking at the back wall."""
+    from .types import CAMERA
+    c = np.zeros(1, CAMERA)
+    c["eye"], c["center"], c["up"], c["fovy_degrees"] = eye, center, up, fovy_degrees
+    return c[0]
+
+
+def pt_params(width, height, spp, num_bounces=8, epsilon=1e-4, frame_id=0, sfactor=1.0, dfactor=0.0,
+              background=(0.0, 0.0, 0.0, 1.0), ambient=(0.0, 0.0, 0.0), flags=0):
+    from .types import PT_PARAMS
+    p = np.zeros(1, PT_PARAMS)
+    p["width"], p["height"], p["spp"], p["num_bounces"] = width, height, spp, num_bounces
+    p["epsilon"], p["frame_id"], p["sfactor"], p["dfactor"] = epsilon, frame_id, sfactor, dfactor
+    p["background"], p["ambient"], p["flags"] = background, ambient, flags
+    return p[0]

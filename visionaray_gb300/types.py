@@ -16,8 +16,21 @@ BVH_NODE = np.dtype([("bbox_min", "<f4", (3,)), ("bbox_max", "<f4", (3,)),
                      ("first", "<u4"), ("num_prims", "<u2"),
                      ("axis", "u1"), ("sign", "u1")])
 
+# path tracing (gbrt.h): gbrt_material, gbrt_area_light, gbrt_camera, gbrt_pt_params
+MATERIAL = np.dtype([("kind", "<u4"), ("color", "<f4", (3,)), ("scale", "<f4")])
+AREA_LIGHT = np.dtype([("geometry", TRIANGLE), ("cl", "<f4", (3,)), ("kl", "<f4")])
+CAMERA = np.dtype([("eye", "<f4", (3,)), ("center", "<f4", (3,)), ("up", "<f4", (3,)),
+                   ("fovy_degrees", "<f4")])
+PT_PARAMS = np.dtype([("width", "<u4"), ("height", "<u4"), ("spp", "<u4"), ("num_bounces", "<u4"),
+                      ("epsilon", "<f4"), ("frame_id", "<u4"), ("sfactor", "<f4"), ("dfactor", "<f4"),
+                      ("background", "<f4", (4,)), ("ambient", "<f4", (3,)), ("flags", "<u4")])
+MATTE, EMISSIVE = 0, 1
+PT_SHADOW_RANGE_FIX = 1
+
 NO_HIT = 0xFFFFFFFF
 FLT_MAX = float(np.finfo(np.float32).max)
 
 assert TRIANGLE.itemsize == 44 and RAY.itemsize == 32
 assert HIT.itemsize == 16 and BVH_NODE.itemsize == 32
+assert MATERIAL.itemsize == 20 and AREA_LIGHT.itemsize == 60 and CAMERA.itemsize == 40
+assert PT_PARAMS.itemsize == 64
