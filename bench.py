@@ -171,6 +171,43 @@ def run_reference(args):
     return 0
 
 
+PT_WIDTH, PT_HEIGHT, PT_SPP, PT_BOUNCES = 1920, 1080, 64, 8
+PT_WORKLOAD = ("path tracing: closed unit box + 0.25^2 ceiling light (emission 15) + 256 noisy icosphere "
+               "blobs (2,478,094 tris, Lambertian albedo U[0.2,0.8]), 1920x1080, 64 spp, depth 8, "
+               "Russian roulette from depth 3")
+
+
+def run_pathtrace(vg, ctx, frames, flags, rprint):
+    """Msamples/s of the path-tracing workload (one frame = 1920x1080 x 64 spp)."""
+    import torch
+    from visionaray_gb300 import scenes
+    tris, mats, lights = scenes.box_scene()
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris, ctx.device))
+    scene = vg.PTScene(bvh, mats, lights)
+    cam = scenes.box_camera()
+    dev = f"cuda:{ctx.device}"
+    accum = torch.zeros((PT_HEIGHT, PT_WIDTH, 4), dtype=torch.float32, device=dev)
+    params = scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES, flags=flags)
+    vg.pathtrace_frame(scene, cam, params, accum=accum)   # warm-up frame
+    ctx.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    launches0 = ctx.launches
+    ev[0].record(ctx.stream)
+    for f in range(frames):
+        p = scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES, frame_id=f + 1,
+                             sfactor=1.0 / (f + 2), dfactor=1.0 - 1.0 / (f + 2), flags=flags)
+        vg.pathtrace_frame(scene, cam, p, accum=accum)
+    ev[1].record(ctx.stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / frames
+    samples = PT_WIDTH * PT_HEIGHT * PT_SPP
+    mean = accum[..., :3].mean().item()
+    return {"workload": PT_WORKLOAD, "flags": flags, "frames": frames, "ms_per_frame": round(ms, 2),
+            "msamples_s": round(samples / (ms * 1e-3) / 1e6, 2), "image_mean": round(mean, 5),
+            "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -299,6 +336,10 @@ def run_ours(args):
                 "frac": round(d["achieved_gbs"] / peak, 4) if d.get("achieved_gbs") else None,
                 "traffic": None, "peak_source": f"{peak_kind} hbm_gbs"}
 
+    pt = None
+    if args.pt_frames > 0:
+        pt = run_pathtrace(vg, ctx, args.pt_frames, 0, rprint)
+
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res = cpu_baseline(tris, closest, ao, rank_print=rprint, sample_every=8, repeats=2)
@@ -317,7 +358,8 @@ def run_ours(args):
             "kernels": per, "roofline": roofline,
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
-            "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base}
+            "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base,
+            "pathtrace": pt}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -332,6 +374,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
     # smaller cases for profiling captures only; the benchmark is the default size
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--origins", type=int, default=ORIGINS)
