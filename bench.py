@@ -232,6 +232,7 @@ def run_ours(args):
     rays_per_step = n_c + n_a
 
     ctx = vg.Context(local)
+    ctx.set_trace_flags(args.trace_flags)
     stream = ctx.stream
 
     # LBVH build, timed separately (build is not part of the traversal metric)
@@ -354,7 +355,8 @@ def run_ours(args):
                        f"REDUCED profiling case: heightfield {args.grid}x{args.grid}, {args.origins} origins",
                        "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
                        "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3)},
+                       "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
+                       "trace_flags": args.trace_flags},
             "kernels": per, "roofline": roofline,
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
@@ -375,6 +377,8 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--trace-flags", type=int, default=1,
+                   help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order)")
     # smaller cases for profiling captures only; the benchmark is the default size
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--origins", type=int, default=ORIGINS)

@@ -104,6 +104,14 @@ gbrt_status gbrt_context_synchronize(gbrt_context* ctx);
 const char* gbrt_last_error(gbrt_context const* ctx);
 int         gbrt_abi_version(void);
 
+/* Ray-query options of a context (GBRT_TRACE_* bits, default 0).  No visionaray
+ * counterpart: visionaray traces each ray in the calling thread, in the caller's
+ * order.  GBRT_TRACE_SORT_RAYS orders a call's rays (from 65,536 rays up) by the Morton
+ * cell of their origin before tracing, so that a warp's rays share their upper tree
+ * path; hits are still returned per input ray and are identical bit for bit.        */
+#define GBRT_TRACE_SORT_RAYS 1u
+gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
+
 /* ------------------------------------------------------------------------------ */
 /* BVH construction                                                                */
 

@@ -154,3 +154,19 @@ def test_full_size_heightfield_sample(oracle):
     compare_closest(got_c[sel], oracle.trace(ref, tris, closest[sel]), closest[sel], tris, oracle)
     sel_a = np.arange(0, len(ao), 389)
     compare_any(got_a[sel_a], oracle.trace(ref, tris, ao[sel_a], any_hit=True), ao[sel_a], tris, oracle)
+
+
+def test_sorted_ray_order_gives_identical_hits():
+    """GBRT_TRACE_SORT_RAYS changes only the order rays are traced in."""
+    tris = scenes.heightfield(grid=512, seed=3)
+    closest, ao = scenes.surface_rays(tris, 1 << 18, seed=9)
+    ctx = vg.Context(0)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    plain = [vg.hits_to_numpy(f(vg.device_rays(r), bvh)) for f, r in ((vg.closest_hit, closest), (vg.any_hit, ao))]
+    ctx.set_trace_flags(ctx.TRACE_SORT_RAYS)
+    srt = [vg.hits_to_numpy(f(vg.device_rays(r), bvh)) for f, r in ((vg.closest_hit, closest), (vg.any_hit, ao))]
+    host = vg.closest_hit(closest, bvh)
+    ctx.synchronize()
+    assert plain[0].tobytes() == srt[0].tobytes()
+    assert plain[1].tobytes() == srt[1].tobytes()
+    assert host.tobytes() == plain[0].tobytes()

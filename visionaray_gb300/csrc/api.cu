@@ -54,6 +54,22 @@ void free_bvh_arrays(gbrt_bvh* b)
     b->sorted_ids = nullptr;
 }
 
+gbrt_status ensure_trace_scratch(gbrt_context* ctx, uint32_t n)
+{
+    size_t bytes = trace_scratch_bytes(n);
+    if (ctx->trace_scratch_bytes >= bytes) return GBRT_OK;
+    if (ctx->trace_scratch)
+    {
+        GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        GBRT_CUDA(ctx, cudaFree(ctx->trace_scratch));
+        ctx->trace_scratch = nullptr;
+        ctx->trace_scratch_bytes = 0;
+    }
+    GBRT_CUDA(ctx, cudaMalloc(&ctx->trace_scratch, bytes));
+    ctx->trace_scratch_bytes = bytes;
+    return GBRT_OK;
+}
+
 gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
 {
     if (ctx->slot_capacity >= rays_per_slot) return GBRT_OK;
@@ -62,17 +78,21 @@ gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
         if (ctx->slot_stream[k]) GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->slot_stream[k]));
         cudaFree(ctx->slot_rays[k]);
         cudaFree(ctx->slot_hits[k]);
-        ctx->slot_rays[k] = ctx->slot_hits[k] = nullptr;
+        cudaFree(ctx->slot_trace_scratch[k]);
+        ctx->slot_rays[k] = ctx->slot_hits[k] = ctx->slot_trace_scratch[k] = nullptr;
     }
     ctx->slot_capacity = 0;
+    ctx->slot_trace_scratch_bytes = 0;
     for (int k = 0; k < gbrt_context::kSlots; ++k)
     {
         if (!ctx->slot_stream[k]) GBRT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->slot_stream[k], cudaStreamNonBlocking));
         if (!ctx->slot_done[k]) GBRT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->slot_done[k], cudaEventDisableTiming));
         GBRT_CUDA(ctx, cudaMalloc(&ctx->slot_rays[k], rays_per_slot * sizeof(gbrt_ray)));
         GBRT_CUDA(ctx, cudaMalloc(&ctx->slot_hits[k], rays_per_slot * sizeof(gbrt_hit)));
+        GBRT_CUDA(ctx, cudaMalloc(&ctx->slot_trace_scratch[k], trace_scratch_bytes(uint32_t(rays_per_slot))));
     }
     ctx->slot_capacity = rays_per_slot;
+    ctx->slot_trace_scratch_bytes = trace_scratch_bytes(uint32_t(rays_per_slot));
     return GBRT_OK;
 }
 
@@ -99,7 +119,7 @@ gbrt_status trace_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h
         GBRT_CUDA(ctx, cudaMemcpyAsync(ctx->slot_rays[k], h_rays + b, size_t(m) * sizeof(gbrt_ray),
                                        cudaMemcpyHostToDevice, s));
         st = trace(ctx, bvh, static_cast<gbrt_ray*>(ctx->slot_rays[k]), m, static_cast<gbrt_hit*>(ctx->slot_hits[k]),
-                   any_hit, s);
+                   any_hit, s, ctx->slot_trace_scratch[k], ctx->slot_trace_scratch_bytes);
         if (st != GBRT_OK) return st;
         GBRT_CUDA(ctx, cudaMemcpyAsync(h_hits + b, ctx->slot_hits[k], size_t(m) * sizeof(gbrt_hit),
                                        cudaMemcpyDeviceToHost, s));
@@ -165,12 +185,22 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
             if (ctx->slot_done[k]) cudaEventDestroy(ctx->slot_done[k]);
             cudaFree(ctx->slot_rays[k]);
             cudaFree(ctx->slot_hits[k]);
+            cudaFree(ctx->slot_trace_scratch[k]);
         }
+        cudaFree(ctx->trace_scratch);
         cudaFree(ctx->scratch);
         cudaFree(ctx->pt_scratch);
         cudaFree(ctx->d_status);
     }
     delete ctx;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (flags & ~GBRT_TRACE_SORT_RAYS) return fail(ctx, GBRT_ERR_INVALID_ARG, "set_trace_flags: unknown flag");
+    ctx->trace_flags = flags;
     return GBRT_OK;
 }
 
@@ -325,7 +355,12 @@ static gbrt_status trace_device(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray
     if (!aligned16(d_rays) || !aligned16(d_hits))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "trace: ray and hit buffers must be 16-byte aligned");
     device_guard g(ctx->device);
-    return trace(ctx, bvh, d_rays, n, d_hits, any_hit, ctx->stream);
+    if (ctx->trace_flags & GBRT_TRACE_SORT_RAYS)
+    {
+        gbrt_status s2 = ensure_trace_scratch(ctx, n);
+        if (s2 != GBRT_OK) return s2;
+    }
+    return trace(ctx, bvh, d_rays, n, d_hits, any_hit, ctx->stream, ctx->trace_scratch, ctx->trace_scratch_bytes);
 }
 
 gbrt_status gbrt_trace_closest_hit(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,

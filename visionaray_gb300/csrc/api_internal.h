@@ -43,6 +43,14 @@ struct gbrt_context
     // Path-tracer wavefront state (grown on demand, freed with the context).
     void* pt_scratch = nullptr;
     size_t pt_scratch_bytes = 0;
+
+    // Ray queries: GBRT_TRACE_* flags and the ray-order scratch of the context stream
+    // and of each host-path slot.
+    uint32_t trace_flags = 0;
+    void* trace_scratch = nullptr;
+    size_t trace_scratch_bytes = 0;
+    void* slot_trace_scratch[kSlots] = { nullptr, nullptr };
+    size_t slot_trace_scratch_bytes = 0;
 };
 
 enum class bvh_kind
@@ -64,6 +72,9 @@ struct gbrt_bvh
     // LBVH only: sorted Morton codes and, per sorted position, the input index.
     uint32_t* sorted_codes = nullptr;
     uint32_t* sorted_ids = nullptr;
+    // Scene bounds (the root box), used to order rays by origin.
+    float lo[3] = { 0.0f, 0.0f, 0.0f };
+    float hi[3] = { 0.0f, 0.0f, 0.0f };
 };
 
 namespace gbrt {
@@ -145,11 +156,20 @@ gbrt_status build_lbvh_in_scratch(gbrt_context* ctx, gbrt_triangle const* d_tris
 size_t radix_sort_scratch_bytes(uint32_t n);
 gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values,
                              uint32_t* keys_alt, uint32_t* values_alt, uint32_t n, int key_bits,
-                             void* scratch);
+                             void* scratch, cudaStream_t stream);
+inline gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values,
+                                    uint32_t* keys_alt, uint32_t* values_alt, uint32_t n, int key_bits,
+                                    void* scratch)
+{
+    return radix_sort_pairs(ctx, keys, values, keys_alt, values_alt, n, key_bits, scratch, ctx->stream);
+}
 
-// traverse.cu
+// traverse.cu: `scratch` (trace_scratch_bytes(n) bytes, may be null when rays are not
+// reordered) holds the ray order.
+size_t trace_scratch_bytes(uint32_t n);
 gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
-                  gbrt_hit* d_hits, bool any_hit, cudaStream_t stream);
+                  gbrt_hit* d_hits, bool any_hit, cudaStream_t stream, void* scratch = nullptr,
+                  size_t scratch_bytes = 0);
 
 } // namespace gbrt
 

@@ -497,9 +497,18 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
                                                         arrivals, bvh->tris, root_height, ctx->d_status);
         GBRT_LAUNCH_CHECK(ctx, "refit_and_emit");
         uint32_t h = 0;
+        bvh2_node root;
         GBRT_CUDA(ctx, cudaMemcpyAsync(&h, root_height, 4, cudaMemcpyDeviceToHost, s));
+        GBRT_CUDA(ctx, cudaMemcpyAsync(&root, bvh->nodes, sizeof(root), cudaMemcpyDeviceToHost, s));
         GBRT_CUDA(ctx, cudaStreamSynchronize(s));
         bvh->height = h;
+        // scene bounds: the union of the root's two child boxes
+        bvh->lo[0] = std::min(root.xy0.x, root.xy1.x);
+        bvh->hi[0] = std::max(root.xy0.y, root.xy1.y);
+        bvh->lo[1] = std::min(root.xy0.z, root.xy1.z);
+        bvh->hi[1] = std::max(root.xy0.w, root.xy1.w);
+        bvh->lo[2] = std::min(root.z01.x, root.z01.z);
+        bvh->hi[2] = std::max(root.z01.y, root.z01.w);
     }
     else
     {
@@ -688,6 +697,11 @@ gbrt_status upload_bvh2(gbrt_context* ctx, gbrt_bvh_node const* nodes, uint32_t 
 
     bvh->num_inner = uint32_t(out_nodes.size());
     bvh->root = nodes[0].num_prims != 0 ? leaf_ref[0] : 0;
+    for (int a = 0; a < 3; ++a)
+    {
+        bvh->lo[a] = nodes[0].bbox_min[a];
+        bvh->hi[a] = nodes[0].bbox_max[a];
+    }
     bvh->height = height;
     bvh->num_prims = uint32_t(out_tris.size());
     if (height + 1 > uint32_t(kStackSize))

@@ -262,7 +262,7 @@ size_t radix_sort_scratch_bytes(uint32_t n)
 }
 
 gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values, uint32_t* keys_alt,
-                             uint32_t* values_alt, uint32_t n, int key_bits, void* scratch)
+                             uint32_t* values_alt, uint32_t n, int key_bits, void* scratch, cudaStream_t stream)
 {
     if (n == 0) return GBRT_OK;
     const uint32_t tiles = num_tiles(n);
@@ -279,15 +279,15 @@ gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values
     for (int p = 0; p < passes; ++p)
     {
         int shift = p * kRadixBits;
-        count_digits<<<tiles, kThreads, 0, ctx->stream>>>(kin, n, shift, counts, tiles);
+        count_digits<<<tiles, kThreads, 0, stream>>>(kin, n, shift, counts, tiles);
         GBRT_LAUNCH_CHECK(ctx, "count_digits");
-        scan_chunk_sums<<<chunks, kScanBlock, 0, ctx->stream>>>(counts, len, sums);
+        scan_chunk_sums<<<chunks, kScanBlock, 0, stream>>>(counts, len, sums);
         GBRT_LAUNCH_CHECK(ctx, "scan_chunk_sums");
-        scan_sums<<<1, kScanBlock, 0, ctx->stream>>>(sums, chunks);
+        scan_sums<<<1, kScanBlock, 0, stream>>>(sums, chunks);
         GBRT_LAUNCH_CHECK(ctx, "scan_sums");
-        scan_apply<<<chunks, kScanBlock, 0, ctx->stream>>>(counts, len, sums);
+        scan_apply<<<chunks, kScanBlock, 0, stream>>>(counts, len, sums);
         GBRT_LAUNCH_CHECK(ctx, "scan_apply");
-        scatter_digits<<<tiles, kThreads, 0, ctx->stream>>>(kin, vin, kout, vout, n, shift, counts,
+        scatter_digits<<<tiles, kThreads, 0, stream>>>(kin, vin, kout, vout, n, shift, counts,
                                                             tiles, 0);
         GBRT_LAUNCH_CHECK(ctx, "scatter_digits");
         std::swap(kin, kout);
@@ -295,8 +295,8 @@ gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values
     }
     if (kin != keys)
     {
-        GBRT_CUDA(ctx, cudaMemcpyAsync(keys, kin, size_t(n) * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-        GBRT_CUDA(ctx, cudaMemcpyAsync(values, vin, size_t(n) * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        GBRT_CUDA(ctx, cudaMemcpyAsync(keys, kin, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream));
+        GBRT_CUDA(ctx, cudaMemcpyAsync(values, vin, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream));
     }
     return GBRT_OK;
 }

@@ -33,6 +33,7 @@ SIGNATURES = {
     "gbrt_context_synchronize": (_i32, [_vp]),
     "gbrt_last_error": (ctypes.c_char_p, [_vp]),
     "gbrt_kernel_launch_count": (_u64, [_vp]),
+    "gbrt_context_set_trace_flags": (_i32, [_vp, _u32]),
     "gbrt_bvh_build_lbvh": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_build_lbvh_host": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_upload_bvh2_host": (_i32, [_vp, _vp, _u32, _vp, _u32, _vp, _u32, _pp]),
@@ -111,6 +112,12 @@ class Context:
 
     def synchronize(self):
         self.check(self.lib.gbrt_context_synchronize(self.h))
+
+    TRACE_SORT_RAYS = 1
+
+    def set_trace_flags(self, flags):
+        """GBRT_TRACE_* options of the ray queries (TRACE_SORT_RAYS: coherent order)."""
+        self.check(self.lib.gbrt_context_set_trace_flags(self.h, int(flags)))
 
     @property
     def launches(self):
