@@ -378,7 +378,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
     p.add_argument("--trace-flags", type=int, default=1,
-                   help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order)")
+                   help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order, 2: 4-wide nodes)")
     # smaller cases for profiling captures only; the benchmark is the default size
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--origins", type=int, default=ORIGINS)

@@ -110,6 +110,11 @@ int         gbrt_abi_version(void);
  * cell of their origin before tracing, so that a warp's rays share their upper tree
  * path; hits are still returned per input ray and are identical bit for bit.        */
 #define GBRT_TRACE_SORT_RAYS 1u
+/* With this flag set when gbrt_bvh_build_lbvh runs, the tree is also collapsed into
+ * 4-wide nodes (leaves of up to 4 triangles), and queries on a context with the flag
+ * traverse those instead of the binary node pairs.  Off by default: on the 8.4M-
+ * triangle heightfield the 128-byte 4-wide nodes trace slower than the 64-byte pairs. */
+#define GBRT_TRACE_WIDE_NODES 2u
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
 
 /* ------------------------------------------------------------------------------ */

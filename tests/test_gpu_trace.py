@@ -170,3 +170,17 @@ def test_sorted_ray_order_gives_identical_hits():
     assert plain[0].tobytes() == srt[0].tobytes()
     assert plain[1].tobytes() == srt[1].tobytes()
     assert host.tobytes() == plain[0].tobytes()
+
+
+def test_wide_and_binary_nodes_agree(oracle):
+    """The 4-wide collapse changes the traversal, not the answers."""
+    tris = scenes.heightfield(grid=256, seed=5)
+    closest, ao = scenes.surface_rays(tris, 1 << 16, seed=11)
+    ctx = vg.Context(0)
+    ctx.set_trace_flags(ctx.TRACE_WIDE_NODES)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    wide_c, wide_a = trace(bvh, closest), trace(bvh, ao, any_hit=True)
+    ctx.set_trace_flags(0)
+    bin_c, bin_a = trace(bvh, closest), trace(bvh, ao, any_hit=True)
+    compare_closest(wide_c, bin_c, closest, tris, oracle)
+    assert ((wide_a["prim_id"] != NO_HIT) == (bin_a["prim_id"] != NO_HIT)).all()

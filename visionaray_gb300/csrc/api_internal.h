@@ -75,6 +75,10 @@ struct gbrt_bvh
     // Scene bounds (the root box), used to order rays by origin.
     float lo[3] = { 0.0f, 0.0f, 0.0f };
     float hi[3] = { 0.0f, 0.0f, 0.0f };
+    // 4-wide tree collapsed from the node pairs (LBVH only; null: traverse the pairs).
+    gbrt::bvh4_node* nodes4 = nullptr;
+    uint32_t num_nodes4 = 0;
+    uint32_t leaf_max4 = 0;
 };
 
 namespace gbrt {

@@ -43,4 +43,20 @@ static_assert(sizeof(tri48) == 48, "triangle is 48 bytes");
 constexpr uint32_t kLastInLeaf = 1u;
 constexpr int kStackSize = 64;   // traversal stack entries (tree height must stay below)
 
+// 4-wide node (128 bytes = eight 128-bit loads), collapsed from the node pairs: the
+// six box planes of the four children in SoA form, so one float4 per plane serves all
+// four slab tests.  count[k] > 0: leaf of count[k] contiguous triangles starting at
+// child[k]; count[k] == 0: inner child, child[k] indexes the 4-wide nodes; count[k] < 0:
+// empty slot.
+struct __align__(16) bvh4_node
+{
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 child;
+    int4 count;
+};
+static_assert(sizeof(bvh4_node) == 128, "4-wide node is 128 bytes");
+
+constexpr int kStack4 = 96;        // 4-wide traversal stack entries (up to 3 per level)
+constexpr int kLeafMax4 = 4;       // triangles per 4-wide leaf (default)
+
 } // namespace gbrt

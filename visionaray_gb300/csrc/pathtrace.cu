@@ -143,9 +143,8 @@ __global__ void __launch_bounds__(kBlock) pt_raygen(frame_buffers fb, uint32_t w
     fb.rng_flags[i] = make_uint2(2u, kLastSpecular);
 }
 
-__global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, const bvh2_node* __restrict__ nodes,
-                                                    const tri48* __restrict__ tris, int32_t root, int32_t num_inner,
-                                                    int32_t num_tris, uint32_t* __restrict__ status)
+template <bool Wide>
+__global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, bvh_view v, uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i == 0)
@@ -157,8 +156,7 @@ __global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, con
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
     float4 r0 = rp[0], r1 = rp[1];
-    trace_result h = traverse_bvh<false>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
-                                         { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = traverse_view<false, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     fb.hits[i] = make_uint4(uint32_t(h.tri), __float_as_uint(h.t), 0u, 0u);
 }
 
@@ -373,17 +371,15 @@ __global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shad
     }
 }
 
-__global__ void __launch_bounds__(kBlock) pt_shadow(frame_buffers fb, const bvh2_node* __restrict__ nodes,
-                                                    const tri48* __restrict__ tris, int32_t root, int32_t num_inner,
-                                                    int32_t num_tris, uint32_t* __restrict__ status)
+template <bool Wide>
+__global__ void __launch_bounds__(kBlock) pt_shadow(frame_buffers fb, bvh_view v, uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     uint32_t n = fb.counts[2];
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(&fb.shadow_rays[i]);
     float4 r0 = rp[0], r1 = rp[1];
-    trace_result h = traverse_bvh<true>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
-                                        { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = traverse_view<true, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     if (h.tri < 0)
     {
         uint32_t p = fb.shadow_path[i];
@@ -610,6 +606,8 @@ extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene con
                             p.background[2] * p.background[3], 1.0f);
     const uint32_t blocks = (n + kBlock - 1) / kBlock;
     cudaStream_t s = ctx->stream;
+    const bvh_view v = view_of(bvh);
+    const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     for (uint32_t smp = 0; smp < p.spp; ++smp)
     {
         sp.sample = smp;
@@ -621,15 +619,19 @@ extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene con
             for (uint32_t b = 0; b < p.num_bounces; ++b)
             {
                 sp.bounce = b;
-                pt_extend<<<blocks, kBlock, 0, s>>>(fb, q, bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
-                                                    int32_t(bvh->num_prims), ctx->d_status);
+                if (wide)
+                    pt_extend<true><<<blocks, kBlock, 0, s>>>(fb, q, v, ctx->d_status);
+                else
+                    pt_extend<false><<<blocks, kBlock, 0, s>>>(fb, q, v, ctx->d_status);
                 GBRT_LAUNCH_CHECK(ctx, "pt_extend");
                 pt_shade<<<blocks, kBlock, 0, s>>>(fb, q, sp, ctx->d_status);
                 GBRT_LAUNCH_CHECK(ctx, "pt_shade");
                 if (scene->num_lights > 0)
                 {
-                    pt_shadow<<<blocks, kBlock, 0, s>>>(fb, bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
-                                                        int32_t(bvh->num_prims), ctx->d_status);
+                    if (wide)
+                        pt_shadow<true><<<blocks, kBlock, 0, s>>>(fb, v, ctx->d_status);
+                    else
+                        pt_shadow<false><<<blocks, kBlock, 0, s>>>(fb, v, ctx->d_status);
                     GBRT_LAUNCH_CHECK(ctx, "pt_shadow");
                 }
                 q ^= 1;

@@ -14,11 +14,8 @@ namespace {
 
 constexpr int kTraceBlock = 128;
 
-template <bool AnyHit>
-__global__ void __launch_bounds__(kTraceBlock) trace_rays(const bvh2_node* __restrict__ nodes,
-                                                          const tri48* __restrict__ tris, int32_t root,
-                                                          int32_t num_inner, int32_t num_tris,
-                                                          const gbrt_ray* __restrict__ rays, uint32_t n,
+template <bool AnyHit, bool Wide>
+__global__ void __launch_bounds__(kTraceBlock) trace_rays(bvh_view v, const gbrt_ray* __restrict__ rays, uint32_t n,
                                                           gbrt_hit* __restrict__ hits,
                                                           uint32_t* __restrict__ status)
 {
@@ -27,20 +24,16 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays(const bvh2_node* __res
 
     float4 r0 = ldg4(&rays[i]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
-    trace_result h = traverse_bvh<AnyHit>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
-                                          { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
-    uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&tris[h.tri].t0).w) : GBRT_NO_HIT;
+    trace_result h = traverse_view<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[i] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
 }
 
 // Rays in the order perm[0..n): ray j = perm[i] writes hit j.
-template <bool AnyHit>
-__global__ void __launch_bounds__(kTraceBlock) trace_rays_permuted(const bvh2_node* __restrict__ nodes,
-                                                                   const tri48* __restrict__ tris, int32_t root,
-                                                                   int32_t num_inner, int32_t num_tris,
-                                                                   const gbrt_ray* __restrict__ rays, uint32_t n,
-                                                                   const uint32_t* __restrict__ perm,
+template <bool AnyHit, bool Wide>
+__global__ void __launch_bounds__(kTraceBlock) trace_rays_permuted(bvh_view v, const gbrt_ray* __restrict__ rays,
+                                                                   uint32_t n, const uint32_t* __restrict__ perm,
                                                                    gbrt_hit* __restrict__ hits,
                                                                    uint32_t* __restrict__ status)
 {
@@ -54,9 +47,8 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_permuted(const bvh2_no
     }
     float4 r0 = ldg4(&rays[j]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[j]) + 1);
-    trace_result h = traverse_bvh<AnyHit>(nodes, tris, root, num_inner, num_tris, { r0.x, r0.y, r0.z },
-                                          { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
-    uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&tris[h.tri].t0).w) : GBRT_NO_HIT;
+    trace_result h = traverse_view<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[j] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
 }
@@ -110,6 +102,8 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         GBRT_LAUNCH_CHECK(ctx, "write_misses");
         return GBRT_OK;
     }
+    const bvh_view v = view_of(bvh);
+    const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     if ((ctx->trace_flags & GBRT_TRACE_SORT_RAYS) && n >= kSortMinRays && scratch &&
         scratch_bytes >= trace_scratch_bytes(n))
     {
@@ -129,24 +123,20 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
                                           stream);
         if (st != GBRT_OK) return st;
         const uint32_t* perm = vals;   // radix_sort_pairs leaves the result in (keys, values)
-        if (any_hit)
-            trace_rays_permuted<true><<<blocks, kTraceBlock, 0, stream>>>(
-                bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner), int32_t(bvh->num_prims), d_rays, n, perm,
-                d_hits, ctx->d_status);
+        auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
+                                                                                    ctx->d_status); };
+        if (wide)
+            any_hit ? launch(trace_rays_permuted<true, true>) : launch(trace_rays_permuted<false, true>);
         else
-            trace_rays_permuted<false><<<blocks, kTraceBlock, 0, stream>>>(
-                bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner), int32_t(bvh->num_prims), d_rays, n, perm,
-                d_hits, ctx->d_status);
+            any_hit ? launch(trace_rays_permuted<true, false>) : launch(trace_rays_permuted<false, false>);
         GBRT_LAUNCH_CHECK(ctx, "trace_rays_permuted");
         return GBRT_OK;
     }
-    if (any_hit)
-        trace_rays<true><<<blocks, kTraceBlock, 0, stream>>>(bvh->nodes, bvh->tris, bvh->root, int32_t(bvh->num_inner),
-                                                             int32_t(bvh->num_prims), d_rays, n, d_hits, ctx->d_status);
+    auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, d_hits, ctx->d_status); };
+    if (wide)
+        any_hit ? launch(trace_rays<true, true>) : launch(trace_rays<false, true>);
     else
-        trace_rays<false><<<blocks, kTraceBlock, 0, stream>>>(bvh->nodes, bvh->tris, bvh->root,
-                                                              int32_t(bvh->num_inner), int32_t(bvh->num_prims), d_rays,
-                                                              n, d_hits, ctx->d_status);
+        any_hit ? launch(trace_rays<true, false>) : launch(trace_rays<false, false>);
     GBRT_LAUNCH_CHECK(ctx, "trace_rays");
     return GBRT_OK;
 }

@@ -118,4 +118,154 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
     return best;
 }
 
+// The same query over the 4-wide nodes (bvh_layout.cuh): one eight-load node fetch
+// tests four boxes; hit leaves are tested at once (so best.t shrinks before the
+// inner children are ordered), the hit inner children are visited nearest first and
+// the others pushed with their entry distance, so a popped entry already beyond the
+// best hit is dropped without a fetch.
+template <bool AnyHit>
+__device__ __forceinline__ trace_result traverse_bvh4(const bvh4_node* __restrict__ nodes4, int32_t num_nodes4,
+                                                      const tri48* __restrict__ tris, int32_t num_tris, f3 o, f3 d,
+                                                      float tmin, float tmax, uint32_t* __restrict__ status)
+{
+    const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
+    trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
+    int stack_node[kStack4];
+    float stack_t[kStack4];
+    int sp = 0;
+    int node = 0;
+
+    while (true)
+    {
+        if (node < 0 || node >= num_nodes4)
+        {
+            atomicOr(status, kStatusBadIndex);
+            break;
+        }
+        const bvh4_node* np = nodes4 + node;
+        float4 lox = ldg4(&np->lox), hix = ldg4(&np->hix);
+        float4 loy = ldg4(&np->loy), hiy = ldg4(&np->hiy);
+        float4 loz = ldg4(&np->loz), hiz = ldg4(&np->hiz);
+        int4 ch4 = __ldg(&np->child);
+        int4 ct4 = __ldg(&np->count);
+        const float lx[4] = { lox.x, lox.y, lox.z, lox.w }, hx[4] = { hix.x, hix.y, hix.z, hix.w };
+        const float ly[4] = { loy.x, loy.y, loy.z, loy.w }, hy[4] = { hiy.x, hiy.y, hiy.z, hiy.w };
+        const float lz[4] = { loz.x, loz.y, loz.z, loz.w }, hz[4] = { hiz.x, hiz.y, hiz.z, hiz.w };
+        const int ch[4] = { ch4.x, ch4.y, ch4.z, ch4.w };
+        const int ct[4] = { ct4.x, ct4.y, ct4.z, ct4.w };
+        float tn[4];
+        bool hit[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            float x0 = (lx[k] - o.x) * ix, x1 = (hx[k] - o.x) * ix;
+            float y0 = (ly[k] - o.y) * iy, y1 = (hy[k] - o.y) * iy;
+            float z0 = (lz[k] - o.z) * iz, z1 = (hz[k] - o.z) * iz;
+            tn[k] = fmaxf(tmin, fmaxf(fminf(x0, x1), fmaxf(fminf(y0, y1), fminf(z0, z1))));
+            float tf = fminf(tmax, fminf(fmaxf(x0, x1), fminf(fmaxf(y0, y1), fmaxf(z0, z1))));
+            hit[k] = ct[k] >= 0 && tf >= tn[k] && tn[k] < best.t;
+        }
+        // leaves first
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (!hit[k] || ct[k] <= 0) continue;
+            int end = ch[k] + ct[k];
+            if (ch[k] < 0 || end > num_tris)
+            {
+                atomicOr(status, kStatusBadIndex);
+                continue;
+            }
+            for (int t = ch[k]; t < end; ++t)
+            {
+                const tri48* tp = tris + t;
+                float4 t0 = ldg4(&tp->t0);
+                float4 t1 = ldg4(&tp->t1);
+                float4 t2 = ldg4(&tp->t2);
+                tri_hit h = intersect_triangle(o, d, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z },
+                                               { t2.x, t2.y, t2.z });
+                if (h.hit && h.t < best.t && h.t >= tmin && h.t <= tmax)
+                {
+                    best = { t, h.t, h.u, h.v };
+                    if (AnyHit) return best;
+                }
+            }
+        }
+        // inner children nearest first: a 4-element insertion order by entry distance
+        int order[4];
+        float dist[4];
+        int m = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (!hit[k] || ct[k] != 0 || !(tn[k] < best.t)) continue;
+            int pos = m;
+            while (pos > 0 && dist[pos - 1] > tn[k])
+            {
+                dist[pos] = dist[pos - 1];
+                order[pos] = order[pos - 1];
+                --pos;
+            }
+            dist[pos] = tn[k];
+            order[pos] = ch[k];
+            ++m;
+        }
+        if (m > 0)
+        {
+            for (int j = m - 1; j >= 1; --j)
+            {
+                if (sp < kStack4)
+                {
+                    stack_node[sp] = order[j];
+                    stack_t[sp] = dist[j];
+                    ++sp;
+                }
+                else
+                {
+                    atomicOr(status, kStatusStackOverflow);
+                }
+            }
+            node = order[0];
+            continue;
+        }
+        // pop the next entry still in front of the best hit
+        node = -1;
+        while (sp > 0)
+        {
+            --sp;
+            if (stack_t[sp] < best.t)
+            {
+                node = stack_node[sp];
+                break;
+            }
+        }
+        if (node < 0) break;
+    }
+    return best;
+}
+
+// Everything a query needs from a BVH handle, passed to kernels by value.
+struct bvh_view
+{
+    const bvh2_node* nodes;
+    const bvh4_node* nodes4;
+    const tri48* tris;
+    int32_t root, num_inner, num_nodes4, num_tris;
+};
+
+inline bvh_view view_of(gbrt_bvh const* b)
+{
+    return { b->nodes, b->nodes4, b->tris, b->root, int32_t(b->num_inner), int32_t(b->num_nodes4),
+             int32_t(b->num_prims) };
+}
+
+// Wide: the 4-wide nodes (present for trees with inner nodes built by the LBVH builder).
+template <bool AnyHit, bool Wide>
+__device__ __forceinline__ trace_result traverse_view(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
+                                                      uint32_t* __restrict__ status)
+{
+    if (Wide) return traverse_bvh4<AnyHit>(v.nodes4, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
+    return traverse_bvh<AnyHit>(v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax, status);
+}
+
 } // namespace gbrt

@@ -114,6 +114,7 @@ class Context:
         self.check(self.lib.gbrt_context_synchronize(self.h))
 
     TRACE_SORT_RAYS = 1
+    TRACE_WIDE_NODES = 2
 
     def set_trace_flags(self, flags):
         """GBRT_TRACE_* options of the ray queries (TRACE_SORT_RAYS: coherent order)."""
