@@ -244,8 +244,9 @@ typedef struct gbrt_camera
 /* One frame of the jittered-blend pixel sampler (pixel_sampler_types.h,
  * detail/sched_common.h:427-526) around pathtracing::kernel (pathtracing.inl:42-233):
  * per pixel, spp jittered samples are averaged, then accum = sfactor * average +
- * dfactor * accum, and color = accum.  Random numbers come from gbrt_rng.h with
- * (frame_id, pixel = y * width + x, sample).                                      */
+ * dfactor * accum, and color = accum (dfactor == 0 overwrites accum without reading
+ * it).  Random numbers come from gbrt_rng.h with (frame_id, pixel = y * width + x,
+ * sample).                                                                        */
 typedef struct gbrt_pt_params
 {
     uint32_t width;
@@ -268,6 +269,10 @@ typedef struct gbrt_pt_params
  * FP64).  Without this flag the kernel reproduces that behaviour bit for bit; with it
  * shadow rays end at distance - 2 * epsilon, as the reference evidently intends.     */
 #define GBRT_PT_SHADOW_RANGE_FIX 1u
+/* Disables Russian roulette (pathtracing.inl:201-213): paths run to num_bounces.  The
+ * differentiable renderer uses it so that finite differences at common random numbers
+ * are smooth in the albedos (a roulette decision would jump).                     */
+#define GBRT_PT_NO_RUSSIAN_ROULETTE 2u
 
 typedef struct gbrt_pt_scene gbrt_pt_scene;
 
@@ -288,6 +293,30 @@ gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene);
 gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene const* scene,
                                  gbrt_camera const* camera, gbrt_pt_params const* params,
                                  float* d_accum, float* d_color);
+
+/* Differentiable rendering (no visionaray counterpart: the reference has no adjoint).
+ * Parameters are per material slot (geom_id), 3 floats each, in device memory: the
+ * albedo of matte slots (replacing their color; scale stays kd) and the emission of
+ * emissive slots (replacing ce; scale stays ls); an area light whose triangle's
+ * geom_id is an emissive slot shines emission[geom_id] * kl.
+ * forward: one frame of the path tracer with those parameters; d_image (RGBA32F)
+ * receives the per-pixel sample average (sfactor/dfactor are ignored).           */
+gbrt_status gbrt_pathtrace_forward(gbrt_context* ctx, gbrt_pt_scene const* scene,
+                                   gbrt_camera const* camera, gbrt_pt_params const* params,
+                                   const float* d_albedo, const float* d_emission, float* d_image);
+
+/* backward: path-replay backpropagation of an image adjoint d_image_adjoint = dL/dI
+ * (RGBA32F, alpha ignored) into d_grad_albedo and d_grad_emission (3 floats per slot,
+ * ADDED to; zero them first).  Each (pixel, sample) path is re-traced from its random
+ * numbers -- the same shading code as the forward frame, so the same path -- and its
+ * vertices swept backwards; nothing of the forward frame is stored (memory O(pixels)).
+ * Gradients are accumulated with warp-reduced FP32 atomics.  Geometry, visibility and
+ * roulette decisions are not differentiated.  num_bounces <= 16.                  */
+gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene const* scene,
+                                    gbrt_camera const* camera, gbrt_pt_params const* params,
+                                    const float* d_albedo, const float* d_emission,
+                                    const float* d_image_adjoint, float* d_grad_albedo,
+                                    float* d_grad_emission);
 
 /* Number of kernels the library launched on this context since creation (the
  * count covers every kernel of every call).                                        */

@@ -73,6 +73,8 @@ class Oracle:
         L.orc_trace.restype = _i32
         L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
         L.orc_pathtrace.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp, _vp]
+        L.orc_pathtrace_adjoint.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _vp, _vp,
+                                            _i32, _i32, _vp, _vp, _vp]
         self.L = L
 
     def _tree(self, h):
@@ -152,6 +154,27 @@ class Oracle:
                              len(materials), _p(lights), len(lights), _p(camera), _p(params), int(mode), nthreads,
                              _p(out), _p(cnt))
         return out, cnt
+
+    def pathtrace_adjoint(self, tree, tris, materials, lights, camera, params, albedo, emission, img_adj,
+                          fp64=True, nthreads=0):
+        """(grad_albedo, grad_emission, image): the path-replay adjoint of sum(I * img_adj)
+        (img_adj (h, w, 4)) at the gbrt_rng.h stream, in double (fp64) or float."""
+        tris = np.ascontiguousarray(tris)
+        materials = np.ascontiguousarray(materials, MATERIAL)
+        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+        params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+        w, h = int(params["width"][0]), int(params["height"][0])
+        a = np.ascontiguousarray(albedo, np.float32) if albedo is not None else None
+        e = np.ascontiguousarray(emission, np.float32) if emission is not None else None
+        adj = np.ascontiguousarray(img_adj, np.float64)
+        ga = np.zeros((len(materials), 3), np.float64)
+        ge = np.zeros((len(materials), 3), np.float64)
+        img = np.zeros((h, w, 4), np.float64)
+        self.L.orc_pathtrace_adjoint(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
+                                     len(materials), _p(lights), len(lights), _p(camera), _p(params), _p(a), _p(e),
+                                     _p(adj), int(fp64), nthreads, _p(ga), _p(ge), _p(img))
+        return ga, ge, img
 
     def intersect_box(self, ray, bmin, bmax):
         ray = np.ascontiguousarray(np.asarray(ray).reshape(1))

@@ -90,6 +90,19 @@ void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32
                    const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba,
                    uint64_t* counters);
 
+/* Path-replay adjoint of the path tracer at the gbrt_rng.h stream: per-slot gradients
+ * of sum(I * img_adj) w.r.t. the albedo / emission parameters (3 per material slot;
+ * either may be NULL to use the materials' colors and skip that gradient), written to
+ * grad_albedo / grad_emission (3 * nmat doubles each); image (may be NULL) receives
+ * the rendered per-pixel average.  fp64 != 0: double arithmetic (the FP64 host
+ * adjoint); else float with the CUDA path's cos/sin.                               */
+void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
+                           const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
+                           const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                           const gbrt_pt_params* p, const float* albedo, const float* emission,
+                           const double* img_adj, int fp64, int nthreads, double* grad_albedo,
+                           double* grad_emission, double* image);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -170,6 +171,31 @@ struct pt_counters
     uint64_t closest = 0, shadow = 0, boxes = 0, tris = 0;
 };
 
+// Differentiable-renderer inputs (null: the materials' own colors) and the per-vertex
+// record the adjoint sweeps backwards.
+struct pt_params_ext
+{
+    const float* albedo = nullptr;
+    const float* emission = nullptr;
+};
+
+enum : uint32_t
+{
+    kMiss = 0,
+    kEmission = 1,
+    kMatte = 2,
+    kEnd = 3,
+};
+
+template <typename T>
+struct vrec
+{
+    uint32_t kind = kMiss, geom = 0, lgeom = 0xFFFFFFFFu, nee = 0;
+    vec<T> thr{ 0, 0, 0 };
+    T sigma = 0, mis = 0, escale = 0, kfac = 0, w = 0, x = 0, b0 = 0, kl = 0, rr = 0;
+    vec<T> lint{ 0, 0, 0 };
+};
+
 // pathtracing::kernel::operator() (detail/pathtracing.inl:42-233) for one camera ray.
 template <typename T>
 inline T trig_cos(T x, bool via_double) { return via_double ? T(std::cos(double(x))) : std::cos(x); }
@@ -179,8 +205,10 @@ inline T trig_sin(T x, bool via_double) { return via_double ? T(std::sin(double(
 template <typename T>
 vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
                 uint32_t nl, gbrt_pt_params const& p, vec<T> ori, vec<T> dir, T tmin, T tmax,
-                gbrt_sample_generator& gen, bool& first_hit, pt_counters& cnt, bool trig_double)
+                gbrt_sample_generator& gen, bool& first_hit, pt_counters& cnt, bool trig_double,
+                pt_params_ext const& ext = {}, vrec<T>* recs = nullptr, int* nrec = nullptr)
 {
+    if (nrec) *nrec = 0;
     const T inv_pi = T(3.18309886183790691216444201928e-01);
     const T pi = T(3.14159265358979323846264338328e+00);
     const T two_pi = T(6.28318530717958623199592693709e+00);
@@ -196,9 +224,15 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
     {
         hit_t<T> hr = traverse(s, ori, dir, tmin, tmax, false, cnt.boxes, cnt.tris);
         ++cnt.closest;
+        vrec<T> rec;
+        rec.thr = throughput;
         if (active && !hr.hit) intensity = intensity + ambient * throughput;
         active = active && hr.hit;
-        if (!active) break;
+        if (!active)
+        {
+            if (recs && *nrec < 16) recs[(*nrec)++] = rec;
+            break;
+        }
         if (bounce == 0) first_hit = true;
 
         tri_t<T> tri = load_tri<T>(s.tris[s.indices[hr.index]]);
@@ -206,9 +240,13 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         vec<T> isect = ori + dir * hr.t;
         vec<T> gn = normalize(cross(tri.e1, tri.e2));
         vec<T> sn = gn;
+        uint32_t geom = tri.geom_id < nmat ? tri.geom_id : 0u;
         gbrt_material m = tri.geom_id < nmat ? mats[tri.geom_id] : gbrt_material{ GBRT_MATERIAL_MATTE, { 0, 0, 0 }, 0 };
         vec<T> mcol = { T(m.color[0]), T(m.color[1]), T(m.color[2]) };
         bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+        if (!emission && ext.albedo) mcol = load<T>(ext.albedo + 3 * geom);
+        if (emission && ext.emission) mcol = load<T>(ext.emission + 3 * geom);
+        rec.geom = geom;
 
         // surf.sample(view_dir, refl_dir, brdf_pdf, inter, gen)
         vec<T> refl = { 0, 0, 0 };
@@ -254,6 +292,9 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                                                           : T(1.0);
         if (active && emission) intensity = intensity + (throughput * mis) * src;
         active = active && !emission && !zero_pdf;
+        rec.kind = emission ? kEmission : (zero_pdf ? kEnd : kMatte);
+        rec.mis = mis;
+        rec.escale = T(m.scale);
 
         vec<T> n = faceforward(sn, view_dir, gn);
         if (nl > 0)
@@ -273,6 +314,8 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             vec<T> lint = { T(lights[light_id].cl[0]) * T(lights[light_id].kl),
                             T(lights[light_id].cl[1]) * T(lights[light_id].kl),
                             T(lights[light_id].cl[2]) * T(lights[light_id].kl) };
+            uint32_t lgeom = lights[light_id].geometry.geom_id;
+            if (ext.emission && lgeom < nmat) lint = load<T>(ext.emission + 3 * lgeom) * T(lights[light_id].kl);
             vec<T> lnormal = normalize(cross(lt.e1, lt.e2));
             T larea = T(0.5) * length(cross(lt.e1, lt.e2));
             T ldotln0 = std::abs(dot(-normalize(ldir), lnormal));
@@ -300,20 +343,37 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                 vec<T> src2 = (shade * inv_pi) / ldotn;
                 T mis2 = power_heuristic(lpdf / T(float(nl)), bpdf);
                 if (active && !sh.hit && ldotn > T(0.0) && ldotln > T(0.0))
+                {
                     intensity = intensity + (((throughput * mis2) * src2) * (ldotn / lpdf)) * T(float(nl));
+                    rec.nee = 1;
+                    rec.lgeom = ext.emission ? lgeom : 0xFFFFFFFFu;
+                    rec.kl = T(lights[light_id].kl);
+                    rec.lint = lint;
+                    rec.w = mis2;
+                    rec.x = lpdf / T(float(nl));
+                    rec.b0 = dot(n2, L) * inv_pi;
+                    rec.kfac = T(m.scale) * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * T(float(nl));
+                }
             }
         }
 
         throughput = throughput * (src * (dot(n, refl) / brdf_pdf));
         if (zero_pdf) throughput = { 0, 0, 0 };
+        rec.sigma = T(m.scale) * inv_pi * (dot(n, refl) / brdf_pdf);
 
-        if (bounce >= 2)
+        if (bounce >= 2 && !(p.flags & GBRT_PT_NO_RUSSIAN_ROULETTE))
         {
             T prob = max_element(throughput);
             bool terminate = T(gen.next()) > prob;
             active = active && !terminate;
             throughput = throughput / prob;
+            rec.rr = prob;
+            if (recs && *nrec < 16) recs[(*nrec)++] = rec;
             if (!active) break;
+        }
+        else if (recs && *nrec < 16)
+        {
+            recs[(*nrec)++] = rec;
         }
         if (!active) break;   // emission / zero pdf: nothing further reaches the image
         ori = isect + refl * eps;
@@ -401,7 +461,178 @@ void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbr
     }
 }
 
+// Reverse sweep over one path's vertices (the adjoint of radiance<T>'s contributions
+// w.r.t. albedo and emission, roulette and geometry decisions held fixed).
+template <typename T>
+void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats, pt_params_ext const& ext,
+           vec<T> ambient, double* ga, double* ge)
+{
+    vec<T> tbar = { 0, 0, 0 };
+    for (int k = nrec - 1; k >= 0; --k)
+    {
+        vrec<T> const& r = recs[k];
+        gbrt_material const& m = mats[r.geom];
+        if (r.kind == kMiss)
+        {
+            tbar = adj * ambient;
+        }
+        else if (r.kind == kEnd)
+        {
+            tbar = { 0, 0, 0 };
+        }
+        else if (r.kind == kEmission)
+        {
+            vec<T> e = ext.emission ? load<T>(ext.emission + 3 * r.geom)
+                                    : vec<T>{ T(m.color[0]), T(m.color[1]), T(m.color[2]) };
+            vec<T> eb = adj * r.thr * (r.mis * r.escale);
+            if (ext.emission)
+            {
+                ge[3 * r.geom + 0] += double(eb.x);
+                ge[3 * r.geom + 1] += double(eb.y);
+                ge[3 * r.geom + 2] += double(eb.z);
+            }
+            tbar = adj * e * (r.mis * r.escale);
+        }
+        else
+        {
+            vec<T> a = ext.albedo ? load<T>(ext.albedo + 3 * r.geom)
+                                  : vec<T>{ T(m.color[0]), T(m.color[1]), T(m.color[2]) };
+            vec<T> ub = tbar;
+            if (r.rr > T(0))
+            {
+                vec<T> uu = r.thr * a * r.sigma;
+                T pr = r.rr;
+                ub = tbar / pr;
+                T pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (pr * pr);
+                if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
+                else if (uu.y >= uu.z) ub.y += pb;
+                else ub.z += pb;
+            }
+            vec<T> abar = ub * r.thr * r.sigma;
+            vec<T> tb = ub * a * r.sigma;
+            if (r.nee)
+            {
+                vec<T> f = r.lint * r.kfac;
+                abar = abar + adj * r.thr * f * r.w;
+                tb = tb + adj * a * f * r.w;
+                T wbar = adj.x * r.thr.x * a.x * f.x + adj.y * r.thr.y * a.y * f.y + adj.z * r.thr.z * a.z * f.z;
+                T yv = r.b0 * max_element(r.thr);
+                T den = r.x * r.x + yv * yv;
+                T g = wbar * (-T(2) * r.x * r.x * yv / (den * den)) * r.b0;
+                if (r.thr.x >= r.thr.y && r.thr.x >= r.thr.z) tb.x += g;
+                else if (r.thr.y >= r.thr.z) tb.y += g;
+                else tb.z += g;
+                if (r.lgeom != 0xFFFFFFFFu)
+                {
+                    vec<T> lb = adj * r.thr * a * (r.w * r.kfac * r.kl);
+                    ge[3 * r.lgeom + 0] += double(lb.x);
+                    ge[3 * r.lgeom + 1] += double(lb.y);
+                    ge[3 * r.lgeom + 2] += double(lb.z);
+                }
+            }
+            if (ext.albedo)
+            {
+                ga[3 * r.geom + 0] += double(abar.x);
+                ga[3 * r.geom + 1] += double(abar.y);
+                ga[3 * r.geom + 2] += double(abar.z);
+            }
+            tbar = tb;
+        }
+    }
+}
+
+template <typename T>
+void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+             uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, pt_params_ext const& ext,
+             const double* img_adj, int nthreads, double* grad_albedo, double* grad_emission, double* image)
+{
+    vec<T> eye = load<T>(cam.eye), center = load<T>(cam.center), up = load<T>(cam.up);
+    vec<T> f = normalize(eye - center);
+    vec<T> sv = normalize(cross(up, f));
+    vec<T> uv = cross(f, sv);
+    T fovy = T(cam.fovy_degrees) * T(1.74532925199432957692369076849e-02);
+    T aspect = T(p.width) / T(p.height);
+    T th = std::tan(fovy / T(2.0));
+    vec<T> U = sv * th * aspect, V = uv * th, W = -f;
+    const vec<T> ambient = { T(p.ambient[0]), T(p.ambient[1]), T(p.ambient[2]) };
+    uint64_t npix = uint64_t(p.width) * p.height;
+    if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::vector<double>> ga(static_cast<size_t>(nthreads), std::vector<double>(3 * size_t(nmat), 0.0));
+    std::vector<std::vector<double>> ge(static_cast<size_t>(nthreads), std::vector<double>(3 * size_t(nmat), 0.0));
+    std::atomic<uint64_t> next{ 0 };
+    auto worker = [&](int tid) {
+        pt_counters cnt;
+        vrec<T> recs[16];
+        for (;;)
+        {
+            uint64_t b = next.fetch_add(64);
+            if (b >= npix) break;
+            for (uint64_t pix = b; pix < std::min(npix, b + 64); ++pix)
+            {
+                T x = T(pix % p.width), y = T(pix / p.width);
+                vec<T> sum = { 0, 0, 0 };
+                for (uint32_t smp = 0; smp < p.spp; ++smp)
+                {
+                    gbrt_sample_generator gen{ p.frame_id, uint32_t(pix), smp, 0u };
+                    T jx = T(gen.next() - 0.5f);
+                    T jy = T(gen.next() - 0.5f);
+                    T sx = (x + jx + T(0.5)) / T(p.width);
+                    T sy = (y + jy + T(0.5)) / T(p.height);
+                    vec<T> d = normalize(U * (T(2.0) * sx - T(1.0)) + V * (T(2.0) * sy - T(1.0)) + W);
+                    bool hit = false;
+                    int nrec = 0;
+                    vec<T> c = radiance<T>(s, mats, nmat, lights, nl, p, eye, d, T(0.0), T(FLT_MAX), gen, hit, cnt,
+                                           std::is_same<T, float>::value, ext, recs, &nrec);
+                    if (!hit) continue;
+                    sum = sum + c;
+                    vec<T> adj = { T(img_adj[4 * pix + 0]) / T(float(p.spp)), T(img_adj[4 * pix + 1]) / T(float(p.spp)),
+                                   T(img_adj[4 * pix + 2]) / T(float(p.spp)) };
+                    sweep<T>(recs, nrec, adj, mats, ext, ambient, ga[size_t(tid)].data(), ge[size_t(tid)].data());
+                }
+                if (image)
+                {
+                    image[4 * pix + 0] = double(sum.x / T(float(p.spp)));
+                    image[4 * pix + 1] = double(sum.y / T(float(p.spp)));
+                    image[4 * pix + 2] = double(sum.z / T(float(p.spp)));
+                    image[4 * pix + 3] = 1.0;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
+    for (auto& t : pool) t.join();
+    for (size_t i = 0; i < 3 * size_t(nmat); ++i)
+    {
+        double a = 0.0, e = 0.0;
+        for (int t = 0; t < nthreads; ++t)
+        {
+            a += ga[size_t(t)][i];
+            e += ge[size_t(t)][i];
+        }
+        grad_albedo[i] = a;
+        grad_emission[i] = e;
+    }
+}
+
 } // namespace
+
+extern "C" void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
+                                      const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
+                                      const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                                      const gbrt_pt_params* p, const float* albedo, const float* emission,
+                                      const double* img_adj, int fp64, int nthreads, double* grad_albedo,
+                                      double* grad_emission, double* image)
+{
+    scene_arrays s{ tris, nodes, num_nodes, indices };
+    pt_params_ext ext;
+    ext.albedo = albedo;
+    ext.emission = emission;
+    if (fp64)
+        adjoint<double>(s, mats, nmat, lights, nl, *cam, *p, ext, img_adj, nthreads, grad_albedo, grad_emission, image);
+    else
+        adjoint<float>(s, mats, nmat, lights, nl, *cam, *p, ext, img_adj, nthreads, grad_albedo, grad_emission, image);
+}
 
 extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                               const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,

@@ -1,0 +1,84 @@
+"""The path-replay adjoint (gbrt_pathtrace_backward) against central finite differences
+of the GPU forward pass at common random numbers, against the oracle's FP32 and FP64
+host adjoints, and the forward pass against the plain frame.  Russian roulette is off
+and the shadow range fixed (visionaray_gb300.inverse.FLAGS) so the image is smooth in
+the albedos; tolerances are stated per test."""
+import numpy as np
+import pytest
+import torch
+
+import visionaray_gb300 as vg
+from oracle import Oracle
+from visionaray_gb300 import inverse, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    ctx = vg.Context(0)
+    tris, mats, lights = scenes.box_scene(n_blobs=2, subdiv=4, seed=1)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    scene = vg.PTScene(bvh, mats, lights)
+    albedo = torch.from_numpy(np.ascontiguousarray(mats["color"], np.float32)).cuda()
+    emission = albedo.clone()
+    params = scenes.pt_params(48, 32, 4, num_bounces=6, frame_id=7, flags=inverse.FLAGS)
+    cam = scenes.box_camera()
+    adj = torch.from_numpy(np.random.default_rng(0).normal(size=(32, 48, 4)).astype(np.float32)).cuda()
+    adj[..., 3] = 0
+    return ctx, tris, mats, lights, scene, albedo, emission, params, cam, adj
+
+
+def loss_of(scene, cam, params, albedo, emission, adj):
+    img = vg.pathtrace_forward(scene, cam, params, albedo, emission)
+    return float((img.double() * adj.double()).sum())
+
+
+def test_forward_equals_plain_frame(setup):
+    ctx, tris, mats, lights, scene, albedo, emission, params, cam, adj = setup
+    img = vg.pathtrace_forward(scene, cam, params, albedo, emission)
+    plain = vg.pathtrace_frame(scene, cam, params)
+    ctx.synchronize()
+    assert torch.equal(img, plain)
+
+
+def test_adjoint_matches_central_differences(setup):
+    ctx, tris, mats, lights, scene, albedo, emission, params, cam, adj = setup
+    ga, ge = vg.pathtrace_backward(scene, cam, params, albedo, emission, adj)
+    ctx.synchronize()
+    ga, ge = ga.cpu().numpy(), ge.cpu().numpy()
+    # parameters with a clear signal: the largest albedo gradients and the light
+    order = np.argsort(-np.abs(ga).ravel())[:12]
+    cases = [("a", int(i) // 3, int(i) % 3) for i in order] + [("e", 12, 0), ("e", 13, 1)]
+    for kind, slot, c in cases:
+        base = (albedo if kind == "a" else emission)
+        h = 1e-3 * max(1.0, float(base[slot, c]))   # 1e-3 on albedos, relative on emission (15)
+        plus, minus = base.clone(), base.clone()
+        plus[slot, c] += h
+        minus[slot, c] -= h
+        step = float(plus[slot, c] - minus[slot, c])   # the float32 perturbation actually applied
+        a_p, e_p = (plus, emission) if kind == "a" else (albedo, plus)
+        a_m, e_m = (minus, emission) if kind == "a" else (albedo, minus)
+        fd = (loss_of(scene, cam, params, a_p, e_p, adj) - loss_of(scene, cam, params, a_m, e_m, adj)) / step
+        g = float((ga if kind == "a" else ge)[slot, c])
+        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6 * np.abs(ga).max(), (kind, slot, c, g, fd)
+
+
+def test_adjoint_matches_host_adjoints(setup, oracle):
+    ctx, tris, mats, lights, scene, albedo, emission, params, cam, adj = setup
+    ga, ge = vg.pathtrace_backward(scene, cam, params, albedo, emission, adj)
+    ctx.synchronize()
+    ga, ge = ga.cpu().numpy().astype(np.float64), ge.cpu().numpy().astype(np.float64)
+    tree = oracle.build_sah(tris)
+    a_np, e_np, adj_np = albedo.cpu().numpy(), emission.cpu().numpy(), adj.cpu().numpy()
+    for fp64, tol in ((False, 1e-4), (True, 2e-3)):
+        ha, he, _ = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, a_np, e_np, adj_np, fp64=fp64)
+        rel_a = np.linalg.norm(ga - ha) / np.linalg.norm(ha)
+        rel_e = np.linalg.norm(ge - he) / np.linalg.norm(he)
+        assert rel_a <= tol and rel_e <= tol, (fp64, rel_a, rel_e)
+
+
+def test_inverse_albedo_reduces_the_loss():
+    res = inverse.optimize(steps=12, width=128, height=128, spp=4, target_spp=32)
+    assert res["losses"][-1] < 0.7 * res["losses"][0]
+    assert res["bwd_ms"] > 0 and res["fwd_ms"] > 0

@@ -8,4 +8,5 @@ from .types import (AREA_LIGHT, BVH_NODE, CAMERA, FLT_MAX, HIT, MATERIAL, NO_HIT
                     PT_PARAMS, PT_SHADOW_RANGE_FIX, RAY, TRIANGLE)
 from .runtime import (Context, GbrtError, IndexBVH, PTScene, any_hit, closest_hit,  # noqa: F401
                       default_context, device_rays, as_device_bytes, hits_to_numpy,
-                      lbvh_builder, load_library, pathtrace_frame)
+                      lbvh_builder, load_library, pathtrace_backward, pathtrace_forward,
+                      pathtrace_frame)

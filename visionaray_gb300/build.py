@@ -25,7 +25,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "lbvh.cu", "noalloc.cu", "pathtrace.cu", "radix_sort.cu", "traverse.cu"]
-CU_HEADERS = ["device_math.cuh", "bvh_layout.cuh", "api_internal.h", "traverse_core.cuh"]
+CU_HEADERS = ["device_math.cuh", "bvh_layout.cuh", "api_internal.h", "traverse_core.cuh", "lbvh_device.cuh"]
 # host code of every unit keeps expressions unfused (-ffp-contract=off) so x86-64 and
 # AArch64 hosts compute the same camera bases and copies
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",

@@ -164,210 +164,294 @@ struct shade_params
 {
     const gbrt_material* materials;
     uint32_t num_materials;
-    const float4* lights;
+    const float4* lights;   // 4 float4 per light: v1 | geom bits, e1, e2, intensity | kl
     uint32_t num_lights;
     const tri48* tris;
     int32_t num_tris;
     float epsilon;
     float3 ambient;
     uint32_t frame, sample, bounce, flags;
+    // differentiable renderer: matte colors and emissive colors (3 floats per material
+    // slot) replacing the materials' own; light intensity = emission[geom] * kl
+    const float* albedo;
+    const float* emission;
 };
 
-// One bounce of pathtracing::kernel::operator() (detail/pathtracing.inl:65-221) for every
-// live path.
-__global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shade_params sp,
-                                                   uint32_t* __restrict__ status)
+struct path_state
+{
+    v3 thr, rad;
+    uint32_t k, flags;
+};
+
+// What the adjoint needs of one path vertex (the throughput entering it and the
+// albedo-independent factors of its contributions).
+enum : uint32_t
+{
+    kVertexMiss = 0,
+    kVertexEmission = 1,
+    kVertexMatte = 2,
+    kVertexEnd = 3,   // matte with a zero pdf: the path stops without contributing
+};
+
+struct vertex_rec
+{
+    uint32_t kind, geom, lgeom, nee;
+    v3 thr;
+    float sigma;      // matte: next throughput = thr * albedo * sigma
+    float mis;        // emission: contribution = thr * mis * emission * scale
+    float escale;     // emission: material scale (ls)
+    float kfac;       // NEE: contribution = w * thr * albedo * lint * kfac
+    float w, x, b0;   // NEE: w = power_heuristic(x, b0 * max(thr))
+    float kl;         // NEE: lint = emission[lgeom] * kl
+    v3 lint;
+    float rr;         // Russian roulette normaliser (0: none)
+};
+
+struct vertex_out
+{
+    bool cont, shadow;
+    v3 next_o, next_d;
+    v3 sh_o, sh_d;
+    float sh_tmax;
+    v3 contrib;
+    vertex_rec rec;
+};
+
+__device__ __forceinline__ v3 param3(const float* a, uint32_t i) { return { a[3 * i], a[3 * i + 1], a[3 * i + 2] }; }
+
+// One bounce of pathtracing::kernel::operator() (detail/pathtracing.inl:65-221) for one
+// path whose ray (ori, dir) hit triangle `tri` at `t` (tri < 0: missed).  Updates the
+// path state, adds emission / ambient to st.rad, and returns the next ray and the NEE
+// shadow ray with its unoccluded contribution.  Shared by the wavefront shade kernel
+// and the adjoint's replay, so both compute bit-identical paths.
+__device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p, uint32_t bounce, v3 ori, v3 dir,
+                                             float tmin, float tmax, int tri, float t, path_state& st,
+                                             vertex_out& out, uint32_t* __restrict__ status)
 {
     const float inv_pi = 3.18309886183790691216444201928e-01f;
     const float pi = 3.14159265358979323846264338328e+00f;
     const float two_pi = 6.28318530717958623199592693709e+00f;
+    out.cont = false;
+    out.shadow = false;
+    vertex_rec& rec = out.rec;
+    rec.kind = kVertexMiss;
+    rec.thr = st.thr;
+    rec.nee = 0;
+    rec.rr = 0.0f;
+    rec.geom = 0;
+    rec.lgeom = 0xFFFFFFFFu;
 
+    if (tri < 0 || tri >= sp.num_tris)
+    {
+        // the ray left the scene: ambient light (pathtracing.inl:71-79)
+        v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
+        st.rad = st.rad + amb * st.thr;
+        return;
+    }
+    if (bounce == 0) st.flags |= kFirstHit;
+    float4 t1 = ldg4(&sp.tris[tri].t1);
+    float4 t2 = ldg4(&sp.tris[tri].t2);
+    v3 e1 = xyz(t1), e2 = xyz(t2);
+    uint32_t geom = __float_as_uint(t1.w);
+    v3 view = -dir;
+    v3 isect = ori + dir * t;
+    v3 gn = normalize3(cross3(e1, e2));
+    v3 sn = gn;
+    gbrt_material m;
+    if (geom < sp.num_materials)
+    {
+        m = sp.materials[geom];
+    }
+    else
+    {
+        atomicOr(status, kStatusBadIndex);
+        m = gbrt_material{ GBRT_MATERIAL_MATTE, { 0.0f, 0.0f, 0.0f }, 0.0f };
+        geom = 0;
+    }
+    bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+    v3 mcol = { m.color[0], m.color[1], m.color[2] };
+    if (!emission && sp.albedo) mcol = param3(sp.albedo, geom);
+    if (emission && sp.emission) mcol = param3(sp.emission, geom);
+    rec.geom = geom;
+
+    v3 refl = { 0.0f, 0.0f, 0.0f };
+    float brdf_pdf;
+    v3 src;
+    if (!emission)
+    {
+        // matte::sample -> lambertian::sample_f (matte.inl:40-56, brdf.h:50-76)
+        v3 nn = faceforward3(sn, view, gn);
+        v3 w = nn;
+        v3 v = fabsf(w.x) > fabsf(w.y) ? normalize3(v3{ -w.z, 0.0f, w.x }) : normalize3(v3{ 0.0f, w.z, -w.y });
+        v3 u = cross3(v, w);
+        // cosine_sample_hemisphere(gen.next(), gen.next()), second argument drawn
+        // first as in the reference build (sampling.h:117-127)
+        float u2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float u1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float r = sqrtf(u1);
+        float theta = two_pi * u2;
+        // cos and sin evaluated in double and rounded once to float
+        float ct = float(cos(double(theta)));
+        float sth = float(sin(double(theta)));
+        v3 s3 = { r * ct, r * sth, sqrtf(1.0f - u1) };
+        refl = normalize3(u * s3.x + v * s3.y + w * s3.z);
+        brdf_pdf = dot3(nn, refl) * inv_pi;
+        src = (mcol * m.scale) * inv_pi;
+    }
+    else
+    {
+        brdf_pdf = 1.0f;   // emissive::sample (emissive.inl:28-44)
+        src = mcol * m.scale;
+    }
+    bool zero_pdf = brdf_pdf <= 0.0f;
+
+    float light_pdf = 0.0f;
+    if (sp.num_lights > 0 && emission)
+    {
+        float A = 0.5f * length3(cross3(e1, e2));
+        float ld = length3(isect - ori);
+        v3 L = normalize3(isect - ori);
+        float ldotln = fabsf(dot3(-L, gn));
+        float solid_angle = (ldotln * A) / (ld * ld);
+        light_pdf = 1.0f / solid_angle;
+    }
+    float mis = (bounce > 0 && sp.num_lights > 0 && !(st.flags & kLastSpecular))
+                    ? power_heuristic(brdf_pdf, light_pdf / float(sp.num_lights))
+                    : 1.0f;
+    if (emission)
+    {
+        st.rad = st.rad + (st.thr * mis) * src;
+        rec.kind = kVertexEmission;
+        rec.mis = mis;
+        rec.escale = m.scale;
+        return;
+    }
+    if (zero_pdf)
+    {
+        rec.kind = kVertexEnd;
+        return;
+    }
+    rec.kind = kVertexMatte;
+    v3 nn = faceforward3(sn, view, gn);
+    if (sp.num_lights > 0)
+    {
+        // sample_random_light + area_light::sample + sample_surface
+        // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
+        float ul = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        int lid = int(ul * float(sp.num_lights));
+        if (lid >= int(sp.num_lights)) lid = int(sp.num_lights) - 1;
+        const float4* lp = sp.lights + 4 * lid;
+        float4 l0 = lp[0], l3 = lp[3];
+        v3 lv1 = xyz(l0), le1 = xyz(lp[1]), le2 = xyz(lp[2]), lint = xyz(l3);
+        uint32_t lgeom = __float_as_uint(l0.w);
+        if (sp.emission && lgeom < sp.num_materials) lint = param3(sp.emission, lgeom) * l3.w;
+        float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
+        float sq = sqrtf(s1);
+        v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
+        v3 ldir = pos - isect;
+        float dist = length3(ldir);
+        v3 lnormal = normalize3(cross3(le1, le2));
+        float larea = 0.5f * length3(cross3(le1, le2));
+        float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
+        float lsolid = (ldotln0 * larea) / (dist * dist);
+        float lpdf = 1.0f / lsolid;
+        v3 L = normalize3(ldir);
+        v3 ln = faceforward3(lnormal, -L, lnormal);
+        float ldotn = dot3(L, nn);
+        float ldotln = fabsf(dot3(-L, ln));
+        float bpdf0 = dot3(nn, L) * inv_pi;
+        float bpdf = bpdf0 * max_elem(st.thr);
+        float ndotl = fmaxf(0.0f, dot3(nn, L));
+        v3 cd = (mcol * m.scale) * inv_pi;
+        v3 shade = ((cd * pi) * lint) * ndotl;
+        v3 src2 = (shade * inv_pi) / ldotn;
+        float x = lpdf / float(sp.num_lights);
+        float mis2 = power_heuristic(x, bpdf);
+        if (ldotn > 0.0f && ldotln > 0.0f)
+        {
+            out.contrib = (((st.thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
+            out.shadow = true;
+            out.sh_o = isect + L * sp.epsilon;
+            out.sh_d = L;
+            out.sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon : dist - sp.epsilon;
+            rec.nee = 1;
+            rec.lgeom = sp.emission ? lgeom : 0xFFFFFFFFu;
+            rec.kl = l3.w;
+            rec.lint = lint;
+            rec.w = mis2;
+            rec.x = x;
+            rec.b0 = bpdf0;
+            // contribution = w * thr * albedo * lint * kfac
+            rec.kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
+        }
+    }
+    float cosp = dot3(nn, refl) / brdf_pdf;
+    st.thr = st.thr * (src * cosp);
+    rec.sigma = m.scale * inv_pi * cosp;
+    bool terminate = false;
+    if (bounce >= 2 && !(sp.flags & GBRT_PT_NO_RUSSIAN_ROULETTE))
+    {
+        // Russian roulette (pathtracing.inl:201-213)
+        float prob = max_elem(st.thr);
+        terminate = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++) > prob;
+        st.thr = st.thr / prob;
+        rec.rr = prob;
+    }
+    if (!terminate)
+    {
+        out.cont = true;
+        out.next_o = isect + refl * sp.epsilon;
+        out.next_d = refl;
+        st.flags &= ~kLastSpecular;
+    }
+    (void)tmin;
+    (void)tmax;
+}
+
+// One bounce for every live path of the queue.
+__global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shade_params sp,
+                                                   uint32_t* __restrict__ status)
+{
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     uint32_t n = fb.counts[q];
     bool live = i < n;
 
-    bool cont = false, shadow = false;
-    v3 next_o{}, next_d{}, sh_o{}, sh_d{};
-    float next_tmin = 0.0f, next_tmax = 0.0f, sh_tmax = 0.0f;
-    float4 contrib{};
+    vertex_out out;
+    out.cont = false;
+    out.shadow = false;
     uint32_t p = 0;
-
+    float tmin = 0.0f, tmax = 0.0f;
     if (live)
     {
         p = fb.path[q][i];
         const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
         float4 r0 = rp[0], r1 = rp[1];
-        v3 ori = { r0.x, r0.y, r0.z }, dir = { r0.w, r1.x, r1.y };
+        tmin = r1.z;
+        tmax = r1.w;
         uint4 hh = fb.hits[i];
-        int tri = int(hh.x);
-        float t = __uint_as_float(hh.y);
-        uint2 st = fb.rng_flags[p];
-        uint32_t k = st.x, flags = st.y;
-        v3 thr = xyz(fb.throughput[p]);
-        float4 rad4 = fb.radiance[p];
-        v3 rad = xyz(rad4);
-
-        if (tri < 0 || tri >= sp.num_tris)
-        {
-            // the ray left the scene: ambient light (pathtracing.inl:71-79)
-            v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
-            rad = rad + amb * thr;
-        }
-        else
-        {
-            if (sp.bounce == 0) flags |= kFirstHit;
-            float4 t1 = ldg4(&sp.tris[tri].t1);
-            float4 t2 = ldg4(&sp.tris[tri].t2);
-            v3 e1 = xyz(t1), e2 = xyz(t2);
-            uint32_t geom = __float_as_uint(t1.w);
-            v3 view = -dir;
-            v3 isect = ori + dir * t;
-            v3 gn = normalize3(cross3(e1, e2));
-            v3 sn = gn;
-            gbrt_material m;
-            if (geom < sp.num_materials)
-            {
-                m = sp.materials[geom];
-            }
-            else
-            {
-                atomicOr(status, kStatusBadIndex);
-                m = gbrt_material{ GBRT_MATERIAL_MATTE, { 0.0f, 0.0f, 0.0f }, 0.0f };
-            }
-            v3 mcol = { m.color[0], m.color[1], m.color[2] };
-            bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
-
-            v3 refl = { 0.0f, 0.0f, 0.0f };
-            float brdf_pdf;
-            v3 src;
-            if (!emission)
-            {
-                // matte::sample -> lambertian::sample_f (matte.inl:40-56, brdf.h:50-76)
-                v3 nn = faceforward3(sn, view, gn);
-                v3 w = nn;
-                v3 v = fabsf(w.x) > fabsf(w.y) ? normalize3(v3{ -w.z, 0.0f, w.x }) : normalize3(v3{ 0.0f, w.z, -w.y });
-                v3 u = cross3(v, w);
-                // cosine_sample_hemisphere(gen.next(), gen.next()), second argument drawn
-                // first as in the reference build (sampling.h:117-127)
-                float u2 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
-                float u1 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
-                float r = sqrtf(u1);
-                float theta = two_pi * u2;
-                // cos and sin evaluated in double and rounded once to float
-                float ct = float(cos(double(theta)));
-                float sth = float(sin(double(theta)));
-                v3 s3 = { r * ct, r * sth, sqrtf(1.0f - u1) };
-                refl = normalize3(u * s3.x + v * s3.y + w * s3.z);
-                brdf_pdf = dot3(nn, refl) * inv_pi;
-                src = (mcol * m.scale) * inv_pi;
-            }
-            else
-            {
-                brdf_pdf = 1.0f;   // emissive::sample (emissive.inl:28-44)
-                src = mcol * m.scale;
-            }
-            bool zero_pdf = brdf_pdf <= 0.0f;
-
-            float light_pdf = 0.0f;
-            if (sp.num_lights > 0 && emission)
-            {
-                float A = 0.5f * length3(cross3(e1, e2));
-                float ld = length3(isect - ori);
-                v3 L = normalize3(isect - ori);
-                float ldotln = fabsf(dot3(-L, gn));
-                float solid_angle = (ldotln * A) / (ld * ld);
-                light_pdf = 1.0f / solid_angle;
-            }
-            float mis = (sp.bounce > 0 && sp.num_lights > 0 && !(flags & kLastSpecular))
-                            ? power_heuristic(brdf_pdf, light_pdf / float(sp.num_lights))
-                            : 1.0f;
-            if (emission)
-            {
-                rad = rad + (thr * mis) * src;
-            }
-            else if (!zero_pdf)
-            {
-                v3 nn = faceforward3(sn, view, gn);
-                if (sp.num_lights > 0)
-                {
-                    // sample_random_light + area_light::sample + sample_surface
-                    // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
-                    float ul = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
-                    int lid = int(ul * float(sp.num_lights));
-                    if (lid >= int(sp.num_lights)) lid = int(sp.num_lights) - 1;
-                    const float4* lp = sp.lights + 4 * lid;
-                    v3 lv1 = xyz(lp[0]), le1 = xyz(lp[1]), le2 = xyz(lp[2]), lint = xyz(lp[3]);
-                    float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
-                    float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, k++);
-                    v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
-                    float sq = sqrtf(s1);
-                    v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
-                    v3 ldir = pos - isect;
-                    float dist = length3(ldir);
-                    v3 lnormal = normalize3(cross3(le1, le2));
-                    float larea = 0.5f * length3(cross3(le1, le2));
-                    float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
-                    float lsolid = (ldotln0 * larea) / (dist * dist);
-                    float lpdf = 1.0f / lsolid;
-                    v3 L = normalize3(ldir);
-                    v3 ln = faceforward3(lnormal, -L, lnormal);
-                    float ldotn = dot3(L, nn);
-                    float ldotln = fabsf(dot3(-L, ln));
-                    float bpdf = dot3(nn, L) * inv_pi;
-                    bpdf = bpdf * max_elem(thr);
-                    float ndotl = fmaxf(0.0f, dot3(nn, L));
-                    v3 cd = (mcol * m.scale) * inv_pi;
-                    v3 shade = ((cd * pi) * lint) * ndotl;
-                    v3 src2 = (shade * inv_pi) / ldotn;
-                    float mis2 = power_heuristic(lpdf / float(sp.num_lights), bpdf);
-                    if (ldotn > 0.0f && ldotln > 0.0f)
-                    {
-                        v3 c = (((thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
-                        contrib = make_float4(c.x, c.y, c.z, 0.0f);
-                        shadow = true;
-                        sh_o = isect + L * sp.epsilon;
-                        sh_d = L;
-                        sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon
-                                                                         : dist - sp.epsilon;
-                    }
-                }
-                thr = thr * (src * (dot3(nn, refl) / brdf_pdf));
-                bool terminate = false;
-                if (sp.bounce >= 2)
-                {
-                    // Russian roulette (pathtracing.inl:201-213)
-                    float prob = max_elem(thr);
-                    terminate = gbrt_rng_u01(sp.frame, p, sp.sample, k++) > prob;
-                    thr = thr / prob;
-                }
-                if (!terminate)
-                {
-                    cont = true;
-                    next_o = isect + refl * sp.epsilon;
-                    next_d = refl;
-                    next_tmin = r1.z;
-                    next_tmax = r1.w;
-                    flags &= ~kLastSpecular;
-                }
-            }
-        }
-        fb.throughput[p] = make_float4(thr.x, thr.y, thr.z, 0.0f);
-        fb.radiance[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
-        fb.rng_flags[p] = make_uint2(k, flags);
+        uint2 rf = fb.rng_flags[p];
+        path_state st{ xyz(fb.throughput[p]), xyz(fb.radiance[p]), rf.x, rf.y };
+        shade_vertex(sp, p, sp.bounce, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, int(hh.x),
+                     __uint_as_float(hh.y), st, out, status);
+        fb.throughput[p] = make_float4(st.thr.x, st.thr.y, st.thr.z, 0.0f);
+        fb.radiance[p] = make_float4(st.rad.x, st.rad.y, st.rad.z, 0.0f);
+        fb.rng_flags[p] = make_uint2(st.k, st.flags);
     }
 
-    uint32_t slot = warp_append(cont, &fb.counts[q ^ 1]);
-    if (cont)
+    uint32_t slot = warp_append(out.cont, &fb.counts[q ^ 1]);
+    if (out.cont)
     {
-        store_ray(&fb.rays[q ^ 1][slot], next_o, next_d, next_tmin, next_tmax);
+        store_ray(&fb.rays[q ^ 1][slot], out.next_o, out.next_d, tmin, tmax);
         fb.path[q ^ 1][slot] = p;
     }
-    uint32_t sslot = warp_append(shadow, &fb.counts[2]);
-    if (shadow)
+    uint32_t sslot = warp_append(out.shadow, &fb.counts[2]);
+    if (out.shadow)
     {
-        store_ray(&fb.shadow_rays[sslot], sh_o, sh_d, sp.epsilon, sh_tmax);
+        store_ray(&fb.shadow_rays[sslot], out.sh_o, out.sh_d, sp.epsilon, out.sh_tmax);
         fb.shadow_path[sslot] = p;
-        fb.shadow_contrib[sslot] = contrib;
+        fb.shadow_contrib[sslot] = make_float4(out.contrib.x, out.contrib.y, out.contrib.z, 0.0f);
     }
 }
 
@@ -419,11 +503,180 @@ __global__ void __launch_bounds__(kBlock) pt_blend(frame_buffers fb, uint32_t n,
     if (i >= n) return;
     float4 s = fb.sum[i];
     float4 a = make_float4(s.x / spp, s.y / spp, s.z / spp, s.w / spp);
-    float4 d = accum[i];
+    // dfactor == 0 overwrites: the previous contents (possibly never written) are not read
+    float4 d = dfactor != 0.0f ? accum[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float4 o = make_float4(a.x * sfactor + d.x * dfactor, a.y * sfactor + d.y * dfactor, a.z * sfactor + d.z * dfactor,
                            a.w * sfactor + d.w * dfactor);
     accum[i] = o;
     if (color) color[i] = o;
+}
+
+constexpr int kMaxReplay = 16;   // path vertices the adjoint keeps (num_bounces limit)
+
+// Adds `val` to base[3 * key ..] for every active lane; lanes with the same key are
+// summed with shuffles first, so each distinct key costs one set of atomics per warp.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warp_add3(float* __restrict__ base, uint32_t key, v3 val, bool active)
+{
+    const uint32_t full = 0xFFFFFFFFu;
+    uint32_t mask = __ballot_sync(full, active);
+    if (!active) return;
+    uint32_t peers = __match_any_sync(mask, key);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    v3 sum = { 0.0f, 0.0f, 0.0f };
+    for (uint32_t m = peers; m; m &= m - 1)
+    {
+        int src = __ffs(m) - 1;
+        sum.x += __shfl_sync(peers, val.x, src);
+        sum.y += __shfl_sync(peers, val.y, src);
+        sum.z += __shfl_sync(peers, val.z, src);
+    }
+    if (lane == leader)
+    {
+        atomicAdd(base + 3 * key + 0, sum.x);
+        atomicAdd(base + 3 * key + 1, sum.y);
+        atomicAdd(base + 3 * key + 2, sum.z);
+    }
+}
+
+// Path-replay backpropagation (Vicini, Speierer & Jakob 2021): one thread per
+// (pixel, sample) re-traces its path from its random-number counter -- the same
+// shade_vertex, so the replay is bit-identical to the forward frame -- keeping only
+// this path's vertices, then sweeps them backwards to turn the pixel's adjoint
+// dL/dI / spp into gradients w.r.t. the albedo of every matte vertex and the emission
+// of every emissive vertex and sampled light.  Memory stays O(pixels): nothing of the
+// forward frame is stored.  Geometry, visibility and the Russian-roulette decision are
+// not differentiated (the roulette's 1 / p weight is).
+template <bool Wide>
+__global__ void __launch_bounds__(kBlock) pt_adjoint(bvh_view v, shade_params sp, camera_basis cam, uint32_t width,
+                                                     uint32_t height, uint32_t spp, uint32_t num_bounces,
+                                                     const float4* __restrict__ img_adj, float* __restrict__ grad_albedo,
+                                                     float* __restrict__ grad_emission, uint32_t* __restrict__ status)
+{
+    const uint32_t full = 0xFFFFFFFFu;
+    const uint32_t npix = width * height;
+    const uint64_t gid = uint64_t(blockIdx.x) * kBlock + threadIdx.x;
+    const bool active = gid < uint64_t(npix) * spp;
+    const uint32_t pixel = active ? uint32_t(gid % npix) : 0u;
+    const uint32_t sample = active ? uint32_t(gid / npix) : 0u;
+    vertex_rec recs[kMaxReplay];
+    int nrec = 0;
+    v3 adj = { 0.0f, 0.0f, 0.0f };
+    if (active)
+    {
+        sp.sample = sample;
+        float x = float(pixel % width), y = float(pixel / width);
+        float jx = gbrt_rng_u01(sp.frame, pixel, sample, 0) - 0.5f;
+        float jy = gbrt_rng_u01(sp.frame, pixel, sample, 1) - 0.5f;
+        float sx = ((x + jx) + 0.5f) / float(width);
+        float sy = ((y + jy) + 0.5f) / float(height);
+        float u = 2.0f * sx - 1.0f;
+        float vv = 2.0f * sy - 1.0f;
+        v3 U = { cam.U.x, cam.U.y, cam.U.z }, V = { cam.V.x, cam.V.y, cam.V.z }, W = { cam.W.x, cam.W.y, cam.W.z };
+        v3 d = normalize3(U * u + V * vv + W);
+        v3 o = { cam.eye.x, cam.eye.y, cam.eye.z };
+        path_state st{ { 1.0f, 1.0f, 1.0f }, { 0.0f, 0.0f, 0.0f }, 2u, kLastSpecular };
+        for (uint32_t bounce = 0; bounce < num_bounces && bounce < uint32_t(kMaxReplay); ++bounce)
+        {
+            trace_result h = traverse_view<false, Wide>(v, { o.x, o.y, o.z }, { d.x, d.y, d.z }, 0.0f, FLT_MAX, status);
+            vertex_out out;
+            shade_vertex(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, status);
+            if (out.shadow)
+            {
+                trace_result sh = traverse_view<true, Wide>(v, { out.sh_o.x, out.sh_o.y, out.sh_o.z },
+                                                            { out.sh_d.x, out.sh_d.y, out.sh_d.z }, sp.epsilon,
+                                                            out.sh_tmax, status);
+                if (sh.tri >= 0) out.rec.nee = 0;   // occluded: no contribution to differentiate
+            }
+            recs[nrec++] = out.rec;
+            if (!out.cont) break;
+            o = out.next_o;
+            d = out.next_d;
+        }
+        if (st.flags & kFirstHit)
+        {
+            float4 a4 = img_adj[pixel];
+            float inv = 1.0f / float(spp);
+            adj = { a4.x * inv, a4.y * inv, a4.z * inv };
+        }
+    }
+    // reverse sweep, warp-uniform so the gradient adds can be reduced per warp
+    int kmax = __reduce_max_sync(full, nrec);
+    v3 tbar = { 0.0f, 0.0f, 0.0f };   // adjoint of the throughput leaving vertex k
+    for (int k = kmax - 1; k >= 0; --k)
+    {
+        bool here = active && k < nrec;
+        v3 abar = { 0.0f, 0.0f, 0.0f }, ebar = { 0.0f, 0.0f, 0.0f }, lbar = { 0.0f, 0.0f, 0.0f };
+        uint32_t geom = 0, lgeom = 0;
+        bool add_a = false, add_e = false, add_l = false;
+        if (here)
+        {
+            vertex_rec const& r = recs[k];
+            geom = r.geom;
+            if (r.kind == kVertexMiss)
+            {
+                tbar = adj * v3{ sp.ambient.x, sp.ambient.y, sp.ambient.z };
+            }
+            else if (r.kind == kVertexEnd)
+            {
+                tbar = { 0.0f, 0.0f, 0.0f };
+            }
+            else if (r.kind == kVertexEmission)
+            {
+                gbrt_material m = sp.materials[geom];
+                v3 e = sp.emission ? param3(sp.emission, geom) : v3{ m.color[0], m.color[1], m.color[2] };
+                ebar = adj * r.thr * (r.mis * r.escale);
+                add_e = sp.emission != nullptr;
+                tbar = adj * e * (r.mis * r.escale);
+            }
+            else
+            {
+                gbrt_material m = sp.materials[geom];
+                v3 a = sp.albedo ? param3(sp.albedo, geom) : v3{ m.color[0], m.color[1], m.color[2] };
+                // throughput update thr' = thr * a * sigma (then / rr)
+                v3 ub = tbar;
+                if (r.rr > 0.0f)
+                {
+                    v3 uu = r.thr * a * r.sigma;
+                    float p = r.rr;
+                    ub = tbar / p;
+                    float pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (p * p);
+                    if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
+                    else if (uu.y >= uu.z) ub.y += pb;
+                    else ub.z += pb;
+                }
+                abar = ub * r.thr * r.sigma;
+                v3 tb = ub * a * r.sigma;
+                if (r.nee)
+                {
+                    // N = w * thr * a * lint * kfac, w = x^2 / (x^2 + y^2), y = b0 * max(thr)
+                    v3 f = r.lint * r.kfac;
+                    abar = abar + adj * r.thr * f * r.w;
+                    tb = tb + adj * a * f * r.w;
+                    float wbar = adj.x * r.thr.x * a.x * f.x + adj.y * r.thr.y * a.y * f.y + adj.z * r.thr.z * a.z * f.z;
+                    float yv = r.b0 * max_elem(r.thr);
+                    float den = r.x * r.x + yv * yv;
+                    float dwdy = -2.0f * r.x * r.x * yv / (den * den);
+                    float g = wbar * dwdy * r.b0;
+                    if (r.thr.x >= r.thr.y && r.thr.x >= r.thr.z) tb.x += g;
+                    else if (r.thr.y >= r.thr.z) tb.y += g;
+                    else tb.z += g;
+                    if (r.lgeom != 0xFFFFFFFFu && r.lgeom < sp.num_materials)
+                    {
+                        lgeom = r.lgeom;
+                        lbar = adj * r.thr * a * (r.w * r.kfac * r.kl);
+                        add_l = true;
+                    }
+                }
+                tbar = tb;
+                add_a = sp.albedo != nullptr;
+            }
+        }
+        warp_add3(grad_albedo, geom, abar, add_a);
+        warp_add3(grad_emission, geom, ebar, add_e);
+        warp_add3(grad_emission, lgeom, lbar, add_l);
+    }
 }
 
 inline size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -541,12 +794,14 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
         for (uint32_t k = 0; k < num_lights; ++k)
         {
             gbrt_triangle const& t = h_lights[k].geometry;
+            uint32_t lg = t.geom_id;
             l[4 * k + 0] = make_float4(t.v1[0], t.v1[1], t.v1[2], 0.0f);
+            memcpy(&l[4 * k + 0].w, &lg, 4);
             l[4 * k + 1] = make_float4(t.e1[0], t.e1[1], t.e1[2], 0.0f);
             l[4 * k + 2] = make_float4(t.e2[0], t.e2[1], t.e2[2], 0.0f);
             // area_light::intensity = cl * kl (area_light.inl:22-25)
             l[4 * k + 3] = make_float4(h_lights[k].cl[0] * h_lights[k].kl, h_lights[k].cl[1] * h_lights[k].kl,
-                                       h_lights[k].cl[2] * h_lights[k].kl, 0.0f);
+                                       h_lights[k].cl[2] * h_lights[k].kl, h_lights[k].kl);
         }
         cudaError_t e = cudaMalloc(&sc->lights, l.size() * sizeof(float4));
         if (e == cudaSuccess) e = cudaMemcpy(sc->lights, l.data(), l.size() * sizeof(float4), cudaMemcpyHostToDevice);
@@ -570,36 +825,56 @@ extern "C" gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene)
     return GBRT_OK;
 }
 
-extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
-                                            gbrt_pt_params const* params, float* d_accum, float* d_color)
+namespace gbrt {
+namespace {
+
+gbrt_status check_frame_args(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
+                             gbrt_pt_params const* params, const void* img, const char* who)
 {
-    if (!ctx) return GBRT_ERR_INVALID_ARG;
-    if (!scene || !camera || !params || !d_accum)
-        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: null argument");
+    if (!scene || !camera || !params || !img) return fail(ctx, GBRT_ERR_INVALID_ARG, std::string(who) + ": null argument");
     gbrt_pt_params const& p = *params;
-    if (p.width == 0 || p.height == 0 || p.spp == 0) return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: empty frame");
+    if (p.width == 0 || p.height == 0 || p.spp == 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, std::string(who) + ": empty frame");
     if (uint64_t(p.width) * p.height > (1ull << 28))
-        return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_frame: more than 2^28 pixels");
-    if ((reinterpret_cast<uintptr_t>(d_accum) & 15u) || (reinterpret_cast<uintptr_t>(d_color) & 15u))
-        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_frame: images must be 16-byte aligned");
-    device_guard g(ctx->device);
-    const uint32_t n = p.width * p.height;
-    frame_buffers fb;
-    gbrt_status st = frame_buffers_for(ctx, n, fb);
-    if (st != GBRT_OK) return st;
-    camera_basis cam = camera_for(*camera, p.width, p.height);
-    gbrt_bvh const* bvh = scene->bvh;
+        return fail(ctx, GBRT_ERR_TOO_LARGE, std::string(who) + ": more than 2^28 pixels");
+    return GBRT_OK;
+}
+
+shade_params shade_params_for(gbrt_pt_scene const* scene, gbrt_pt_params const& p, const float* albedo,
+                              const float* emission)
+{
     shade_params sp;
     sp.materials = scene->materials;
     sp.num_materials = scene->num_materials;
     sp.lights = scene->lights;
     sp.num_lights = scene->num_lights;
-    sp.tris = bvh->tris;
-    sp.num_tris = int32_t(bvh->num_prims);
+    sp.tris = scene->bvh->tris;
+    sp.num_tris = int32_t(scene->bvh->num_prims);
     sp.epsilon = p.epsilon;
     sp.ambient = make_float3(p.ambient[0], p.ambient[1], p.ambient[2]);
     sp.frame = p.frame_id;
+    sp.sample = 0;
+    sp.bounce = 0;
     sp.flags = p.flags;
+    sp.albedo = albedo;
+    sp.emission = emission;
+    return sp;
+}
+
+// One frame of the wavefront path tracer into accum (blended) and color.
+gbrt_status render_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const& camera,
+                         gbrt_pt_params const& p, const float* albedo, const float* emission, float* d_accum,
+                         float* d_color)
+{
+    if ((reinterpret_cast<uintptr_t>(d_accum) & 15u) || (reinterpret_cast<uintptr_t>(d_color) & 15u))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace: images must be 16-byte aligned");
+    const uint32_t n = p.width * p.height;
+    frame_buffers fb;
+    gbrt_status st = frame_buffers_for(ctx, n, fb);
+    if (st != GBRT_OK) return st;
+    camera_basis cam = camera_for(camera, p.width, p.height);
+    gbrt_bvh const* bvh = scene->bvh;
+    shade_params sp = shade_params_for(scene, p, albedo, emission);
     // background: ambient_light(bg.xyz, bg.w).intensity with alpha 1 (kernels.h:172-174,
     // pathtracing.inl:62)
     float4 bg = make_float4(p.background[0] * p.background[3], p.background[1] * p.background[3],
@@ -643,5 +918,70 @@ extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene con
     pt_blend<<<blocks, kBlock, 0, s>>>(fb, n, float(p.spp), p.sfactor, p.dfactor, reinterpret_cast<float4*>(d_accum),
                                        reinterpret_cast<float4*>(d_color));
     GBRT_LAUNCH_CHECK(ctx, "pt_blend");
+    return GBRT_OK;
+}
+
+} // namespace
+} // namespace gbrt
+
+extern "C" gbrt_status gbrt_pathtrace_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
+                                            gbrt_pt_params const* params, float* d_accum, float* d_color)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    gbrt_status st = check_frame_args(ctx, scene, camera, params, d_accum, "pathtrace_frame");
+    if (st != GBRT_OK) return st;
+    device_guard g(ctx->device);
+    return render_frame(ctx, scene, *camera, *params, nullptr, nullptr, d_accum, d_color);
+}
+
+extern "C" gbrt_status gbrt_pathtrace_forward(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
+                                              gbrt_pt_params const* params, const float* d_albedo,
+                                              const float* d_emission, float* d_image)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    gbrt_status st = check_frame_args(ctx, scene, camera, params, d_image, "pathtrace_forward");
+    if (st != GBRT_OK) return st;
+    if (!d_albedo || !d_emission) return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_forward: null parameters");
+    gbrt_pt_params p = *params;
+    p.sfactor = 1.0f;   // the image is this frame alone
+    p.dfactor = 0.0f;
+    device_guard g(ctx->device);
+    return render_frame(ctx, scene, *camera, p, d_albedo, d_emission, d_image, nullptr);
+}
+
+extern "C" gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_camera const* camera,
+                                               gbrt_pt_params const* params, const float* d_albedo,
+                                               const float* d_emission, const float* d_image_adjoint,
+                                               float* d_grad_albedo, float* d_grad_emission)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    gbrt_status st = check_frame_args(ctx, scene, camera, params, d_image_adjoint, "pathtrace_backward");
+    if (st != GBRT_OK) return st;
+    if (!d_albedo || !d_emission || !d_grad_albedo || !d_grad_emission)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_backward: null parameter or gradient array");
+    if (reinterpret_cast<uintptr_t>(d_image_adjoint) & 15u)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_backward: adjoint image must be 16-byte aligned");
+    gbrt_pt_params const& p = *params;
+    if (p.num_bounces > uint32_t(kMaxReplay))
+        return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_backward: at most 16 bounces");
+    gbrt_bvh const* bvh = scene->bvh;
+    if (bvh->num_prims == 0 || scene->num_materials == 0) return GBRT_OK;   // nothing to differentiate
+    device_guard g(ctx->device);
+    camera_basis cam = camera_for(*camera, p.width, p.height);
+    shade_params sp = shade_params_for(scene, p, d_albedo, d_emission);
+    const uint64_t paths = uint64_t(p.width) * p.height * p.spp;
+    if (paths > (1ull << 31)) return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_backward: more than 2^31 paths");
+    const uint32_t blocks = uint32_t((paths + kBlock - 1) / kBlock);
+    const bvh_view v = view_of(bvh);
+    const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
+    if (wide)
+        pt_adjoint<true><<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
+                                                             reinterpret_cast<const float4*>(d_image_adjoint),
+                                                             d_grad_albedo, d_grad_emission, ctx->d_status);
+    else
+        pt_adjoint<false><<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
+                                                              reinterpret_cast<const float4*>(d_image_adjoint),
+                                                              d_grad_albedo, d_grad_emission, ctx->d_status);
+    GBRT_LAUNCH_CHECK(ctx, "pt_adjoint");
     return GBRT_OK;
 }

@@ -1,0 +1,90 @@
+"""Inverse rendering of per-primitive albedo with the path-replay adjoint.
+
+The workload: the path-tracing box scene reduced to ~4k triangles (2 blobs of 2,000),
+a target image rendered from hidden albedos, and Adam steps on the albedos from a
+uniform start, each step a forward frame, the L2 image loss and the backward pass
+(gbrt_pathtrace_forward / gbrt_pathtrace_backward).  Random numbers are common
+(frame_id fixed) between the forward and backward pass of a step.
+"""
+import time
+
+import numpy as np
+
+from . import runtime as rt
+from . import scenes
+from .types import PT_NO_RUSSIAN_ROULETTE, PT_SHADOW_RANGE_FIX
+
+FLAGS = PT_SHADOW_RANGE_FIX | PT_NO_RUSSIAN_ROULETTE
+
+
+def setup(n_blobs=2, subdiv=10, seed=1, hidden_seed=5, ctx=None):
+    """(scene, tris, materials, lights, hidden albedo, emission) on the GPU."""
+    import torch
+    ctx = ctx or rt.default_context()
+    tris, mats, lights = scenes.box_scene(n_blobs=n_blobs, subdiv=subdiv, seed=seed)
+    bvh = rt.lbvh_builder(ctx).build(rt.as_device_bytes(tris, ctx.device))
+    scene = rt.PTScene(bvh, mats, lights)
+    rng = np.random.default_rng(hidden_seed)
+    hidden = rng.uniform(0.1, 0.9, size=(len(mats), 3)).astype(np.float32)
+    dev = f"cuda:{ctx.device}"
+    emission = torch.from_numpy(np.ascontiguousarray(mats["color"], np.float32)).to(dev)
+    return scene, tris, mats, lights, torch.from_numpy(hidden).to(dev), emission
+
+
+def l2_adjoint(image, target):
+    """L = mean over pixels of sum over RGB of (I - T)^2, and dL/dI (alpha zero)."""
+    import torch
+    d = image[..., :3] - target[..., :3]
+    npix = image.shape[0] * image.shape[1]
+    loss = (d.double() ** 2).sum() / npix
+    adj = torch.zeros_like(image)
+    adj[..., :3] = 2.0 * d / npix
+    return float(loss), adj
+
+
+def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_spp=256, ctx=None, log=None):
+    """Adam on the albedos.  Returns a dict with the loss history, the parameter error
+    and the mean forward / backward times (CUDA events)."""
+    import torch
+    ctx = ctx or rt.default_context()
+    scene, tris, mats, lights, hidden, emission = setup(ctx=ctx)
+    cam = scenes.box_camera()
+    tparams = scenes.pt_params(width, height, target_spp, num_bounces=depth, frame_id=1000, flags=FLAGS)
+    target = rt.pathtrace_forward(scene, cam, tparams, hidden, emission)
+    albedo = torch.full_like(hidden, 0.5)
+    m = torch.zeros_like(albedo)
+    v = torch.zeros_like(albedo)
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fwd_ms, bwd_ms, losses = [], [], []
+    image = None
+    for it in range(steps):
+        params = scenes.pt_params(width, height, spp, num_bounces=depth, frame_id=it, flags=FLAGS)
+        ev[0].record(ctx.stream)
+        image = rt.pathtrace_forward(scene, cam, params, albedo, emission, image=image)
+        ev[1].record(ctx.stream)
+        loss, adj = l2_adjoint(image, target)
+        grad_a = torch.zeros_like(albedo)
+        grad_e = torch.zeros_like(emission)
+        ev[2].record(ctx.stream)
+        e3 = torch.cuda.Event(enable_timing=True)
+        rt.pathtrace_backward(scene, cam, params, albedo, emission, adj, grad_a, grad_e)
+        e3.record(ctx.stream)
+        torch.cuda.synchronize()
+        fwd_ms.append(ev[0].elapsed_time(ev[1]))
+        bwd_ms.append(ev[2].elapsed_time(e3))
+        losses.append(loss)
+        # Adam (Kingma & Ba 2015), albedo kept in [0, 1]
+        m.mul_(b1).add_(grad_a, alpha=1 - b1)
+        v.mul_(b2).addcmul_(grad_a, grad_a, value=1 - b2)
+        mh = m / (1 - b1 ** (it + 1))
+        vh = v / (1 - b2 ** (it + 1))
+        albedo.sub_(lr * mh / (vh.sqrt() + eps)).clamp_(0.0, 1.0)
+        if log and (it % 20 == 0 or it == steps - 1):
+            log(f"step {it} loss {loss:.6g}")
+    ctx.synchronize()
+    seen = (grad_a.abs().sum(1) > 0).cpu().numpy()
+    err0 = float((0.5 - hidden).abs().mean())
+    err = float((albedo - hidden).abs()[torch.from_numpy(seen).to(albedo.device)].mean()) if seen.any() else err0
+    return {"losses": losses, "fwd_ms": float(np.median(fwd_ms)), "bwd_ms": float(np.median(bwd_ms)),
+            "albedo_error_start": err0, "albedo_error_end_seen": err, "triangles": int(len(tris))}

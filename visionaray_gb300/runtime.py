@@ -49,6 +49,8 @@ SIGNATURES = {
     "gbrt_pt_scene_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_pt_scene_destroy": (_i32, [_vp]),
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbrt_pathtrace_forward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbrt_pathtrace_backward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -305,3 +307,37 @@ def pathtrace_frame(scene, camera, params, accum=None, color=None):
     cptr = _dptr(color) if color is not None else None
     ctx.check(ctx.lib.gbrt_pathtrace_frame(ctx.h, scene.h, _hptr(cam), _hptr(par), _dptr(accum), cptr))
     return accum
+
+
+def pathtrace_forward(scene, camera, params, albedo, emission, image=None):
+    """Differentiable renderer, forward: image (h, w, 4) of one frame with per-slot
+    albedo / emission parameters ((num_materials, 3) float32 CUDA tensors)."""
+    torch = _torch()
+    ctx = scene.ctx
+    cam = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+    par = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+    w, h = int(par["width"][0]), int(par["height"][0])
+    if image is None:
+        image = torch.empty((h, w, 4), dtype=torch.float32, device=f"cuda:{ctx.device}")
+    ctx.check(ctx.lib.gbrt_pathtrace_forward(ctx.h, scene.h, _hptr(cam), _hptr(par), _dptr(albedo),
+                                             _dptr(emission), _dptr(image)))
+    return image
+
+
+def pathtrace_backward(scene, camera, params, albedo, emission, image_adjoint, grad_albedo=None,
+                       grad_emission=None):
+    """Differentiable renderer, backward (path replay): gradients of sum(I * image_adjoint)
+    w.r.t. albedo and emission, added to grad_albedo / grad_emission (zeros if None)."""
+    torch = _torch()
+    ctx = scene.ctx
+    cam = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+    par = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+    if grad_albedo is None:
+        grad_albedo = torch.zeros_like(albedo)
+    if grad_emission is None:
+        grad_emission = torch.zeros_like(emission)
+    adj = image_adjoint.contiguous()
+    ctx.check(ctx.lib.gbrt_pathtrace_backward(ctx.h, scene.h, _hptr(cam), _hptr(par), _dptr(albedo),
+                                              _dptr(emission), _dptr(adj), _dptr(grad_albedo),
+                                              _dptr(grad_emission)))
+    return grad_albedo, grad_emission

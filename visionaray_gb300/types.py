@@ -26,6 +26,7 @@ PT_PARAMS = np.dtype([("width", "<u4"), ("height", "<u4"), ("spp", "<u4"), ("num
                       ("background", "<f4", (4,)), ("ambient", "<f4", (3,)), ("flags", "<u4")])
 MATTE, EMISSIVE = 0, 1
 PT_SHADOW_RANGE_FIX = 1
+PT_NO_RUSSIAN_ROULETTE = 2
 
 NO_HIT = 0xFFFFFFFF
 FLT_MAX = float(np.finfo(np.float32).max)
