@@ -208,6 +208,115 @@ def run_pathtrace(vg, ctx, frames, flags, rprint):
             "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
 
 
+BATCH_WORKLOAD = ("512 random-soup scenes (triangle counts log-uniform in [1k, 1M], vertex offsets 0.5/cbrt(n)), "
+                  "seeded cameras, square resolutions from {64,128,256,512}, 1 spp of 1 primary ray + 2 diffuse "
+                  "bounces, matte 0.7 under white ambient light; one step = build every scene + render one frame "
+                  "of every scene")
+
+
+def run_batch(vg, ctx, steps, plain_steps, rprint):
+    """The batched graph (build + frame of 512 scenes in one CUDA graph, autotuned
+    persistent launch) against the plain per-scene loop (gbrt_bvh_build_lbvh +
+    gbrt_pathtrace_frame per scene) on the same GPU; Msamples/s of both and whether
+    their images are bit-identical."""
+    import torch
+    from visionaray_gb300 import scenes
+    from visionaray_gb300.types import AREA_LIGHT
+    t0 = time.time()
+    tris, offsets, cams, params, mats = scenes.batch_workload()
+    gen_s = time.time() - t0
+    ns = len(offsets) - 1
+    d_tris = vg.as_device_bytes(tris, ctx.device)
+    del tris
+    batch = vg.Batch(offsets, ctx)
+    batch.set_frames(cams, params, mats)
+    batch.build(d_tris)
+    images = batch.new_images()
+    t0 = time.time()
+    best, tune_ms = batch.autotune(images, reps=1)
+    tune_s = time.time() - t0
+    height = batch.height()
+    samples = int(batch.pixel_offsets[-1]) * int(params["spp"][0])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    for _ in range(3):
+        batch.run_graph(d_tris, images)
+    ctx.synchronize()
+    launches0 = ctx.launches
+    ev[0].record(ctx.stream)
+    for _ in range(steps):
+        batch.run_graph(d_tris, images)
+    ev[1].record(ctx.stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    batch_ms = ev[0].elapsed_time(ev[1]) / steps
+    batch_launches = (ctx.launches - launches0) // steps
+    # the frame alone (persistent kernel), for the breakdown
+    ev[0].record(ctx.stream)
+    batch.pathtrace(images)
+    ev[1].record(ctx.stream)
+    torch.cuda.synchronize()
+    frame_ms = ev[0].elapsed_time(ev[1])
+
+    plain_images = torch.full_like(images, -1.0)
+    no_lights = np.zeros(0, AREA_LIGHT)
+    views = []
+    for s in range(ns):
+        a, b = int(batch.pixel_offsets[s]), int(batch.pixel_offsets[s + 1])
+        views.append(plain_images[a:b].view(int(params["height"][s]), int(params["width"][s]), 4))
+
+    def plain_step():
+        builder = vg.lbvh_builder(ctx)
+        for s in range(ns):
+            bvh = builder.build(d_tris[int(offsets[s]) * 44:int(offsets[s + 1]) * 44])
+            sc = vg.PTScene(bvh, mats, no_lights)
+            vg.pathtrace_frame(sc, cams[s], params[s], accum=views[s])
+            sc.close()
+            bvh.close()
+
+    plain_step()   # warm-up (grows the context scratch to the largest scene)
+    ctx.synchronize()
+    launches0 = ctx.launches
+    torch.cuda.synchronize()
+    ev[0].record(ctx.stream)
+    for _ in range(plain_steps):
+        plain_step()
+    ev[1].record(ctx.stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    plain_ms = ev[0].elapsed_time(ev[1]) / plain_steps
+    plain_launches = (ctx.launches - launches0) // plain_steps
+    identical = bool(torch.equal(images.view(torch.int32), plain_images.view(torch.int32)))
+    mean = float(images[:, :3].mean().item())
+    res = {"workload": BATCH_WORKLOAD, "scenes": ns, "triangles": int(offsets[-1]),
+           "samples_per_step": samples, "generate_s": round(gen_s, 1), "tallest_tree": height,
+           "batched": {"ms_per_step": round(batch_ms, 2), "msamples_s": round(samples / (batch_ms * 1e-3) / 1e6, 2),
+                       "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
+                       "steps": steps, "launch": {k: int(best[k]) for k in best.dtype.names},
+                       "autotune_frame_ms": round(float(tune_ms), 2), "autotune_s": round(tune_s, 1)},
+           "plain": {"ms_per_step": round(plain_ms, 2), "msamples_s": round(samples / (plain_ms * 1e-3) / 1e6, 2),
+                     "gpu_launches_per_step": int(plain_launches), "steps": plain_steps},
+           "speedup": round(plain_ms / batch_ms, 2), "images_bit_identical": identical,
+           "image_mean": round(mean, 5)}
+    batch.close()
+    del d_tris, images, plain_images, views
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_adjoint(ctx, steps, rprint):
+    """The inverse-albedo workload: `steps` Adam steps of forward frame + L2 loss +
+    path-replay adjoint; median forward / backward times and their ratio."""
+    from visionaray_gb300 import inverse
+    r = inverse.optimize(steps=steps, ctx=ctx)
+    return {"workload": "inverse albedo on the box scene reduced to 4,014 triangles (2 blobs, subdiv 10): "
+                        "512x512, 16 spp, depth 6 forward + L2 loss + adjoint per step, target 256 spp",
+            "steps": steps, "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
+            "bwd_over_fwd": round(r["bwd_ms"] / r["fwd_ms"], 3), "loss_start": round(r["losses"][0], 6),
+            "loss_end": round(r["losses"][-1], 6), "albedo_error_start": round(r["albedo_error_start"], 4),
+            "albedo_error_end_seen": round(r["albedo_error_end_seen"], 4)}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -341,6 +450,14 @@ def run_ours(args):
     if args.pt_frames > 0:
         pt = run_pathtrace(vg, ctx, args.pt_frames, 0, rprint)
 
+    batched = None
+    if args.batch_steps > 0:
+        batched = run_batch(vg, ctx, args.batch_steps, args.batch_plain_steps, rprint)
+
+    adjoint = None
+    if args.adjoint_steps > 0:
+        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint)
+
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res = cpu_baseline(tris, closest, ao, rank_print=rprint, sample_every=8, repeats=2)
@@ -361,7 +478,7 @@ def run_ours(args):
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
             "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base,
-            "pathtrace": pt}
+            "pathtrace": pt, "batched_pathtrace": batched, "adjoint": adjoint}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -377,6 +494,9 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--batch-steps", type=int, default=3, help="timed batched-graph steps (0: skip)")
+    p.add_argument("--batch-plain-steps", type=int, default=1, help="timed plain per-scene loop steps")
+    p.add_argument("--adjoint-steps", type=int, default=200, help="inverse-albedo Adam steps (0: skip)")
     p.add_argument("--trace-flags", type=int, default=1,
                    help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order, 2: 4-wide nodes)")
     # smaller cases for profiling captures only; the benchmark is the default size

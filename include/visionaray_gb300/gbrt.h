@@ -318,6 +318,87 @@ gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene const* scen
                                     const float* d_image_adjoint, float* d_grad_albedo,
                                     float* d_grad_emission);
 
+/* ------------------------------------------------------------------------------ */
+/* Batches of scenes (no visionaray counterpart: the reference builds and renders one
+ * scene per call, lbvh.h:681-844 and cuda_sched.inl:226-246).                      */
+
+typedef struct gbrt_batch gbrt_batch;
+
+/* Creates a batch of num_scenes scenes over one concatenated triangle array: scene s
+ * owns triangles [h_offsets[s], h_offsets[s + 1]) (h_offsets: num_scenes + 1 host
+ * entries, non-decreasing, h_offsets[0] = 0).  Allocates the whole BVH arena and the
+ * build temporaries once, so the build and frame calls below only enqueue kernels.   */
+gbrt_status gbrt_batch_create(gbrt_context* ctx, uint32_t const* h_offsets, uint32_t num_scenes,
+                              gbrt_batch** out);
+gbrt_status gbrt_batch_destroy(gbrt_batch* batch);
+
+/* Builds every scene's LBVH in one pass (per-scene Morton normalisation, one sort by
+ * (scene, code), Karras hierarchies and refit over all segments): each scene's tree is
+ * the one gbrt_bvh_build_lbvh builds for that scene alone.  Enqueue only
+ * (asynchronous, no allocation, no synchronisation).                              */
+gbrt_status gbrt_batch_build(gbrt_context* ctx, gbrt_batch* batch, gbrt_triangle const* d_tris);
+
+/* Reference-layout export of scene s (as gbrt_bvh_export_bvh2 for that scene).     */
+gbrt_status gbrt_batch_export_bvh2(gbrt_context* ctx, gbrt_batch const* batch, uint32_t scene,
+                                   gbrt_bvh_node* d_nodes, uint32_t* d_indices);
+
+/* closest_hit of rays of all scenes in one launch: scene s traces rays
+ * [h_ray_offsets[s], h_ray_offsets[s + 1]) (num_scenes + 1 host entries).          */
+gbrt_status gbrt_batch_trace_closest_hit(gbrt_context* ctx, gbrt_batch const* batch,
+                                         gbrt_ray const* d_rays, uint32_t const* h_ray_offsets,
+                                         gbrt_hit* d_hits);
+
+/* Per-scene frame setup for gbrt_batch_pathtrace: h_cameras / h_params (num_scenes
+ * entries; params' sfactor / dfactor ignored, each scene's image is overwritten) and
+ * materials (indexed by geom_id, shared by all scenes).  Copies to the device.       */
+gbrt_status gbrt_batch_set_frames(gbrt_context* ctx, gbrt_batch* batch, gbrt_camera const* h_cameras,
+                                  gbrt_pt_params const* h_params, gbrt_material const* h_materials,
+                                  uint32_t num_materials);
+
+/* Launch shape of gbrt_batch_pathtrace (the autotuner's search space).            */
+#define GBRT_BATCH_ORDER_ROWS 0u    /* a warp's pixels are consecutive in a row       */
+#define GBRT_BATCH_ORDER_BLOCKS 1u  /* a warp's 32 pixels are an 8x4 screen block
+                                       (scenes with width % 8 == 0, height % 4 == 0;
+                                       rows otherwise)                                */
+typedef struct gbrt_batch_launch
+{
+    uint32_t block;  /* threads per block: 128, 256 or 512                         */
+    uint32_t tile;   /* pixels a warp takes from the work queue per grab: 32 or 64  */
+    uint32_t stack;  /* traversal stack entries: 16, 24, 32 or 64 (a tree taller
+                        than this sets GBRT_ERR_STACK_OVERFLOW)                     */
+    uint32_t order;  /* GBRT_BATCH_ORDER_*                                          */
+} gbrt_batch_launch;
+
+/* Sets / reads the launch shape (default {128, 32, 64, ROWS}).                      */
+gbrt_status gbrt_batch_set_launch(gbrt_batch* batch, gbrt_batch_launch const* launch);
+gbrt_status gbrt_batch_get_launch(gbrt_batch const* batch, gbrt_batch_launch* out);
+
+/* Tallest tree of the last gbrt_batch_build (edges from a root to its deepest leaf);
+ * synchronises the context stream.                                                 */
+gbrt_status gbrt_batch_height(gbrt_context* ctx, gbrt_batch const* batch, uint32_t* out);
+
+/* One frame of every scene in a single persistent launch: warps take tiles of pixels of
+ * any scene from one atomic work queue and run the path tracer (the same shading as
+ * gbrt_pathtrace_frame, so scene s's image equals the one gbrt_pathtrace_frame
+ * renders with its camera and params).  d_images: RGBA32F, 16-byte aligned, scene s at
+ * pixel offset sum_{t<s} width_t * height_t.  Area lights are not supported here
+ * (ambient light only).  Enqueue only.                                             */
+gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch const* batch, float* d_images);
+
+/* gbrt_batch_build + gbrt_batch_pathtrace captured once into a CUDA graph and
+ * replayed on the context stream on every call (re-captured when d_tris, d_images,
+ * the frames or the launch shape change).                                          */
+gbrt_status gbrt_batch_run_graph(gbrt_context* ctx, gbrt_batch* batch, gbrt_triangle const* d_tris,
+                                 float* d_images);
+
+/* Autotuner: times gbrt_batch_pathtrace (after gbrt_batch_build and
+ * gbrt_batch_set_frames) over every launch shape of the search space whose stack
+ * holds the tallest tree, `reps` runs each after one warm-up run, and keeps the
+ * fastest (also written to *best, with its time per frame in *best_ms; either may be
+ * NULL).  Shapes whose run raised a status are skipped.  d_images is overwritten.   */
+gbrt_status gbrt_batch_autotune(gbrt_context* ctx, gbrt_batch* batch, float* d_images, uint32_t reps,
+                                gbrt_batch_launch* best, float* best_ms);
+
 /* Number of kernels the library launched on this context since creation (the
  * count covers every kernel of every call).                                        */
 uint64_t gbrt_kernel_launch_count(gbrt_context const* ctx);

@@ -4,9 +4,9 @@ closest_hit / any_hit traversal behind the C ABI of include/visionaray_gb300/gbr
 The Python layer is a thin host-side mirror of the reference's interface
 (runtime.py); all work runs in the CUDA kernels of libgbrt.so.
 """
-from .types import (AREA_LIGHT, BVH_NODE, CAMERA, FLT_MAX, HIT, MATERIAL, NO_HIT,  # noqa: F401
-                    PT_PARAMS, PT_SHADOW_RANGE_FIX, RAY, TRIANGLE)
-from .runtime import (Context, GbrtError, IndexBVH, PTScene, any_hit, closest_hit,  # noqa: F401
+from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, FLT_MAX, HIT, MATERIAL,  # noqa: F401
+                    NO_HIT, PT_PARAMS, PT_SHADOW_RANGE_FIX, RAY, TRIANGLE)
+from .runtime import (Batch, Context, GbrtError, IndexBVH, PTScene, any_hit, closest_hit,  # noqa: F401
                       default_context, device_rays, as_device_bytes, hits_to_numpy,
                       lbvh_builder, load_library, pathtrace_backward, pathtrace_forward,
                       pathtrace_frame)

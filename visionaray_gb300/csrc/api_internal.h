@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/visionaray_gb300/gbrt.h"
 #include "bvh_layout.cuh"
@@ -79,6 +80,46 @@ struct gbrt_bvh
     gbrt::bvh4_node* nodes4 = nullptr;
     uint32_t num_nodes4 = 0;
     uint32_t leaf_max4 = 0;
+};
+
+// Many scenes built and traced as one arena (batch.cu, batch_pt.cu).  Scene s owns
+// the sorted primitives [offsets[s], offsets[s + 1]) and the inner node pairs
+// [inner_offsets[s], inner_offsets[s + 1]); its root is roots[s] (an inner index, ~leaf
+// for a one-triangle scene, INT32_MIN for an empty one).
+struct gbrt_batch
+{
+    int device = 0;
+    uint32_t num_scenes = 0;
+    uint32_t total = 0;         // primitives of all scenes
+    uint32_t total_inner = 0;   // inner node pairs of all scenes
+    std::vector<uint32_t> offsets, inner_offsets;
+    std::vector<int32_t> roots;
+    uint32_t* d_offsets = nullptr;
+    uint32_t* d_inner_offsets = nullptr;
+    int32_t* d_roots = nullptr;
+    gbrt::bvh2_node* nodes = nullptr;
+    gbrt::tri48* tris = nullptr;
+    uint32_t* sorted_codes = nullptr;
+    uint32_t* sorted_ids = nullptr;
+    uint32_t* d_height = nullptr;   // the tallest scene tree (atomicMax)
+    void* scratch = nullptr;        // build temporaries, sized at creation
+    size_t scratch_bytes = 0;
+    // frame setup (gbrt_batch_set_frames)
+    void* d_frames = nullptr;       // per-scene camera basis, frame size, root (batch_pt.cu)
+    uint32_t* d_pixel_offsets = nullptr;
+    uint32_t total_pixels = 0;
+    uint32_t frames_set = 0;        // scenes whose frames are on the device (0 or num_scenes)
+    gbrt_material* d_materials = nullptr;
+    uint32_t num_materials = 0;
+    uint32_t* d_work = nullptr;     // persistent-kernel work counter
+    gbrt_batch_launch launch = { 128, 32, 64, GBRT_BATCH_ORDER_ROWS };
+    // the captured build + frame
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_launches = 0;    // kernels per replay
+    bool graph_dirty = true;
+    const void* graph_tris = nullptr;
+    void* graph_images = nullptr;
 };
 
 namespace gbrt {
@@ -174,6 +215,12 @@ size_t trace_scratch_bytes(uint32_t n);
 gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n,
                   gbrt_hit* d_hits, bool any_hit, cudaStream_t stream, void* scratch = nullptr,
                   size_t scratch_bytes = 0);
+
+// batch.cu: the batched build, enqueued on `stream` (allocates nothing, does not
+// synchronise, so it can be captured).
+gbrt_status batch_build(gbrt_context* ctx, gbrt_batch* b, gbrt_triangle const* d_tris, cudaStream_t stream);
+// batch_pt.cu: the batched frame on `stream`.
+gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_images, cudaStream_t stream);
 
 } // namespace gbrt
 

@@ -1,0 +1,346 @@
+// Path-tracing shading shared by the wavefront renderer and its adjoint (pathtrace.cu)
+// and the batched persistent renderer (batch_pt.cu): the vector helpers in the
+// reference's float arithmetic, the pinhole camera, and one bounce of
+// pathtracing::kernel (shade_vertex).  Every unit including this header is compiled
+// with --fmad=false, so all of them evaluate these expressions identically.
+#pragma once
+
+#include "traverse_core.cuh"
+
+#include "../../include/visionaray_gb300/gbrt_rng.h"
+
+#include <cmath>
+
+namespace gbrt {
+namespace {
+
+constexpr uint32_t kLastSpecular = 1u;
+constexpr uint32_t kFirstHit = 2u;
+
+struct v3
+{
+    float x, y, z;
+};
+__device__ __forceinline__ v3 operator+(v3 a, v3 b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
+__device__ __forceinline__ v3 operator-(v3 a, v3 b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+__device__ __forceinline__ v3 operator-(v3 a) { return { -a.x, -a.y, -a.z }; }
+__device__ __forceinline__ v3 operator*(v3 a, v3 b) { return { a.x * b.x, a.y * b.y, a.z * b.z }; }
+__device__ __forceinline__ v3 operator*(v3 a, float s) { return { a.x * s, a.y * s, a.z * s }; }
+__device__ __forceinline__ v3 operator/(v3 a, float s) { return { a.x / s, a.y / s, a.z / s }; }
+__device__ __forceinline__ float dot3(v3 u, v3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+__device__ __forceinline__ v3 cross3(v3 u, v3 v)
+{
+    return { u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x };
+}
+__device__ __forceinline__ float length3(v3 v) { return sqrtf(dot3(v, v)); }
+// normalize(v) = v * (1 / sqrt(dot(v, v))) (math/detail/vector3.inl:332-335)
+__device__ __forceinline__ v3 normalize3(v3 v) { return v * (1.0f / sqrtf(dot3(v, v))); }
+__device__ __forceinline__ v3 faceforward3(v3 n, v3 i, v3 nref) { return dot3(nref, i) < 0.0f ? -n : n; }
+__device__ __forceinline__ float max_elem(v3 v)
+{
+    float m = v.x < v.y ? v.y : v.x;
+    return m < v.z ? v.z : m;
+}
+__device__ __forceinline__ float power_heuristic(float p1, float p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
+__device__ __forceinline__ v3 xyz(float4 a) { return { a.x, a.y, a.z }; }
+
+struct camera_basis
+{
+    float3 eye, U, V, W;
+};
+
+// Primary ray direction of `pixel` for sample `sample`: jitter x drawn before y
+// (detail/sched_common.h:209-233) through the pinhole camera
+// (detail/pinhole_camera.inl:103-120).
+__device__ __forceinline__ v3 primary_dir(camera_basis const& cam, uint32_t width, uint32_t height, uint32_t frame,
+                                          uint32_t pixel, uint32_t sample)
+{
+    float x = float(pixel % width), y = float(pixel / width);
+    float jx = gbrt_rng_u01(frame, pixel, sample, 0) - 0.5f;
+    float jy = gbrt_rng_u01(frame, pixel, sample, 1) - 0.5f;
+    float sx = ((x + jx) + 0.5f) / float(width);
+    float sy = ((y + jy) + 0.5f) / float(height);
+    float u = 2.0f * sx - 1.0f;
+    float v = 2.0f * sy - 1.0f;
+    v3 U = { cam.U.x, cam.U.y, cam.U.z }, V = { cam.V.x, cam.V.y, cam.V.z }, W = { cam.W.x, cam.W.y, cam.W.z };
+    return normalize3(U * u + V * v + W);
+}
+
+struct shade_params
+{
+    const gbrt_material* materials;
+    uint32_t num_materials;
+    const float4* lights;   // 4 float4 per light: v1 | geom bits, e1, e2, intensity | kl
+    uint32_t num_lights;
+    const tri48* tris;
+    int32_t num_tris;
+    float epsilon;
+    float3 ambient;
+    uint32_t frame, sample, bounce, flags;
+    // differentiable renderer: matte colors and emissive colors (3 floats per material
+    // slot) replacing the materials' own; light intensity = emission[geom] * kl
+    const float* albedo;
+    const float* emission;
+};
+
+struct path_state
+{
+    v3 thr, rad;
+    uint32_t k, flags;
+};
+
+// What the adjoint needs of one path vertex (the throughput entering it and the
+// albedo-independent factors of its contributions).
+enum : uint32_t
+{
+    kVertexMiss = 0,
+    kVertexEmission = 1,
+    kVertexMatte = 2,
+    kVertexEnd = 3,   // matte with a zero pdf: the path stops without contributing
+};
+
+struct vertex_rec
+{
+    uint32_t kind, geom, lgeom, nee;
+    v3 thr;
+    float sigma;      // matte: next throughput = thr * albedo * sigma
+    float mis;        // emission: contribution = thr * mis * emission * scale
+    float escale;     // emission: material scale (ls)
+    float kfac;       // NEE: contribution = w * thr * albedo * lint * kfac
+    float w, x, b0;   // NEE: w = power_heuristic(x, b0 * max(thr))
+    float kl;         // NEE: lint = emission[lgeom] * kl
+    v3 lint;
+    float rr;         // Russian roulette normaliser (0: none)
+};
+
+struct vertex_out
+{
+    bool cont, shadow;
+    v3 next_o, next_d;
+    v3 sh_o, sh_d;
+    float sh_tmax;
+    v3 contrib;
+    vertex_rec rec;
+};
+
+__device__ __forceinline__ v3 param3(const float* a, uint32_t i) { return { a[3 * i], a[3 * i + 1], a[3 * i + 2] }; }
+
+// One bounce of pathtracing::kernel::operator() (detail/pathtracing.inl:65-221) for one
+// path whose ray (ori, dir) hit triangle `tri` at `t` (tri < 0: missed).  Updates the
+// path state, adds emission / ambient to st.rad, and returns the next ray and the NEE
+// shadow ray with its unoccluded contribution.  Shared by the wavefront shade kernel
+// and the adjoint's replay, so both compute bit-identical paths.
+__device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p, uint32_t bounce, v3 ori, v3 dir,
+                                             float tmin, float tmax, int tri, float t, path_state& st,
+                                             vertex_out& out, uint32_t* __restrict__ status)
+{
+    const float inv_pi = 3.18309886183790691216444201928e-01f;
+    const float pi = 3.14159265358979323846264338328e+00f;
+    const float two_pi = 6.28318530717958623199592693709e+00f;
+    out.cont = false;
+    out.shadow = false;
+    vertex_rec& rec = out.rec;
+    rec.kind = kVertexMiss;
+    rec.thr = st.thr;
+    rec.nee = 0;
+    rec.rr = 0.0f;
+    rec.geom = 0;
+    rec.lgeom = 0xFFFFFFFFu;
+
+    if (tri < 0 || tri >= sp.num_tris)
+    {
+        // the ray left the scene: ambient light (pathtracing.inl:71-79)
+        v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
+        st.rad = st.rad + amb * st.thr;
+        return;
+    }
+    if (bounce == 0) st.flags |= kFirstHit;
+    float4 t1 = ldg4(&sp.tris[tri].t1);
+    float4 t2 = ldg4(&sp.tris[tri].t2);
+    v3 e1 = xyz(t1), e2 = xyz(t2);
+    uint32_t geom = __float_as_uint(t1.w);
+    v3 view = -dir;
+    v3 isect = ori + dir * t;
+    v3 gn = normalize3(cross3(e1, e2));
+    v3 sn = gn;
+    gbrt_material m;
+    if (geom < sp.num_materials)
+    {
+        m = sp.materials[geom];
+    }
+    else
+    {
+        atomicOr(status, kStatusBadIndex);
+        m = gbrt_material{ GBRT_MATERIAL_MATTE, { 0.0f, 0.0f, 0.0f }, 0.0f };
+        geom = 0;
+    }
+    bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+    v3 mcol = { m.color[0], m.color[1], m.color[2] };
+    if (!emission && sp.albedo) mcol = param3(sp.albedo, geom);
+    if (emission && sp.emission) mcol = param3(sp.emission, geom);
+    rec.geom = geom;
+
+    v3 refl = { 0.0f, 0.0f, 0.0f };
+    float brdf_pdf;
+    v3 src;
+    if (!emission)
+    {
+        // matte::sample -> lambertian::sample_f (matte.inl:40-56, brdf.h:50-76)
+        v3 nn = faceforward3(sn, view, gn);
+        v3 w = nn;
+        v3 v = fabsf(w.x) > fabsf(w.y) ? normalize3(v3{ -w.z, 0.0f, w.x }) : normalize3(v3{ 0.0f, w.z, -w.y });
+        v3 u = cross3(v, w);
+        // cosine_sample_hemisphere(gen.next(), gen.next()), second argument drawn
+        // first as in the reference build (sampling.h:117-127)
+        float u2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float u1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float r = sqrtf(u1);
+        float theta = two_pi * u2;
+        // cos and sin evaluated in double and rounded once to float
+        float ct = float(cos(double(theta)));
+        float sth = float(sin(double(theta)));
+        v3 s3 = { r * ct, r * sth, sqrtf(1.0f - u1) };
+        refl = normalize3(u * s3.x + v * s3.y + w * s3.z);
+        brdf_pdf = dot3(nn, refl) * inv_pi;
+        src = (mcol * m.scale) * inv_pi;
+    }
+    else
+    {
+        brdf_pdf = 1.0f;   // emissive::sample (emissive.inl:28-44)
+        src = mcol * m.scale;
+    }
+    bool zero_pdf = brdf_pdf <= 0.0f;
+
+    float light_pdf = 0.0f;
+    if (sp.num_lights > 0 && emission)
+    {
+        float A = 0.5f * length3(cross3(e1, e2));
+        float ld = length3(isect - ori);
+        v3 L = normalize3(isect - ori);
+        float ldotln = fabsf(dot3(-L, gn));
+        float solid_angle = (ldotln * A) / (ld * ld);
+        light_pdf = 1.0f / solid_angle;
+    }
+    float mis = (bounce > 0 && sp.num_lights > 0 && !(st.flags & kLastSpecular))
+                    ? power_heuristic(brdf_pdf, light_pdf / float(sp.num_lights))
+                    : 1.0f;
+    if (emission)
+    {
+        st.rad = st.rad + (st.thr * mis) * src;
+        rec.kind = kVertexEmission;
+        rec.mis = mis;
+        rec.escale = m.scale;
+        return;
+    }
+    if (zero_pdf)
+    {
+        rec.kind = kVertexEnd;
+        return;
+    }
+    rec.kind = kVertexMatte;
+    v3 nn = faceforward3(sn, view, gn);
+    if (sp.num_lights > 0)
+    {
+        // sample_random_light + area_light::sample + sample_surface
+        // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
+        float ul = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        int lid = int(ul * float(sp.num_lights));
+        if (lid >= int(sp.num_lights)) lid = int(sp.num_lights) - 1;
+        const float4* lp = sp.lights + 4 * lid;
+        float4 l0 = lp[0], l3 = lp[3];
+        v3 lv1 = xyz(l0), le1 = xyz(lp[1]), le2 = xyz(lp[2]), lint = xyz(l3);
+        uint32_t lgeom = __float_as_uint(l0.w);
+        if (sp.emission && lgeom < sp.num_materials) lint = param3(sp.emission, lgeom) * l3.w;
+        float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
+        float sq = sqrtf(s1);
+        v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
+        v3 ldir = pos - isect;
+        float dist = length3(ldir);
+        v3 lnormal = normalize3(cross3(le1, le2));
+        float larea = 0.5f * length3(cross3(le1, le2));
+        float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
+        float lsolid = (ldotln0 * larea) / (dist * dist);
+        float lpdf = 1.0f / lsolid;
+        v3 L = normalize3(ldir);
+        v3 ln = faceforward3(lnormal, -L, lnormal);
+        float ldotn = dot3(L, nn);
+        float ldotln = fabsf(dot3(-L, ln));
+        float bpdf0 = dot3(nn, L) * inv_pi;
+        float bpdf = bpdf0 * max_elem(st.thr);
+        float ndotl = fmaxf(0.0f, dot3(nn, L));
+        v3 cd = (mcol * m.scale) * inv_pi;
+        v3 shade = ((cd * pi) * lint) * ndotl;
+        v3 src2 = (shade * inv_pi) / ldotn;
+        float x = lpdf / float(sp.num_lights);
+        float mis2 = power_heuristic(x, bpdf);
+        if (ldotn > 0.0f && ldotln > 0.0f)
+        {
+            out.contrib = (((st.thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
+            out.shadow = true;
+            out.sh_o = isect + L * sp.epsilon;
+            out.sh_d = L;
+            out.sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon : dist - sp.epsilon;
+            rec.nee = 1;
+            rec.lgeom = sp.emission ? lgeom : 0xFFFFFFFFu;
+            rec.kl = l3.w;
+            rec.lint = lint;
+            rec.w = mis2;
+            rec.x = x;
+            rec.b0 = bpdf0;
+            // contribution = w * thr * albedo * lint * kfac
+            rec.kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
+        }
+    }
+    float cosp = dot3(nn, refl) / brdf_pdf;
+    st.thr = st.thr * (src * cosp);
+    rec.sigma = m.scale * inv_pi * cosp;
+    bool terminate = false;
+    if (bounce >= 2 && !(sp.flags & GBRT_PT_NO_RUSSIAN_ROULETTE))
+    {
+        // Russian roulette (pathtracing.inl:201-213)
+        float prob = max_elem(st.thr);
+        terminate = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++) > prob;
+        st.thr = st.thr / prob;
+        rec.rr = prob;
+    }
+    if (!terminate)
+    {
+        out.cont = true;
+        out.next_o = isect + refl * sp.epsilon;
+        out.next_d = refl;
+        st.flags &= ~kLastSpecular;
+    }
+    (void)tmin;
+    (void)tmax;
+}
+
+// pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) in float, with
+// perspective()'s fovy in radians and aspect = width / height.
+camera_basis camera_for(gbrt_camera const& c, uint32_t width, uint32_t height)
+{
+    auto sub = [](const float* a, const float* b) { return float3{ a[0] - b[0], a[1] - b[1], a[2] - b[2] }; };
+    auto dot = [](float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+    auto cross = [](float3 u, float3 v) {
+        return float3{ u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x };
+    };
+    auto scale = [](float3 a, float s) { return float3{ a.x * s, a.y * s, a.z * s }; };
+    auto normalize = [&](float3 v) { return scale(v, 1.0f / std::sqrt(dot(v, v))); };
+    float3 f = normalize(sub(c.eye, c.center));
+    float3 up = { c.up[0], c.up[1], c.up[2] };
+    float3 s = normalize(cross(up, f));
+    float3 u = cross(f, s);
+    float fovy = c.fovy_degrees * 1.74532925199432957692369076849e-02f;
+    float aspect = float(width) / float(height);
+    float th = std::tan(fovy / 2.0f);
+    camera_basis b;
+    b.eye = { c.eye[0], c.eye[1], c.eye[2] };
+    b.U = scale(scale(s, th), aspect);
+    b.V = scale(u, th);
+    b.W = { -f.x, -f.y, -f.z };
+    return b;
+}
+
+} // namespace
+} // namespace gbrt

@@ -28,7 +28,9 @@ struct trace_result
     float t, u, v;
 };
 
-template <bool AnyHit>
+// Stack: entries of the per-thread stack; a tree taller than that sets
+// kStatusStackOverflow and skips the subtrees that did not fit.
+template <bool AnyHit, int Stack = kStackSize>
 __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict__ nodes,
                                                      const tri48* __restrict__ tris, int32_t root,
                                                      int32_t num_inner, int32_t num_tris, f3 o, f3 d,
@@ -37,7 +39,7 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
     trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
 
-    int stack[kStackSize];
+    int stack[Stack];
     int sp = 0;
     int node = root;
 
@@ -76,7 +78,7 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
                 bool first0 = tn0 < tn1;   // ties go to child 1, as intersect.inl:283
                 int near_child = first0 ? link.x : link.y;
                 int far_child = first0 ? link.y : link.x;
-                if (sp < kStackSize)
+                if (sp < Stack)
                     stack[sp++] = far_child;
                 else
                     atomicOr(status, kStatusStackOverflow);
@@ -242,6 +244,22 @@ __device__ __forceinline__ trace_result traverse_bvh4(const bvh4_node* __restric
         if (node < 0) break;
     }
     return best;
+}
+
+// Segment lookup of the batched kernels: the s with offs[s] <= i < offs[s + 1]
+// (offs: count + 1 non-decreasing entries, offs[count] > i).
+__device__ __forceinline__ uint32_t upper_segment(const uint32_t* __restrict__ offs, uint32_t count, uint32_t i)
+{
+    uint32_t lo = 0, hi = count;
+    while (lo < hi)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&offs[mid + 1]) <= i)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
 // Everything a query needs from a BVH handle, passed to kernels by value.

@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS, RAY, TRIANGLE
+from .types import AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS, RAY, TRIANGLE
 
 LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
 
@@ -51,6 +51,18 @@ SIGNATURES = {
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_forward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_backward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbrt_batch_create": (_i32, [_vp, _vp, _u32, _pp]),
+    "gbrt_batch_destroy": (_i32, [_vp]),
+    "gbrt_batch_build": (_i32, [_vp, _vp, _vp]),
+    "gbrt_batch_export_bvh2": (_i32, [_vp, _vp, _u32, _vp, _vp]),
+    "gbrt_batch_trace_closest_hit": (_i32, [_vp, _vp, _vp, _vp, _vp]),
+    "gbrt_batch_set_frames": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32]),
+    "gbrt_batch_set_launch": (_i32, [_vp, _vp]),
+    "gbrt_batch_get_launch": (_i32, [_vp, _vp]),
+    "gbrt_batch_height": (_i32, [_vp, _vp, _vp]),
+    "gbrt_batch_pathtrace": (_i32, [_vp, _vp, _vp]),
+    "gbrt_batch_run_graph": (_i32, [_vp, _vp, _vp, _vp]),
+    "gbrt_batch_autotune": (_i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
 }
 
 _lib = None
@@ -341,3 +353,112 @@ def pathtrace_backward(scene, camera, params, albedo, emission, image_adjoint, g
                                               _dptr(emission), _dptr(adj), _dptr(grad_albedo),
                                               _dptr(grad_emission)))
     return grad_albedo, grad_emission
+
+
+class Batch:
+    """Many scenes in one BVH arena (gbrt_batch): scene s owns the triangles
+    [offsets[s], offsets[s + 1]) of one concatenated TRIANGLE array.  No visionaray
+    counterpart: the reference builds and renders one scene per call."""
+
+    def __init__(self, offsets, ctx=None):
+        self.ctx = ctx or default_context()
+        self.offsets = np.ascontiguousarray(offsets, np.uint32)
+        self.num_scenes = len(self.offsets) - 1
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbrt_batch_create(self.ctx.h, _hptr(self.offsets), self.num_scenes,
+                                                      ctypes.byref(h)))
+        self.h = h
+        self.pixel_offsets = None
+
+    def build(self, tris):
+        """tris: torch uint8 CUDA tensor of the concatenated triangles (44 bytes each)."""
+        self.ctx.check(self.ctx.lib.gbrt_batch_build(self.ctx.h, self.h, _dptr(tris)))
+
+    def export_bvh2(self, scene):
+        """(nodes, indices) of one scene in the cuda_index_bvh layout."""
+        torch = _torch()
+        n = int(self.offsets[scene + 1] - self.offsets[scene])
+        nn = 2 * n - 1 if n else 0
+        dev = f"cuda:{self.ctx.device}"
+        nodes = torch.empty(max(nn, 1) * 32, dtype=torch.uint8, device=dev)
+        idx = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        self.ctx.check(self.ctx.lib.gbrt_batch_export_bvh2(self.ctx.h, self.h, scene, _dptr(nodes), _dptr(idx)))
+        self.ctx.synchronize()
+        return (nodes.cpu().numpy()[: nn * 32].view(BVH_NODE), idx.cpu().numpy()[:n].view(np.uint32))
+
+    def closest_hit(self, rays, ray_offsets, out=None):
+        """closest_hit of every scene's rays in one launch: scene s traces rays
+        [ray_offsets[s], ray_offsets[s + 1]) of the (n, 8) float32 device tensor."""
+        torch = _torch()
+        ro = np.ascontiguousarray(ray_offsets, np.uint32)
+        n = int(ro[-1])
+        hits = out if out is not None else torch.empty((max(n, 1), 4), dtype=torch.float32, device=rays.device)
+        self.ctx.check(self.ctx.lib.gbrt_batch_trace_closest_hit(self.ctx.h, self.h, _dptr(rays), _hptr(ro),
+                                                                 _dptr(hits)))
+        return hits
+
+    def set_frames(self, cameras, params, materials):
+        cams = np.ascontiguousarray(cameras, CAMERA)
+        pars = np.ascontiguousarray(params, PT_PARAMS)
+        mats = np.ascontiguousarray(materials, MATERIAL)
+        self.ctx.check(self.ctx.lib.gbrt_batch_set_frames(self.ctx.h, self.h, _hptr(cams), _hptr(pars),
+                                                          _hptr(mats), len(mats)))
+        px = pars["width"].astype(np.uint64) * pars["height"].astype(np.uint64)
+        self.pixel_offsets = np.concatenate([[0], np.cumsum(px)]).astype(np.uint64)
+
+    @property
+    def launch(self):
+        out = np.zeros(1, BATCH_LAUNCH)
+        self.ctx.check(self.ctx.lib.gbrt_batch_get_launch(self.h, _hptr(out)))
+        return out[0]
+
+    @launch.setter
+    def launch(self, value):
+        arr = np.asarray([tuple(int(v) for v in value)], BATCH_LAUNCH)
+        self.ctx.check(self.ctx.lib.gbrt_batch_set_launch(self.h, _hptr(arr)))
+
+    def height(self):
+        out = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.gbrt_batch_height(self.ctx.h, self.h, ctypes.byref(out)))
+        return out.value
+
+    def new_images(self):
+        torch = _torch()
+        return torch.empty((max(int(self.pixel_offsets[-1]), 1), 4), dtype=torch.float32,
+                           device=f"cuda:{self.ctx.device}")
+
+    def pathtrace(self, images=None):
+        """One frame of every scene in one persistent launch -> (total_pixels, 4) images."""
+        images = images if images is not None else self.new_images()
+        self.ctx.check(self.ctx.lib.gbrt_batch_pathtrace(self.ctx.h, self.h, _dptr(images)))
+        return images
+
+    def run_graph(self, tris, images):
+        """build + pathtrace replayed from one CUDA graph."""
+        self.ctx.check(self.ctx.lib.gbrt_batch_run_graph(self.ctx.h, self.h, _dptr(tris), _dptr(images)))
+        return images
+
+    def autotune(self, images, reps=2):
+        """Picks the fastest launch shape; returns (launch record, ms per frame)."""
+        best = np.zeros(1, BATCH_LAUNCH)
+        ms = ctypes.c_float()
+        self.ctx.check(self.ctx.lib.gbrt_batch_autotune(self.ctx.h, self.h, _dptr(images), reps, _hptr(best),
+                                                        ctypes.byref(ms)))
+        return best[0], ms.value
+
+    def image(self, images, scene, params):
+        """Scene s's (h, w, 4) view of the batch images."""
+        p = np.asarray(params, PT_PARAMS).reshape(-1)[scene]
+        a, b = int(self.pixel_offsets[scene]), int(self.pixel_offsets[scene + 1])
+        return images[a:b].reshape(int(p["height"]), int(p["width"]), 4)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbrt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -120,3 +120,46 @@ def pt_params(width, height, spp, num_bounces=8, epsilon=1e-4, frame_id=0, sfact
     p["epsilon"], p["frame_id"], p["sfactor"], p["dfactor"] = epsilon, frame_id, sfactor, dfactor
     p["background"], p["ambient"], p["flags"] = background, ambient, flags
     return p[0]
+
+
+BATCH_SIDES = (64, 128, 256, 512)
+
+
+def batch_workload(num_scenes=512, seed=3, n_min=1000, n_max=1_000_000, spp=1, num_bounces=3, frame_id=0):
+    """The batched workload: `num_scenes` random soups (the soup generator with the
+    offset scale 0.5 / cbrt(n)) whose triangle counts are log-uniform in
+    [n_min, n_max], each with a seeded camera on a sphere around the soup looking at its
+    centre and a square resolution drawn from BATCH_SIDES; one matte material of
+    albedo 0.7, white ambient light, `spp` samples of 1 primary ray + (num_bounces - 1)
+    diffuse bounces.  Returns (triangles, offsets, cameras, params, materials)."""
+    import math
+
+    from .types import CAMERA, MATERIAL, MATTE, PT_PARAMS
+    lib = _load()
+    counts = np.empty(num_scenes, np.int64)
+    lo, hi = math.log(n_min), math.log(n_max)
+    for s in range(num_scenes):
+        counts[s] = int(round(math.exp(lo + u01(seed, 1, s) * (hi - lo))))
+    offsets = np.zeros(num_scenes + 1, np.uint32)
+    offsets[1:] = np.cumsum(counts)
+    tris = np.empty(int(offsets[-1]), TRIANGLE)
+    cams = np.zeros(num_scenes, CAMERA)
+    params = np.zeros(num_scenes, PT_PARAMS)
+    for s in range(num_scenes):
+        n = int(counts[s])
+        view = tris[int(offsets[s]):int(offsets[s + 1])]
+        lib.gbrt_scene_soup(n, seed * 1000003 + s, 0.5 / n ** (1.0 / 3.0), _ptr(view))
+        z = 2.0 * u01(seed, 2, s) - 1.0
+        phi = 2.0 * math.pi * u01(seed, 4, s)
+        r = math.sqrt(max(0.0, 1.0 - z * z))
+        d = (r * math.cos(phi), r * math.sin(phi), z)
+        cams[s]["eye"] = (0.5 + 1.6 * d[0], 0.5 + 1.6 * d[1], 0.5 + 1.6 * d[2])
+        cams[s]["center"] = (0.5, 0.5, 0.5)
+        cams[s]["up"] = (0.0, 0.0, 1.0) if abs(d[1]) > 0.9 else (0.0, 1.0, 0.0)
+        cams[s]["fovy_degrees"] = 50.0
+        side = BATCH_SIDES[min(int(u01(seed, 3, s) * len(BATCH_SIDES)), len(BATCH_SIDES) - 1)]
+        params[s] = pt_params(side, side, spp, num_bounces=num_bounces, frame_id=frame_id,
+                              ambient=(1.0, 1.0, 1.0))
+    mats = np.zeros(1, MATERIAL)
+    mats["kind"], mats["color"], mats["scale"] = MATTE, 0.7, 1.0
+    return tris, offsets, cams, params, mats
