@@ -42,6 +42,12 @@ N_NODE_CLOSEST, N_TRI_CLOSEST = 76.92786217, 7.44575715   # B_ray = 2867.1 bytes
 N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
+# of the full-size workload with the default ray order; profiles/
+# trace_rays_permuted_heightfield_2048_dram.md).
+TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.32e9 + 0.170e9, 2.63e9 + 0.547e9
+
+
 def b_ray(n_node, n_tri):
     return 32 + 16 + n_node * 32 + n_tri * 48
 
@@ -441,10 +447,14 @@ def run_ours(args):
         per[name] = rec
     dom = max(per, key=lambda k: per[k]["ms_per_launch"] * 1)
     d = per[dom]
-    roofline = {"bound": "hbm", "kernel": f"trace_rays<{'true' if dom == 'any' else 'false'}>",
+    roofline = {"bound": "hbm", "kernel": (f"trace_rays_permuted<{1 if dom == 'any' else 0}, 0>" if args.trace_flags & 1 else
+                           f"trace_rays<{1 if dom == 'any' else 0}, 0>"),
                 "achieved": d.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
                 "frac": round(d["achieved_gbs"] / peak, 4) if d.get("achieved_gbs") else None,
-                "traffic": None, "peak_source": f"{peak_kind} hbm_gbs"}
+                "traffic": ((TRAFFIC_ANY if dom == "any" else TRAFFIC_CLOSEST)
+                            if (args.grid, args.origins, args.trace_flags) == (GRID, ORIGINS, 1) else None),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size capture",
+                "peak_source": f"{peak_kind} hbm_gbs"}
 
     pt = None
     if args.pt_frames > 0:
