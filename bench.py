@@ -348,6 +348,7 @@ def run_ours(args):
 
     ctx = vg.Context(local)
     ctx.set_trace_flags(args.trace_flags)
+    ctx.set_trace_refill(args.trace_refill)
     stream = ctx.stream
 
     # LBVH build, timed separately (build is not part of the traversal metric)
@@ -483,7 +484,7 @@ def run_ours(args):
                        "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
                        "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
-                       "trace_flags": args.trace_flags},
+                       "trace_flags": args.trace_flags, "trace_refill": args.trace_refill},
             "kernels": per, "roofline": roofline,
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
@@ -508,7 +509,10 @@ def main():
     p.add_argument("--batch-plain-steps", type=int, default=1, help="timed plain per-scene loop steps")
     p.add_argument("--adjoint-steps", type=int, default=200, help="inverse-albedo Adam steps (0: skip)")
     p.add_argument("--trace-flags", type=int, default=1,
-                   help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order, 2: 4-wide nodes)")
+                   help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order, 2: 4-wide nodes, "
+                        "4: persistent traversal)")
+    p.add_argument("--trace-refill", type=int, default=8,
+                   help="persistent traversal (flag 4): idle lanes of a warp that trigger a refill")
     # smaller cases for profiling captures only; the benchmark is the default size
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--origins", type=int, default=ORIGINS)

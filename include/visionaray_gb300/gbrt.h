@@ -115,7 +115,15 @@ int         gbrt_abi_version(void);
  * traverse those instead of the binary node pairs.  Off by default: on the 8.4M-
  * triangle heightfield the 128-byte 4-wide nodes trace slower than the 64-byte pairs. */
 #define GBRT_TRACE_WIDE_NODES 2u
+/* Persistent traversal: a grid that just fills the GPU, whose warps refill idle lanes
+ * with new rays from an atomic counter instead of idling until their slowest ray ends
+ * (node pairs only; hits identical bit for bit).                                     */
+#define GBRT_TRACE_PERSISTENT 4u
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
+
+/* Persistent traversal: a warp refills once at least min_idle_lanes (1..32, default 8)
+ * of its lanes are idle.                                                           */
+gbrt_status gbrt_context_set_trace_refill(gbrt_context* ctx, uint32_t min_idle_lanes);
 
 /* ------------------------------------------------------------------------------ */
 /* BVH construction                                                                */

@@ -172,6 +172,27 @@ def test_sorted_ray_order_gives_identical_hits():
     assert host.tobytes() == plain[0].tobytes()
 
 
+@pytest.mark.parametrize("refill", [1, 8, 32])
+def test_persistent_traversal_gives_identical_hits(refill):
+    """GBRT_TRACE_PERSISTENT (with and without the ray order) changes only which lane
+    traces which ray and when; every hit is the one-thread-per-ray kernel's."""
+    tris = scenes.heightfield(grid=512, seed=3)
+    closest, ao = scenes.surface_rays(tris, 1 << 18, seed=9)
+    ctx = vg.Context(0)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    queries = ((vg.closest_hit, closest), (vg.any_hit, ao), (vg.closest_hit, closest[:1000]))
+    plain = [vg.hits_to_numpy(f(vg.device_rays(r), bvh)) for f, r in queries]
+    ctx.set_trace_refill(refill)
+    for flags in (ctx.TRACE_PERSISTENT, ctx.TRACE_PERSISTENT | ctx.TRACE_SORT_RAYS):
+        ctx.set_trace_flags(flags)
+        got = [vg.hits_to_numpy(f(vg.device_rays(r), bvh)) for f, r in queries]
+        host = vg.any_hit(ao, bvh)
+        ctx.synchronize()
+        for g, p in zip(got, plain):
+            assert g.tobytes() == p.tobytes(), f"flags {flags}"
+        assert host.tobytes() == plain[1].tobytes()
+
+
 def test_wide_and_binary_nodes_agree(oracle):
     """The 4-wide collapse changes the traversal, not the answers."""
     tris = scenes.heightfield(grid=256, seed=5)

@@ -201,9 +201,18 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags)
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;
-    if (flags & ~(GBRT_TRACE_SORT_RAYS | GBRT_TRACE_WIDE_NODES))
+    if (flags & ~(GBRT_TRACE_SORT_RAYS | GBRT_TRACE_WIDE_NODES | GBRT_TRACE_PERSISTENT))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "set_trace_flags: unknown flag");
     ctx->trace_flags = flags;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_set_trace_refill(gbrt_context* ctx, uint32_t min_idle_lanes)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (min_idle_lanes < 1 || min_idle_lanes > 32)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_trace_refill: 1 to 32 lanes");
+    ctx->trace_refill = min_idle_lanes;
     return GBRT_OK;
 }
 
@@ -358,7 +367,7 @@ static gbrt_status trace_device(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray
     if (!aligned16(d_rays) || !aligned16(d_hits))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "trace: ray and hit buffers must be 16-byte aligned");
     device_guard g(ctx->device);
-    if (ctx->trace_flags & GBRT_TRACE_SORT_RAYS)
+    if (ctx->trace_flags & (GBRT_TRACE_SORT_RAYS | GBRT_TRACE_PERSISTENT))
     {
         gbrt_status s2 = ensure_trace_scratch(ctx, n);
         if (s2 != GBRT_OK) return s2;

@@ -48,6 +48,7 @@ struct gbrt_context
     // Ray queries: GBRT_TRACE_* flags and the ray-order scratch of the context stream
     // and of each host-path slot.
     uint32_t trace_flags = 0;
+    uint32_t trace_refill = 8;   // persistent traversal: idle lanes that trigger a refill
     void* trace_scratch = nullptr;
     size_t trace_scratch_bytes = 0;
     void* slot_trace_scratch[kSlots] = { nullptr, nullptr };

@@ -13,9 +13,35 @@ namespace gbrt {
 namespace {
 
 constexpr int kTraceBlock = 128;
+// Entries of the traversal stack held in shared memory (the rest in local memory):
+// 16 x 128 threads x 4 B = 8 KB per block.
+constexpr int kSharedStack = 16;
+// Resident blocks the register allocation must allow (launch bounds): 12 blocks of 128
+// threads = 48 warps per SM at <= 40 registers (the closest-hit variant spills a few
+// words, and still runs faster than at 47 registers and 40 warps).
+constexpr int kMinBlocksAny = 12, kMinBlocksClosest = 12;
+
+// One ray through the node pairs (stack top in shared memory) or the 4-wide nodes.
+template <bool AnyHit, bool Wide>
+__device__ __forceinline__ trace_result trace_one(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
+                                                  uint32_t* __restrict__ status)
+{
+    if constexpr (Wide)
+    {
+        return traverse_bvh4<AnyHit>(v.nodes4, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
+    }
+    else
+    {
+        __shared__ int stack_mem[kSharedStack * kTraceBlock];
+        shared_stack<kSharedStack, kStackSize, kTraceBlock> stack;
+        stack.col = stack_mem + threadIdx.x;
+        return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
+                                         status);
+    }
+}
 
 template <bool AnyHit, bool Wide>
-__global__ void __launch_bounds__(kTraceBlock) trace_rays(bvh_view v, const gbrt_ray* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBlocksClosest) trace_rays(bvh_view v, const gbrt_ray* __restrict__ rays, uint32_t n,
                                                           gbrt_hit* __restrict__ hits,
                                                           uint32_t* __restrict__ status)
 {
@@ -24,7 +50,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays(bvh_view v, const gbrt
 
     float4 r0 = ldg4(&rays[i]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
-    trace_result h = traverse_view<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = trace_one<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[i] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
@@ -32,7 +58,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays(bvh_view v, const gbrt
 
 // Rays in the order perm[0..n): ray j = perm[i] writes hit j.
 template <bool AnyHit, bool Wide>
-__global__ void __launch_bounds__(kTraceBlock) trace_rays_permuted(bvh_view v, const gbrt_ray* __restrict__ rays,
+__global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBlocksClosest) trace_rays_permuted(bvh_view v, const gbrt_ray* __restrict__ rays,
                                                                    uint32_t n, const uint32_t* __restrict__ perm,
                                                                    gbrt_hit* __restrict__ hits,
                                                                    uint32_t* __restrict__ status)
@@ -47,10 +73,172 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_permuted(bvh_view v, c
     }
     float4 r0 = ldg4(&rays[j]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[j]) + 1);
-    trace_result h = traverse_view<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = trace_one<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[j] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
+}
+
+// Persistent traversal with per-lane refill (Aila & Laine 2009, "persistent
+// while-while" with dynamic ray fetch): a grid that just fills the GPU; each warp takes
+// ray indices off one atomic counter for its idle lanes, one warp-aggregated atomic per
+// refill, once at least `refill_min` lanes are idle (or all are).  An iteration walks
+// every busy lane to its next leaf, tests that leaf and pops the stack; a lane whose
+// traversal ends stores its hit and is refilled, so lanes no longer idle until the
+// slowest ray of their warp finishes.  The visit order of each ray is traverse_bvh's,
+// so the hits are identical bit for bit.  perm (may be null): lane k traces ray
+// perm[k].
+template <bool AnyHit>
+__global__ void __launch_bounds__(kTraceBlock) trace_rays_dynamic(bvh_view v, const gbrt_ray* __restrict__ rays,
+                                                                  uint32_t n, const uint32_t* __restrict__ perm,
+                                                                  gbrt_hit* __restrict__ hits,
+                                                                  uint32_t* __restrict__ next_ray, uint32_t refill_min,
+                                                                  uint32_t* __restrict__ status)
+{
+    const uint32_t full = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lanes_below = (1u << lane) - 1u;
+    int stack[kStackSize];
+    int sp = 0;
+    int node = kEmptyLink;
+    uint32_t ray = 0;
+    bool have = false;
+    bool drained = false;   // warp-uniform: the counter has passed n
+    f3 o = { 0.0f, 0.0f, 0.0f }, d = { 0.0f, 0.0f, 0.0f };
+    float ix = 0.0f, iy = 0.0f, iz = 0.0f, tmin = 0.0f, tmax = 0.0f;
+    trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
+
+    for (;;)
+    {
+        const uint32_t idle = __ballot_sync(full, !have);
+        const uint32_t nidle = __popc(idle);
+        if (!drained && nidle != 0 && (nidle >= refill_min || idle == full))
+        {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (int(lane) == leader) base = atomicAdd(next_ray, nidle);
+            base = __shfl_sync(full, base, leader);
+            drained = uint64_t(base) + nidle >= uint64_t(n);
+            if (!have)
+            {
+                const uint64_t k = uint64_t(base) + __popc(idle & lanes_below);
+                if (k < n)
+                {
+                    const uint32_t j = perm ? __ldg(&perm[k]) : uint32_t(k);
+                    if (j < n)
+                    {
+                        float4 r0 = ldg4(&rays[j]);
+                        float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[j]) + 1);
+                        o = { r0.x, r0.y, r0.z };
+                        d = { r0.w, r1.x, r1.y };
+                        tmin = r1.z;
+                        tmax = r1.w;
+                        ix = safe_rcp(d.x);
+                        iy = safe_rcp(d.y);
+                        iz = safe_rcp(d.z);
+                        best = { -1, FLT_MAX, 0.0f, 0.0f };
+                        sp = 0;
+                        node = v.root;
+                        ray = j;
+                        have = true;
+                    }
+                    else
+                    {
+                        atomicOr(status, kStatusBadIndex);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, have)) break;
+        if (!have) continue;
+
+        // inner nodes until a leaf or the end of the traversal (traverse_bvh's loop)
+        while (node >= 0)
+        {
+            if (node >= v.num_inner)
+            {
+                atomicOr(status, kStatusBadIndex);
+                node = kEmptyLink;
+                break;
+            }
+            const bvh2_node* np = v.nodes + node;
+            float4 a = ldg4(&np->xy0);
+            float4 b = ldg4(&np->xy1);
+            float4 z = ldg4(&np->z01);
+            int4 link = __ldg(&np->link);
+            float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
+            float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
+            float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;
+            float lx1 = (b.x - o.x) * ix, hx1 = (b.y - o.x) * ix;
+            float ly1 = (b.z - o.y) * iy, hy1 = (b.w - o.y) * iy;
+            float lz1 = (z.z - o.z) * iz, hz1 = (z.w - o.z) * iz;
+            float tn0 = fmaxf(tmin, fmaxf(fminf(lx0, hx0), fmaxf(fminf(ly0, hy0), fminf(lz0, hz0))));
+            float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
+            float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
+            float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
+            bool h0 = tf0 >= tn0 && tn0 < best.t;
+            bool h1 = tf1 >= tn1 && tn1 < best.t;
+            if (h0 && h1)
+            {
+                bool first0 = tn0 < tn1;
+                int near_child = first0 ? link.x : link.y;
+                int far_child = first0 ? link.y : link.x;
+                if (sp < kStackSize)
+                    stack[sp++] = far_child;
+                else
+                    atomicOr(status, kStatusStackOverflow);
+                node = near_child;
+            }
+            else if (h0 || h1)
+            {
+                node = h0 ? link.x : link.y;
+            }
+            else
+            {
+                node = sp > 0 ? stack[--sp] : kEmptyLink;
+            }
+        }
+        bool done = node == kEmptyLink;
+        if (!done)
+        {
+            for (int t = ~node;; ++t)
+            {
+                if (t >= v.num_tris)
+                {
+                    atomicOr(status, kStatusBadIndex);
+                    break;
+                }
+                const tri48* tp = v.tris + t;
+                float4 t0 = ldg4(&tp->t0);
+                float4 t1 = ldg4(&tp->t1);
+                float4 t2 = ldg4(&tp->t2);
+                tri_hit h = intersect_triangle(o, d, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z }, { t2.x, t2.y, t2.z });
+                if (h.hit && h.t < best.t && h.t >= tmin && h.t <= tmax)
+                {
+                    best = { t, h.t, h.u, h.v };
+                    if (AnyHit)
+                    {
+                        done = true;
+                        break;
+                    }
+                }
+                if (__float_as_uint(t2.w) & kLastInLeaf) break;
+            }
+            if (!done)
+            {
+                node = sp > 0 ? stack[--sp] : kEmptyLink;
+                done = node == kEmptyLink;
+            }
+        }
+        if (done)
+        {
+            uint32_t prim = best.tri >= 0 ? __float_as_uint(ldg4(&v.tris[best.tri].t0).w) : GBRT_NO_HIT;
+            reinterpret_cast<uint4*>(hits)[ray] =
+                make_uint4(prim, __float_as_uint(best.t), __float_as_uint(best.u), __float_as_uint(best.v));
+            have = false;
+            node = kEmptyLink;
+        }
+    }
 }
 
 // 24-bit Morton key of each ray's origin cell (8 bits per axis of the scene box).
@@ -86,9 +274,13 @@ inline size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 } // namespace
 
+// Scratch of one trace call: the persistent kernel's ray counter, then the ray order's
+// keys / values (double-buffered) and the sort's own scratch.
+constexpr size_t kCounterBytes = 256;
+
 size_t trace_scratch_bytes(uint32_t n)
 {
-    return 4 * align256(size_t(n) * 4) + align256(radix_sort_scratch_bytes(n));
+    return kCounterBytes + 4 * align256(size_t(n) * 4) + align256(radix_sort_scratch_bytes(n));
 }
 
 gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays, uint32_t n, gbrt_hit* d_hits,
@@ -104,10 +296,12 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
     }
     const bvh_view v = view_of(bvh);
     const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
-    if ((ctx->trace_flags & GBRT_TRACE_SORT_RAYS) && n >= kSortMinRays && scratch &&
-        scratch_bytes >= trace_scratch_bytes(n))
+    const bool have_scratch = scratch && scratch_bytes >= trace_scratch_bytes(n);
+    const bool persistent = (ctx->trace_flags & GBRT_TRACE_PERSISTENT) && !wide && have_scratch;
+    const uint32_t* perm = nullptr;
+    if ((ctx->trace_flags & GBRT_TRACE_SORT_RAYS) && n >= kSortMinRays && have_scratch)
     {
-        char* base = static_cast<char*>(scratch);
+        char* base = static_cast<char*>(scratch) + kCounterBytes;
         size_t w = align256(size_t(n) * 4);
         uint32_t* keys = reinterpret_cast<uint32_t*>(base);
         uint32_t* vals = reinterpret_cast<uint32_t*>(base + w);
@@ -122,14 +316,31 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         gbrt_status st = radix_sort_pairs(ctx, keys, vals, keys_alt, vals_alt, n, kOriginKeyBits, base + 4 * w,
                                           stream);
         if (st != GBRT_OK) return st;
-        const uint32_t* perm = vals;   // radix_sort_pairs leaves the result in (keys, values)
-        auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
-                                                                                    ctx->d_status); };
-        if (wide)
-            any_hit ? launch(trace_rays_permuted<true, true>) : launch(trace_rays_permuted<false, true>);
-        else
-            any_hit ? launch(trace_rays_permuted<true, false>) : launch(trace_rays_permuted<false, false>);
-        GBRT_LAUNCH_CHECK(ctx, "trace_rays_permuted");
+        perm = vals;   // radix_sort_pairs leaves the result in (keys, values)
+        if (!persistent)
+        {
+            auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
+                                                                                        ctx->d_status); };
+            if (wide)
+                any_hit ? launch(trace_rays_permuted<true, true>) : launch(trace_rays_permuted<false, true>);
+            else
+                any_hit ? launch(trace_rays_permuted<true, false>) : launch(trace_rays_permuted<false, false>);
+            GBRT_LAUNCH_CHECK(ctx, "trace_rays_permuted");
+            return GBRT_OK;
+        }
+    }
+    if (persistent)
+    {
+        uint32_t* counter = static_cast<uint32_t*>(scratch);
+        auto kernel = any_hit ? trace_rays_dynamic<true> : trace_rays_dynamic<false>;
+        int per_sm = 0;
+        GBRT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceBlock, 0));
+        uint32_t grid = uint32_t(ctx->num_sms) * uint32_t(per_sm > 0 ? per_sm : 1);
+        if (grid > blocks) grid = blocks;
+        GBRT_CUDA(ctx, cudaMemsetAsync(counter, 0, 4, stream));
+        kernel<<<grid, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits, counter, ctx->trace_refill,
+                                                 ctx->d_status);
+        GBRT_LAUNCH_CHECK(ctx, "trace_rays_dynamic");
         return GBRT_OK;
     }
     auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, d_hits, ctx->d_status); };

@@ -28,18 +28,47 @@ struct trace_result
     float t, u, v;
 };
 
-// Stack: entries of the per-thread stack; a tree taller than that sets
-// kStatusStackOverflow and skips the subtrees that did not fit.
-template <bool AnyHit, int Stack = kStackSize>
-__device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict__ nodes,
-                                                     const tri48* __restrict__ tris, int32_t root,
-                                                     int32_t num_inner, int32_t num_tris, f3 o, f3 d,
-                                                     float tmin, float tmax, uint32_t* __restrict__ status)
+// Per-thread traversal stacks: `capacity` entries, set(i, v) / get(i).
+template <int N>
+struct local_stack
+{
+    static constexpr int capacity = N;
+    int e[N];
+    __device__ __forceinline__ void set(int i, int v) { e[i] = v; }
+    __device__ __forceinline__ int get(int i) const { return e[i]; }
+};
+
+// The first Shared entries in shared memory, one column per thread (entry i of a thread
+// at col[i * Stride], Stride = threads per block), so the 32 lanes of a warp touch 32
+// different banks whatever their stack depths; deeper entries in local memory.
+template <int Shared, int Total, int Stride>
+struct shared_stack
+{
+    static_assert(Total > Shared, "the local part holds at least one entry");
+    static constexpr int capacity = Total;
+    int* col;
+    int spill[Total - Shared];
+    __device__ __forceinline__ void set(int i, int v)
+    {
+        if (i < Shared)
+            col[i * Stride] = v;
+        else
+            spill[i - Shared] = v;
+    }
+    __device__ __forceinline__ int get(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
+};
+
+// A tree taller than the stack's capacity sets kStatusStackOverflow and skips the
+// subtrees that did not fit.
+template <bool AnyHit, class StackT>
+__device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const bvh2_node* __restrict__ nodes,
+                                                          const tri48* __restrict__ tris, int32_t root,
+                                                          int32_t num_inner, int32_t num_tris, f3 o, f3 d,
+                                                          float tmin, float tmax, uint32_t* __restrict__ status)
 {
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
     trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
 
-    int stack[Stack];
     int sp = 0;
     int node = root;
 
@@ -78,8 +107,8 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
                 bool first0 = tn0 < tn1;   // ties go to child 1, as intersect.inl:283
                 int near_child = first0 ? link.x : link.y;
                 int far_child = first0 ? link.y : link.x;
-                if (sp < Stack)
-                    stack[sp++] = far_child;
+                if (sp < StackT::capacity)
+                    stack.set(sp++, far_child);
                 else
                     atomicOr(status, kStatusStackOverflow);
                 node = near_child;
@@ -90,7 +119,7 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
             }
             else
             {
-                node = sp > 0 ? stack[--sp] : kEmptyLink;
+                node = sp > 0 ? stack.get(--sp) : kEmptyLink;
             }
         }
         if (node == kEmptyLink) break;
@@ -115,9 +144,20 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
             }
             if (__float_as_uint(t2.w) & kLastInLeaf) break;
         }
-        node = sp > 0 ? stack[--sp] : kEmptyLink;
+        node = sp > 0 ? stack.get(--sp) : kEmptyLink;
     }
     return best;
+}
+
+// Stack: entries of a local-memory stack.
+template <bool AnyHit, int Stack = kStackSize>
+__device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict__ nodes,
+                                                     const tri48* __restrict__ tris, int32_t root,
+                                                     int32_t num_inner, int32_t num_tris, f3 o, f3 d,
+                                                     float tmin, float tmax, uint32_t* __restrict__ status)
+{
+    local_stack<Stack> stack;
+    return traverse_bvh_with<AnyHit>(stack, nodes, tris, root, num_inner, num_tris, o, d, tmin, tmax, status);
 }
 
 // The same query over the 4-wide nodes (bvh_layout.cuh): one eight-load node fetch

@@ -34,6 +34,7 @@ SIGNATURES = {
     "gbrt_last_error": (ctypes.c_char_p, [_vp]),
     "gbrt_kernel_launch_count": (_u64, [_vp]),
     "gbrt_context_set_trace_flags": (_i32, [_vp, _u32]),
+    "gbrt_context_set_trace_refill": (_i32, [_vp, _u32]),
     "gbrt_bvh_build_lbvh": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_build_lbvh_host": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_upload_bvh2_host": (_i32, [_vp, _vp, _u32, _vp, _u32, _vp, _u32, _pp]),
@@ -129,10 +130,15 @@ class Context:
 
     TRACE_SORT_RAYS = 1
     TRACE_WIDE_NODES = 2
+    TRACE_PERSISTENT = 4
 
     def set_trace_flags(self, flags):
         """GBRT_TRACE_* options of the ray queries (TRACE_SORT_RAYS: coherent order)."""
         self.check(self.lib.gbrt_context_set_trace_flags(self.h, int(flags)))
+
+    def set_trace_refill(self, min_idle_lanes):
+        """Persistent traversal: idle lanes of a warp that trigger a refill (1..32)."""
+        self.check(self.lib.gbrt_context_set_trace_refill(self.h, int(min_idle_lanes)))
 
     @property
     def launches(self):
