@@ -249,6 +249,12 @@ typedef struct gbrt_camera
     float fovy_degrees;
 } gbrt_camera;
 
+/* pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) for a width x height
+ * image: out = {eye, U, V, W} (12 floats); the primary ray through pixel coordinates
+ * (x, y) has direction normalize(U * (2 (x + 0.5) / width - 1) + V * (2 (y + 0.5) /
+ * height - 1) + W) (pinhole_camera.inl:103-120).  Host-only, no context.            */
+gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint32_t width, uint32_t height, float* out);
+
 /* One frame of the jittered-blend pixel sampler (pixel_sampler_types.h,
  * detail/sched_common.h:427-526) around pathtracing::kernel (pathtracing.inl:42-233):
  * per pixel, spp jittered samples are averaged, then accum = sfactor * average +

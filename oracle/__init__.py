@@ -137,6 +137,9 @@ class Oracle:
         return hits
 
     PT_FLOAT, PT_DOUBLE, PT_FLOAT_TRIG_DOUBLE = 0, 1, 2
+    # or-ed into a mode: the hemisphere sample's two draws in argument order, as
+    # visionaray's device build evaluates them (its CPU build draws the second first)
+    PT_DRAWS_IN_ORDER = 4
 
     def pathtrace(self, tree, tris, materials, lights, camera, params, mode=1, nthreads=0):
         """Per-pixel average RGBA (height, width, 4) of one frame, and the counters

@@ -1,0 +1,133 @@
+"""Times visionaray's own GPU kernels beside the product's on the same GB300.
+
+BENCHMARK INFRASTRUCTURE (runs the reference's device code from
+oracle/_ref/vsnray_ref_gpu.cubin through oracle/ref_gpu.py):
+
+    python oracle/bench_reference_gpu.py [--reps 5] [--pt-spp 64]
+
+Workloads are bench.py's: the 2048x2048 heightfield (8,388,608 triangles) with
+4,194,304 closest-hit and 33,554,432 any-hit AO rays, traced by visionaray's
+closest_hit / any_hit over the cuda_index_bvh that its GPU lbvh_builder produces for
+these triangles (the product's export, byte-identical to it), one thread per ray, best
+of 64/128/256-thread blocks; and the closed-box path-tracing scene at 1920x1080,
+depth 8, through pathtracing::kernel one thread per pixel in cuda_sched's 16x16 blocks.
+The product runs its default configuration on the same inputs.  Times are CUDA events
+on the launching stream, median of `reps` after a warm-up; prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def timed(fn, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.median(out)
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--reps", type=int, default=5)
+    p.add_argument("--pt-spp", type=int, default=64)
+    p.add_argument("--grid", type=int, default=2048)
+    p.add_argument("--origins", type=int, default=1 << 22)
+    args = p.parse_args()
+
+    import torch
+
+    import bench
+    import visionaray_gb300 as vg
+    from oracle import ref_gpu
+    from visionaray_gb300 import build, scenes
+    from visionaray_gb300.types import NO_HIT
+
+    build.build()
+    ref = ref_gpu.ReferenceGPU(0)
+    ctx = vg.default_context(0)
+    ctx.set_trace_flags(ctx.TRACE_SORT_RAYS)
+
+    tris, closest, ao = bench.workload(print, grid=args.grid, origins=args.origins)
+    d_tris = vg.as_device_bytes(tris)
+    bvh = vg.lbvh_builder(ctx).build(d_tris)
+    tree = ref.tree(d_tris, bvh)
+    d_c, d_a = vg.device_rays(closest), vg.device_rays(ao)
+    h_c = torch.empty((len(closest), 4), dtype=torch.float32, device="cuda:0")
+    h_a = torch.empty((len(ao), 4), dtype=torch.float32, device="cuda:0")
+    r_c, r_a = torch.empty_like(h_c), torch.empty_like(h_a)
+
+    res = {"workload": bench.WORKLOAD, "reps": args.reps}
+    ours_c = timed(lambda: vg.closest_hit(d_c, bvh, out=h_c), args.reps)
+    ours_a = timed(lambda: vg.any_hit(d_a, bvh, out=h_a), args.reps)
+    ref_c, ref_a = {}, {}
+    for block in (64, 128, 256):
+        ref_c[block] = timed(lambda: ref.trace(tree, d_c, r_c, any_hit=False, block=block), args.reps)
+        ref_a[block] = timed(lambda: ref.trace(tree, d_a, r_a, any_hit=True, block=block), args.reps)
+    bc, ba = min(ref_c, key=ref_c.get), min(ref_a, key=ref_a.get)
+    ctx.synchronize()
+    hc, rc = vg.hits_to_numpy(h_c), vg.hits_to_numpy(r_c)
+    ha, ra = vg.hits_to_numpy(h_a), vg.hits_to_numpy(r_a)
+    n_rays = len(closest) + len(ao)
+    res["ours"] = {"closest_ms": round(ours_c, 3), "any_ms": round(ours_a, 3),
+                   "mrays_s": round(n_rays / ((ours_c + ours_a) * 1e-3) / 1e6, 1),
+                   "closest_mrays_s": round(len(closest) / (ours_c * 1e-3) / 1e6, 1),
+                   "any_mrays_s": round(len(ao) / (ours_a * 1e-3) / 1e6, 1)}
+    res["reference_gpu"] = {"closest_ms": round(ref_c[bc], 3), "any_ms": round(ref_a[ba], 3),
+                            "closest_block": bc, "any_block": ba,
+                            "mrays_s": round(n_rays / ((ref_c[bc] + ref_a[ba]) * 1e-3) / 1e6, 1),
+                            "closest_mrays_s": round(len(closest) / (ref_c[bc] * 1e-3) / 1e6, 1),
+                            "any_mrays_s": round(len(ao) / (ref_a[ba] * 1e-3) / 1e6, 1),
+                            "all_blocks_ms": {"closest": {k: round(v, 3) for k, v in ref_c.items()},
+                                              "any": {k: round(v, 3) for k, v in ref_a.items()}}}
+    res["traversal_speedup"] = round((ref_c[bc] + ref_a[ba]) / (ours_c + ours_a), 2)
+    hit_o, hit_r = hc["prim_id"] != NO_HIT, rc["prim_id"] != NO_HIT
+    res["agreement"] = {"closest_prim_equal": float((hc["prim_id"] == rc["prim_id"]).mean()),
+                        "closest_hit_flag_equal": float((hit_o == hit_r).mean()),
+                        "ao_occlusion_equal": float(((ha["prim_id"] != NO_HIT) == (ra["prim_id"] != NO_HIT)).mean())}
+    res["tree_height"] = bvh.counts[2]
+    del d_c, d_a, h_c, h_a, r_c, r_a, tree, bvh, d_tris
+    torch.cuda.empty_cache()
+
+    # path tracing: the box scene
+    tris, mats, lights = scenes.box_scene()
+    d_tris = vg.as_device_bytes(tris)
+    bvh = vg.lbvh_builder(ctx).build(d_tris)
+    scene = vg.PTScene(bvh, mats, lights)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(bench.PT_WIDTH, bench.PT_HEIGHT, args.pt_spp, num_bounces=bench.PT_BOUNCES)
+    img_o = torch.zeros((bench.PT_HEIGHT, bench.PT_WIDTH, 4), dtype=torch.float32, device="cuda:0")
+    ms_o = timed(lambda: vg.pathtrace_frame(scene, cam, params, accum=img_o), max(1, args.reps // 2))
+    rscene = ref.pt_scene(ref.tree(d_tris, bvh), mats, lights)
+    img_r = torch.zeros_like(img_o)
+    ms_r = timed(lambda: ref.pathtrace(rscene, cam, params, img_r), max(1, args.reps // 2))
+    ctx.synchronize()
+    samples = bench.PT_WIDTH * bench.PT_HEIGHT * args.pt_spp
+    a, b = img_o[..., :3].double(), img_r[..., :3].double()
+    res["pathtrace"] = {"workload": bench.PT_WORKLOAD.replace("64 spp", f"{args.pt_spp} spp"),
+                        "ours_ms": round(ms_o, 2), "reference_gpu_ms": round(ms_r, 2),
+                        "ours_msamples_s": round(samples / (ms_o * 1e-3) / 1e6, 1),
+                        "reference_gpu_msamples_s": round(samples / (ms_r * 1e-3) / 1e6, 1),
+                        "speedup": round(ms_r / ms_o, 2),
+                        "image_mean": [round(float(a.mean()), 5), round(float(b.mean()), 5)],
+                        "rmse": float(torch.sqrt(((a - b) ** 2).mean()))}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -82,8 +82,9 @@ void orc_trace_linear(const gbrt_triangle* tris, uint32_t ntris, const gbrt_ray*
  * arrays, at the gbrt_rng.h random stream.  mode 0: float, the host's cosf/sinf (the
  * reference build's arithmetic); 1: double (the FP64 oracle); 2: float with the
  * hemisphere sample's cos/sin evaluated in double and rounded once (the CUDA path's
- * arithmetic).  counters (may be NULL) receives {closest rays, shadow rays, box tests,
- * triangle tests}.                                                                 */
+ * arithmetic); mode | 4: the hemisphere sample's two draws in argument order (the
+ * order visionaray's device build evaluates them in).  counters (may be NULL)
+ * receives {closest rays, shadow rays, box tests, triangle tests}.                 */
 void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                    const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
                    const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,

@@ -177,6 +177,10 @@ struct pt_params_ext
 {
     const float* albedo = nullptr;
     const float* emission = nullptr;
+    // cosine_sample_hemisphere(gen.next(), gen.next()) (sampling.h:117-127): the order
+    // of the two draws is unspecified C++; visionaray's CPU build (g++) draws the second
+    // argument first, its device build (nvcc) the first argument first
+    bool draws_in_order = false;
 };
 
 enum : uint32_t
@@ -261,8 +265,17 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             vec<T> u = cross(v, w);
             // cosine_sample_hemisphere(gen.next(), gen.next()): the reference build
             // evaluates the second argument first
-            T u2 = T(gen.next());
-            T u1 = T(gen.next());
+            T u1, u2;
+            if (ext.draws_in_order)
+            {
+                u1 = T(gen.next());
+                u2 = T(gen.next());
+            }
+            else
+            {
+                u2 = T(gen.next());
+                u1 = T(gen.next());
+            }
             T r = std::sqrt(u1);
             T theta = two_pi * u2;
             vec<T> sp = { r * trig_cos(theta, trig_double), r * trig_sin(theta, trig_double),
@@ -386,7 +399,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
 template <typename T>
 void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
             uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, int nthreads, double* out,
-            pt_counters& total, bool trig_double)
+            pt_counters& total, bool trig_double, pt_params_ext const& ext = {})
 {
     // pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) in T
     vec<T> eye = load<T>(cam.eye), center = load<T>(cam.center), up = load<T>(cam.up);
@@ -427,7 +440,7 @@ void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbr
                     vec<T> d = normalize(U * u + V * v + W);
                     bool hit = false;
                     vec<T> c = radiance<T>(s, mats, nmat, lights, nl, p, eye, d, T(0.0), T(FLT_MAX), gen, hit,
-                                           per[size_t(tid)], trig_double);
+                                           per[size_t(tid)], trig_double, ext);
                     if (hit)
                     {
                         sum = sum + c;
@@ -641,10 +654,13 @@ extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* no
 {
     scene_arrays s{ tris, nodes, num_nodes, indices };
     pt_counters c;
+    pt_params_ext ext;
+    ext.draws_in_order = (mode & 4) != 0;   // the device build's draw order
+    mode &= 3;
     if (mode == 1)
-        render<double>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, false);
+        render<double>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, false, ext);
     else
-        render<float>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, mode == 2);
+        render<float>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, mode == 2, ext);
     if (counters)
     {
         counters[0] = c.closest;

@@ -9,4 +9,4 @@ from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, FLT_MAX, HIT, MA
 from .runtime import (Batch, Context, GbrtError, IndexBVH, PTScene, any_hit, closest_hit,  # noqa: F401
                       default_context, device_rays, as_device_bytes, hits_to_numpy,
                       lbvh_builder, load_library, pathtrace_backward, pathtrace_forward,
-                      pathtrace_frame)
+                      pathtrace_frame, pinhole_camera_basis)

@@ -7,6 +7,9 @@ GPU host):
   oracle/_build/liboracle.so               CPU oracle (test infrastructure)
   oracle/_ref/libvsnray_ref.so             visionaray's own CPU code, only where its
                                            headers are present (test infrastructure)
+  oracle/_ref/vsnray_ref_gpu.cubin         visionaray's own GPU traversal and path tracer
+                                           (device code, sm_103a), only where its headers
+                                           are present (benchmark infrastructure)
 Translation units compile in parallel; an up-to-date output is not rebuilt.
 """
 import os
@@ -41,6 +44,8 @@ LIBGBRT = os.path.join(LIB, "libgbrt.so")
 LIBSCENES = os.path.join(LIB, "libgbrt_scenes.so")
 LIBORACLE = os.path.join(ORACLE, "_build", "liboracle.so")
 LIBREF = os.path.join(ORACLE, "_ref", "libvsnray_ref.so")
+REFCUBIN = os.path.join(ORACLE, "_ref", "vsnray_ref_gpu.cubin")
+REFCUBIN_EXACT = os.path.join(ORACLE, "_ref", "vsnray_ref_gpu_exact.cubin")
 
 
 def _stale(out, deps):
@@ -96,6 +101,19 @@ def build(verbose=False, with_reference=True):
         os.makedirs(os.path.dirname(LIBREF), exist_ok=True)
         jobs.append(("reference", oracle_flags + ["-w", "-DNDEBUG", "-I" + REFERENCE_INCLUDE, "-o", LIBREF,
                                                   ref_src, "-lpthread"]))
+    # visionaray's own GPU traversal and path-tracing kernel as device code only (a cubin
+    # runs on the GPU host whatever its CPU); built only where the headers are
+    # (default nvcc contraction, as visionaray's own build; and a --fmad=false twin whose
+    # arithmetic is the CPU reference's, for parity checks)
+    ref_gpu_src = os.path.join(ORACLE, "ref_gpu.cu")
+    ref_gpu_deps = [ref_gpu_src, os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h"),
+                    os.path.join(ROOT, "include", "visionaray_gb300", "gbrt_rng.h")]
+    for cubin, extra in ((REFCUBIN, []), (REFCUBIN_EXACT, ["--fmad=false"])):
+        if have_ref and _stale(cubin, ref_gpu_deps):
+            os.makedirs(os.path.dirname(cubin), exist_ok=True)
+            jobs.append(("reference-gpu", [NVCC, "-cubin"] + ARCH + extra + [
+                "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-w", "-I" + REFERENCE_INCLUDE, ref_gpu_src,
+                "-o", cubin]))
     if verbose:
         for n, c in jobs:
             print(n, " ".join(c))

@@ -488,6 +488,20 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
     return GBRT_OK;
 }
 
+extern "C" gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint32_t width, uint32_t height, float* out)
+{
+    if (!camera || !out || width == 0 || height == 0) return GBRT_ERR_INVALID_ARG;
+    camera_basis b = camera_for(*camera, width, height);
+    const float3 v[4] = { b.eye, b.U, b.V, b.W };
+    for (int k = 0; k < 4; ++k)
+    {
+        out[3 * k + 0] = v[k].x;
+        out[3 * k + 1] = v[k].y;
+        out[3 * k + 2] = v[k].z;
+    }
+    return GBRT_OK;
+}
+
 extern "C" gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene)
 {
     if (!scene) return GBRT_ERR_INVALID_ARG;

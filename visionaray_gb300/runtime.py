@@ -49,6 +49,7 @@ SIGNATURES = {
     "gbrt_trace_any_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_pt_scene_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_pt_scene_destroy": (_i32, [_vp]),
+    "gbrt_pinhole_camera_basis": (_i32, [_vp, _u32, _u32, _vp]),
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_forward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_backward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -308,6 +309,16 @@ class PTScene:
             self.close()
         except Exception:
             pass
+
+
+def pinhole_camera_basis(camera, width, height):
+    """pinhole_camera::begin_frame: (eye, U, V, W) as a (4, 3) float32 array."""
+    cam = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+    out = np.zeros((4, 3), np.float32)
+    st = load_library().gbrt_pinhole_camera_basis(_hptr(cam), int(width), int(height), _hptr(out))
+    if st != 0:
+        raise GbrtError(st, "gbrt_pinhole_camera_basis: bad camera or size")
+    return out
 
 
 def pathtrace_frame(scene, camera, params, accum=None, color=None):
