@@ -45,7 +45,7 @@ N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
 # of the full-size workload with the default ray order; profiles/
 # trace_rays_permuted_heightfield_2048_dram.md).
-TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.32e9 + 0.170e9, 2.63e9 + 0.547e9
+TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.37e9 + 0.154e9, 2.60e9 + 0.526e9
 
 
 def b_ray(n_node, n_tri):
@@ -220,7 +220,7 @@ BATCH_WORKLOAD = ("512 random-soup scenes (triangle counts log-uniform in [1k, 1
                   "of every scene")
 
 
-def run_batch(vg, ctx, steps, plain_steps, rprint):
+def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_000_000):
     """The batched graph (build + frame of 512 scenes in one CUDA graph, autotuned
     persistent launch) against the plain per-scene loop (gbrt_bvh_build_lbvh +
     gbrt_pathtrace_frame per scene) on the same GPU; Msamples/s of both and whether
@@ -229,7 +229,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint):
     from visionaray_gb300 import scenes
     from visionaray_gb300.types import AREA_LIGHT
     t0 = time.time()
-    tris, offsets, cams, params, mats = scenes.batch_workload()
+    tris, offsets, cams, params, mats = scenes.batch_workload(num_scenes=num_scenes, n_max=max_tris)
     gen_s = time.time() - t0
     ns = len(offsets) - 1
     d_tris = vg.as_device_bytes(tris, ctx.device)
@@ -294,7 +294,9 @@ def run_batch(vg, ctx, steps, plain_steps, rprint):
     plain_launches = (ctx.launches - launches0) // plain_steps
     identical = bool(torch.equal(images.view(torch.int32), plain_images.view(torch.int32)))
     mean = float(images[:, :3].mean().item())
-    res = {"workload": BATCH_WORKLOAD, "scenes": ns, "triangles": int(offsets[-1]),
+    workload = BATCH_WORKLOAD if (num_scenes, max_tris) == (512, 1_000_000) else (
+        f"REDUCED profiling case: {num_scenes} scenes, triangle counts log-uniform in [1k, {max_tris}]")
+    res = {"workload": workload, "scenes": ns, "triangles": int(offsets[-1]),
            "samples_per_step": samples, "generate_s": round(gen_s, 1), "tallest_tree": height,
            "batched": {"ms_per_step": round(batch_ms, 2), "msamples_s": round(samples / (batch_ms * 1e-3) / 1e6, 2),
                        "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
@@ -463,7 +465,8 @@ def run_ours(args):
 
     batched = None
     if args.batch_steps > 0:
-        batched = run_batch(vg, ctx, args.batch_steps, args.batch_plain_steps, rprint)
+        batched = run_batch(vg, ctx, args.batch_steps, args.batch_plain_steps, rprint, args.batch_scenes,
+                            args.batch_max_tris)
 
     adjoint = None
     if args.adjoint_steps > 0:
@@ -508,6 +511,8 @@ def main():
     p.add_argument("--batch-steps", type=int, default=3, help="timed batched-graph steps (0: skip)")
     p.add_argument("--batch-plain-steps", type=int, default=1, help="timed plain per-scene loop steps")
     p.add_argument("--adjoint-steps", type=int, default=200, help="inverse-albedo Adam steps (0: skip)")
+    p.add_argument("--batch-scenes", type=int, default=512, help="(profiling only) scenes of the batch leg")
+    p.add_argument("--batch-max-tris", type=int, default=1_000_000, help="(profiling only) largest batch scene")
     p.add_argument("--trace-flags", type=int, default=1,
                    help="GBRT_TRACE_* bits of the ray queries (1: coherent ray order, 2: 4-wide nodes, "
                         "4: persistent traversal)")
