@@ -280,19 +280,28 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
             sc.close()
             bvh.close()
 
-    plain_step()   # warm-up (grows the context scratch to the largest scene)
-    ctx.synchronize()
-    launches0 = ctx.launches
-    torch.cuda.synchronize()
-    ev[0].record(ctx.stream)
-    for _ in range(plain_steps):
-        plain_step()
-    ev[1].record(ctx.stream)
-    torch.cuda.synchronize()
-    ctx.synchronize()
-    plain_ms = ev[0].elapsed_time(ev[1]) / plain_steps
-    plain_launches = (ctx.launches - launches0) // plain_steps
-    identical = bool(torch.equal(images.view(torch.int32), plain_images.view(torch.int32)))
+    def time_plain():
+        plain_step()   # warm-up (grows the context scratch to the largest scene)
+        ctx.synchronize()
+        launches0 = ctx.launches
+        torch.cuda.synchronize()
+        ev[0].record(ctx.stream)
+        for _ in range(plain_steps):
+            plain_step()
+        ev[1].record(ctx.stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        plain_ms = ev[0].elapsed_time(ev[1]) / plain_steps
+        plain_launches = (ctx.launches - launches0) // plain_steps
+        identical = bool(torch.equal(images.view(torch.int32), plain_images.view(torch.int32)))
+        return ({"ms_per_step": round(plain_ms, 2), "msamples_s": round(samples / (plain_ms * 1e-3) / 1e6, 2),
+                 "gpu_launches_per_step": int(plain_launches), "steps": plain_steps},
+                round(plain_ms / batch_ms, 2), identical)
+
+    if plain_steps <= 0:
+        res_plain, speedup, identical = None, None, None
+    else:
+        res_plain, speedup, identical = time_plain()
     mean = float(images[:, :3].mean().item())
     workload = BATCH_WORKLOAD if (num_scenes, max_tris) == (512, 1_000_000) else (
         f"REDUCED profiling case: {num_scenes} scenes, triangle counts log-uniform in [1k, {max_tris}]")
@@ -302,9 +311,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
                        "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
                        "steps": steps, "launch": {k: int(best[k]) for k in best.dtype.names},
                        "autotune_frame_ms": round(float(tune_ms), 2), "autotune_s": round(tune_s, 1)},
-           "plain": {"ms_per_step": round(plain_ms, 2), "msamples_s": round(samples / (plain_ms * 1e-3) / 1e6, 2),
-                     "gpu_launches_per_step": int(plain_launches), "steps": plain_steps},
-           "speedup": round(plain_ms / batch_ms, 2), "images_bit_identical": identical,
+           "plain": res_plain, "speedup": speedup, "images_bit_identical": identical,
            "image_mean": round(mean, 5)}
     batch.close()
     del d_tris, images, plain_images, views
