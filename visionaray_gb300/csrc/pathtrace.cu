@@ -38,6 +38,14 @@ namespace gbrt {
 namespace {
 
 constexpr int kBlock = 128;
+// Traversal kernels (extend, shadow): the stack's first entries in shared memory and
+// launch bounds for 12 resident blocks (48 warps), as the ray-query kernels.
+constexpr int kPtSharedStack = 16;
+constexpr int kPtMinBlocks = 12;
+// The adjoint's replay kernel: resident blocks its registers must allow -- 16 blocks
+// (64 warps, 32 registers; the vertex records live in local memory anyway): backward
+// 15.4 -> 13.0 ms per inverse-rendering step (8 blocks 13.4, 12 blocks 14.3).
+constexpr int kAdjointMinBlocks = 16;
 
 struct frame_buffers
 {
@@ -99,7 +107,8 @@ __global__ void __launch_bounds__(kBlock) pt_raygen(frame_buffers fb, uint32_t w
 }
 
 template <bool Wide>
-__global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, bvh_view v, uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend(frame_buffers fb, int q, bvh_view v,
+                                                                  uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i == 0)
@@ -111,7 +120,8 @@ __global__ void __launch_bounds__(kBlock) pt_extend(frame_buffers fb, int q, bvh
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
     float4 r0 = rp[0], r1 = rp[1];
-    trace_result h = traverse_view<false, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = traverse_view_shared<false, Wide, kBlock, kPtSharedStack>(v, { r0.x, r0.y, r0.z },
+                                                                              { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     fb.hits[i] = make_uint4(uint32_t(h.tri), __float_as_uint(h.t), 0u, 0u);
 }
 
@@ -162,14 +172,16 @@ __global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shad
 }
 
 template <bool Wide>
-__global__ void __launch_bounds__(kBlock) pt_shadow(frame_buffers fb, bvh_view v, uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow(frame_buffers fb, bvh_view v,
+                                                                  uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     uint32_t n = fb.counts[2];
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(&fb.shadow_rays[i]);
     float4 r0 = rp[0], r1 = rp[1];
-    trace_result h = traverse_view<true, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = traverse_view_shared<true, Wide, kBlock, kPtSharedStack>(v, { r0.x, r0.y, r0.z },
+                                                                             { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     if (h.tri < 0)
     {
         uint32_t p = fb.shadow_path[i];
@@ -255,7 +267,7 @@ __device__ __forceinline__ void warp_add3(float* __restrict__ base, uint32_t key
 // forward frame is stored.  Geometry, visibility and the Russian-roulette decision are
 // not differentiated (the roulette's 1 / p weight is).
 template <bool Wide>
-__global__ void __launch_bounds__(kBlock) pt_adjoint(bvh_view v, shade_params sp, camera_basis cam, uint32_t width,
+__global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view v, shade_params sp, camera_basis cam, uint32_t width,
                                                      uint32_t height, uint32_t spp, uint32_t num_bounces,
                                                      const float4* __restrict__ img_adj, float* __restrict__ grad_albedo,
                                                      float* __restrict__ grad_emission, uint32_t* __restrict__ status)

@@ -26,18 +26,7 @@ template <bool AnyHit, bool Wide>
 __device__ __forceinline__ trace_result trace_one(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
                                                   uint32_t* __restrict__ status)
 {
-    if constexpr (Wide)
-    {
-        return traverse_bvh4<AnyHit>(v.nodes4, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
-    }
-    else
-    {
-        __shared__ int stack_mem[kSharedStack * kTraceBlock];
-        shared_stack<kSharedStack, kStackSize, kTraceBlock> stack;
-        stack.col = stack_mem + threadIdx.x;
-        return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
-                                         status);
-    }
+    return traverse_view_shared<AnyHit, Wide, kTraceBlock, kSharedStack>(v, o, d, tmin, tmax, status);
 }
 
 template <bool AnyHit, bool Wide>

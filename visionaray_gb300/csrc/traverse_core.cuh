@@ -326,4 +326,24 @@ __device__ __forceinline__ trace_result traverse_view(bvh_view const& v, f3 o, f
     return traverse_bvh<AnyHit>(v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax, status);
 }
 
+// A query through the node pairs with the stack's first Shared entries in shared
+// memory (a column per thread of a Block-thread block), or through the 4-wide nodes.
+template <bool AnyHit, bool Wide, int Block, int Shared>
+__device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
+                                                             uint32_t* __restrict__ status)
+{
+    if constexpr (Wide)
+    {
+        return traverse_bvh4<AnyHit>(v.nodes4, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
+    }
+    else
+    {
+        __shared__ int stack_mem[Shared * Block];
+        shared_stack<Shared, kStackSize, Block> stack;
+        stack.col = stack_mem + threadIdx.x;
+        return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
+                                         status);
+    }
+}
+
 } // namespace gbrt
