@@ -319,14 +319,14 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     return res
 
 
-def run_adjoint(ctx, steps, rprint):
+def run_adjoint(ctx, steps, rprint, flags=0):
     """The inverse-albedo workload: `steps` Adam steps of forward frame + L2 loss +
     path-replay adjoint; median forward / backward times and their ratio."""
     from visionaray_gb300 import inverse
-    r = inverse.optimize(steps=steps, ctx=ctx)
+    r = inverse.optimize(steps=steps, ctx=ctx, extra_flags=flags)
     return {"workload": "inverse albedo on the box scene reduced to 4,014 triangles (2 blobs, subdiv 10): "
                         "512x512, 16 spp, depth 6 forward + L2 loss + adjoint per step, target 256 spp",
-            "steps": steps, "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
+            "steps": steps, "flags": int(inverse.FLAGS | flags), "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
             "bwd_over_fwd": round(r["bwd_ms"] / r["fwd_ms"], 3), "loss_start": round(r["losses"][0], 6),
             "loss_end": round(r["losses"][-1], 6), "albedo_error_start": round(r["albedo_error_start"], 4),
             "albedo_error_end_seen": round(r["albedo_error_end_seen"], 4)}
@@ -468,7 +468,7 @@ def run_ours(args):
 
     pt = None
     if args.pt_frames > 0:
-        pt = run_pathtrace(vg, ctx, args.pt_frames, 0, rprint)
+        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint)
 
     batched = None
     if args.batch_steps > 0:
@@ -477,7 +477,7 @@ def run_ours(args):
 
     adjoint = None
     if args.adjoint_steps > 0:
-        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint)
+        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint, args.pt_flags)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -515,6 +515,8 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--pt-flags", type=int, default=0,
+                   help="GBRT_PT_* scheduling bits of the path-tracing and adjoint legs (4: megakernel)")
     p.add_argument("--batch-steps", type=int, default=3, help="timed batched-graph steps (0: skip)")
     p.add_argument("--batch-plain-steps", type=int, default=1, help="timed plain per-scene loop steps")
     p.add_argument("--adjoint-steps", type=int, default=200, help="inverse-albedo Adam steps (0: skip)")

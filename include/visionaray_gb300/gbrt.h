@@ -287,6 +287,11 @@ typedef struct gbrt_pt_params
  * differentiable renderer uses it so that finite differences at common random numbers
  * are smooth in the albedos (a roulette decision would jump).                     */
 #define GBRT_PT_NO_RUSSIAN_ROULETTE 2u
+/* Scheduling only: one thread per pixel runs all its samples and bounces (one launch
+ * per frame, shadow rays traced in-thread) instead of the wavefront passes.  Same
+ * arithmetic and random numbers: the images are identical bit for bit.  About 2x
+ * slower than the wavefront on the box and inverse-rendering workloads (GB300).     */
+#define GBRT_PT_MEGAKERNEL 4u
 
 typedef struct gbrt_pt_scene gbrt_pt_scene;
 

@@ -94,3 +94,40 @@ def test_full_box_scene_reduced_resolution(oracle):
     s = stats(gpu, ref)
     assert s["exact"] >= 0.97, s
     assert s["rmse"] <= 0.02 * s["mean"], s
+
+
+@pytest.mark.parametrize("flags", [0, PT_SHADOW_RANGE_FIX, PT_SHADOW_RANGE_FIX | 2])
+def test_megakernel_equals_wavefront(small_box, flags):
+    """GBRT_PT_MEGAKERNEL changes the scheduling only: same image bit for bit, including
+    the progressive blend and the color output."""
+    from visionaray_gb300.types import PT_MEGAKERNEL
+    tris, mats, lights, cam = small_box
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    scene = vg.PTScene(bvh, mats, lights)
+    out = []
+    for mega in (0, PT_MEGAKERNEL):
+        accum = torch.zeros((48, 80, 4), dtype=torch.float32, device="cuda:0")
+        color = torch.zeros_like(accum)
+        for f in range(3):
+            p = scenes.pt_params(80, 48, 3, num_bounces=6, frame_id=20 + f, sfactor=1.0 / (f + 1),
+                                 dfactor=1.0 - 1.0 / (f + 1), flags=flags | mega)
+            vg.pathtrace_frame(scene, cam, p, accum=accum, color=color)
+        bvh.ctx.synchronize()
+        out.append((accum.cpu().numpy(), color.cpu().numpy()))
+    assert out[0][0].tobytes() == out[1][0].tobytes()
+    assert out[0][1].tobytes() == out[1][1].tobytes()
+
+
+def test_megakernel_equals_wavefront_ambient_and_empty():
+    from visionaray_gb300.types import AREA_LIGHT, MATERIAL, PT_MEGAKERNEL
+    tris = scenes.soup(5000, seed=8, offset=0.03)
+    mats = np.zeros(1, MATERIAL)
+    mats["color"], mats["scale"] = (0.6, 0.7, 0.8), 1.0
+    cam = scenes.box_camera(eye=(0.5, 0.5, -1.0), center=(0.5, 0.5, 0.5), fovy_degrees=45.0)
+    for t in (tris, tris[:0]):
+        bvh = vg.lbvh_builder().build(vg.as_device_bytes(t) if len(t) else t)
+        scene = vg.PTScene(bvh, mats, np.zeros(0, AREA_LIGHT))
+        imgs = [vg.pathtrace_frame(scene, cam, scenes.pt_params(33, 17, 4, num_bounces=4, ambient=(1.0, 0.5, 0.25),
+                                                                background=(0.1, 0.2, 0.3, 0.5), flags=m)).cpu()
+                for m in (0, PT_MEGAKERNEL)]
+        assert imgs[0].numpy().tobytes() == imgs[1].numpy().tobytes()

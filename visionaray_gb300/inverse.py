@@ -42,14 +42,15 @@ def l2_adjoint(image, target):
     return float(loss), adj
 
 
-def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_spp=256, ctx=None, log=None):
+def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_spp=256, ctx=None, log=None,
+             extra_flags=0):
     """Adam on the albedos.  Returns a dict with the loss history, the parameter error
     and the mean forward / backward times (CUDA events)."""
     import torch
     ctx = ctx or rt.default_context()
     scene, tris, mats, lights, hidden, emission = setup(ctx=ctx)
     cam = scenes.box_camera()
-    tparams = scenes.pt_params(width, height, target_spp, num_bounces=depth, frame_id=1000, flags=FLAGS)
+    tparams = scenes.pt_params(width, height, target_spp, num_bounces=depth, frame_id=1000, flags=FLAGS | extra_flags)
     target = rt.pathtrace_forward(scene, cam, tparams, hidden, emission)
     albedo = torch.full_like(hidden, 0.5)
     m = torch.zeros_like(albedo)
@@ -59,7 +60,7 @@ def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_
     fwd_ms, bwd_ms, losses = [], [], []
     image = None
     for it in range(steps):
-        params = scenes.pt_params(width, height, spp, num_bounces=depth, frame_id=it, flags=FLAGS)
+        params = scenes.pt_params(width, height, spp, num_bounces=depth, frame_id=it, flags=FLAGS | extra_flags)
         ev[0].record(ctx.stream)
         image = rt.pathtrace_forward(scene, cam, params, albedo, emission, image=image)
         ev[1].record(ctx.stream)
