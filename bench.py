@@ -226,11 +226,19 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     gbrt_pathtrace_frame per scene) on the same GPU; Msamples/s of both and whether
     their images are bit-identical."""
     import torch
-    from visionaray_gb300 import scenes
+    from visionaray_gb300 import replicas, scenes
     from visionaray_gb300.types import AREA_LIGHT
     t0 = time.time()
     tris, offsets, cams, params, mats = scenes.batch_workload(num_scenes=num_scenes, n_max=max_tris)
     gen_s = time.time() - t0
+    world, rank, _ = replicas.world_from_env()
+    if world > 1:
+        # whole scenes per rank, balanced by cost; every rank computes the same partition
+        mine = replicas.partition(replicas.scene_costs(offsets, params), world)[rank]
+        tris = np.concatenate([tris[int(offsets[s]):int(offsets[s + 1])] for s in mine])
+        sizes = [int(offsets[s + 1] - offsets[s]) for s in mine]
+        offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+        cams, params = cams[mine], params[mine]
     ns = len(offsets) - 1
     d_tris = vg.as_device_bytes(tris, ctx.device)
     del tris
@@ -242,7 +250,9 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     best, tune_ms = batch.autotune(images, reps=1)
     tune_s = time.time() - t0
     height = batch.height()
-    samples = int(batch.pixel_offsets[-1]) * int(params["spp"][0])
+    # the whole job's samples (every rank renders its own scenes)
+    samples = int(replicas.reduce_over_ranks(int(batch.pixel_offsets[-1]) * int(params["spp"][0]), "sum",
+                                             f"cuda:{ctx.device}"))
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
     for _ in range(3):
@@ -255,7 +265,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     ev[1].record(ctx.stream)
     torch.cuda.synchronize()
     ctx.synchronize()
-    batch_ms = ev[0].elapsed_time(ev[1]) / steps
+    batch_ms = replicas.reduce_over_ranks(ev[0].elapsed_time(ev[1]) / steps, "max", f"cuda:{ctx.device}")
     batch_launches = (ctx.launches - launches0) // steps
     # the frame alone (persistent kernel), for the breakdown
     ev[0].record(ctx.stream)
@@ -291,9 +301,10 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
         ev[1].record(ctx.stream)
         torch.cuda.synchronize()
         ctx.synchronize()
-        plain_ms = ev[0].elapsed_time(ev[1]) / plain_steps
+        plain_ms = replicas.reduce_over_ranks(ev[0].elapsed_time(ev[1]) / plain_steps, "max", f"cuda:{ctx.device}")
         plain_launches = (ctx.launches - launches0) // plain_steps
-        identical = bool(torch.equal(images.view(torch.int32), plain_images.view(torch.int32)))
+        differ = 0.0 if torch.equal(images.view(torch.int32), plain_images.view(torch.int32)) else 1.0
+        identical = replicas.reduce_over_ranks(differ, "sum", f"cuda:{ctx.device}") == 0.0
         return ({"ms_per_step": round(plain_ms, 2), "msamples_s": round(samples / (plain_ms * 1e-3) / 1e6, 2),
                  "gpu_launches_per_step": int(plain_launches), "steps": plain_steps},
                 round(plain_ms / batch_ms, 2), identical)
@@ -305,7 +316,9 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     mean = float(images[:, :3].mean().item())
     workload = BATCH_WORKLOAD if (num_scenes, max_tris) == (512, 1_000_000) else (
         f"REDUCED profiling case: {num_scenes} scenes, triangle counts log-uniform in [1k, {max_tris}]")
-    res = {"workload": workload, "scenes": ns, "triangles": int(offsets[-1]),
+    res = {"workload": workload, "scenes": int(replicas.reduce_over_ranks(ns, "sum", f"cuda:{ctx.device}")),
+           "parallelism": f"scenes partitioned over {world} GPU(s)" if world > 1 else "one GPU",
+           "triangles": int(replicas.reduce_over_ranks(int(offsets[-1]), "sum", f"cuda:{ctx.device}")),
            "samples_per_step": samples, "generate_s": round(gen_s, 1), "tallest_tree": height,
            "batched": {"ms_per_step": round(batch_ms, 2), "msamples_s": round(samples / (batch_ms * 1e-3) / 1e6, 2),
                        "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
@@ -339,11 +352,8 @@ def run_ours(args):
     import visionaray_gb300 as vg
     from visionaray_gb300.types import HIT
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    from visionaray_gb300 import replicas
+    world, rank, local = replicas.init("nccl")
     torch.cuda.set_device(local)
     dev = f"cuda:{local}"
 
@@ -395,8 +405,7 @@ def run_ours(args):
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = ctx.launches
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         start.record(stream)
@@ -404,17 +413,13 @@ def run_ours(args):
             step(events[k])
         stop.record(stream)
         torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     gpu_launches = ctx.launches - launches0
     ctx.synchronize()   # raises on a flagged stack overflow / bad index
     total_ms = start.elapsed_time(stop)
     t_closest = [e[0].elapsed_time(e[1]) for e in events]
     t_any = [e[1].elapsed_time(e[2]) for e in events]
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.reduce_over_ranks(total_ms, "max", dev)   # the slowest rank
     ms_per_step = total_ms / args.steps
     value = world * rays_per_step * args.steps / (total_ms * 1e-3) / 1e6
 
@@ -428,17 +433,13 @@ def run_ours(args):
     e2e_steps = max(1, min(args.steps, 5))
     vg.closest_hit(np_c, bvh, out=np_oc)
     vg.any_hit(np_a, bvh, out=np_oa)
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         vg.closest_hit(np_c, bvh, out=np_oc)
         vg.any_hit(np_a, bvh, out=np_oa)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.reduce_over_ranks(e2e_s, "max", dev)
     e2e_value = world * rays_per_step / e2e_s / 1e6
     # the host path must give the device path's answers
     same = bool((np_oc.view(np.uint8) == h_closest.cpu().numpy().view(np.uint8).reshape(-1)).all())
@@ -503,6 +504,7 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
+        import torch.distributed as dist
         dist.destroy_process_group()
     return 0
 

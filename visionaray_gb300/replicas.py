@@ -1,0 +1,77 @@
+"""Multi-GPU host logic of the benchmark: one process per GPU, no collective on the data
+path.
+
+Rays, pixels and whole scenes are independent (visionaray's schedulers hand every
+pixel to its own thread, detail/cuda_sched.inl:43-49), so nothing is exchanged between
+GPUs while tracing.  Two ways of using N GPUs follow from that:
+  replicas   every rank runs the whole workload (the heightfield traversal, weak
+             scaling); the job's rate is N x work / the slowest rank's time
+  scenes     a batch of independent scenes is partitioned across ranks by cost
+             (longest-processing-time greedy), each rank builds and renders its share
+             (strong scaling of a fixed batch)
+The only collectives are on timings (a max over ranks), run outside the timed work.
+Rendezvous: MASTER_ADDR defaults to 127.0.0.1.
+"""
+import os
+
+
+def world_from_env():
+    """(world_size, rank, local_rank) from torchrun's environment (1, 0, 0 without it)."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def init(backend):
+    """Initialises the default process group when world_size > 1; returns (world, rank, local)."""
+    import torch.distributed as dist
+    world, rank, local = world_from_env()
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def reduce_over_ranks(value, op="max", device="cpu"):
+    """max / sum of a float over all ranks (the value itself on one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def partition(costs, world):
+    """Longest-processing-time greedy assignment of items with the given costs to `world`
+    ranks: items by decreasing cost (index breaks ties), each to the least-loaded rank
+    (lowest rank breaks ties).  Returns one ascending index list per rank; every rank
+    computes the same answer locally, so no communication is needed."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i))
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += float(costs[i])
+    return [sorted(p) for p in parts]
+
+
+def scene_costs(offsets, params):
+    """Cost model of one batched scene: triangles (the build) plus pixels x samples x
+    bounces (the frame), in comparable units."""
+    costs = []
+    for s in range(len(offsets) - 1):
+        tris = int(offsets[s + 1]) - int(offsets[s])
+        p = params[s]
+        work = int(p["width"]) * int(p["height"]) * int(p["spp"]) * max(int(p["num_bounces"]), 1)
+        costs.append(tris + 4 * work)
+    return costs
