@@ -169,6 +169,13 @@ gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* 
 gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh,
                                  gbrt_bvh_node* d_nodes, uint32_t* d_indices);
 
+/* bvh_refitter::refit(tree, prims, n) (detail/bvh/refit.h:25-117) on the GPU: new
+ * positions of the same n triangles (device, the build's input order); the tree keeps
+ * its topology and leaf order, the leaf triangles and every node box are recomputed
+ * (bottom-up, one pass).  For trees built by gbrt_bvh_build_lbvh; a 4-wide collapse is
+ * dropped.  Synchronises the context stream.                                        */
+gbrt_status gbrt_bvh_refit(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris, uint32_t n);
+
 /* LBVH build that allocates no device memory, for callers that cannot allocate:
  * hosts that own the whole device-memory budget and give a library only its output
  * buffers, and per-frame rebuild loops where cudaMalloc/cudaFree would synchronise

@@ -149,6 +149,26 @@ private:
     context* ctx_;
 };
 
+// bvh_refitter (detail/bvh/refit.h:25-117), GPU refit of an LBVH-built tree to new
+// positions of its primitives (device, the build's order).
+struct bvh_refitter
+{
+    explicit bvh_refitter(context& ctx) : ctx_(&ctx) {}
+
+    template <typename P>
+    void refit(cuda_index_bvh& tree, P const* d_primitives, size_t num_prims)
+    {
+        static_assert(sizeof(P) == sizeof(gbrt_triangle), "P must be laid out as basic_triangle<3, float, unsigned>");
+        if (num_prims > 0xFFFFFFFFu) throw error(GBRT_ERR_TOO_LARGE, "bvh_refitter::refit: too many primitives");
+        check(gbrt_bvh_refit(ctx_->get(), tree.get(), reinterpret_cast<gbrt_triangle const*>(d_primitives),
+                             uint32_t(num_prims)),
+              ctx_->get(), "gbrt_bvh_refit");
+    }
+
+private:
+    context* ctx_;
+};
+
 // Batched closest_hit / any_hit over one BVH (device buffers, asynchronous on the
 // context stream).
 inline void closest_hit(context& ctx, cuda_index_bvh const& bvh, gbrt_ray const* d_rays, size_t n, gbrt_hit* d_hits)

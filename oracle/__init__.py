@@ -64,6 +64,7 @@ class Oracle:
         L.orc_morton_codes.argtypes = [_vp, _u32, _vp]
         L.orc_karras_children.argtypes = [_vp, _u32, _vp, _vp]
         L.orc_sah_cost.argtypes = [_vp, _u32, _f32, _f32, _f32]
+        L.orc_refit.argtypes = [_vp, _u32, _vp, _vp, _vp]
         L.orc_sah_cost.restype = _f32
         L.orc_intersect_triangle.argtypes = [_vp, _vp, _vp]
         L.orc_intersect_triangle.restype = _i32
@@ -179,6 +180,14 @@ class Oracle:
                                      _p(adj), int(fp64), nthreads, _p(ga), _p(ge), _p(img))
         return ga, ge, img
 
+    def refit(self, tree, tris):
+        """bvh_refitter::refit: the tree's nodes with boxes recomputed from `tris`."""
+        nodes = np.ascontiguousarray(tree.nodes, BVH_NODE)
+        out = np.empty_like(nodes)
+        tris = np.ascontiguousarray(tris)
+        self.L.orc_refit(_p(nodes), len(nodes), _p(np.ascontiguousarray(tree.indices, np.uint32)), _p(tris), _p(out))
+        return Tree(out, tree.indices)
+
     def intersect_box(self, ray, bmin, bmax):
         ray = np.ascontiguousarray(np.asarray(ray).reshape(1))
         lo = np.ascontiguousarray(bmin, np.float32)
@@ -219,6 +228,7 @@ class Reference:
         L.ref_trace.argtypes = [_vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.ref_trace.restype = _i32
         L.ref_pathtrace.argtypes = [_vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _i32]
+        L.ref_refit.argtypes = [_vp, _vp, _u32]
         self.L = L
 
     class Handle:
@@ -238,6 +248,11 @@ class Reference:
 
         def sah_cost(self):
             return self.L.ref_sah_cost(self.h)
+
+        def refit(self, tris):
+            """bvh_refitter::refit to new positions of the same triangles."""
+            tris = np.ascontiguousarray(tris)
+            self.L.ref_refit(self.h, _p(tris), len(tris))
 
         def trace(self, rays, any_hit=False, nthreads=0, counters=False):
             rays = np.ascontiguousarray(rays)

@@ -910,6 +910,44 @@ extern "C" float orc_sah_cost(const gbrt_bvh_node* nodes, uint32_t num_nodes, fl
     return ci * (a_i / a_r) + cl * (a_l / a_r) + cp * (a_ln / a_r);
 }
 
+// bvh_refitter::refit (detail/bvh/refit.h:25-117): every node's box becomes the union of
+// its subtree's primitive bounds (the new positions), gathered depth first with child 0
+// before child 1 as the reference's per-node walk does; topology, child / primitive
+// links and traversal hints are kept.
+extern "C" void orc_refit(const gbrt_bvh_node* nodes, uint32_t num_nodes, const uint32_t* indices,
+                          const gbrt_triangle* tris, gbrt_bvh_node* out)
+{
+    for (uint32_t i = 0; i < num_nodes; ++i)
+    {
+        box b;
+        b.invalidate();
+        std::vector<uint32_t> stack{ i };
+        while (!stack.empty())
+        {
+            uint32_t a = stack.back();
+            stack.pop_back();
+            gbrt_bvh_node const& nd = nodes[a];
+            if (nd.num_prims == 0)
+            {
+                stack.push_back(nd.first_child_or_prim + 1);
+                stack.push_back(nd.first_child_or_prim);
+            }
+            else
+            {
+                for (uint32_t j = nd.first_child_or_prim; j < nd.first_child_or_prim + nd.num_prims; ++j)
+                    b.insert(tri_bounds(tris[indices[j]]));
+            }
+        }
+        out[i] = nodes[i];
+        out[i].bbox_min[0] = b.lo.x;
+        out[i].bbox_min[1] = b.lo.y;
+        out[i].bbox_min[2] = b.lo.z;
+        out[i].bbox_max[0] = b.hi.x;
+        out[i].bbox_max[1] = b.hi.y;
+        out[i].bbox_max[2] = b.hi.z;
+    }
+}
+
 extern "C" int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* tri, gbrt_hit* out)
 {
     hit_rec h = intersect_tri(*ray, *tri);

@@ -57,6 +57,11 @@ void orc_karras_children(const uint32_t* sorted_codes, uint32_t n, int32_t* left
 float orc_sah_cost(const gbrt_bvh_node* nodes, uint32_t num_nodes, float ci, float cl, float cp);
 
 /* Single ray / triangle test (math/intersect.h:176-229); returns the hit flag.     */
+/* bvh_refitter::refit (detail/bvh/refit.h:25-117): out = nodes with every box
+ * recomputed from the triangles' (new) bounds, topology unchanged.                 */
+void orc_refit(const gbrt_bvh_node* nodes, uint32_t num_nodes, const uint32_t* indices,
+               const gbrt_triangle* tris, gbrt_bvh_node* out);
+
 int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* tri, gbrt_hit* out);
 
 /* Scalar ray / box slab test (math/intersect.h:44-62, no tmin/tmax clamp); returns

@@ -23,6 +23,7 @@
 #include <visionaray/math/math.h>
 #include <visionaray/pinhole_camera.h>
 #include <visionaray/traverse.h>
+#include <visionaray/detail/bvh/refit.h>
 #include <visionaray/detail/bvh/statistics.h>
 
 #include "../include/visionaray_gb300/gbrt_rng.h"
@@ -106,6 +107,16 @@ void ref_copy(void* h, gbrt_bvh_node* nodes, uint32_t* indices)
 }
 
 void ref_free(void* h) { delete static_cast<ref_tree*>(h); }
+
+// bvh_refitter::refit (detail/bvh/refit.h:25-117) of the tree to new positions of its
+// n triangles (input order).
+void ref_refit(void* h, const gbrt_triangle* tris, uint32_t n)
+{
+    auto* t = static_cast<ref_tree*>(h);
+    t->prims = to_prims(tris, n);
+    bvh_refitter refitter;
+    refitter.refit(t->tree, t->prims.data(), t->prims.size());
+}
 
 float ref_sah_cost(void* h) { return sah_cost(static_cast<ref_tree*>(h)->tree); }
 

@@ -85,3 +85,35 @@ def test_rebuild_reuses_context_scratch():
         gpu_build(scenes.soup(30000, seed=seed))
     assert ctx.launches > before
     ctx.synchronize()
+
+
+@pytest.mark.parametrize("n", [1, 2, 777, 50000])
+def test_refit_equals_reference_refitter(oracle, n):
+    """gbrt_bvh_refit = bvh_refitter::refit on the exported tree (pinned to the
+    reference by tests/test_oracle_reference.py), and queries on the refitted tree find
+    the moved triangles."""
+    from oracle import Tree
+    from .parity import compare_closest
+    tris = scenes.soup(n, seed=31, offset=0.02)
+    moved = tris.copy()
+    rng = np.random.default_rng(n)
+    moved["v1"] += rng.uniform(-0.1, 0.1, size=(n, 3)).astype(np.float32)
+    moved["e2"] *= np.float32(0.7)
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    nodes0, idx0 = bvh.export_bvh2()
+    bvh.refit(vg.as_device_bytes(moved))
+    nodes1, idx1 = bvh.export_bvh2()
+    want = oracle.refit(Tree(nodes0, idx0), moved)
+    assert nodes1.tobytes() == want.nodes.tobytes()
+    assert np.array_equal(idx1, idx0)
+    rays = scenes.pinhole_rays(64, 64)
+    got = vg.hits_to_numpy(vg.closest_hit(vg.device_rays(rays), bvh))
+    bvh.ctx.synchronize()
+    compare_closest(got, oracle.trace(oracle.build_sah(moved), moved, rays), rays, moved, oracle)
+
+
+def test_refit_rejects_other_counts():
+    tris = scenes.soup(100, seed=2)
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    with pytest.raises(vg.GbrtError):
+        bvh.refit(vg.as_device_bytes(tris[:99]))

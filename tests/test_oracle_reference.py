@@ -53,3 +53,21 @@ def test_karras_children_random_codes(oracle, ref):
         l1, r1 = oracle.karras_children(codes)
         l2, r2 = ref.karras_children(codes)
         assert np.array_equal(l1, l2) and np.array_equal(r1, r2), n
+
+
+@pytest.mark.parametrize("max_leaf", [1, 4])
+def test_refit_matches_reference(oracle, ref, max_leaf):
+    """The oracle's refit restatement equals visionaray's bvh_refitter on its own SAH
+    tree after the triangles move."""
+    tris = scenes.soup(3000, seed=21)
+    moved = tris.copy()
+    rng = np.random.default_rng(4)
+    moved["v1"] += rng.uniform(-0.05, 0.05, size=(len(tris), 3)).astype(np.float32)
+    moved["e1"] *= np.float32(1.3)
+    h = ref.build_sah(tris, max_leaf=max_leaf)
+    before = h.tree()
+    h.refit(moved)
+    after = h.tree()
+    mine = oracle.refit(before, moved)
+    assert mine.nodes.tobytes() == after.nodes.tobytes()
+    assert np.array_equal(mine.indices, after.indices)

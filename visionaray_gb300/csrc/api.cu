@@ -341,6 +341,16 @@ gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* 
     return GBRT_OK;
 }
 
+gbrt_status gbrt_bvh_refit(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris, uint32_t n)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!bvh || (n > 0 && !d_tris)) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: null argument");
+    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: not an LBVH");
+    if (n != bvh->num_prims) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: triangle count differs from the build");
+    device_guard g(ctx->device);
+    return refit_lbvh(ctx, bvh, d_tris);
+}
+
 gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes, uint32_t* d_indices)
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;

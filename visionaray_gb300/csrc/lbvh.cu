@@ -413,6 +413,27 @@ __global__ void export_single_leaf(const tri48* __restrict__ tris, const uint32_
     indices[0] = 0;
 }
 
+// Leaf parents of a built tree, for a refit: inner node i writes (i << 1) | side for
+// each leaf child.
+__global__ void __launch_bounds__(kBlock) leaf_parents_of(const bvh2_node* __restrict__ nodes, int num_inner,
+                                                          int num_leaves, int* __restrict__ leaf_parent,
+                                                          uint32_t* __restrict__ status)
+{
+    int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= num_inner) return;
+    int4 link = __ldg(&nodes[i].link);
+    const int child[2] = { link.x, link.y };
+    for (int side = 0; side < 2; ++side)
+    {
+        if (child[side] >= 0) continue;
+        int j = ~child[side];
+        if (j < num_leaves)
+            leaf_parent[j] = (i << 1) | side;
+        else
+            atomicOr(status, kStatusBadIndex);
+    }
+}
+
 __global__ void emit_single(gbrt_triangle const* __restrict__ tris_in, tri48* __restrict__ tris_out)
 {
     tri_in t = load_tri(tris_in, 0);
@@ -594,6 +615,55 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
     }
     if (bvh->height + 1 > uint32_t(kStackSize))
         return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "LBVH height exceeds the traversal stack");
+    return GBRT_OK;
+}
+
+// bvh_refitter::refit (detail/bvh/refit.h:25-117) on the GPU: the tree keeps its
+// topology and leaf order; the leaf triangles are re-emitted from the new positions and
+// every node's boxes recomputed bottom-up by the build's refit kernel (second arrival
+// continues).  The 4-wide collapse, if any, is dropped (queries fall back to the pairs).
+gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris)
+{
+    const uint32_t n = bvh->num_prims;
+    if (n == 0) return GBRT_OK;
+    cudaStream_t s = ctx->stream;
+    if (bvh->nodes4)
+    {
+        GBRT_CUDA(ctx, cudaStreamSynchronize(s));
+        cudaFree(bvh->nodes4);
+        bvh->nodes4 = nullptr;
+        bvh->num_nodes4 = 0;
+    }
+    if (n == 1)
+    {
+        emit_single<<<1, 1, 0, s>>>(d_tris, bvh->tris);
+        GBRT_LAUNCH_CHECK(ctx, "emit_single");
+        return GBRT_OK;
+    }
+    const size_t off_parent = 0, off_arrivals = align_up(size_t(n) * 4), off_height = align_up(off_arrivals + size_t(n) * 4);
+    gbrt_status st = ensure_scratch(ctx, off_height + 256);
+    if (st != GBRT_OK) return st;
+    char* base = static_cast<char*>(ctx->scratch);
+    int* leaf_parent = reinterpret_cast<int*>(base + off_parent);
+    uint32_t* arrivals = reinterpret_cast<uint32_t*>(base + off_arrivals);
+    uint32_t* root_height = reinterpret_cast<uint32_t*>(base + off_height);
+    GBRT_CUDA(ctx, cudaMemsetAsync(leaf_parent, 0xFF, size_t(n) * 4, s));
+    GBRT_CUDA(ctx, cudaMemsetAsync(arrivals, 0, size_t(n) * 4, s));
+    leaf_parents_of<<<blocks_for(bvh->num_inner), kBlock, 0, s>>>(bvh->nodes, int(bvh->num_inner), int(n),
+                                                                  leaf_parent, ctx->d_status);
+    GBRT_LAUNCH_CHECK(ctx, "leaf_parents_of");
+    refit_and_emit<<<blocks_for(n), kBlock, 0, s>>>(d_tris, bvh->sorted_ids, int(n), leaf_parent, bvh->nodes, arrivals,
+                                                    bvh->tris, root_height, ctx->d_status);
+    GBRT_LAUNCH_CHECK(ctx, "refit_and_emit");
+    bvh2_node root;
+    GBRT_CUDA(ctx, cudaMemcpyAsync(&root, bvh->nodes, sizeof(root), cudaMemcpyDeviceToHost, s));
+    GBRT_CUDA(ctx, cudaStreamSynchronize(s));
+    bvh->lo[0] = std::min(root.xy0.x, root.xy1.x);
+    bvh->hi[0] = std::max(root.xy0.y, root.xy1.y);
+    bvh->lo[1] = std::min(root.xy0.z, root.xy1.z);
+    bvh->hi[1] = std::max(root.xy0.w, root.xy1.w);
+    bvh->lo[2] = std::min(root.z01.x, root.z01.z);
+    bvh->hi[2] = std::max(root.z01.y, root.z01.w);
     return GBRT_OK;
 }
 

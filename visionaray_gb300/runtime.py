@@ -41,6 +41,7 @@ SIGNATURES = {
     "gbrt_bvh_destroy": (_i32, [_vp]),
     "gbrt_bvh_counts": (_i32, [_vp, _vp, _vp, _vp]),
     "gbrt_bvh_export_bvh2": (_i32, [_vp, _vp, _vp, _vp]),
+    "gbrt_bvh_refit": (_i32, [_vp, _vp, _vp, _u32]),
     "gbrt_bvh_morton_codes": (_i32, [_vp, _vp, _vp]),
     "gbrt_bvh_build_lbvh_noalloc": (_i32, [_vp, _vp, _u32, _vp, _vp]),
     "gbrt_trace_closest_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
@@ -218,6 +219,13 @@ class IndexBVH:
         self.ctx.synchronize()
         return (nodes.cpu().numpy()[: nn * 32].view(BVH_NODE),
                 idx.cpu().numpy()[:n].view(np.uint32))
+
+    def refit(self, tris):
+        """bvh_refitter::refit: new positions of the same triangles (torch uint8 CUDA tensor,
+        n x 44 bytes, the build's input order); topology kept, boxes recomputed."""
+        n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
+        self.ctx.check(self.ctx.lib.gbrt_bvh_refit(self.ctx.h, self.h, _dptr(tris), n))
+        return self
 
     def morton_codes(self):
         torch = _torch()
