@@ -345,6 +345,55 @@ gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene const* scen
                                     float* d_grad_emission);
 
 /* ------------------------------------------------------------------------------ */
+/* Two-level instancing: index_bvh_inst_t (bvh.h:678-782) and the top-level BVH over
+ * instances, traversed as intersect(ray, instance) does (detail/bvh/intersect.inl:
+ * 362-394): the ray is carried into the instance's space and its tree traversed.      */
+
+/* An instance: a bottom-level tree and visionaray's mat4x3 transform, 4 columns of 3
+ * floats (col0, col1, col2, col3).  As in index_bvh_inst_t(ref, transform), the
+ * linear map is top_left(transform) (matrix4x3.inl:206-219: row i of the map is
+ * column i of the matrix) and the translation is col3: world = top_left * p + col3.
+ * The inverse is computed as the reference does (matrix3.inl:285-305, float) and a
+ * ray is mapped as transform_ray (bvh.h:742-750): ori' = A (ori - col3), dir' = A dir. */
+typedef struct gbrt_instance
+{
+    gbrt_bvh const* blas;
+    float transform[12];
+} gbrt_instance;
+
+/* hit_record_bvh_inst (detail/bvh/hit_record.h:57-75): prim_id of the instance's
+ * triangle, inst_id = the instance's index (GBRT_NO_HIT on a miss), t, u, v in the
+ * instance space's parameterisation (t is the world ray's parameter), geom_id.      */
+typedef struct gbrt_hit_inst
+{
+    uint32_t prim_id;
+    uint32_t inst_id;
+    float    t;
+    float    u;
+    float    v;
+    uint32_t geom_id;
+    uint32_t reserved[2];
+} gbrt_hit_inst;
+
+typedef struct gbrt_tlas gbrt_tlas;
+
+/* Builds the top-level tree over h_instances (host array; the bottom-level trees must
+ * outlive the tlas): instance bounds as get_bounds(instance) computes them
+ * (detail/bvh/get_bounds.inl:30-56: the 8 corners of the tree's root box mapped to
+ * world space), a median-split hierarchy of node pairs over them (one instance per
+ * leaf).  Synchronous.                                                              */
+gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h_instances, uint32_t num_instances,
+                            gbrt_tlas** out);
+gbrt_status gbrt_tlas_destroy(gbrt_tlas* tlas);
+
+/* closest_hit / any_hit over the instances (device rays and hits, 16-byte aligned):
+ * per ray, the closest (any) hit of any instance within [tmin, tmax].               */
+gbrt_status gbrt_tlas_trace_closest_hit(gbrt_context* ctx, gbrt_tlas const* tlas, gbrt_ray const* d_rays,
+                                        uint32_t n, gbrt_hit_inst* d_hits);
+gbrt_status gbrt_tlas_trace_any_hit(gbrt_context* ctx, gbrt_tlas const* tlas, gbrt_ray const* d_rays,
+                                    uint32_t n, gbrt_hit_inst* d_hits);
+
+/* ------------------------------------------------------------------------------ */
 /* Batches of scenes (no visionaray counterpart: the reference builds and renders one
  * scene per call, lbvh.h:681-844 and cuda_sched.inl:226-246).                      */
 

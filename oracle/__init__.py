@@ -65,6 +65,7 @@ class Oracle:
         L.orc_karras_children.argtypes = [_vp, _u32, _vp, _vp]
         L.orc_sah_cost.argtypes = [_vp, _u32, _f32, _f32, _f32]
         L.orc_refit.argtypes = [_vp, _u32, _vp, _vp, _vp]
+        L.orc_trace_instances.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
         L.orc_sah_cost.restype = _f32
         L.orc_intersect_triangle.argtypes = [_vp, _vp, _vp]
         L.orc_intersect_triangle.restype = _i32
@@ -188,6 +189,29 @@ class Oracle:
         self.L.orc_refit(_p(nodes), len(nodes), _p(np.ascontiguousarray(tree.indices, np.uint32)), _p(tris), _p(out))
         return Tree(out, tree.indices)
 
+    def trace_instances(self, instances, rays, any_hit=False, nthreads=0):
+        """Two-level query, brute force over instances = [(tree, tris, transform12)]."""
+        from visionaray_gb300.types import HIT_INST
+
+        class Inst(ctypes.Structure):
+            _fields_ = [("nodes", _vp), ("num_nodes", _u32), ("indices", _vp), ("tris", _vp),
+                        ("transform", ctypes.c_float * 12)]
+        keep = []
+        arr = (Inst * max(len(instances), 1))()
+        for k, (tree, tris, xf) in enumerate(instances):
+            nodes = np.ascontiguousarray(tree.nodes, BVH_NODE)
+            idx = np.ascontiguousarray(tree.indices, np.uint32)
+            tr = np.ascontiguousarray(tris)
+            keep += [nodes, idx, tr]
+            arr[k].nodes, arr[k].num_nodes = nodes.ctypes.data, len(nodes)
+            arr[k].indices, arr[k].tris = idx.ctypes.data, tr.ctypes.data
+            arr[k].transform[:] = [float(x) for x in np.asarray(xf, np.float32).reshape(12)]
+        rays = np.ascontiguousarray(rays)
+        out = np.zeros(len(rays), HIT_INST)
+        self.L.orc_trace_instances(ctypes.addressof(arr), len(instances), _p(rays), len(rays), int(any_hit),
+                                   nthreads, _p(out))
+        return out
+
     def intersect_box(self, ray, bmin, bmax):
         ray = np.ascontiguousarray(np.asarray(ray).reshape(1))
         lo = np.ascontiguousarray(bmin, np.float32)
@@ -229,6 +253,7 @@ class Reference:
         L.ref_trace.restype = _i32
         L.ref_pathtrace.argtypes = [_vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _i32]
         L.ref_refit.argtypes = [_vp, _vp, _u32]
+        L.ref_trace_instances.argtypes = [_u32, _vp, _vp, _u32, _vp, _vp, _vp, _u64, _i32, _vp]
         self.L = L
 
     class Handle:
@@ -268,6 +293,21 @@ class Reference:
     def build_lbvh_cpu(self, tris, max_leaf=4):
         tris = np.ascontiguousarray(tris)
         return Reference.Handle(self.L, self.L.ref_build_lbvh_cpu(_p(tris), len(tris), max_leaf))
+
+    def trace_instances(self, meshes, inst_mesh, transforms, rays, any_hit=False):
+        """visionaray's own two-level query: meshes = [tris], instance k = mesh
+        inst_mesh[k] with the mat4x3 transforms[k] (12 floats)."""
+        from visionaray_gb300.types import HIT_INST
+        meshes = [np.ascontiguousarray(m) for m in meshes]
+        ptrs = (ctypes.c_void_p * len(meshes))(*[m.ctypes.data for m in meshes])
+        sizes = np.array([len(m) for m in meshes], np.uint32)
+        im = np.ascontiguousarray(inst_mesh, np.uint32)
+        xf = np.ascontiguousarray(transforms, np.float32).reshape(-1)
+        rays = np.ascontiguousarray(rays)
+        out = np.zeros(len(rays), HIT_INST)
+        self.L.ref_trace_instances(len(meshes), ctypes.addressof(ptrs), _p(sizes), len(im), _p(im), _p(xf), _p(rays),
+                                   len(rays), int(any_hit), _p(out))
+        return out
 
     def lbvh_sorted_refs(self, tris):
         tris = np.ascontiguousarray(tris)

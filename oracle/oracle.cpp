@@ -948,6 +948,84 @@ extern "C" void orc_refit(const gbrt_bvh_node* nodes, uint32_t num_nodes, const 
     }
 }
 
+namespace {
+
+// The reference's float 3x3 inverse (math/detail/matrix3.inl:285-305, det2 math.h:
+// 616-621): cofactors over the determinant, m[r][c].
+void inverse3(const float m[3][3], float r[3][3])
+{
+    auto det2 = [](float m00, float m01, float m10, float m11) { return m00 * m11 - m10 * m01; };
+    float a00 = det2(m[1][1], m[1][2], m[2][1], m[2][2]);
+    float a01 = det2(m[1][0], m[1][2], m[2][0], m[2][2]);
+    float a02 = det2(m[1][0], m[1][1], m[2][0], m[2][1]);
+    float a10 = det2(m[0][1], m[0][2], m[2][1], m[2][2]);
+    float a11 = det2(m[0][0], m[0][2], m[2][0], m[2][2]);
+    float a12 = det2(m[0][0], m[0][1], m[2][0], m[2][1]);
+    float a20 = det2(m[0][1], m[0][2], m[1][1], m[1][2]);
+    float a21 = det2(m[0][0], m[0][2], m[1][0], m[1][2]);
+    float a22 = det2(m[0][0], m[0][1], m[1][0], m[1][1]);
+    float det = m[0][0] * a00 - m[0][1] * a01 + m[0][2] * a02;
+    r[0][0] = +a00 / det; r[1][0] = -a01 / det; r[2][0] = +a02 / det;
+    r[0][1] = -a10 / det; r[1][1] = +a11 / det; r[2][1] = -a12 / det;
+    r[0][2] = +a20 / det; r[1][2] = -a21 / det; r[2][2] = +a22 / det;
+}
+
+} // namespace
+
+extern "C" void orc_trace_instances(const orc_instance* instances, uint32_t num_instances, const gbrt_ray* rays,
+                                    uint64_t nrays, int any_hit, int nthreads, gbrt_hit_inst* hits)
+{
+    // index_bvh_inst_t(ref, transform): affine_inv = inverse(top_left(transform)) with
+    // top_left's row i = column i; trans_inv = -column 3 (bvh.h:694-700)
+    std::vector<std::array<float, 12>> xf(num_instances);
+    for (uint32_t k = 0; k < num_instances; ++k)
+    {
+        float tl[3][3], inv[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) tl[r][c] = instances[k].transform[3 * r + c];
+        inverse3(tl, inv);
+        for (int r = 0; r < 3; ++r)
+        {
+            for (int c = 0; c < 3; ++c) xf[k][size_t(4 * r + c)] = inv[r][c];
+            xf[k][size_t(4 * r + 3)] = -instances[k].transform[9 + r];
+        }
+    }
+    parallel_chunks(nrays, nthreads, [&](int, uint64_t b, uint64_t e) {
+        uint64_t lb = 0, lt = 0;
+        for (uint64_t i = b; i < e; ++i)
+        {
+            gbrt_hit_inst best{ GBRT_NO_HIT, GBRT_NO_HIT, FLT_MAX, 0.0f, 0.0f, 0u, { 0u, 0u } };
+            gbrt_ray const& r = rays[i];
+            for (uint32_t k = 0; k < num_instances; ++k)
+            {
+                if (instances[k].num_nodes == 0) continue;
+                auto const& a = xf[k];
+                // transform_ray (bvh.h:748-755): ori' = A (ori + trans_inv), dir' = A dir
+                float p[3] = { r.ori[0] + a[3], r.ori[1] + a[7], r.ori[2] + a[11] };
+                gbrt_ray t = r;
+                for (int row = 0; row < 3; ++row)
+                {
+                    t.ori[row] = a[size_t(4 * row)] * p[0] + a[size_t(4 * row + 1)] * p[1] + a[size_t(4 * row + 2)] * p[2];
+                    t.dir[row] = a[size_t(4 * row)] * r.dir[0] + a[size_t(4 * row + 1)] * r.dir[1] +
+                                 a[size_t(4 * row + 2)] * r.dir[2];
+                }
+                gbrt_hit h;
+                trace_one(instances[k].nodes, instances[k].indices, instances[k].tris, t, any_hit != 0, h, lb, lt);
+                if (h.prim_id != GBRT_NO_HIT && h.t < best.t)
+                {
+                    best.prim_id = h.prim_id;
+                    best.inst_id = k;
+                    best.t = h.t;
+                    best.u = h.u;
+                    best.v = h.v;
+                    if (any_hit) break;
+                }
+            }
+            hits[i] = best;
+        }
+    });
+}
+
 extern "C" int orc_intersect_triangle(const gbrt_ray* ray, const gbrt_triangle* tri, gbrt_hit* out)
 {
     hit_rec h = intersect_tri(*ray, *tri);

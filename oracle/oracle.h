@@ -57,6 +57,23 @@ void orc_karras_children(const uint32_t* sorted_codes, uint32_t n, int32_t* left
 float orc_sah_cost(const gbrt_bvh_node* nodes, uint32_t num_nodes, float ci, float cl, float cp);
 
 /* Single ray / triangle test (math/intersect.h:176-229); returns the hit flag.     */
+/* Two-level instancing (index_bvh_inst_t, bvh.h:678-782; intersect.inl:362-394),
+ * brute force over the instances in index order: per instance the ray is mapped with
+ * the reference's float inverse of top_left(transform) (matrix3.inl:285-305,
+ * matrix4x3.inl:206-219) and traced through that instance's tree as orc_trace does;
+ * a hit replaces the best one when strictly closer (is_closer).  hits: gbrt_hit_inst
+ * (geom_id 0).                                                                     */
+typedef struct orc_instance
+{
+    const gbrt_bvh_node* nodes;
+    uint32_t num_nodes;
+    const uint32_t* indices;
+    const gbrt_triangle* tris;
+    float transform[12];
+} orc_instance;
+void orc_trace_instances(const orc_instance* instances, uint32_t num_instances, const gbrt_ray* rays,
+                         uint64_t nrays, int any_hit, int nthreads, gbrt_hit_inst* hits);
+
 /* bvh_refitter::refit (detail/bvh/refit.h:25-117): out = nodes with every box
  * recomputed from the triangles' (new) bounds, topology unchanged.                 */
 void orc_refit(const gbrt_bvh_node* nodes, uint32_t num_nodes, const uint32_t* indices,

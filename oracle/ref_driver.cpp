@@ -205,6 +205,52 @@ int ref_trace(void* h, const gbrt_ray* rays, uint64_t nrays, int any_hit_flag, i
     return 0;
 }
 
+// Two-level instancing with visionaray's own types: a binned-SAH index_bvh per mesh,
+// index_bvh_inst_t instances (bvh.h:678-782, via index_bvh::inst(transform),
+// bvh.h:933-936) with set_inst_id(k), a binned-SAH top-level index_bvh over the
+// instances, and closest_hit / any_hit through it (intersect.inl:362-394).
+// mesh_tris[m] holds mesh_sizes[m] triangles; instance k uses mesh inst_mesh[k] and
+// the mat4x3 columns transforms[12k .. 12k+11].
+void ref_trace_instances(uint32_t num_meshes, const gbrt_triangle* const* mesh_tris, const uint32_t* mesh_sizes,
+                         uint32_t num_instances, const uint32_t* inst_mesh, const float* transforms,
+                         const gbrt_ray* rays, uint64_t nrays, int any_hit_flag, gbrt_hit_inst* hits)
+{
+    using blas_t = index_bvh<triangle_t>;
+    using inst_t = blas_t::bvh_inst;
+    std::vector<std::vector<triangle_t>> prims(num_meshes);
+    std::vector<blas_t> blas(num_meshes);
+    binned_sah_builder builder;
+    for (uint32_t m = 0; m < num_meshes; ++m)
+    {
+        prims[m] = to_prims(mesh_tris[m], mesh_sizes[m]);
+        blas[m] = builder.build(blas_t{}, prims[m].data(), prims[m].size());
+    }
+    std::vector<inst_t> insts;
+    for (uint32_t k = 0; k < num_instances; ++k)
+    {
+        const float* t = transforms + 12 * size_t(k);
+        mat4x3 xf(vec3(t[0], t[1], t[2]), vec3(t[3], t[4], t[5]), vec3(t[6], t[7], t[8]), vec3(t[9], t[10], t[11]));
+        insts.push_back(blas[inst_mesh[k]].inst(xf));
+        insts.back().set_inst_id(int(k));
+    }
+    index_bvh<inst_t> tlas = builder.build(index_bvh<inst_t>{}, insts.data(), insts.size());
+    auto tref = tlas.ref();
+    for (uint64_t i = 0; i < nrays; ++i)
+    {
+        basic_ray<float> r;
+        std::memcpy(&r, &rays[i], sizeof(r));
+        auto hr = any_hit_flag ? any_hit(r, &tref, &tref + 1) : closest_hit(r, &tref, &tref + 1);
+        gbrt_hit_inst& h = hits[i];
+        h.prim_id = hr.hit ? hr.prim_id : GBRT_NO_HIT;
+        h.inst_id = hr.hit ? unsigned(hr.inst_id) : GBRT_NO_HIT;
+        h.t = hr.t;
+        h.u = hr.u;
+        h.v = hr.v;
+        h.geom_id = hr.hit ? hr.geom_id : 0u;
+        h.reserved[0] = h.reserved[1] = 0u;
+    }
+}
+
 // visionaray's pathtracing::kernel (detail/pathtracing.inl:42-233) over a binned-SAH
 // index_bvh, generic_material<matte, emissive> per geom_id and triangle area lights,
 // driven per (pixel, sample) by the gbrt_rng.h stream: the jittered primary ray

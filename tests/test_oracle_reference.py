@@ -71,3 +71,21 @@ def test_refit_matches_reference(oracle, ref, max_leaf):
     mine = oracle.refit(before, moved)
     assert mine.nodes.tobytes() == after.nodes.tobytes()
     assert np.array_equal(mine.indices, after.indices)
+
+
+def test_instances_match_reference(oracle, ref):
+    """The oracle's two-level query (inverse, transform_ray, per-instance closest hit,
+    is_closer) equals visionaray's index_bvh over index_bvh_inst_t."""
+    from .instancing import compare_inst, make_instances, make_rays
+    meshes, inst_mesh, transforms = make_instances()
+    rays = make_rays()
+    trees = [oracle.build_sah(m) for m in meshes]
+    insts = [(trees[m], meshes[m], transforms[k]) for k, m in enumerate(inst_mesh)]
+    for any_hit in (False, True):
+        want = ref.trace_instances(meshes, inst_mesh, transforms, rays, any_hit=any_hit)
+        got = oracle.trace_instances(insts, rays, any_hit=any_hit)
+        assert (want["prim_id"] != 0xFFFFFFFF).sum() > len(rays) // 4
+        if any_hit:
+            assert ((want["prim_id"] == 0xFFFFFFFF) == (got["prim_id"] == 0xFFFFFFFF)).all()
+        else:
+            assert compare_inst(got, want) <= len(rays) // 1000

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cfloat>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -74,9 +75,10 @@ struct gbrt_bvh
     // LBVH only: sorted Morton codes and, per sorted position, the input index.
     uint32_t* sorted_codes = nullptr;
     uint32_t* sorted_ids = nullptr;
-    // Scene bounds (the root box), used to order rays by origin.
-    float lo[3] = { 0.0f, 0.0f, 0.0f };
-    float hi[3] = { 0.0f, 0.0f, 0.0f };
+    // Scene bounds (the root box; invalid for an empty tree), used to order rays by
+    // origin and to bound instances.
+    float lo[3] = { FLT_MAX, FLT_MAX, FLT_MAX };
+    float hi[3] = { -FLT_MAX, -FLT_MAX, -FLT_MAX };
     // 4-wide tree collapsed from the node pairs (LBVH only; null: traverse the pairs).
     gbrt::bvh4_node* nodes4 = nullptr;
     uint32_t num_nodes4 = 0;

@@ -1,0 +1,415 @@
+// Two-level instancing: a top-level tree of node pairs over instances, each a bottom-
+// level tree (gbrt_bvh) and visionaray's mat4x3 transform (index_bvh_inst_t, bvh.h:
+// 678-782).  A query walks the top-level tree; at an instance leaf it maps the ray
+// into the instance's space exactly as transform_ray does (bvh.h:748-755: ori' =
+// A (ori + trans_inv), dir' = A dir, the 3x3 product in the reference's operation
+// order) and traverses the instance's tree with the best distance so far as its bound,
+// which accepts the same hits as the reference's per-instance closest hit followed by
+// the strict is_closer test (intersect.inl:362-394, update_if.h:45-107).
+//
+// The top-level tree is built on the host: instance counts are small next to triangle
+// counts, and the reference builds its top-level tree on the host too (the viewer's
+// index_bvh over bvh_inst, viewer.cpp:647-661).
+
+#include "traverse_core.cuh"
+
+#include <algorithm>
+#include <new>
+#include <numeric>
+#include <vector>
+
+struct gbrt_tlas
+{
+    int device = 0;
+    uint32_t num_instances = 0;
+    uint32_t num_inner = 0;
+    int32_t root = INT32_MIN;
+    gbrt::bvh2_node* nodes = nullptr;   // top-level node pairs, leaves ~instance
+    float4* records = nullptr;          // 3 float4 per instance: rows of A | trans_inv
+    gbrt::bvh_view* views = nullptr;    // the instance's bottom-level tree
+};
+
+namespace gbrt {
+namespace {
+
+constexpr int kBlock = 128;
+
+// The reference's float 3x3 algebra (math/detail/matrix3.inl, math.h:616-621), m[r][c].
+struct m3
+{
+    float m[3][3];
+};
+
+inline float det2(float m00, float m01, float m10, float m11) { return m00 * m11 - m10 * m01; }
+
+// inverse(matrix<3,3>) (matrix3.inl:285-305): cofactors over the determinant.
+m3 inverse3(m3 const& x)
+{
+    auto m = [&](int r, int c) { return x.m[r][c]; };
+    float a00 = det2(m(1, 1), m(1, 2), m(2, 1), m(2, 2));
+    float a01 = det2(m(1, 0), m(1, 2), m(2, 0), m(2, 2));
+    float a02 = det2(m(1, 0), m(1, 1), m(2, 0), m(2, 1));
+    float a10 = det2(m(0, 1), m(0, 2), m(2, 1), m(2, 2));
+    float a11 = det2(m(0, 0), m(0, 2), m(2, 0), m(2, 2));
+    float a12 = det2(m(0, 0), m(0, 1), m(2, 0), m(2, 1));
+    float a20 = det2(m(0, 1), m(0, 2), m(1, 1), m(1, 2));
+    float a21 = det2(m(0, 0), m(0, 2), m(1, 0), m(1, 2));
+    float a22 = det2(m(0, 0), m(0, 1), m(1, 0), m(1, 1));
+    float det = m(0, 0) * a00 - m(0, 1) * a01 + m(0, 2) * a02;
+    // the result's constructor takes its arguments column by column
+    m3 r;
+    r.m[0][0] = +a00 / det;
+    r.m[1][0] = -a01 / det;
+    r.m[2][0] = +a02 / det;
+    r.m[0][1] = -a10 / det;
+    r.m[1][1] = +a11 / det;
+    r.m[2][1] = -a12 / det;
+    r.m[0][2] = +a20 / det;
+    r.m[1][2] = -a21 / det;
+    r.m[2][2] = +a22 / det;
+    return r;
+}
+
+// matrix<3,3> * vector<3> (matrix3.inl:226-234)
+inline void mul3(m3 const& a, const float v[3], float out[3])
+{
+    for (int r = 0; r < 3; ++r) out[r] = a.m[r][0] * v[0] + a.m[r][1] * v[1] + a.m[r][2] * v[2];
+}
+
+struct box
+{
+    float lo[3], hi[3];
+};
+
+inline float vmin(float a, float b) { return a < b ? a : b; }
+inline float vmax(float a, float b) { return a < b ? b : a; }
+
+// get_bounds(instance) (detail/bvh/get_bounds.inl:30-56): affine = inverse(affine_inv),
+// trans = -trans_inv, the 8 corners of the tree's root box (aabb.inl:305-324 order)
+// mapped by affine * v + trans and inserted into an invalid box.
+box instance_bounds(m3 const& affine_inv, const float trans_inv[3], gbrt_bvh const* blas)
+{
+    box r;
+    for (int a = 0; a < 3; ++a)
+    {
+        r.lo[a] = FLT_MAX;
+        r.hi[a] = -FLT_MAX;
+    }
+    if (blas->num_prims == 0) return r;
+    m3 affine = inverse3(affine_inv);
+    float trans[3] = { -trans_inv[0], -trans_inv[1], -trans_inv[2] };
+    const float* mn = blas->lo;
+    const float* mx = blas->hi;
+    const float corners[8][3] = { { mx[0], mx[1], mx[2] }, { mn[0], mx[1], mx[2] }, { mn[0], mn[1], mx[2] },
+                                  { mx[0], mn[1], mx[2] }, { mn[0], mx[1], mn[2] }, { mx[0], mx[1], mn[2] },
+                                  { mx[0], mn[1], mn[2] }, { mn[0], mn[1], mn[2] } };
+    for (auto const& c : corners)
+    {
+        float w[3];
+        mul3(affine, c, w);
+        for (int a = 0; a < 3; ++a)
+        {
+            float v = w[a] + trans[a];
+            r.lo[a] = vmin(r.lo[a], v);
+            r.hi[a] = vmax(r.hi[a], v);
+        }
+    }
+    return r;
+}
+
+box merge(box const& a, box const& b)
+{
+    box r;
+    for (int k = 0; k < 3; ++k)
+    {
+        r.lo[k] = vmin(a.lo[k], b.lo[k]);
+        r.hi[k] = vmax(a.hi[k], b.hi[k]);
+    }
+    return r;
+}
+
+// Median split on the longest axis of the centroid bounds, one instance per leaf;
+// returns the link of the subtree (inner index, or ~instance).
+int32_t build_top(std::vector<uint32_t>& ids, size_t first, size_t last, std::vector<box> const& boxes,
+                  std::vector<bvh2_node>& nodes, box& out_box)
+{
+    if (last - first == 1)
+    {
+        out_box = boxes[ids[first]];
+        return ~int32_t(ids[first]);
+    }
+    float clo[3] = { FLT_MAX, FLT_MAX, FLT_MAX }, chi[3] = { -FLT_MAX, -FLT_MAX, -FLT_MAX };
+    for (size_t i = first; i < last; ++i)
+        for (int a = 0; a < 3; ++a)
+        {
+            float c = 0.5f * (boxes[ids[i]].lo[a] + boxes[ids[i]].hi[a]);
+            clo[a] = vmin(clo[a], c);
+            chi[a] = vmax(chi[a], c);
+        }
+    int axis = 0;
+    for (int a = 1; a < 3; ++a)
+        if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+    size_t mid = first + (last - first) / 2;
+    std::nth_element(ids.begin() + first, ids.begin() + mid, ids.begin() + last, [&](uint32_t a, uint32_t b) {
+        float ca = boxes[a].lo[axis] + boxes[a].hi[axis], cb = boxes[b].lo[axis] + boxes[b].hi[axis];
+        return ca < cb || (ca == cb && a < b);
+    });
+    int32_t self = int32_t(nodes.size());
+    nodes.emplace_back();
+    box lb, rb;
+    int32_t l = build_top(ids, first, mid, boxes, nodes, lb);
+    int32_t r = build_top(ids, mid, last, boxes, nodes, rb);
+    bvh2_node& nd = nodes[size_t(self)];
+    nd.xy0 = make_float4(lb.lo[0], lb.hi[0], lb.lo[1], lb.hi[1]);
+    nd.xy1 = make_float4(rb.lo[0], rb.hi[0], rb.lo[1], rb.hi[1]);
+    nd.z01 = make_float4(lb.lo[2], lb.hi[2], rb.lo[2], rb.hi[2]);
+    nd.link = make_int4(l, r, 0, 0);
+    out_box = merge(lb, rb);
+    return self;
+}
+
+struct tlas_view
+{
+    const bvh2_node* nodes;
+    const float4* records;
+    const bvh_view* views;
+    int32_t root, num_inner, num_instances;
+};
+
+template <bool AnyHit>
+__global__ void __launch_bounds__(kBlock) tlas_trace(tlas_view tv, const gbrt_ray* __restrict__ rays, uint32_t n,
+                                                     gbrt_hit_inst* __restrict__ hits, uint32_t* __restrict__ status)
+{
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    float4 r0 = ldg4(&rays[i]);
+    float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
+    const f3 o = { r0.x, r0.y, r0.z }, d = { r0.w, r1.x, r1.y };
+    const float tmin = r1.z, tmax = r1.w;
+    const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
+    float best_t = FLT_MAX, best_u = 0.0f, best_v = 0.0f;
+    int best_inst = -1, best_tri = -1;
+    int stack[32];
+    int sp = 0;
+    int node = tv.root;
+    bool done = false;
+    while (node != kEmptyLink && !done)
+    {
+        while (node >= 0)
+        {
+            if (node >= tv.num_inner)
+            {
+                atomicOr(status, kStatusBadIndex);
+                node = kEmptyLink;
+                break;
+            }
+            const bvh2_node* np = tv.nodes + node;
+            float4 a = ldg4(&np->xy0), b = ldg4(&np->xy1), z = ldg4(&np->z01);
+            int4 link = __ldg(&np->link);
+            float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
+            float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
+            float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;
+            float lx1 = (b.x - o.x) * ix, hx1 = (b.y - o.x) * ix;
+            float ly1 = (b.z - o.y) * iy, hy1 = (b.w - o.y) * iy;
+            float lz1 = (z.z - o.z) * iz, hz1 = (z.w - o.z) * iz;
+            float tn0 = fmaxf(tmin, fmaxf(fminf(lx0, hx0), fmaxf(fminf(ly0, hy0), fminf(lz0, hz0))));
+            float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
+            float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
+            float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
+            bool h0 = tf0 >= tn0 && tn0 < best_t;
+            bool h1 = tf1 >= tn1 && tn1 < best_t;
+            if (h0 && h1)
+            {
+                bool first0 = tn0 < tn1;
+                if (sp < 32)
+                    stack[sp++] = first0 ? link.y : link.x;
+                else
+                    atomicOr(status, kStatusStackOverflow);
+                node = first0 ? link.x : link.y;
+            }
+            else if (h0 || h1)
+            {
+                node = h0 ? link.x : link.y;
+            }
+            else
+            {
+                node = sp > 0 ? stack[--sp] : kEmptyLink;
+            }
+        }
+        if (node == kEmptyLink) break;
+        const int inst = ~node;
+        if (inst >= tv.num_instances)
+        {
+            atomicOr(status, kStatusBadIndex);
+            break;
+        }
+        // transform_ray (bvh.h:748-755) with the instance's inverse, then its tree
+        const float4 ra = tv.records[3 * inst + 0], rb = tv.records[3 * inst + 1], rc = tv.records[3 * inst + 2];
+        const float px = __fadd_rn(o.x, ra.w), py = __fadd_rn(o.y, rb.w), pz = __fadd_rn(o.z, rc.w);
+        f3 oo = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, px), __fmul_rn(ra.y, py)), __fmul_rn(ra.z, pz)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, px), __fmul_rn(rb.y, py)), __fmul_rn(rb.z, pz)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, px), __fmul_rn(rc.y, py)), __fmul_rn(rc.z, pz)) };
+        f3 dd = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, d.x), __fmul_rn(ra.y, d.y)), __fmul_rn(ra.z, d.z)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, d.x), __fmul_rn(rb.y, d.y)), __fmul_rn(rb.z, d.z)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, d.x), __fmul_rn(rc.y, d.y)), __fmul_rn(rc.z, d.z)) };
+        const bvh_view bv = tv.views[inst];
+        if (bv.num_tris > 0)
+        {
+            local_stack<kStackSize> bstack;
+            trace_result h = traverse_bvh_with<AnyHit>(bstack, bv.nodes, bv.tris, bv.root, bv.num_inner, bv.num_tris,
+                                                       oo, dd, tmin, tmax, status, best_t);
+            if (h.tri >= 0)
+            {
+                best_t = h.t;
+                best_u = h.u;
+                best_v = h.v;
+                best_tri = h.tri;
+                best_inst = inst;
+                if (AnyHit) done = true;
+            }
+        }
+        node = sp > 0 ? stack[--sp] : kEmptyLink;
+    }
+    uint4 w0, w1;
+    if (best_inst >= 0)
+    {
+        const bvh_view bv = tv.views[best_inst];
+        float4 t0 = ldg4(&bv.tris[best_tri].t0), t1 = ldg4(&bv.tris[best_tri].t1);
+        w0 = make_uint4(__float_as_uint(t0.w), uint32_t(best_inst), __float_as_uint(best_t), __float_as_uint(best_u));
+        w1 = make_uint4(__float_as_uint(best_v), __float_as_uint(t1.w), 0u, 0u);
+    }
+    else
+    {
+        w0 = make_uint4(GBRT_NO_HIT, GBRT_NO_HIT, __float_as_uint(FLT_MAX), 0u);
+        w1 = make_uint4(0u, 0u, 0u, 0u);
+    }
+    reinterpret_cast<uint4*>(hits)[2 * size_t(i)] = w0;
+    reinterpret_cast<uint4*>(hits)[2 * size_t(i) + 1] = w1;
+}
+
+void free_tlas(gbrt_tlas* t)
+{
+    cudaFree(t->nodes);
+    cudaFree(t->records);
+    cudaFree(t->views);
+}
+
+} // namespace
+} // namespace gbrt
+
+using namespace gbrt;
+
+extern "C" gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h_instances, uint32_t num_instances,
+                                       gbrt_tlas** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out || (num_instances && !h_instances)) return fail(ctx, GBRT_ERR_INVALID_ARG, "tlas_build: null argument");
+    *out = nullptr;
+    if (num_instances > (1u << 24)) return fail(ctx, GBRT_ERR_TOO_LARGE, "tlas_build: more than 2^24 instances");
+    for (uint32_t k = 0; k < num_instances; ++k)
+        if (!h_instances[k].blas) return fail(ctx, GBRT_ERR_INVALID_ARG, "tlas_build: instance without a tree");
+    std::vector<float4> records(size_t(num_instances) * 3);
+    std::vector<bvh_view> views(num_instances);
+    std::vector<box> boxes(num_instances);
+    for (uint32_t k = 0; k < num_instances; ++k)
+    {
+        gbrt_instance const& in = h_instances[k];
+        // index_bvh_inst_t(ref, transform) (bvh.h:694-700): affine_inv =
+        // inverse(top_left(transform)), trans_inv = -transform(3)
+        m3 tl;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) tl.m[r][c] = in.transform[3 * r + c];
+        m3 ainv = inverse3(tl);
+        float tinv[3] = { -in.transform[9], -in.transform[10], -in.transform[11] };
+        for (int r = 0; r < 3; ++r) records[3 * k + r] = make_float4(ainv.m[r][0], ainv.m[r][1], ainv.m[r][2], tinv[r]);
+        views[k] = view_of(in.blas);
+        boxes[k] = instance_bounds(ainv, tinv, in.blas);
+    }
+    std::vector<bvh2_node> nodes;
+    int32_t root = INT32_MIN;
+    if (num_instances > 0)
+    {
+        std::vector<uint32_t> ids(num_instances);
+        std::iota(ids.begin(), ids.end(), 0u);
+        nodes.reserve(num_instances);
+        box all;
+        root = build_top(ids, 0, num_instances, boxes, nodes, all);
+    }
+    device_guard g(ctx->device);
+    auto* t = new (std::nothrow) gbrt_tlas;
+    if (!t) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "tlas_build: host allocation");
+    t->device = ctx->device;
+    t->num_instances = num_instances;
+    t->num_inner = uint32_t(nodes.size());
+    t->root = root;
+    cudaError_t e = cudaSuccess;
+    if (num_instances > 0)
+    {
+        if ((e = cudaMalloc(&t->records, records.size() * sizeof(float4))) == cudaSuccess &&
+            (e = cudaMalloc(&t->views, views.size() * sizeof(bvh_view))) == cudaSuccess)
+        {
+            e = cudaMemcpy(t->records, records.data(), records.size() * sizeof(float4), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(t->views, views.data(), views.size() * sizeof(bvh_view), cudaMemcpyHostToDevice);
+        }
+        if (e == cudaSuccess && !nodes.empty())
+        {
+            e = cudaMalloc(&t->nodes, nodes.size() * sizeof(bvh2_node));
+            if (e == cudaSuccess)
+                e = cudaMemcpy(t->nodes, nodes.data(), nodes.size() * sizeof(bvh2_node), cudaMemcpyHostToDevice);
+        }
+    }
+    if (e != cudaSuccess)
+    {
+        free_tlas(t);
+        delete t;
+        return check_cuda(ctx, e, "tlas_build");
+    }
+    *out = t;
+    return GBRT_OK;
+}
+
+extern "C" gbrt_status gbrt_tlas_destroy(gbrt_tlas* tlas)
+{
+    if (!tlas) return GBRT_ERR_INVALID_ARG;
+    device_guard g(tlas->device);
+    free_tlas(tlas);
+    delete tlas;
+    return GBRT_OK;
+}
+
+namespace {
+
+gbrt_status tlas_trace_call(gbrt_context* ctx, gbrt_tlas const* tlas, gbrt_ray const* d_rays, uint32_t n,
+                            gbrt_hit_inst* d_hits, bool any_hit)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!tlas || (n && (!d_rays || !d_hits))) return fail(ctx, GBRT_ERR_INVALID_ARG, "tlas_trace: null argument");
+    if ((reinterpret_cast<uintptr_t>(d_rays) & 15u) || (reinterpret_cast<uintptr_t>(d_hits) & 15u))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "tlas_trace: rays and hits must be 16-byte aligned");
+    if (n == 0) return GBRT_OK;
+    device_guard g(ctx->device);
+    tlas_view tv{ tlas->nodes, tlas->records, tlas->views, tlas->num_instances > 0 ? tlas->root : kEmptyLink,
+                  int32_t(tlas->num_inner), int32_t(tlas->num_instances) };
+    const uint32_t blocks = (n + kBlock - 1) / kBlock;
+    if (any_hit)
+        tlas_trace<true><<<blocks, kBlock, 0, ctx->stream>>>(tv, d_rays, n, d_hits, ctx->d_status);
+    else
+        tlas_trace<false><<<blocks, kBlock, 0, ctx->stream>>>(tv, d_rays, n, d_hits, ctx->d_status);
+    GBRT_LAUNCH_CHECK(ctx, "tlas_trace");
+    return GBRT_OK;
+}
+
+} // namespace
+
+extern "C" gbrt_status gbrt_tlas_trace_closest_hit(gbrt_context* ctx, gbrt_tlas const* tlas, gbrt_ray const* d_rays,
+                                                   uint32_t n, gbrt_hit_inst* d_hits)
+{
+    return tlas_trace_call(ctx, tlas, d_rays, n, d_hits, false);
+}
+
+extern "C" gbrt_status gbrt_tlas_trace_any_hit(gbrt_context* ctx, gbrt_tlas const* tlas, gbrt_ray const* d_rays,
+                                               uint32_t n, gbrt_hit_inst* d_hits)
+{
+    return tlas_trace_call(ctx, tlas, d_rays, n, d_hits, true);
+}

@@ -474,6 +474,38 @@ inline size_t align_up(size_t v) { return (v + 255) & ~size_t(255); }
 
 } // namespace
 
+// The box of a one-triangle tree: get_bounds(triangle) (math/detail/triangle.inl:43-52)
+// on the host, from the device triangle.
+gbrt_status set_single_box(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris)
+{
+    gbrt_triangle t;
+    GBRT_CUDA(ctx, cudaMemcpyAsync(&t, d_tris, sizeof(t), cudaMemcpyDeviceToHost, ctx->stream));
+    GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    auto mn = [](float a, float b) { return a < b ? a : b; };
+    auto mx = [](float a, float b) { return a < b ? b : a; };
+    for (int a = 0; a < 3; ++a)
+    {
+        float p1 = t.v1[a] + t.e1[a], p2 = t.v1[a] + t.e2[a];
+        bvh->lo[a] = mn(mn(mn(FLT_MAX, t.v1[a]), p1), p2);
+        bvh->hi[a] = mx(mx(mx(-FLT_MAX, t.v1[a]), p1), p2);
+    }
+    return GBRT_OK;
+}
+
+// The scene box: the union of the root's two child boxes with the reference's min / max
+// (x < y ? x : y), as the exported root node holds it.
+void set_scene_box(gbrt_bvh* bvh, bvh2_node const& root)
+{
+    auto mn = [](float a, float b) { return a < b ? a : b; };
+    auto mx = [](float a, float b) { return a < b ? b : a; };
+    bvh->lo[0] = mn(root.xy0.x, root.xy1.x);
+    bvh->hi[0] = mx(root.xy0.y, root.xy1.y);
+    bvh->lo[1] = mn(root.xy0.z, root.xy1.z);
+    bvh->hi[1] = mx(root.xy0.w, root.xy1.w);
+    bvh->lo[2] = mn(root.z01.x, root.z01.z);
+    bvh->hi[2] = mx(root.z01.y, root.z01.w);
+}
+
 gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh)
 {
     bvh->kind = bvh_kind::lbvh;
@@ -569,12 +601,7 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
         GBRT_CUDA(ctx, cudaStreamSynchronize(s));
         bvh->height = h;
         // scene bounds: the union of the root's two child boxes
-        bvh->lo[0] = std::min(root.xy0.x, root.xy1.x);
-        bvh->hi[0] = std::max(root.xy0.y, root.xy1.y);
-        bvh->lo[1] = std::min(root.xy0.z, root.xy1.z);
-        bvh->hi[1] = std::max(root.xy0.w, root.xy1.w);
-        bvh->lo[2] = std::min(root.z01.x, root.z01.z);
-        bvh->hi[2] = std::max(root.z01.y, root.z01.w);
+        set_scene_box(bvh, root);
 
         if (ctx->trace_flags & GBRT_TRACE_WIDE_NODES)
         {
@@ -612,6 +639,8 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
         // one triangle: it is the root leaf (lbvh.h:428-433)
         emit_single<<<1, 1, 0, s>>>(d_tris, bvh->tris);
         GBRT_LAUNCH_CHECK(ctx, "emit_single");
+        st = set_single_box(ctx, bvh, d_tris);
+        if (st != GBRT_OK) return st;
     }
     if (bvh->height + 1 > uint32_t(kStackSize))
         return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "LBVH height exceeds the traversal stack");
@@ -638,7 +667,7 @@ gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_
     {
         emit_single<<<1, 1, 0, s>>>(d_tris, bvh->tris);
         GBRT_LAUNCH_CHECK(ctx, "emit_single");
-        return GBRT_OK;
+        return set_single_box(ctx, bvh, d_tris);
     }
     const size_t off_parent = 0, off_arrivals = align_up(size_t(n) * 4), off_height = align_up(off_arrivals + size_t(n) * 4);
     gbrt_status st = ensure_scratch(ctx, off_height + 256);
@@ -658,12 +687,7 @@ gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_
     bvh2_node root;
     GBRT_CUDA(ctx, cudaMemcpyAsync(&root, bvh->nodes, sizeof(root), cudaMemcpyDeviceToHost, s));
     GBRT_CUDA(ctx, cudaStreamSynchronize(s));
-    bvh->lo[0] = std::min(root.xy0.x, root.xy1.x);
-    bvh->hi[0] = std::max(root.xy0.y, root.xy1.y);
-    bvh->lo[1] = std::min(root.xy0.z, root.xy1.z);
-    bvh->hi[1] = std::max(root.xy0.w, root.xy1.w);
-    bvh->lo[2] = std::min(root.z01.x, root.z01.z);
-    bvh->hi[2] = std::max(root.z01.y, root.z01.w);
+    set_scene_box(bvh, root);
     return GBRT_OK;
 }
 

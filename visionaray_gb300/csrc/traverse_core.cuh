@@ -59,15 +59,18 @@ struct shared_stack
 };
 
 // A tree taller than the stack's capacity sets kStatusStackOverflow and skips the
-// subtrees that did not fit.
+// subtrees that did not fit.  t_best: a hit must be strictly closer than this (a
+// closer hit found elsewhere, e.g. in another instance); the result's t is t_best
+// when nothing closer was found.
 template <bool AnyHit, class StackT>
 __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const bvh2_node* __restrict__ nodes,
                                                           const tri48* __restrict__ tris, int32_t root,
                                                           int32_t num_inner, int32_t num_tris, f3 o, f3 d,
-                                                          float tmin, float tmax, uint32_t* __restrict__ status)
+                                                          float tmin, float tmax, uint32_t* __restrict__ status,
+                                                          float t_best = FLT_MAX)
 {
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
-    trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
+    trace_result best{ -1, t_best, 0.0f, 0.0f };
 
     int sp = 0;
     int node = root;

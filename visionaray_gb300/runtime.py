@@ -15,7 +15,8 @@ import os
 
 import numpy as np
 
-from .types import AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS, RAY, TRIANGLE
+from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, HIT_INST, INSTANCE, MATERIAL, PT_PARAMS, RAY,
+                    TRIANGLE)
 
 LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
 
@@ -54,6 +55,10 @@ SIGNATURES = {
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_forward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_backward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbrt_tlas_build": (_i32, [_vp, _vp, _u32, _pp]),
+    "gbrt_tlas_destroy": (_i32, [_vp]),
+    "gbrt_tlas_trace_closest_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
+    "gbrt_tlas_trace_any_hit": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_batch_create": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_batch_destroy": (_i32, [_vp]),
     "gbrt_batch_build": (_i32, [_vp, _vp, _vp]),
@@ -487,3 +492,52 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class TLAS:
+    """The top-level tree over instances (index_bvh<index_bvh_inst_t>): instances is a
+    list of (IndexBVH, transform) with transform visionaray's mat4x3 as 12 floats
+    (columns 0..3; the linear map's row i is column i, the translation column 3).
+    Keeps the bottom-level trees alive."""
+
+    def __init__(self, instances, ctx=None):
+        self.ctx = ctx or default_context()
+        self.blas = [b for b, _ in instances]
+        arr = np.zeros(len(instances), INSTANCE)
+        for k, (b, xf) in enumerate(instances):
+            arr[k]["blas"] = b.h.value or 0
+            arr[k]["transform"] = np.asarray(xf, np.float32).reshape(12)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbrt_tlas_build(self.ctx.h, _hptr(arr), len(arr), ctypes.byref(h)))
+        self.h = h
+
+    def _trace(self, rays, any_hit, out):
+        torch = _torch()
+        n = rays.numel() * rays.element_size() // RAY.itemsize
+        hits = out if out is not None else torch.empty((max(n, 1), 8), dtype=torch.float32, device=rays.device)
+        fn = self.ctx.lib.gbrt_tlas_trace_any_hit if any_hit else self.ctx.lib.gbrt_tlas_trace_closest_hit
+        self.ctx.check(fn(self.ctx.h, self.h, _dptr(rays), n, _dptr(hits)))
+        return hits
+
+    def closest_hit(self, rays, out=None):
+        """Device rays (n, 8) float32 -> (n, 8) hit records (HIT_INST bytes)."""
+        return self._trace(rays, False, out)
+
+    def any_hit(self, rays, out=None):
+        return self._trace(rays, True, out)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbrt_tlas_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hits_inst_to_numpy(t, n=None):
+    a = t.detach().cpu().numpy().reshape(-1).view(HIT_INST)
+    return a if n is None else a[:n]

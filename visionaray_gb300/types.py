@@ -24,6 +24,9 @@ CAMERA = np.dtype([("eye", "<f4", (3,)), ("center", "<f4", (3,)), ("up", "<f4", 
 PT_PARAMS = np.dtype([("width", "<u4"), ("height", "<u4"), ("spp", "<u4"), ("num_bounces", "<u4"),
                       ("epsilon", "<f4"), ("frame_id", "<u4"), ("sfactor", "<f4"), ("dfactor", "<f4"),
                       ("background", "<f4", (4,)), ("ambient", "<f4", (3,)), ("flags", "<u4")])
+INSTANCE = np.dtype([("blas", "<u8"), ("transform", "<f4", (12,))])
+HIT_INST = np.dtype([("prim_id", "<u4"), ("inst_id", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),
+                     ("geom_id", "<u4"), ("reserved", "<u4", (2,))])
 BATCH_LAUNCH = np.dtype([("block", "<u4"), ("tile", "<u4"), ("stack", "<u4"), ("order", "<u4")])
 MATTE, EMISSIVE = 0, 1
 BATCH_ORDER_ROWS, BATCH_ORDER_BLOCKS = 0, 1
@@ -38,3 +41,4 @@ assert TRIANGLE.itemsize == 44 and RAY.itemsize == 32
 assert HIT.itemsize == 16 and BVH_NODE.itemsize == 32
 assert MATERIAL.itemsize == 20 and AREA_LIGHT.itemsize == 60 and CAMERA.itemsize == 40
 assert PT_PARAMS.itemsize == 64 and BATCH_LAUNCH.itemsize == 16
+assert INSTANCE.itemsize == 56 and HIT_INST.itemsize == 32
