@@ -230,7 +230,11 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_dynamic(bvh_view v, co
     }
 }
 
-// 24-bit Morton key of each ray's origin cell (8 bits per axis of the scene box).
+// Ray order: origin cells per axis of the scene box (2^kCellBits), Morton-interleaved.
+constexpr int kCellBits = 8;
+constexpr int kCells = 1 << kCellBits;
+
+// Morton key of each ray's origin cell (kCellBits bits per axis of the scene box).
 __global__ void __launch_bounds__(kTraceBlock) ray_origin_keys(const gbrt_ray* __restrict__ rays, uint32_t n,
                                                                float3 lo, float3 scale, uint32_t* __restrict__ keys,
                                                                uint32_t* __restrict__ values)
@@ -243,7 +247,7 @@ __global__ void __launch_bounds__(kTraceBlock) ray_origin_keys(const gbrt_ray* _
 #pragma unroll
     for (int a = 0; a < 3; ++a)
     {
-        float v = fminf(fmaxf(q[a], 0.0f), 255.0f);   // NaN (degenerate ray) lands in cell 0
+        float v = fminf(fmaxf(q[a], 0.0f), float(kCells - 1));   // NaN (degenerate ray) lands in cell 0
         c[a] = uint32_t(v);
     }
     keys[i] = morton3(c[0], c[1], c[2]);
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(kTraceBlock) write_misses(gbrt_hit* __restrict
 }
 
 constexpr uint32_t kSortMinRays = 1u << 16;   // below this the order costs more than it saves
-constexpr int kOriginKeyBits = 24;
+constexpr int kOriginKeyBits = 3 * kCellBits;
 
 inline size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
@@ -298,8 +302,9 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         uint32_t* vals_alt = reinterpret_cast<uint32_t*>(base + 3 * w);
         float3 lo = make_float3(bvh->lo[0], bvh->lo[1], bvh->lo[2]);
         float ext[3] = { bvh->hi[0] - bvh->lo[0], bvh->hi[1] - bvh->lo[1], bvh->hi[2] - bvh->lo[2] };
-        float3 scale = make_float3(ext[0] > 0.0f ? 256.0f / ext[0] : 0.0f, ext[1] > 0.0f ? 256.0f / ext[1] : 0.0f,
-                                   ext[2] > 0.0f ? 256.0f / ext[2] : 0.0f);
+        const float cells = float(kCells);
+        float3 scale = make_float3(ext[0] > 0.0f ? cells / ext[0] : 0.0f, ext[1] > 0.0f ? cells / ext[1] : 0.0f,
+                                   ext[2] > 0.0f ? cells / ext[2] : 0.0f);
         ray_origin_keys<<<blocks, kTraceBlock, 0, stream>>>(d_rays, n, lo, scale, keys, vals);
         GBRT_LAUNCH_CHECK(ctx, "ray_origin_keys");
         gbrt_status st = radix_sort_pairs(ctx, keys, vals, keys_alt, vals_alt, n, kOriginKeyBits, base + 4 * w,
