@@ -299,6 +299,10 @@ typedef struct gbrt_pt_params
  * arithmetic and random numbers: the images are identical bit for bit.  About 2x
  * slower than the wavefront on the box and inverse-rendering workloads (GB300).     */
 #define GBRT_PT_MEGAKERNEL 4u
+/* Scheduling only: each bounce's ray and shadow queues are ordered by the Morton cell
+ * of their origins before they are traced (images identical bit for bit).  Slower on
+ * the box scene (GB300): the per-bounce sort costs more than the coherence it buys.  */
+#define GBRT_PT_SORT_QUEUES 8u
 
 typedef struct gbrt_pt_scene gbrt_pt_scene;
 

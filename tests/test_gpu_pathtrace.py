@@ -131,3 +131,20 @@ def test_megakernel_equals_wavefront_ambient_and_empty():
                                                                 background=(0.1, 0.2, 0.3, 0.5), flags=m)).cpu()
                 for m in (0, PT_MEGAKERNEL)]
         assert imgs[0].numpy().tobytes() == imgs[1].numpy().tobytes()
+
+
+@pytest.mark.parametrize("flags", [0, PT_SHADOW_RANGE_FIX])
+def test_sorted_queues_equal_unsorted(small_box, flags):
+    """GBRT_PT_SORT_QUEUES orders each bounce's ray and shadow queues by origin cell;
+    the paths and the image are unchanged bit for bit."""
+    from visionaray_gb300.types import PT_SORT_QUEUES
+    tris, mats, lights, cam = small_box
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    scene = vg.PTScene(bvh, mats, lights)
+    out = []
+    for extra in (0, PT_SORT_QUEUES):
+        p = scenes.pt_params(96, 64, 4, num_bounces=8, frame_id=5, flags=flags | extra)
+        img = vg.pathtrace_frame(scene, cam, p)
+        bvh.ctx.synchronize()
+        out.append(img.cpu().numpy())
+    assert out[0].tobytes() == out[1].tobytes()

@@ -33,6 +33,7 @@ BATCH_ORDER_ROWS, BATCH_ORDER_BLOCKS = 0, 1
 PT_SHADOW_RANGE_FIX = 1
 PT_NO_RUSSIAN_ROULETTE = 2
 PT_MEGAKERNEL = 4
+PT_SORT_QUEUES = 8
 
 NO_HIT = 0xFFFFFFFF
 FLT_MAX = float(np.finfo(np.float32).max)
