@@ -282,7 +282,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
         views.append(plain_images[a:b].view(int(params["height"][s]), int(params["width"][s]), 4))
 
     def plain_step():
-        builder = vg.lbvh_builder(ctx)
+        builder = vg.ploc_builder(ctx) if args.builder == "ploc" else vg.lbvh_builder(ctx)
         for s in range(ns):
             bvh = builder.build(d_tris[int(offsets[s]) * 44:int(offsets[s + 1]) * 44])
             sc = vg.PTScene(bvh, mats, no_lights)
@@ -374,7 +374,7 @@ def run_ours(args):
     d_tris = vg.as_device_bytes(tris, local)
     torch.cuda.synchronize()
     b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    builder = vg.lbvh_builder(ctx)
+    builder = vg.ploc_builder(ctx) if args.builder == "ploc" else vg.lbvh_builder(ctx)
     bvh = builder.build(d_tris)   # warm (allocates the context scratch)
     del bvh
     b0.record(stream)
@@ -503,7 +503,7 @@ def run_ours(args):
                        "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
                        "trace_flags": args.trace_flags, "trace_refill": args.trace_refill,
-                       "warmup_steps_run": done},
+                       "warmup_steps_run": done, "builder": args.builder},
             "kernels": per, "roofline": roofline,
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
@@ -525,6 +525,8 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--builder", choices=["lbvh", "ploc"], default="lbvh",
+                   help="tree of the traversal leg: the LBVH (the workload's builder) or the PLOC build")
     p.add_argument("--pt-flags", type=int, default=0,
                    help="GBRT_PT_* scheduling bits of the path-tracing and adjoint legs (4: megakernel)")
     p.add_argument("--batch-steps", type=int, default=3, help="timed batched-graph steps (0: skip)")

@@ -160,6 +160,14 @@ gbrt_status gbrt_bvh_destroy(gbrt_bvh* bvh);
 gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* num_bvh2_nodes,
                             uint32_t* depth_bound);
 
+/* High-quality build (no visionaray counterpart; the reference's GPU builder is the
+ * LBVH): parallel locally-ordered clustering (Meister & Bittner 2018) from the Morton
+ * order -- mutual nearest neighbours within 16 positions by union surface area merge,
+ * level by level -- giving trees close to the binned SAH builder's (sah.h:176-807) at
+ * GPU build speed.  Same handle, traversal and refit as an LBVH; export_bvh2 writes
+ * the generic index_bvh layout (breadth first, children adjacent).  Synchronous.    */
+gbrt_status gbrt_bvh_build_ploc(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh** out);
+
 /* Writes the tree in visionaray's cuda_index_bvh node layout, exactly as the
  * reference's lbvh::collapse kernel emits it (detail/bvh/lbvh.h:374-451): root at 0,
  * the children of Karras inner node i at 1+2i and 2+2i, leaves with one primitive

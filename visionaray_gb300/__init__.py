@@ -8,5 +8,5 @@ from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, FLT_MAX, HIT, MA
                     NO_HIT, PT_PARAMS, PT_SHADOW_RANGE_FIX, RAY, TRIANGLE)
 from .runtime import (TLAS, Batch, Context, GbrtError, IndexBVH, PTScene, any_hit, closest_hit,  # noqa: F401
                       default_context, device_rays, as_device_bytes, hits_inst_to_numpy, hits_to_numpy,
-                      lbvh_builder, load_library, pathtrace_backward, pathtrace_forward,
+                      lbvh_builder, load_library, pathtrace_backward, pathtrace_forward, ploc_builder,
                       pathtrace_frame, pinhole_camera_basis)

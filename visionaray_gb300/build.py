@@ -28,7 +28,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "batch.cu", "batch_pt.cu", "instances.cu", "lbvh.cu", "noalloc.cu", "pathtrace.cu",
-              "radix_sort.cu", "traverse.cu"]
+              "ploc.cu", "radix_sort.cu", "traverse.cu"]
 CU_HEADERS = ["device_math.cuh", "bvh_layout.cuh", "api_internal.h", "traverse_core.cuh", "lbvh_device.cuh",
               "pt_shade.cuh"]
 # host code of every unit keeps expressions unfused (-ffp-contract=off) so x86-64 and

@@ -272,6 +272,31 @@ gbrt_status gbrt_bvh_build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, 
     return GBRT_OK;
 }
 
+gbrt_status gbrt_bvh_build_ploc(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_ploc: null output");
+    *out = nullptr;
+    if (n > 0 && !d_tris) return fail(ctx, GBRT_ERR_INVALID_ARG, "build_ploc: null triangles");
+    if (n > kMaxPrims) return fail(ctx, GBRT_ERR_TOO_LARGE, "build_ploc: more than 2^29 triangles");
+    if ((reinterpret_cast<uintptr_t>(d_tris) & 3u) != 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "build_ploc: triangles not 4-byte aligned");
+    device_guard g(ctx->device);
+    auto* bvh = new (std::nothrow) gbrt_bvh;
+    if (!bvh) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "build_ploc: host allocation");
+    bvh->device = ctx->device;
+    gbrt_status st = build_ploc(ctx, d_tris, n, bvh);
+    if (st != GBRT_OK)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        free_bvh_arrays(bvh);
+        delete bvh;
+        return st;
+    }
+    *out = bvh;
+    return GBRT_OK;
+}
+
 gbrt_status gbrt_bvh_build_lbvh_host(gbrt_context* ctx, gbrt_triangle const* h_tris, uint32_t n, gbrt_bvh** out)
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;
@@ -345,7 +370,8 @@ gbrt_status gbrt_bvh_refit(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;
     if (!bvh || (n > 0 && !d_tris)) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: null argument");
-    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: not an LBVH");
+    if (bvh->kind != bvh_kind::lbvh && bvh->kind != bvh_kind::ploc)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: not a GPU-built tree");
     if (n != bvh->num_prims) return fail(ctx, GBRT_ERR_INVALID_ARG, "refit: triangle count differs from the build");
     device_guard g(ctx->device);
     return refit_lbvh(ctx, bvh, d_tris);

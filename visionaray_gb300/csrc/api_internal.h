@@ -60,6 +60,7 @@ enum class bvh_kind
 {
     lbvh,
     uploaded,
+    ploc,   // ploc.cu: same node pairs and Morton-ordered leaves as the LBVH
 };
 
 struct gbrt_bvh
@@ -152,6 +153,11 @@ gbrt_status ensure_scratch(gbrt_context* ctx, size_t bytes);
 // lbvh.cu
 gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh);
 gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris);
+gbrt_status morton_order(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, uint32_t* codes_out,
+                         uint32_t* ids_out);
+// ploc.cu
+gbrt_status build_ploc(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh);
+gbrt_status export_generic(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes, uint32_t* d_indices);
 gbrt_status export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes,
                         uint32_t* d_indices);
 gbrt_status morton_codes_input_order(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes);

@@ -685,15 +685,46 @@ gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_
                                                     bvh->tris, root_height, ctx->d_status);
     GBRT_LAUNCH_CHECK(ctx, "refit_and_emit");
     bvh2_node root;
-    GBRT_CUDA(ctx, cudaMemcpyAsync(&root, bvh->nodes, sizeof(root), cudaMemcpyDeviceToHost, s));
+    GBRT_CUDA(ctx, cudaMemcpyAsync(&root, bvh->nodes + (bvh->root > 0 ? bvh->root : 0), sizeof(root),
+                                   cudaMemcpyDeviceToHost, s));
     GBRT_CUDA(ctx, cudaStreamSynchronize(s));
     set_scene_box(bvh, root);
     return GBRT_OK;
 }
 
+// Morton order of n triangles (the LBVH build's first three stages): codes_out[j] /
+// ids_out[j] = the code and the input index of the j-th triangle in order.  Uses the
+// context scratch; stream-ordered, no synchronisation.
+gbrt_status morton_order(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, uint32_t* codes_out,
+                         uint32_t* ids_out)
+{
+    if (n == 0) return GBRT_OK;
+    cudaStream_t s = ctx->stream;
+    size_t off_centroids = 0;
+    size_t off_keys_alt = align_up(off_centroids + size_t(n) * 16);
+    size_t off_vals_alt = align_up(off_keys_alt + size_t(n) * 4);
+    size_t off_cb = align_up(off_vals_alt + size_t(n) * 4);
+    size_t off_sort = align_up(off_cb + 8 * 4);
+    gbrt_status st = ensure_scratch(ctx, off_sort + radix_sort_scratch_bytes(n));
+    if (st != GBRT_OK) return st;
+    char* base = static_cast<char*>(ctx->scratch);
+    float4* centroids = reinterpret_cast<float4*>(base + off_centroids);
+    int* cb = reinterpret_cast<int*>(base + off_cb);
+    init_build_words<<<1, 8, 0, s>>>(cb);
+    GBRT_LAUNCH_CHECK(ctx, "init_build_words");
+    uint32_t grid = std::min<uint32_t>(blocks_for(n), uint32_t(ctx->num_sms) * 8);
+    centroid_bounds<<<grid, kBlock, 0, s>>>(d_tris, n, centroids, cb);
+    GBRT_LAUNCH_CHECK(ctx, "centroid_bounds");
+    morton_codes<<<blocks_for(n), kBlock, 0, s>>>(centroids, n, cb, codes_out, ids_out);
+    GBRT_LAUNCH_CHECK(ctx, "morton_codes");
+    return radix_sort_pairs(ctx, codes_out, ids_out, reinterpret_cast<uint32_t*>(base + off_keys_alt),
+                            reinterpret_cast<uint32_t*>(base + off_vals_alt), n, 30, base + off_sort);
+}
+
 gbrt_status export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d_nodes, uint32_t* d_indices)
 {
-    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "export_bvh2: not an LBVH");
+    if (bvh->kind == bvh_kind::ploc) return export_generic(ctx, bvh, d_nodes, d_indices);
+    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "export_bvh2: not a built tree");
     uint32_t n = bvh->num_prims;
     if (n == 0) return GBRT_OK;
     cudaStream_t s = ctx->stream;
@@ -713,7 +744,8 @@ gbrt_status export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_bvh_node* d
 
 gbrt_status morton_codes_input_order(gbrt_context* ctx, gbrt_bvh const* bvh, uint32_t* d_codes)
 {
-    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "morton_codes: not an LBVH");
+    if (bvh->kind != bvh_kind::lbvh && bvh->kind != bvh_kind::ploc)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "morton_codes: not a built tree");
     if (bvh->num_prims == 0) return GBRT_OK;
     scatter_codes<<<blocks_for(bvh->num_prims), kBlock, 0, ctx->stream>>>(bvh->sorted_codes, bvh->sorted_ids,
                                                                            bvh->num_prims, d_codes);

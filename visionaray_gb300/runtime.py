@@ -38,6 +38,7 @@ SIGNATURES = {
     "gbrt_context_set_trace_refill": (_i32, [_vp, _u32]),
     "gbrt_bvh_build_lbvh": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_build_lbvh_host": (_i32, [_vp, _vp, _u32, _pp]),
+    "gbrt_bvh_build_ploc": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_upload_bvh2_host": (_i32, [_vp, _vp, _u32, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_bvh_destroy": (_i32, [_vp]),
     "gbrt_bvh_counts": (_i32, [_vp, _vp, _vp, _vp]),
@@ -269,6 +270,22 @@ class lbvh_builder:
         else:
             n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
             ctx.check(ctx.lib.gbrt_bvh_build_lbvh(ctx.h, _dptr(tris), n, ctypes.byref(h)))
+        return IndexBVH(ctx, h)
+
+
+class ploc_builder:
+    """High-quality GPU build (parallel locally-ordered clustering); no visionaray
+    counterpart.  Same IndexBVH handle as lbvh_builder."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+
+    def build(self, tris):
+        """tris: torch uint8 CUDA tensor of n*44 bytes."""
+        ctx = self.ctx
+        h = ctypes.c_void_p()
+        n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
+        ctx.check(ctx.lib.gbrt_bvh_build_ploc(ctx.h, _dptr(tris), n, ctypes.byref(h)))
         return IndexBVH(ctx, h)
 
 
