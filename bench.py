@@ -183,12 +183,13 @@ PT_WORKLOAD = ("path tracing: closed unit box + 0.25^2 ceiling light (emission 1
                "Russian roulette from depth 3")
 
 
-def run_pathtrace(vg, ctx, frames, flags, rprint):
+def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc"):
     """Msamples/s of the path-tracing workload (one frame = 1920x1080 x 64 spp)."""
     import torch
     from visionaray_gb300 import scenes
     tris, mats, lights = scenes.box_scene()
-    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris, ctx.device))
+    make = vg.ploc_builder if builder == "ploc" else vg.lbvh_builder
+    bvh = make(ctx).build(vg.as_device_bytes(tris, ctx.device))
     scene = vg.PTScene(bvh, mats, lights)
     cam = scenes.box_camera()
     dev = f"cuda:{ctx.device}"
@@ -209,7 +210,7 @@ def run_pathtrace(vg, ctx, frames, flags, rprint):
     ms = ev[0].elapsed_time(ev[1]) / frames
     samples = PT_WIDTH * PT_HEIGHT * PT_SPP
     mean = accum[..., :3].mean().item()
-    return {"workload": PT_WORKLOAD, "flags": flags, "frames": frames, "ms_per_frame": round(ms, 2),
+    return {"workload": PT_WORKLOAD, "flags": flags, "builder": builder, "frames": frames, "ms_per_frame": round(ms, 2),
             "msamples_s": round(samples / (ms * 1e-3) / 1e6, 2), "image_mean": round(mean, 5),
             "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
 
@@ -332,14 +333,14 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     return res
 
 
-def run_adjoint(ctx, steps, rprint, flags=0):
+def run_adjoint(ctx, steps, rprint, flags=0, builder="ploc"):
     """The inverse-albedo workload: `steps` Adam steps of forward frame + L2 loss +
     path-replay adjoint; median forward / backward times and their ratio."""
     from visionaray_gb300 import inverse
-    r = inverse.optimize(steps=steps, ctx=ctx, extra_flags=flags)
+    r = inverse.optimize(steps=steps, ctx=ctx, extra_flags=flags, builder=builder)
     return {"workload": "inverse albedo on the box scene reduced to 4,014 triangles (2 blobs, subdiv 10): "
                         "512x512, 16 spp, depth 6 forward + L2 loss + adjoint per step, target 256 spp",
-            "steps": steps, "flags": int(inverse.FLAGS | flags), "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
+            "steps": steps, "flags": int(inverse.FLAGS | flags), "builder": builder, "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
             "bwd_over_fwd": round(r["bwd_ms"] / r["fwd_ms"], 3), "loss_start": round(r["losses"][0], 6),
             "loss_end": round(r["losses"][-1], 6), "albedo_error_start": round(r["albedo_error_start"], 4),
             "albedo_error_end_seen": round(r["albedo_error_end_seen"], 4)}
@@ -474,9 +475,36 @@ def run_ours(args):
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size capture",
                 "peak_source": f"{peak_kind} hbm_gbs"}
 
+    # the same rays through the PLOC tree (a higher-quality GPU build; the workload's
+    # builder is the LBVH, so this is reported beside the line's value, not as it)
+    alt = None
+    if args.builder == "lbvh" and not args.no_ploc:
+        b0.record(stream)
+        pbvh = vg.ploc_builder(ctx).build(d_tris)
+        b1.record(stream)
+        torch.cuda.synchronize()
+        p_build = b0.elapsed_time(b1)
+        pev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        saved, bvh = bvh, pbvh
+        for _ in range(max(3, args.warmup)):
+            step()
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            step(pev[k])
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        pc = statistics.mean(e[0].elapsed_time(e[1]) for e in pev)
+        pa = statistics.mean(e[1].elapsed_time(e[2]) for e in pev)
+        alt = {"builder": "ploc", "build_ms": round(p_build, 3),
+               "value": round(rays_per_step / ((pc + pa) * 1e-3) / 1e6, 2),
+               "closest_mrays_s": round(n_c / (pc * 1e-3) / 1e6, 2), "any_mrays_s": round(n_a / (pa * 1e-3) / 1e6, 2),
+               "note": "same rays and hits (ties aside) through a PLOC tree; not the workload's LBVH"}
+        bvh = saved
+        del pbvh
+
     pt = None
     if args.pt_frames > 0:
-        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint)
+        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint, args.pt_builder)
 
     batched = None
     if args.batch_steps > 0:
@@ -485,7 +513,7 @@ def run_ours(args):
 
     adjoint = None
     if args.adjoint_steps > 0:
-        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint, args.pt_flags)
+        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint, args.pt_flags, args.pt_builder)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -508,7 +536,7 @@ def run_ours(args):
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
                     "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same},
             "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base,
-            "pathtrace": pt, "batched_pathtrace": batched, "adjoint": adjoint}
+            "ploc_tree": alt, "pathtrace": pt, "batched_pathtrace": batched, "adjoint": adjoint}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -525,8 +553,11 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--no-ploc", action="store_true", help="skip the traversal through the PLOC tree")
     p.add_argument("--builder", choices=["lbvh", "ploc"], default="lbvh",
                    help="tree of the traversal leg: the LBVH (the workload's builder) or the PLOC build")
+    p.add_argument("--pt-builder", choices=["lbvh", "ploc"], default="ploc",
+                   help="tree of the path-tracing and adjoint legs (their workloads name no builder)")
     p.add_argument("--pt-flags", type=int, default=0,
                    help="GBRT_PT_* scheduling bits of the path-tracing and adjoint legs (4: megakernel)")
     p.add_argument("--batch-steps", type=int, default=3, help="timed batched-graph steps (0: skip)")

@@ -17,12 +17,13 @@ from .types import PT_NO_RUSSIAN_ROULETTE, PT_SHADOW_RANGE_FIX
 FLAGS = PT_SHADOW_RANGE_FIX | PT_NO_RUSSIAN_ROULETTE
 
 
-def setup(n_blobs=2, subdiv=10, seed=1, hidden_seed=5, ctx=None):
+def setup(n_blobs=2, subdiv=10, seed=1, hidden_seed=5, ctx=None, builder="lbvh"):
     """(scene, tris, materials, lights, hidden albedo, emission) on the GPU."""
     import torch
     ctx = ctx or rt.default_context()
     tris, mats, lights = scenes.box_scene(n_blobs=n_blobs, subdiv=subdiv, seed=seed)
-    bvh = rt.lbvh_builder(ctx).build(rt.as_device_bytes(tris, ctx.device))
+    make = rt.ploc_builder if builder == "ploc" else rt.lbvh_builder
+    bvh = make(ctx).build(rt.as_device_bytes(tris, ctx.device))
     scene = rt.PTScene(bvh, mats, lights)
     rng = np.random.default_rng(hidden_seed)
     hidden = rng.uniform(0.1, 0.9, size=(len(mats), 3)).astype(np.float32)
@@ -43,12 +44,12 @@ def l2_adjoint(image, target):
 
 
 def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_spp=256, ctx=None, log=None,
-             extra_flags=0):
+             extra_flags=0, builder="lbvh"):
     """Adam on the albedos.  Returns a dict with the loss history, the parameter error
     and the mean forward / backward times (CUDA events)."""
     import torch
     ctx = ctx or rt.default_context()
-    scene, tris, mats, lights, hidden, emission = setup(ctx=ctx)
+    scene, tris, mats, lights, hidden, emission = setup(ctx=ctx, builder=builder)
     cam = scenes.box_camera()
     tparams = scenes.pt_params(width, height, target_spp, num_bounces=depth, frame_id=1000, flags=FLAGS | extra_flags)
     target = rt.pathtrace_forward(scene, cam, tparams, hidden, emission)
