@@ -283,7 +283,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
         views.append(plain_images[a:b].view(int(params["height"][s]), int(params["width"][s]), 4))
 
     def plain_step():
-        builder = vg.ploc_builder(ctx) if args.builder == "ploc" else vg.lbvh_builder(ctx)
+        builder = vg.lbvh_builder(ctx)
         for s in range(ns):
             bvh = builder.build(d_tris[int(offsets[s]) * 44:int(offsets[s + 1]) * 44])
             sc = vg.PTScene(bvh, mats, no_lights)
