@@ -82,10 +82,10 @@ def build(verbose=False, with_reference=True):
         objs.append(o)
         if _stale(o, [s] + headers):
             jobs.append((src, [NVCC] + NVCC_FLAGS + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o]))
-    scenes_src = os.path.join(CSRC, "scenes.cpp")
-    if _stale(LIBSCENES, [scenes_src, os.path.join(CSRC, "scenes.h")]):
+    scenes_srcs = [os.path.join(CSRC, "scenes.cpp"), os.path.join(CSRC, "obj.cpp")]
+    if _stale(LIBSCENES, scenes_srcs + [os.path.join(CSRC, "scenes.h")]):
         jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
-                                "-ffp-contract=off", "-Wall", scenes_src, "-o", LIBSCENES]))
+                                "-ffp-contract=off", "-Wall"] + scenes_srcs + ["-o", LIBSCENES]))
     # the oracle flags are those of oracle/Makefile (kept for manual builds)
     oracle_flags = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"]
     oracle_srcs = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "pathtrace.cpp")]

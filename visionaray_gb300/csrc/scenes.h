@@ -61,6 +61,18 @@ uint64_t gbrt_scene_box_count(uint32_t n_blobs, uint32_t subdiv);
 void gbrt_scene_box(uint32_t n_blobs, uint32_t subdiv, uint64_t seed, float light_y,
                     gbrt_triangle* tris, float* albedo);
 
+/* Wavefront OBJ ingestion (the reference viewer's load_obj, src/common/
+ * obj_loader.cpp): vertices, faces as triangle fans with 1-based or negative
+ * indices, degenerate triangles rejected, prim_id = running index, geom_id = the
+ * material slot activated by the last known "usemtl" (names from the files of
+ * "mtllib").  Writes up to `capacity` triangles to out (may be NULL) and returns the
+ * triangle count, -1 when the file cannot be read.                               */
+int64_t gbrt_obj_load(const char* path, gbrt_triangle* out, uint64_t capacity);
+/* The material slots of that file as matte (Kd) or emissive (Ke != 0) materials, one
+ * per activated usemtl (a single default slot when there is none); returns the slot
+ * count, -1 when the file cannot be read.                                          */
+int64_t gbrt_obj_materials(const char* path, gbrt_material* out, uint64_t capacity);
+
 /* Uniform float in [0,1) of the counter-based generator used above (exposed so that
  * tests can reproduce any value).                                                  */
 float gbrt_scene_u01(uint64_t seed, uint64_t stream, uint64_t index);

@@ -163,3 +163,27 @@ def batch_workload(num_scenes=512, seed=3, n_min=1000, n_max=1_000_000, spp=1, n
     mats = np.zeros(1, MATERIAL)
     mats["kind"], mats["color"], mats["scale"] = MATTE, 0.7, 1.0
     return tris, offsets, cams, params, mats
+
+
+def load_obj(path):
+    """(triangles, materials) of a Wavefront OBJ file, as the reference viewer's loader
+    reads its geometry (fans, negative indices, degenerate faces dropped, geom_id per
+    usemtl slot); materials are matte (Kd) or emissive (Ke) per slot."""
+    from .types import MATERIAL
+    lib = _load()
+    if not hasattr(lib.gbrt_obj_load, "_typed"):
+        lib.gbrt_obj_load.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64]
+        lib.gbrt_obj_load.restype = ctypes.c_int64
+        lib.gbrt_obj_materials.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64]
+        lib.gbrt_obj_materials.restype = ctypes.c_int64
+        lib.gbrt_obj_load._typed = True
+    p = str(path).encode()
+    n = lib.gbrt_obj_load(p, None, 0)
+    if n < 0:
+        raise FileNotFoundError(path)
+    tris = np.empty(n, TRIANGLE)
+    lib.gbrt_obj_load(p, _ptr(tris), n)
+    m = lib.gbrt_obj_materials(p, None, 0)
+    mats = np.zeros(m, MATERIAL)
+    lib.gbrt_obj_materials(p, _ptr(mats), m)
+    return tris, mats
