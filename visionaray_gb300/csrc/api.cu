@@ -98,13 +98,14 @@ gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
     return GBRT_OK;
 }
 
-// Host-buffer trace: chunks alternate between two slots, each on its own stream, so
-// the copy-in of one chunk overlaps the traversal and copy-out of the other.
+// Host-buffer trace: chunks alternate between the slots, each on its own stream, so
+// the copy-in of one chunk overlaps the traversal and copy-out of the others.
+constexpr int kHostChunkLog2 = 22;   // 4M rays (128 MB) per chunk
 gbrt_status trace_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits,
                        bool any_hit)
 {
     if (n == 0) return GBRT_OK;
-    const size_t chunk = std::min<size_t>(n, size_t(1) << 22);   // 4M rays (128 MB) per slot
+    const size_t chunk = std::min<size_t>(n, size_t(1) << kHostChunkLog2);   // rays per slot
     gbrt_status st = ensure_slots(ctx, chunk);
     if (st != GBRT_OK) return st;
     // work queued on the context stream (e.g. the build) must finish first
