@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GBRT_ABI_VERSION 1
+#define GBRT_ABI_VERSION 2
 
 typedef enum gbrt_status
 {
@@ -232,17 +232,29 @@ gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
 /* ------------------------------------------------------------------------------ */
 /* Path tracing                                                                    */
 
-/* One material per geom_id (materials[geom_id], get_surface.h:158): visionaray's
- * matte (Lambertian, detail/material/matte.inl; cd = color, kd = scale) or emissive
- * (detail/material/emissive.inl; ce = color, ls = scale), the two members of the
- * generic_material the path-tracing configurations use.                           */
+/* One material per geom_id (materials[geom_id], get_surface.h:158), a member of
+ * visionaray's generic_material:
+ *   matte    (Lambertian, detail/material/matte.inl): cd = color, kd = scale
+ *   emissive (detail/material/emissive.inl): ce = color, ls = scale
+ *   mirror   (detail/material/mirror.inl, specular_reflection brdf.h:292-357):
+ *            cr = color, kr = scale, conductor Fresnel with ior and absorption
+ *   glass    (detail/material/glass.inl, specular_transmission brdf.h:359-470):
+ *            ct = color, kt = scale, cr = color2, kr = scale2, ior
+ * (the path-tracing configurations use matte and emissive).                       */
 #define GBRT_MATERIAL_MATTE    0u
 #define GBRT_MATERIAL_EMISSIVE 1u
+#define GBRT_MATERIAL_MIRROR   2u
+#define GBRT_MATERIAL_GLASS    3u
 typedef struct gbrt_material
 {
     uint32_t kind;
     float    color[3];
     float    scale;
+    float    ior[3];
+    float    absorption[3];
+    float    color2[3];
+    float    scale2;
+    uint32_t reserved;
 } gbrt_material;
 
 /* area_light<float, basic_triangle<3, float>> (area_light.h, detail/area_light.inl:

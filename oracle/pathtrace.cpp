@@ -6,7 +6,10 @@
 // Restates detail/pathtracing.inl:42-233 with, for the materials and lights the
 // configurations use: matte + lambertian (detail/material/matte.inl:40-70,
 // brdf.h:26-84), emissive (detail/material/emissive.inl:20-44), area_light on a
-// triangle (detail/area_light.inl:27-53), sample_random_light (sampling.h:195-213),
+// triangle (detail/area_light.inl:27-53), mirror (detail/material/mirror.inl,
+// specular_reflection at brdf.h:293-352, conductor Fresnel at fresnel.h:18-35), glass
+// (detail/material/glass.inl, specular_transmission at brdf.h:360-469, dielectric
+// Fresnel at fresnel.h:37-56), sample_random_light (sampling.h:195-213),
 // cosine_sample_hemisphere (sampling.h:117-127), power_heuristic (sampling.h:73-79),
 // sample_surface on a triangle (math/detail/triangle.inl:69-83), get_surface /
 // get_normal / get_area (get_surface.h:129-160, get_normal.h:108-113,
@@ -189,6 +192,7 @@ enum : uint32_t
     kEmission = 1,
     kMatte = 2,
     kEnd = 3,
+    kSpecular = 4,
 };
 
 template <typename T>
@@ -198,6 +202,7 @@ struct vrec
     vec<T> thr{ 0, 0, 0 };
     T sigma = 0, mis = 0, escale = 0, kfac = 0, w = 0, x = 0, b0 = 0, kl = 0, rr = 0;
     vec<T> lint{ 0, 0, 0 };
+    vec<T> spec{ 0, 0, 0 };   // a specular vertex's throughput factor src * cos / pdf
 };
 
 // pathtracing::kernel::operator() (detail/pathtracing.inl:42-233) for one camera ray.
@@ -248,7 +253,9 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         gbrt_material m = tri.geom_id < nmat ? mats[tri.geom_id] : gbrt_material{ GBRT_MATERIAL_MATTE, { 0, 0, 0 }, 0 };
         vec<T> mcol = { T(m.color[0]), T(m.color[1]), T(m.color[2]) };
         bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
-        if (!emission && ext.albedo) mcol = load<T>(ext.albedo + 3 * geom);
+        const bool mirror = m.kind == GBRT_MATERIAL_MIRROR, glass = m.kind == GBRT_MATERIAL_GLASS;
+        const bool specular = mirror || glass;
+        if (!emission && !specular && ext.albedo) mcol = load<T>(ext.albedo + 3 * geom);
         if (emission && ext.emission) mcol = load<T>(ext.emission + 3 * geom);
         rec.geom = geom;
 
@@ -256,7 +263,77 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         vec<T> refl = { 0, 0, 0 };
         T brdf_pdf;
         vec<T> src;
-        if (!emission)
+        if (mirror)
+        {
+            // specular_reflection::sample_f (brdf.h:317-340) with the conductor Fresnel
+            // term (fresnel.h:18-35), on the unflipped shading normal
+            vec<T> wo = view_dir;
+            refl = T(2.0) * dot(sn, wo) * sn - wo;
+            brdf_pdf = T(1.0);
+            T cosi = std::abs(dot(sn, wo));
+            T f[3];
+            for (int c = 0; c < 3; ++c)
+            {
+                T eta = T(m.ior[c]), k = T(m.absorption[c]);
+                T rs2 = ((eta * eta + k * k) - T(2.0) * eta * cosi + cosi * cosi) /
+                        ((eta * eta + k * k) + T(2.0) * eta * cosi + cosi * cosi);
+                T rp2 = ((eta * eta + k * k) * cosi * cosi - T(2.0) * eta * cosi + T(1.0)) /
+                        ((eta * eta + k * k) * cosi * cosi + T(2.0) * eta * cosi + T(1.0));
+                f[c] = ((rs2 + rp2) / T(2.0)) * (T(m.color[c]) * T(m.scale));
+            }
+            T dn = std::abs(dot(sn, refl));
+            src = { f[0] / dn, f[1] / dn, f[2] / dn };
+        }
+        else if (glass)
+        {
+            // specular_transmission::sample_f (brdf.h:385-456), dielectric Fresnel term
+            // (fresnel.h:37-56) evaluated with (ior1, ior2) as the reference passes them
+            vec<T> wo = view_dir;
+            T cosi = dot(sn, wo);
+            cosi = cosi < T(1.0) ? cosi : T(1.0);
+            cosi = T(-1.0) < cosi ? cosi : T(-1.0);
+            bool entering = cosi > T(0.0);
+            vec<T> N = entering ? sn : -sn;
+            const T ior1[3] = { T(1.0), T(1.0), T(1.0) };
+            const T ior2[3] = { T(m.ior[0]), T(m.ior[1]), T(m.ior[2]) };
+            T etai0 = entering ? ior1[0] : ior2[0], etat0 = entering ? ior2[0] : ior1[0];
+            if (!entering) cosi = std::abs(cosi);
+            T eta = etai0 / etat0;
+            T sini = std::sqrt(std::max(T(0.0), T(1.0) - cosi * cosi));
+            T sint = eta * sini;
+            T cost = std::sqrt(std::max(T(0.0), T(1.0) - sint * sint));
+            T R[3];
+            for (int c = 0; c < 3; ++c)
+            {
+                T rs = (ior1[c] * cosi - ior2[c] * cost) / (ior1[c] * cosi + ior2[c] * cost);
+                T rp = (ior2[c] * cosi - ior1[c] * cost) / (ior2[c] * cosi + ior1[c] * cost);
+                R[c] = (rs * rs + rp * rp) / T(2.0);
+            }
+            if (sint >= T(1.0)) R[0] = R[1] = R[2] = T(1.0);
+            // refract(wo, N, eta) (vector.inl:695-707) and reflect(wo, N)
+            T rc = dot(N, wo);
+            T rsin = std::max(T(0.0), T(1.0) - rc * rc);
+            T rsint = eta * eta * rsin;
+            vec<T> refracted = rsint >= T(1.0) ? vec<T>{ 0, 0, 0 } : eta * -wo + (eta * rc - std::sqrt(T(1.0) - rsint)) * N;
+            vec<T> reflected = T(2.0) * dot(N, wo) * N - wo;
+            T u = T(gen.next());
+            T val[3];
+            if (u < R[0])
+            {
+                refl = reflected;
+                brdf_pdf = R[0];
+                for (int c = 0; c < 3; ++c) val[c] = R[c] * (T(m.color2[c]) * T(m.scale2));
+            }
+            else
+            {
+                refl = normalize(refracted);
+                brdf_pdf = T(1.0) - R[0];
+                for (int c = 0; c < 3; ++c) val[c] = (T(1.0) - R[c]) * (T(m.color[c]) * T(m.scale));
+            }
+            T dn = dot(N, refl);
+            src = { val[0] / dn, val[1] / dn, val[2] / dn };
+        }
+        else if (!emission)
         {
             vec<T> n = faceforward(sn, view_dir, gn);
             vec<T> w = n;
@@ -305,7 +382,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                                                           : T(1.0);
         if (active && emission) intensity = intensity + (throughput * mis) * src;
         active = active && !emission && !zero_pdf;
-        rec.kind = emission ? kEmission : (zero_pdf ? kEnd : kMatte);
+        rec.kind = emission ? kEmission : (zero_pdf ? kEnd : (specular ? kSpecular : kMatte));
         rec.mis = mis;
         rec.escale = T(m.scale);
 
@@ -344,7 +421,8 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             T shadow_tmax = (p.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - eps - eps : dist - eps;
             hit_t<T> sh = traverse(s, isect + L * eps, L, eps, shadow_tmax, true, cnt.boxes, cnt.tris);
             ++cnt.shadow;
-            if (!emission)
+            // a specular surface's shade() is 0 (brdf.h:306-315, 374-383): no contribution
+            if (!emission && !specular)
             {
                 vec<T> n2 = faceforward(sn, view_dir, gn);
                 T bpdf = dot(n2, L) * inv_pi;
@@ -370,6 +448,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             }
         }
 
+        rec.spec = src * (dot(n, refl) / brdf_pdf);
         throughput = throughput * (src * (dot(n, refl) / brdf_pdf));
         if (zero_pdf) throughput = { 0, 0, 0 };
         rec.sigma = T(m.scale) * inv_pi * (dot(n, refl) / brdf_pdf);
@@ -391,7 +470,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         if (!active) break;   // emission / zero pdf: nothing further reaches the image
         ori = isect + refl * eps;
         dir = refl;
-        last_specular = false;
+        last_specular = specular;
     }
     return intensity;
 }
@@ -492,6 +571,22 @@ void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats,
         else if (r.kind == kEnd)
         {
             tbar = { 0, 0, 0 };
+        }
+        else if (r.kind == kSpecular)
+        {
+            // thr' = thr * spec (then / rr): a fixed factor, nothing to differentiate
+            vec<T> ub = tbar;
+            if (r.rr > T(0))
+            {
+                vec<T> uu = r.thr * r.spec;
+                T pr = r.rr;
+                ub = tbar / pr;
+                T pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (pr * pr);
+                if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
+                else if (uu.y >= uu.z) ub.y += pb;
+                else ub.z += pb;
+            }
+            tbar = ub * r.spec;
         }
         else if (r.kind == kEmission)
         {

@@ -109,6 +109,19 @@ def pathtrace_case(ref, samples):
             "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
 
 
+def specular_pathtrace_case(ref, samples):
+    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(64, 48, 4, num_bounces=8, epsilon=1e-4, frame_id=5)
+    img = ref.pathtrace(tris, mats, lights, cam, params)
+    samples["pt_specular_image"] = img
+    return {"scene": {"kind": "specular_box", "n_blobs": 8, "subdiv": 8, "seed": 1},
+            "camera": "scenes.box_camera()", "params": {"width": 64, "height": 48, "spp": 4, "num_bounces": 8,
+                                                        "epsilon": 1e-4, "frame_id": 5, "flags": 0},
+            "triangles_sha256": digest(tris), "materials_sha256": digest(mats),
+            "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
+
+
 def main():
     if not Reference.available():
         raise SystemExit("oracle/_ref/libvsnray_ref.so is missing: build it where the visionaray "
@@ -119,7 +132,8 @@ def main():
            "sample_stride": SAMPLE_STRIDE,
            "soup": soup_case(ref, samples),
            "heightfield": heightfield_case(ref, samples),
-           "pathtrace": pathtrace_case(ref, samples)}
+           "pathtrace": pathtrace_case(ref, samples),
+           "pathtrace_specular": specular_pathtrace_case(ref, samples)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "golden_samples.npz"), **samples)

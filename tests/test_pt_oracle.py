@@ -47,6 +47,43 @@ def test_golden_image(oracle, small_box, golden):
         assert (np.abs(img - ref).max(axis=2) == 0).mean() > 0.5
 
 
+def test_golden_specular_image(oracle, golden):
+    """Mirror (conductor Fresnel) and glass (dielectric Fresnel, refraction, total
+    internal reflection) blobs in the box, against the reference kernel's image."""
+    meta, samples = golden
+    g = meta["pathtrace_specular"]
+    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+    assert digest(tris) == g["triangles_sha256"] and digest(mats) == g["materials_sha256"]
+    pr = g["params"]
+    params = scenes.pt_params(pr["width"], pr["height"], pr["spp"], num_bounces=pr["num_bounces"],
+                              epsilon=pr["epsilon"], frame_id=pr["frame_id"])
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, scenes.box_camera(), params,
+                              mode=Oracle.PT_FLOAT)
+    img = img.astype(np.float32)
+    ref = samples["pt_specular_image"]
+    if Reference.available():
+        assert np.array_equal(img, ref)
+    else:
+        assert np.allclose(img.reshape(-1, 4).mean(0), ref.reshape(-1, 4).mean(0), rtol=0.03)
+        assert (np.abs(img - ref).max(axis=2) == 0).mean() > 0.5
+
+
+@pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+@pytest.mark.parametrize("frame,spp,bounces", [(0, 2, 8), (5, 3, 3), (9, 1, 1)])
+def test_fp32_oracle_is_the_reference_kernel_specular(oracle, frame, spp, bounces):
+    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(40, 24, spp, num_bounces=bounces, frame_id=frame)
+    ref = Reference().pathtrace(tris, mats, lights, cam, params)
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT)
+    assert np.array_equal(img.astype(np.float32), ref)
+    # the specular blobs change the image: the same geometry all matte differs
+    _, matte, _ = scenes.box_scene(n_blobs=8, subdiv=8, seed=1)
+    plain, _ = oracle.pathtrace(oracle.build_sah(tris), tris, matte, lights, cam, params, mode=Oracle.PT_FLOAT)
+    changed = (np.abs(plain.astype(np.float32) - ref).max(axis=2) > 0).mean()
+    assert changed > (0.05 if bounces > 1 else 0.0), changed
+
+
 @pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
 @pytest.mark.parametrize("frame,spp,bounces", [(0, 2, 8), (5, 3, 3), (9, 1, 1)])
 def test_fp32_oracle_is_the_reference_kernel(oracle, small_box, frame, spp, bounces):
@@ -94,3 +131,45 @@ def test_shadow_range_fix_makes_fp32_and_fp64_agree(oracle, small_box):
     assert g32[..., :3].mean() > 1.1 * g64[..., :3].mean()
     assert f64[..., :3].mean() > 2.0 * g64[..., :3].mean()
     assert cnt[0] > 48 * 32 * 4 and cnt[1] > 0
+
+
+def test_oracle_adjoint_through_specular_vertices(oracle):
+    """The FP64 host adjoint on a box with mirror and glass blobs against central
+    differences of the FP64 forward pass at common random numbers (roulette off,
+    shadow range fixed, so the image is smooth in the albedos): specular vertices pass
+    the adjoint through their fixed factor."""
+    from visionaray_gb300 import inverse
+    tris, mats, lights = scenes.specular_box_scene(n_blobs=3, subdiv=4, seed=1)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(32, 24, 2, num_bounces=6, frame_id=7, flags=inverse.FLAGS)
+    tree = oracle.build_sah(tris)
+    albedo = np.ascontiguousarray(mats["color"], np.float32)
+    emission = albedo.copy()
+    adj = np.random.default_rng(0).normal(size=(24, 32, 4))
+    adj[..., 3] = 0
+    ga, ge, img = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, albedo, emission, adj)
+    _, _, again = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, albedo, emission, adj)
+    assert np.array_equal(img, again)
+
+    def loss(a, e):
+        return float((oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, a, e, adj)[2] * adj).sum())
+
+    matte = mats["kind"] == 0
+    cand = np.argsort(-np.abs(ga[matte]).ravel())[:6]
+    slots = np.flatnonzero(matte)
+    cases = [("a", int(slots[i // 3]), int(i % 3)) for i in cand] + [("e", 12, 0)]
+    for kind, slot, c in cases:
+        base = albedo if kind == "a" else emission
+        h = np.float32(1e-2 * max(1.0, float(base[slot, c])))
+        plus, minus = base.copy(), base.copy()
+        plus[slot, c] += h
+        minus[slot, c] -= h
+        step = float(plus[slot, c]) - float(minus[slot, c])
+        if kind == "a":
+            fd = (loss(plus, emission) - loss(minus, emission)) / step
+        else:
+            fd = (loss(albedo, plus) - loss(albedo, minus)) / step
+        g = float((ga if kind == "a" else ge)[slot, c])
+        # the image is a polynomial in the albedos (a slot met twice on a path enters
+        # squared): central differences carry an O(h^2) term, 1e-4 relative bounds it
+        assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(ga).max(), (kind, slot, c, g, fd)

@@ -205,6 +205,7 @@ extern "C" int64_t gbrt_obj_materials(const char* path, gbrt_material* out, uint
         for (size_t k = 0; k < slots && k < capacity; ++k)
         {
             mtl m = d.slots.empty() ? mtl{} : d.slots[k];
+            out[k] = gbrt_material{};
             bool emits = m.ke[0] > 0.0f || m.ke[1] > 0.0f || m.ke[2] > 0.0f;
             out[k].kind = emits ? GBRT_MATERIAL_EMISSIVE : GBRT_MATERIAL_MATTE;
             for (int a = 0; a < 3; ++a) out[k].color[a] = emits ? m.ke[a] : m.kd[a];

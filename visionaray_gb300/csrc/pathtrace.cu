@@ -488,6 +488,22 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
             {
                 tbar = { 0.0f, 0.0f, 0.0f };
             }
+            else if (r.kind == kVertexSpecular)
+            {
+                // thr' = thr * spec (then / rr): a fixed factor, nothing to differentiate
+                v3 ub = tbar;
+                if (r.rr > 0.0f)
+                {
+                    v3 uu = r.thr * r.spec;
+                    float p = r.rr;
+                    ub = tbar / p;
+                    float pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (p * p);
+                    if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
+                    else if (uu.y >= uu.z) ub.y += pb;
+                    else ub.z += pb;
+                }
+                tbar = ub * r.spec;
+            }
             else if (r.kind == kVertexEmission)
             {
                 gbrt_material m = sp.materials[geom];

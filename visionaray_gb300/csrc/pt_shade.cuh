@@ -97,6 +97,7 @@ enum : uint32_t
     kVertexEmission = 1,
     kVertexMatte = 2,
     kVertexEnd = 3,   // matte with a zero pdf: the path stops without contributing
+    kVertexSpecular = 4,   // mirror / glass: next throughput = thr * spec (not differentiated)
 };
 
 struct vertex_rec
@@ -111,6 +112,7 @@ struct vertex_rec
     float kl;         // NEE: lint = emission[lgeom] * kl
     v3 lint;
     float rr;         // Russian roulette normaliser (0: none)
+    v3 spec;          // specular: next throughput = thr * spec (then / rr)
 };
 
 struct vertex_out
@@ -175,15 +177,88 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         geom = 0;
     }
     bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
+    const bool mirror = m.kind == GBRT_MATERIAL_MIRROR, glass = m.kind == GBRT_MATERIAL_GLASS;
+    const bool specular = mirror || glass;
     v3 mcol = { m.color[0], m.color[1], m.color[2] };
-    if (!emission && sp.albedo) mcol = param3(sp.albedo, geom);
+    if (!emission && !specular && sp.albedo) mcol = param3(sp.albedo, geom);
     if (emission && sp.emission) mcol = param3(sp.emission, geom);
     rec.geom = geom;
 
     v3 refl = { 0.0f, 0.0f, 0.0f };
     float brdf_pdf;
     v3 src;
-    if (!emission)
+    if (mirror)
+    {
+        // mirror::sample -> specular_reflection::sample_f(sr.normal, view) (brdf.h:317-340):
+        // wi = reflect(wo, n), pdf 1, conductor Fresnel (fresnel.h:18-35) * cr * kr / |n.wi|
+        const v3 wo = view;
+        refl = sn * (2.0f * dot3(sn, wo)) - wo;
+        brdf_pdf = 1.0f;
+        const float cosi = fabsf(dot3(sn, wo));
+        const float cr[3] = { mcol.x, mcol.y, mcol.z };
+        float f[3];
+        for (int c = 0; c < 3; ++c)
+        {
+            const float eta = m.ior[c], k = m.absorption[c];
+            const float a = eta * eta + k * k;
+            const float rs2 = ((a - 2.0f * eta * cosi) + cosi * cosi) / ((a + 2.0f * eta * cosi) + cosi * cosi);
+            const float rp2 = ((a * cosi * cosi - 2.0f * eta * cosi) + 1.0f) / ((a * cosi * cosi + 2.0f * eta * cosi) + 1.0f);
+            f[c] = ((rs2 + rp2) / 2.0f) * (cr[c] * m.scale);
+        }
+        const float dn = fabsf(dot3(sn, refl));
+        src = { f[0] / dn, f[1] / dn, f[2] / dn };
+    }
+    else if (glass)
+    {
+        // glass::sample -> specular_transmission::sample_f(sr.normal, view) (brdf.h:385-456)
+        const v3 wo = view;
+        float cosi = dot3(sn, wo);
+        cosi = cosi < 1.0f ? cosi : 1.0f;          // clamp(x, -1, 1) = max(-1, min(x, 1))
+        cosi = -1.0f < cosi ? cosi : -1.0f;
+        const bool entering = cosi > 0.0f;
+        const v3 N = entering ? sn : -sn;
+        const float ior1[3] = { 1.0f, 1.0f, 1.0f }, ior2[3] = { m.ior[0], m.ior[1], m.ior[2] };
+        const float etai0 = entering ? ior1[0] : ior2[0], etat0 = entering ? ior2[0] : ior1[0];
+        if (!entering) cosi = fabsf(cosi);
+        const float eta = etai0 / etat0;
+        const float sini = sqrtf(fmaxf(0.0f, 1.0f - cosi * cosi));
+        const float sint = eta * sini;
+        const float cost = sqrtf(fmaxf(0.0f, 1.0f - sint * sint));
+        // fresnel_reflectance(dielectric_tag, ior1, ior2, cosi, cost) (fresnel.h:37-56)
+        float R[3];
+        for (int c = 0; c < 3; ++c)
+        {
+            const float rs = (ior1[c] * cosi - ior2[c] * cost) / (ior1[c] * cosi + ior2[c] * cost);
+            const float rp = (ior2[c] * cosi - ior1[c] * cost) / (ior2[c] * cosi + ior1[c] * cost);
+            R[c] = (rs * rs + rp * rp) / 2.0f;
+        }
+        if (sint >= 1.0f) R[0] = R[1] = R[2] = 1.0f;   // total internal reflection
+        // refract(wo, N, eta) (vector.inl:695-707; not normalised) and reflect(wo, N)
+        const float rc = dot3(N, wo);
+        const float rsin = fmaxf(0.0f, 1.0f - rc * rc);
+        const float rsint = eta * eta * rsin;
+        const v3 refracted = rsint >= 1.0f ? v3{ 0.0f, 0.0f, 0.0f } : (-wo) * eta + N * (eta * rc - sqrtf(1.0f - rsint));
+        const v3 reflected = N * (2.0f * dot3(N, wo)) - wo;
+        const float u = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+        float val[3];
+        if (u < R[0])
+        {
+            refl = reflected;
+            brdf_pdf = R[0];
+            const float cr[3] = { m.color2[0], m.color2[1], m.color2[2] };
+            for (int c = 0; c < 3; ++c) val[c] = R[c] * (cr[c] * m.scale2);
+        }
+        else
+        {
+            refl = normalize3(refracted);
+            brdf_pdf = 1.0f - R[0];
+            const float ct[3] = { mcol.x, mcol.y, mcol.z };
+            for (int c = 0; c < 3; ++c) val[c] = (1.0f - R[c]) * (ct[c] * m.scale);
+        }
+        const float dn = dot3(N, refl);
+        src = { val[0] / dn, val[1] / dn, val[2] / dn };
+    }
+    else if (!emission)
     {
         // matte::sample -> lambertian::sample_f (matte.inl:40-56, brdf.h:50-76)
         v3 nn = faceforward3(sn, view, gn);
@@ -237,9 +312,15 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         rec.kind = kVertexEnd;
         return;
     }
-    rec.kind = kVertexMatte;
+    rec.kind = specular ? kVertexSpecular : kVertexMatte;
     v3 nn = faceforward3(sn, view, gn);
-    if (sp.num_lights > 0)
+    if (sp.num_lights > 0 && specular)
+    {
+        // the reference samples a light here too (three draws) but a specular
+        // surface's shade() is 0, so the next-event contribution is zero
+        st.k += 3;
+    }
+    else if (sp.num_lights > 0)
     {
         // sample_random_light + area_light::sample + sample_surface
         // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
@@ -294,6 +375,7 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         }
     }
     float cosp = dot3(nn, refl) / brdf_pdf;
+    rec.spec = src * cosp;
     st.thr = st.thr * (src * cosp);
     rec.sigma = m.scale * inv_pi * cosp;
     bool terminate = false;
@@ -310,7 +392,11 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         out.cont = true;
         out.next_o = isect + refl * sp.epsilon;
         out.next_d = refl;
-        st.flags &= ~kLastSpecular;
+        // last_specular = inter is a specular reflection or transmission
+        if (specular)
+            st.flags |= kLastSpecular;
+        else
+            st.flags &= ~kLastSpecular;
     }
     (void)tmin;
     (void)tmax;

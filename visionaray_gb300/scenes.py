@@ -104,6 +104,33 @@ def box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
     return tris, mats, lights
 
 
+def specular_box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
+    """box_scene with every third blob a gold-like mirror (conductor Fresnel: ior
+    (0.27, 0.42, 1.35), absorption (3.4, 2.3, 1.8)) and every third, from the third on,
+    clear glass (ior 1.5, transmission and reflection colors 1): the specular materials
+    on closed, noisy surfaces, so paths refract in and out and meet total internal
+    reflection.  Returns (triangles, materials per geom_id, area lights)."""
+    from .types import GLASS, MIRROR
+    tris, mats, lights = box_scene(n_blobs, subdiv, seed, light_y, emission)
+    per = 20 * subdiv * subdiv
+    for b in range(n_blobs):
+        sl = slice(14 + b * per, 14 + (b + 1) * per)
+        if b % 3 == 1:
+            mats["kind"][sl] = MIRROR
+            mats["color"][sl] = (0.95, 0.9, 0.8)
+            mats["scale"][sl] = 1.0
+            mats["ior"][sl] = (0.27, 0.42, 1.35)
+            mats["absorption"][sl] = (3.4, 2.3, 1.8)
+        elif b % 3 == 2:
+            mats["kind"][sl] = GLASS
+            mats["color"][sl] = (1.0, 1.0, 1.0)
+            mats["scale"][sl] = 1.0
+            mats["color2"][sl] = (1.0, 1.0, 1.0)
+            mats["scale2"][sl] = 1.0
+            mats["ior"][sl] = (1.5, 1.5, 1.5)
+    return tris, mats, lights
+
+
 def box_camera(eye=(0.5, 0.5, 0.02), center=(0.5, 0.5, 1.0), up=(0.0, 1.0, 0.0), fovy_degrees=60.0):
     """Camera inside the closed box, near the front wall, looking at the back wall."""
     from .types import CAMERA
