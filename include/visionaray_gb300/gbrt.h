@@ -236,15 +236,19 @@ gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
  * visionaray's generic_material:
  *   matte    (Lambertian, detail/material/matte.inl): cd = color, kd = scale
  *   emissive (detail/material/emissive.inl): ce = color, ls = scale
- *   mirror   (detail/material/mirror.inl, specular_reflection brdf.h:292-357):
+ *   mirror   (detail/material/mirror.inl, specular_reflection brdf.h:293-352):
  *            cr = color, kr = scale, conductor Fresnel with ior and absorption
- *   glass    (detail/material/glass.inl, specular_transmission brdf.h:359-470):
+ *   glass    (detail/material/glass.inl, specular_transmission brdf.h:360-469):
  *            ct = color, kt = scale, cr = color2, kr = scale2, ior
+ *   plastic  (detail/material/plastic.inl, lambertian + blinn brdf.h:26-84, 118-191):
+ *            cd = color, kd = scale, cs = color2, ks = scale2,
+ *            specular_exp = exponent
  * (the path-tracing configurations use matte and emissive).                       */
 #define GBRT_MATERIAL_MATTE    0u
 #define GBRT_MATERIAL_EMISSIVE 1u
 #define GBRT_MATERIAL_MIRROR   2u
 #define GBRT_MATERIAL_GLASS    3u
+#define GBRT_MATERIAL_PLASTIC  4u
 typedef struct gbrt_material
 {
     uint32_t kind;
@@ -254,7 +258,7 @@ typedef struct gbrt_material
     float    absorption[3];
     float    color2[3];
     float    scale2;
-    uint32_t reserved;
+    float    exponent;
 } gbrt_material;
 
 /* area_light<float, basic_triangle<3, float>> (area_light.h, detail/area_light.inl:

@@ -9,7 +9,8 @@
 // triangle (detail/area_light.inl:27-53), mirror (detail/material/mirror.inl,
 // specular_reflection at brdf.h:293-352, conductor Fresnel at fresnel.h:18-35), glass
 // (detail/material/glass.inl, specular_transmission at brdf.h:360-469, dielectric
-// Fresnel at fresnel.h:37-56), sample_random_light (sampling.h:195-213),
+// Fresnel at fresnel.h:37-56), plastic (detail/material/plastic.inl, lambertian and
+// blinn at brdf.h:26-84, 118-191), sample_random_light (sampling.h:195-213),
 // cosine_sample_hemisphere (sampling.h:117-127), power_heuristic (sampling.h:73-79),
 // sample_surface on a triangle (math/detail/triangle.inl:69-83), get_surface /
 // get_normal / get_area (get_surface.h:129-160, get_normal.h:108-113,
@@ -193,6 +194,7 @@ enum : uint32_t
     kMatte = 2,
     kEnd = 3,
     kSpecular = 4,
+    kPlastic = 5,
 };
 
 template <typename T>
@@ -202,7 +204,8 @@ struct vrec
     vec<T> thr{ 0, 0, 0 };
     T sigma = 0, mis = 0, escale = 0, kfac = 0, w = 0, x = 0, b0 = 0, kl = 0, rr = 0;
     vec<T> lint{ 0, 0, 0 };
-    vec<T> spec{ 0, 0, 0 };   // a specular vertex's throughput factor src * cos / pdf
+    vec<T> spec{ 0, 0, 0 };   // a specular or plastic vertex's throughput factor src * cos / pdf
+    vec<T> gnee{ 0, 0, 0 };   // plastic next-event contribution = w * thr * gnee * lint
 };
 
 // pathtracing::kernel::operator() (detail/pathtracing.inl:42-233) for one camera ray.
@@ -210,6 +213,42 @@ template <typename T>
 inline T trig_cos(T x, bool via_double) { return via_double ? T(std::cos(double(x))) : std::cos(x); }
 template <typename T>
 inline T trig_sin(T x, bool via_double) { return via_double ? T(std::sin(double(x))) : std::sin(x); }
+
+template <typename T>
+inline T trig_pow(T x, T y, bool via_double) { return via_double ? T(std::pow(double(x), double(y))) : std::pow(x, y); }
+
+// blinn::f (brdf.h:128-141) in T
+template <typename T>
+vec<T> blinn_f(gbrt_material const& m, vec<T> n, vec<T> wo, vec<T> wi, bool trig_double)
+{
+    const T pi = T(3.14159265358979323846264338328e+00);
+    vec<T> h = normalize(wo + wi);
+    T hdotn = std::max(T(0.0), dot(h, n));
+    T sat = std::max(T(0.0), std::min(dot(wi, h), T(1.0)));
+    T fr = trig_pow(T(1.0) - sat, T(5.0), trig_double);
+    T nfactor = (T(m.exponent) + T(2.0)) / (T(8.0) * pi);
+    T lobe = trig_pow(hdotn, T(m.exponent), trig_double);
+    T out[3];
+    for (int c = 0; c < 3; ++c)
+    {
+        T spec = T(m.color2[c]) * T(m.scale2);
+        T schlick = spec + (T(1.0) - spec) * fr;
+        out[c] = (schlick * nfactor) * lobe;
+    }
+    return { out[0], out[1], out[2] };
+}
+
+// blinn::pdf (brdf.h:182-190) in T
+template <typename T>
+T blinn_pdf(gbrt_material const& m, vec<T> n, vec<T> wo, vec<T> wi, bool trig_double)
+{
+    const T pi = T(3.14159265358979323846264338328e+00);
+    vec<T> h = normalize(wi + wo);
+    T costheta = dot(n, h);
+    T vdoth = dot(wo, h);
+    return ((T(m.exponent) + T(1.0)) * trig_pow(costheta, T(m.exponent), trig_double)) /
+           (T(2.0) * pi * T(4.0) * vdoth);
+}
 
 template <typename T>
 vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
@@ -254,8 +293,10 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         vec<T> mcol = { T(m.color[0]), T(m.color[1]), T(m.color[2]) };
         bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
         const bool mirror = m.kind == GBRT_MATERIAL_MIRROR, glass = m.kind == GBRT_MATERIAL_GLASS;
+        const bool plastic = m.kind == GBRT_MATERIAL_PLASTIC;
         const bool specular = mirror || glass;
-        if (!emission && !specular && ext.albedo) mcol = load<T>(ext.albedo + 3 * geom);
+        bool glossy = false;
+        if (!emission && !specular && !plastic && ext.albedo) mcol = load<T>(ext.albedo + 3 * geom);
         if (emission && ext.emission) mcol = load<T>(ext.emission + 3 * geom);
         rec.geom = geom;
 
@@ -333,6 +374,61 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             T dn = dot(N, refl);
             src = { val[0] / dn, val[1] / dn, val[2] / dn };
         }
+        else if (plastic)
+        {
+            // plastic::sample (detail/material/plastic.inl:42-95): the lobe drawn by the
+            // mean reflectances, whose own pdf is returned (no selection probability)
+            T prob_diff = ((T(m.color[0]) + T(m.color[1])) + T(m.color[2])) / T(3.0) * T(m.scale);
+            T prob_spec = ((T(m.color2[0]) + T(m.color2[1])) + T(m.color2[2])) / T(3.0) * T(m.scale2);
+            bool all_zero = prob_diff == T(0.0) && prob_spec == T(0.0);
+            prob_diff = all_zero ? T(0.5) : prob_diff;
+            prob_spec = all_zero ? T(0.5) : prob_spec;
+            prob_diff = prob_diff / (prob_diff + prob_spec);
+            T u = T(gen.next());
+            vec<T> n = faceforward(sn, view_dir, gn);
+            vec<T> w = n;
+            vec<T> v = std::abs(w.x) > std::abs(w.y) ? normalize(vec<T>{ -w.z, T(0), w.x })
+                                                     : normalize(vec<T>{ T(0), w.z, -w.y });
+            vec<T> uu = cross(v, w);
+            if (u < prob_diff)
+            {
+                T u1, u2;
+                if (ext.draws_in_order)
+                {
+                    u1 = T(gen.next());
+                    u2 = T(gen.next());
+                }
+                else
+                {
+                    u2 = T(gen.next());
+                    u1 = T(gen.next());
+                }
+                T r = std::sqrt(u1);
+                T theta = two_pi * u2;
+                vec<T> sp = { r * trig_cos(theta, trig_double), r * trig_sin(theta, trig_double),
+                              std::sqrt(T(1.0) - u1) };
+                refl = normalize(uu * sp.x + v * sp.y + w * sp.z);
+                brdf_pdf = dot(n, refl) * inv_pi;
+                src = (mcol * T(m.scale)) * inv_pi;
+            }
+            else
+            {
+                // blinn::sample_f (brdf.h:143-180)
+                T u1 = T(gen.next());
+                T u2 = T(gen.next());
+                T costheta = trig_pow(u1, T(1.0) / (T(m.exponent) + T(1.0)), trig_double);
+                T sintheta = std::sqrt(std::max(T(0.0), T(1.0) - costheta * costheta));
+                T phi = u2 * two_pi;
+                vec<T> h = normalize(sintheta * trig_cos(phi, trig_double) * uu +
+                                     sintheta * trig_sin(phi, trig_double) * v + costheta * w);
+                refl = T(2.0) * dot(h, view_dir) * h - view_dir;
+                T vdoth = dot(view_dir, h);
+                brdf_pdf = ((T(m.exponent) + T(1.0)) * trig_pow(costheta, T(m.exponent), trig_double)) /
+                           (T(2.0) * pi * T(4.0) * vdoth);
+                src = blinn_f(m, n, view_dir, refl, trig_double);
+                glossy = true;
+            }
+        }
         else if (!emission)
         {
             vec<T> n = faceforward(sn, view_dir, gn);
@@ -382,7 +478,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                                                           : T(1.0);
         if (active && emission) intensity = intensity + (throughput * mis) * src;
         active = active && !emission && !zero_pdf;
-        rec.kind = emission ? kEmission : (zero_pdf ? kEnd : (specular ? kSpecular : kMatte));
+        rec.kind = emission ? kEmission : (zero_pdf ? kEnd : (specular ? kSpecular : (plastic ? kPlastic : kMatte)));
         rec.mis = mis;
         rec.escale = T(m.scale);
 
@@ -425,12 +521,16 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
             if (!emission && !specular)
             {
                 vec<T> n2 = faceforward(sn, view_dir, gn);
-                T bpdf = dot(n2, L) * inv_pi;
+                // surf.pdf(view, L, inter): the lobe the sample chose (plastic.inl:97-110)
+                T bpdf = glossy ? blinn_pdf(m, n2, view_dir, L, trig_double) : dot(n2, L) * inv_pi;
+                T b0 = bpdf;
                 T prob = max_element(throughput);
                 bpdf = bpdf * prob;
                 T ndotl = std::max(T(0.0), dot(n2, L));
                 vec<T> cd = (mcol * T(m.scale)) * inv_pi;
-                vec<T> shade = ((cd * pi) * lint) * ndotl;
+                // plastic::shade (plastic.inl:20-39): (diffuse + Blinn) * pi * intensity * n.l
+                vec<T> brdf = plastic ? cd + blinn_f(m, n2, view_dir, L, trig_double) : cd;
+                vec<T> shade = ((brdf * pi) * lint) * ndotl;
                 vec<T> src2 = (shade * inv_pi) / ldotn;
                 T mis2 = power_heuristic(lpdf / T(float(nl)), bpdf);
                 if (active && !sh.hit && ldotn > T(0.0) && ldotln > T(0.0))
@@ -442,8 +542,9 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                     rec.lint = lint;
                     rec.w = mis2;
                     rec.x = lpdf / T(float(nl));
-                    rec.b0 = dot(n2, L) * inv_pi;
+                    rec.b0 = b0;
                     rec.kfac = T(m.scale) * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * T(float(nl));
+                    rec.gnee = brdf * (pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * T(float(nl)));
                 }
             }
         }
@@ -572,7 +673,7 @@ void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats,
         {
             tbar = { 0, 0, 0 };
         }
-        else if (r.kind == kSpecular)
+        else if (r.kind == kSpecular || r.kind == kPlastic)
         {
             // thr' = thr * spec (then / rr): a fixed factor, nothing to differentiate
             vec<T> ub = tbar;
@@ -586,7 +687,28 @@ void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats,
                 else if (uu.y >= uu.z) ub.y += pb;
                 else ub.z += pb;
             }
-            tbar = ub * r.spec;
+            vec<T> tb = ub * r.spec;
+            if (r.kind == kPlastic && r.nee)
+            {
+                // N = w * thr * gnee * lint, w = x^2 / (x^2 + y^2), y = b0 * max(thr)
+                vec<T> f = r.gnee * r.lint;
+                tb = tb + adj * f * r.w;
+                T wbar = adj.x * r.thr.x * f.x + adj.y * r.thr.y * f.y + adj.z * r.thr.z * f.z;
+                T yv = r.b0 * max_element(r.thr);
+                T den = r.x * r.x + yv * yv;
+                T g = wbar * (-T(2) * r.x * r.x * yv / (den * den)) * r.b0;
+                if (r.thr.x >= r.thr.y && r.thr.x >= r.thr.z) tb.x += g;
+                else if (r.thr.y >= r.thr.z) tb.y += g;
+                else tb.z += g;
+                if (r.lgeom != 0xFFFFFFFFu)
+                {
+                    vec<T> lb = adj * r.thr * r.gnee * (r.w * r.kl);
+                    ge[3 * r.lgeom + 0] += double(lb.x);
+                    ge[3 * r.lgeom + 1] += double(lb.y);
+                    ge[3 * r.lgeom + 2] += double(lb.z);
+                }
+            }
+            tbar = tb;
         }
         else if (r.kind == kEmission)
         {

@@ -252,7 +252,7 @@ void ref_trace_instances(uint32_t num_meshes, const gbrt_triangle* const* mesh_t
 }
 
 // visionaray's pathtracing::kernel (detail/pathtracing.inl:42-233) over a binned-SAH
-// index_bvh, generic_material<matte, emissive, mirror, glass> per geom_id and triangle area lights,
+// index_bvh, generic_material<matte, emissive, mirror, glass, plastic> per geom_id and triangle area lights,
 // driven per (pixel, sample) by the gbrt_rng.h stream: the jittered primary ray
 // (sched_common.h:209-233, jitter x drawn before y) through visionaray's own
 // pinhole_camera, samples averaged and blended into accum as sample_pixel_impl does
@@ -261,7 +261,7 @@ void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* m
                    const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam, const gbrt_pt_params* p,
                    float* accum, int nthreads)
 {
-    using mat_t = generic_material<matte<float>, emissive<float>, mirror<float>, glass<float>>;
+    using mat_t = generic_material<matte<float>, emissive<float>, mirror<float>, glass<float>, plastic<float>>;
     using light_t = area_light<float, triangle_t>;
     auto prims = to_prims(tris, n);
     binned_sah_builder builder;
@@ -297,6 +297,18 @@ void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* m
             g.kr() = mats[i].scale2;
             g.ior() = from_rgb(vec3(mats[i].ior[0], mats[i].ior[1], mats[i].ior[2]));
             materials[i] = g;
+        }
+        else if (mats[i].kind == GBRT_MATERIAL_PLASTIC)
+        {
+            plastic<float> pl;
+            pl.ca() = from_rgb(vec3(0.0f));
+            pl.ka() = 0.0f;
+            pl.cd() = from_rgb(c);
+            pl.kd() = mats[i].scale;
+            pl.cs() = from_rgb(vec3(mats[i].color2[0], mats[i].color2[1], mats[i].color2[2]));
+            pl.ks() = mats[i].scale2;
+            pl.specular_exp() = mats[i].exponent;
+            materials[i] = pl;
         }
         else
         {

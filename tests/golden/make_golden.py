@@ -109,15 +109,22 @@ def pathtrace_case(ref, samples):
             "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
 
 
-def specular_pathtrace_case(ref, samples):
-    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+def material_pathtrace_case(ref, samples, kind, frame_id):
+    """scenes.specular_box_scene (mirror, glass) or scenes.glossy_box_scene (plus
+    plastic) at 64 x 48, 4 spp."""
+    if kind == "specular_box":
+        tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+        scene = {"kind": kind, "n_blobs": 8, "subdiv": 8, "seed": 1}
+    else:
+        tris, mats, lights = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+        scene = {"kind": kind, "n_blobs": 10, "subdiv": 8, "seed": 1}
     cam = scenes.box_camera()
-    params = scenes.pt_params(64, 48, 4, num_bounces=8, epsilon=1e-4, frame_id=5)
+    params = scenes.pt_params(64, 48, 4, num_bounces=8, epsilon=1e-4, frame_id=frame_id)
     img = ref.pathtrace(tris, mats, lights, cam, params)
-    samples["pt_specular_image"] = img
-    return {"scene": {"kind": "specular_box", "n_blobs": 8, "subdiv": 8, "seed": 1},
+    samples["pt_%s_image" % kind.split("_")[0]] = img
+    return {"scene": scene,
             "camera": "scenes.box_camera()", "params": {"width": 64, "height": 48, "spp": 4, "num_bounces": 8,
-                                                        "epsilon": 1e-4, "frame_id": 5, "flags": 0},
+                                                        "epsilon": 1e-4, "frame_id": frame_id, "flags": 0},
             "triangles_sha256": digest(tris), "materials_sha256": digest(mats),
             "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
 
@@ -133,7 +140,8 @@ def main():
            "soup": soup_case(ref, samples),
            "heightfield": heightfield_case(ref, samples),
            "pathtrace": pathtrace_case(ref, samples),
-           "pathtrace_specular": specular_pathtrace_case(ref, samples)}
+           "pathtrace_specular": material_pathtrace_case(ref, samples, "specular_box", 5),
+           "pathtrace_glossy": material_pathtrace_case(ref, samples, "glossy_box", 6)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "golden_samples.npz"), **samples)

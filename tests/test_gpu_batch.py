@@ -177,20 +177,21 @@ def test_batch_autotune_picks_a_clean_shape(batch_setup, plain):
         assert batch.image(images, s, params).cpu().numpy().tobytes() == plain[s].tobytes()
 
 
-def test_batch_specular_materials_bit_identical():
-    """A shared material table with matte, mirror and glass slots (geom_id = prim_id
-    mod 3): batched images equal the per-scene frames bit for bit."""
-    from visionaray_gb300.types import GLASS, MATERIAL, MIRROR
+def test_batch_materials_bit_identical():
+    """A shared material table with matte, mirror, glass and plastic slots (geom_id =
+    prim_id mod 4): batched images equal the per-scene frames bit for bit."""
+    from visionaray_gb300.types import GLASS, MATERIAL, MIRROR, PLASTIC
     counts = [900, 3, 2500, 0, 60]
     tris, offsets, cams, params, _ = make_batch_inputs(counts, seed=9)
-    tris["geom_id"] = tris["prim_id"] % 3
-    mats = np.zeros(3, MATERIAL)
-    mats["kind"] = (0, MIRROR, GLASS)
-    mats["color"] = ((0.7, 0.6, 0.5), (0.9, 0.9, 0.8), (1.0, 1.0, 1.0))
+    tris["geom_id"] = tris["prim_id"] % 4
+    mats = np.zeros(4, MATERIAL)
+    mats["kind"] = (0, MIRROR, GLASS, PLASTIC)
+    mats["color"] = ((0.7, 0.6, 0.5), (0.9, 0.9, 0.8), (1.0, 1.0, 1.0), (0.2, 0.5, 0.7))
     mats["scale"] = 1.0
-    mats["ior"] = ((1.0, 1.0, 1.0), (0.27, 0.42, 1.35), (1.5, 1.5, 1.5))
+    mats["ior"] = ((1.0, 1.0, 1.0), (0.27, 0.42, 1.35), (1.5, 1.5, 1.5), (1.0, 1.0, 1.0))
     mats["absorption"][1] = (3.4, 2.3, 1.8)
     mats["color2"][2], mats["scale2"][2] = (1.0, 1.0, 1.0), 1.0
+    mats["color2"][3], mats["scale2"][3], mats["exponent"][3] = (0.5, 0.5, 0.5), 1.0, 24.0
     params["num_bounces"] = 6
     d_tris = vg.as_device_bytes(tris)
     batch = vg.Batch(offsets)

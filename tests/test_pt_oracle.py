@@ -47,12 +47,21 @@ def test_golden_image(oracle, small_box, golden):
         assert (np.abs(img - ref).max(axis=2) == 0).mean() > 0.5
 
 
-def test_golden_specular_image(oracle, golden):
-    """Mirror (conductor Fresnel) and glass (dielectric Fresnel, refraction, total
-    internal reflection) blobs in the box, against the reference kernel's image."""
+MATERIAL_SCENES = {
+    # mirror (conductor Fresnel) and glass (dielectric Fresnel, refraction, total
+    # internal reflection) blobs
+    "specular": lambda: scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1),
+    # plus plastic blobs and plastic walls (lobe choice, Blinn sampling and glossy NEE)
+    "glossy": lambda: scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MATERIAL_SCENES))
+def test_golden_material_images(oracle, golden, name):
+    """The material scenes against the reference kernel's images."""
     meta, samples = golden
-    g = meta["pathtrace_specular"]
-    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+    g = meta["pathtrace_" + name]
+    tris, mats, lights = MATERIAL_SCENES[name]()
     assert digest(tris) == g["triangles_sha256"] and digest(mats) == g["materials_sha256"]
     pr = g["params"]
     params = scenes.pt_params(pr["width"], pr["height"], pr["spp"], num_bounces=pr["num_bounces"],
@@ -60,7 +69,7 @@ def test_golden_specular_image(oracle, golden):
     img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, scenes.box_camera(), params,
                               mode=Oracle.PT_FLOAT)
     img = img.astype(np.float32)
-    ref = samples["pt_specular_image"]
+    ref = samples["pt_%s_image" % name]
     if Reference.available():
         assert np.array_equal(img, ref)
     else:
@@ -69,16 +78,17 @@ def test_golden_specular_image(oracle, golden):
 
 
 @pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+@pytest.mark.parametrize("name", sorted(MATERIAL_SCENES))
 @pytest.mark.parametrize("frame,spp,bounces", [(0, 2, 8), (5, 3, 3), (9, 1, 1)])
-def test_fp32_oracle_is_the_reference_kernel_specular(oracle, frame, spp, bounces):
-    tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
+def test_fp32_oracle_is_the_reference_kernel_materials(oracle, name, frame, spp, bounces):
+    tris, mats, lights = MATERIAL_SCENES[name]()
     cam = scenes.box_camera()
     params = scenes.pt_params(40, 24, spp, num_bounces=bounces, frame_id=frame)
     ref = Reference().pathtrace(tris, mats, lights, cam, params)
     img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT)
     assert np.array_equal(img.astype(np.float32), ref)
-    # the specular blobs change the image: the same geometry all matte differs
-    _, matte, _ = scenes.box_scene(n_blobs=8, subdiv=8, seed=1)
+    # the materials change the image: the same geometry all matte differs
+    _, matte, _ = scenes.box_scene(n_blobs=(len(tris) - 14) // (20 * 8 * 8), subdiv=8, seed=1)
     plain, _ = oracle.pathtrace(oracle.build_sah(tris), tris, matte, lights, cam, params, mode=Oracle.PT_FLOAT)
     changed = (np.abs(plain.astype(np.float32) - ref).max(axis=2) > 0).mean()
     assert changed > (0.05 if bounces > 1 else 0.0), changed
@@ -134,12 +144,13 @@ def test_shadow_range_fix_makes_fp32_and_fp64_agree(oracle, small_box):
 
 
 def test_oracle_adjoint_through_specular_vertices(oracle):
-    """The FP64 host adjoint on a box with mirror and glass blobs against central
-    differences of the FP64 forward pass at common random numbers (roulette off,
-    shadow range fixed, so the image is smooth in the albedos): specular vertices pass
-    the adjoint through their fixed factor."""
+    """The FP64 host adjoint on a box with mirror, glass and plastic blobs and plastic
+    walls against central differences of the FP64 forward pass at common random
+    numbers (roulette off, shadow range fixed, so the image is smooth in the albedos):
+    specular and plastic vertices pass the adjoint through their fixed factor, and a
+    plastic vertex's next-event term through its MIS weight and the light's emission."""
     from visionaray_gb300 import inverse
-    tris, mats, lights = scenes.specular_box_scene(n_blobs=3, subdiv=4, seed=1)
+    tris, mats, lights = scenes.glossy_box_scene(n_blobs=5, subdiv=4, seed=1)
     cam = scenes.box_camera()
     params = scenes.pt_params(32, 24, 2, num_bounces=6, frame_id=7, flags=inverse.FLAGS)
     tree = oracle.build_sah(tris)

@@ -33,6 +33,7 @@ struct gbrt_pt_scene
     uint32_t num_materials = 0;
     float4* lights = nullptr;   // 4 float4 per light: v1, e1, e2, intensity (cl * kl)
     uint32_t num_lights = 0;
+    bool extended = false;      // some material is a mirror, glass or plastic
 };
 
 namespace gbrt {
@@ -47,6 +48,9 @@ constexpr int kPtMinBlocks = 12;
 // (64 warps, 32 registers; the vertex records live in local memory anyway): backward
 // 15.4 -> 13.0 ms per inverse-rendering step (8 blocks 13.4, 12 blocks 14.3).
 constexpr int kAdjointMinBlocks = 16;
+// The shading kernel: 8 resident blocks (32 warps, at most 64 registers), the occupancy
+// it has without the out-of-line material samplers' call overhead.
+constexpr int kShadeMinBlocks = 8;
 
 struct frame_buffers
 {
@@ -185,7 +189,7 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend_sorted(frame_b
 }
 
 // One bounce for every live path of the queue.
-__global__ void __launch_bounds__(kBlock) pt_shade(frame_buffers fb, int q, shade_params sp,
+__global__ void __launch_bounds__(kBlock, kShadeMinBlocks) pt_shade(frame_buffers fb, int q, shade_params sp,
                                                    uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
@@ -414,6 +418,35 @@ __device__ __forceinline__ void warp_add3(float* __restrict__ base, uint32_t key
     }
 }
 
+// Adjoint of thr' = u / p, p = max(u), the Russian-roulette normaliser with the
+// decision held fixed: d/du of tbar . u / p.
+__device__ __forceinline__ v3 roulette_adjoint(v3 tbar, v3 u, float p)
+{
+    v3 ub = tbar / p;
+    float pb = -(tbar.x * u.x + tbar.y * u.y + tbar.z * u.z) / (p * p);
+    if (u.x >= u.y && u.x >= u.z) ub.x += pb;
+    else if (u.y >= u.z) ub.y += pb;
+    else ub.z += pb;
+    return ub;
+}
+
+// Adjoint w.r.t. the throughput of a next-event contribution N = w * thr * f with
+// w = x^2 / (x^2 + y^2), y = b0 * max(thr) (the MIS weight's BSDF pdf scaled by the
+// throughput, pathtracing.inl:180-182): adds dN/dthr . adj to tb.
+__device__ __forceinline__ v3 nee_throughput_adjoint(vertex_rec const& r, v3 adj, v3 f, v3 tb)
+{
+    tb = tb + adj * f * r.w;
+    float wbar = adj.x * r.thr.x * f.x + adj.y * r.thr.y * f.y + adj.z * r.thr.z * f.z;
+    float yv = r.b0 * max_elem(r.thr);
+    float den = r.x * r.x + yv * yv;
+    float dwdy = -2.0f * r.x * r.x * yv / (den * den);
+    float g = wbar * dwdy * r.b0;
+    if (r.thr.x >= r.thr.y && r.thr.x >= r.thr.z) tb.x += g;
+    else if (r.thr.y >= r.thr.z) tb.y += g;
+    else tb.z += g;
+    return tb;
+}
+
 // Path-replay backpropagation (Vicini, Speierer & Jakob 2021): one thread per
 // (pixel, sample) re-traces its path from its random-number counter -- the same
 // shade_vertex, so the replay is bit-identical to the forward frame -- keeping only
@@ -422,7 +455,7 @@ __device__ __forceinline__ void warp_add3(float* __restrict__ base, uint32_t key
 // of every emissive vertex and sampled light.  Memory stays O(pixels): nothing of the
 // forward frame is stored.  Geometry, visibility and the Russian-roulette decision are
 // not differentiated (the roulette's 1 / p weight is).
-template <bool Wide>
+template <bool Wide, bool Extended>
 __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view v, shade_params sp, camera_basis cam, uint32_t width,
                                                      uint32_t height, uint32_t spp, uint32_t num_bounces,
                                                      const float4* __restrict__ img_adj, float* __restrict__ grad_albedo,
@@ -447,7 +480,7 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
         {
             trace_result h = traverse_view<false, Wide>(v, { o.x, o.y, o.z }, { d.x, d.y, d.z }, 0.0f, FLT_MAX, status);
             vertex_out out;
-            shade_vertex(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, status);
+            shade_vertex<Extended>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, status);
             if (out.shadow)
             {
                 trace_result sh = traverse_view<true, Wide>(v, { out.sh_o.x, out.sh_o.y, out.sh_o.z },
@@ -488,66 +521,50 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
             {
                 tbar = { 0.0f, 0.0f, 0.0f };
             }
-            else if (r.kind == kVertexSpecular)
+            else if (r.kind == kVertexSpecular || r.kind == kVertexPlastic)
             {
                 // thr' = thr * spec (then / rr): a fixed factor, nothing to differentiate
-                v3 ub = tbar;
-                if (r.rr > 0.0f)
+                v3 ub = r.rr > 0.0f ? roulette_adjoint(tbar, r.thr * r.f.spec, r.rr) : tbar;
+                v3 tb = ub * r.f.spec;
+                if (r.kind == kVertexPlastic && r.nee)
                 {
-                    v3 uu = r.thr * r.spec;
-                    float p = r.rr;
-                    ub = tbar / p;
-                    float pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (p * p);
-                    if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
-                    else if (uu.y >= uu.z) ub.y += pb;
-                    else ub.z += pb;
+                    // N = w * thr * gnee * lint
+                    tb = nee_throughput_adjoint(r, adj, r.gnee * r.lint, tb);
+                    if (r.lgeom != 0xFFFFFFFFu && r.lgeom < sp.num_materials)
+                    {
+                        lgeom = r.lgeom;
+                        lbar = adj * r.thr * r.gnee * (r.w * r.kl);
+                        add_l = true;
+                    }
                 }
-                tbar = ub * r.spec;
+                tbar = tb;
             }
             else if (r.kind == kVertexEmission)
             {
                 gbrt_material m = sp.materials[geom];
                 v3 e = sp.emission ? param3(sp.emission, geom) : v3{ m.color[0], m.color[1], m.color[2] };
-                ebar = adj * r.thr * (r.mis * r.escale);
+                ebar = adj * r.thr * (r.f.emit.mis * r.f.emit.scale);
                 add_e = sp.emission != nullptr;
-                tbar = adj * e * (r.mis * r.escale);
+                tbar = adj * e * (r.f.emit.mis * r.f.emit.scale);
             }
             else
             {
                 gbrt_material m = sp.materials[geom];
                 v3 a = sp.albedo ? param3(sp.albedo, geom) : v3{ m.color[0], m.color[1], m.color[2] };
                 // throughput update thr' = thr * a * sigma (then / rr)
-                v3 ub = tbar;
-                if (r.rr > 0.0f)
-                {
-                    v3 uu = r.thr * a * r.sigma;
-                    float p = r.rr;
-                    ub = tbar / p;
-                    float pb = -(tbar.x * uu.x + tbar.y * uu.y + tbar.z * uu.z) / (p * p);
-                    if (uu.x >= uu.y && uu.x >= uu.z) ub.x += pb;
-                    else if (uu.y >= uu.z) ub.y += pb;
-                    else ub.z += pb;
-                }
-                abar = ub * r.thr * r.sigma;
-                v3 tb = ub * a * r.sigma;
+                v3 ub = r.rr > 0.0f ? roulette_adjoint(tbar, r.thr * a * r.f.sigma, r.rr) : tbar;
+                abar = ub * r.thr * r.f.sigma;
+                v3 tb = ub * a * r.f.sigma;
                 if (r.nee)
                 {
-                    // N = w * thr * a * lint * kfac, w = x^2 / (x^2 + y^2), y = b0 * max(thr)
-                    v3 f = r.lint * r.kfac;
+                    // N = w * thr * a * gnee * lint
+                    v3 f = r.gnee * r.lint;
                     abar = abar + adj * r.thr * f * r.w;
-                    tb = tb + adj * a * f * r.w;
-                    float wbar = adj.x * r.thr.x * a.x * f.x + adj.y * r.thr.y * a.y * f.y + adj.z * r.thr.z * a.z * f.z;
-                    float yv = r.b0 * max_elem(r.thr);
-                    float den = r.x * r.x + yv * yv;
-                    float dwdy = -2.0f * r.x * r.x * yv / (den * den);
-                    float g = wbar * dwdy * r.b0;
-                    if (r.thr.x >= r.thr.y && r.thr.x >= r.thr.z) tb.x += g;
-                    else if (r.thr.y >= r.thr.z) tb.y += g;
-                    else tb.z += g;
+                    tb = nee_throughput_adjoint(r, adj, a * f, tb);
                     if (r.lgeom != 0xFFFFFFFFu && r.lgeom < sp.num_materials)
                     {
                         lgeom = r.lgeom;
-                        lbar = adj * r.thr * a * (r.w * r.kfac * r.kl);
+                        lbar = adj * r.thr * a * r.gnee * (r.w * r.kl);
                         add_l = true;
                     }
                 }
@@ -635,6 +652,11 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
     sc->device = ctx->device;
     sc->num_materials = num_materials;
     sc->num_lights = num_lights;
+    for (uint32_t k = 0; k < num_materials; ++k)
+    {
+        const uint32_t kind = h_materials[k].kind;
+        sc->extended |= kind == GBRT_MATERIAL_MIRROR || kind == GBRT_MATERIAL_GLASS || kind == GBRT_MATERIAL_PLASTIC;
+    }
     auto cleanup = [&]() {
         cudaFree(sc->materials);
         cudaFree(sc->lights);
@@ -906,14 +928,12 @@ extern "C" gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene 
     const uint32_t blocks = uint32_t((paths + kBlock - 1) / kBlock);
     const bvh_view v = view_of(bvh);
     const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
-    if (wide)
-        pt_adjoint<true><<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
-                                                             reinterpret_cast<const float4*>(d_image_adjoint),
-                                                             d_grad_albedo, d_grad_emission, ctx->d_status);
-    else
-        pt_adjoint<false><<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
-                                                              reinterpret_cast<const float4*>(d_image_adjoint),
-                                                              d_grad_albedo, d_grad_emission, ctx->d_status);
+    // matte / emissive scenes get the replay without the other materials' branches
+    auto kernel = wide ? (scene->extended ? pt_adjoint<true, true> : pt_adjoint<true, false>)
+                       : (scene->extended ? pt_adjoint<false, true> : pt_adjoint<false, false>);
+    kernel<<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
+                                               reinterpret_cast<const float4*>(d_image_adjoint), d_grad_albedo,
+                                               d_grad_emission, ctx->d_status);
     GBRT_LAUNCH_CHECK(ctx, "pt_adjoint");
     return GBRT_OK;
 }

@@ -43,6 +43,41 @@ __device__ __forceinline__ float max_elem(v3 v)
 }
 __device__ __forceinline__ float power_heuristic(float p1, float p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
 __device__ __forceinline__ v3 xyz(float4 a) { return { a.x, a.y, a.z }; }
+// pow, cos and sin evaluated in double and rounded once to float
+__device__ __forceinline__ float pow_d(float x, float y) { return float(pow(double(x), double(y))); }
+__device__ __forceinline__ float cos_d(float x) { return float(cos(double(x))); }
+__device__ __forceinline__ float sin_d(float x) { return float(sin(double(x))); }
+
+// blinn::f (brdf.h:128-141): Schlick's Fresnel term on cs * ks and the normalised
+// Blinn-Phong lobe
+__device__ __forceinline__ v3 blinn_f(gbrt_material const& m, v3 n, v3 wo, v3 wi)
+{
+    const float pi = 3.14159265358979323846264338328e+00f;
+    v3 h = normalize3(wo + wi);
+    float hdotn = fmaxf(0.0f, dot3(h, n));
+    float sat = fmaxf(0.0f, fminf(dot3(wi, h), 1.0f));   // saturate (math/detail/math.h:537-540)
+    float fr = pow_d(1.0f - sat, 5.0f);
+    float nfactor = (m.exponent + 2.0f) / (8.0f * pi);
+    float lobe = pow_d(hdotn, m.exponent);
+    float out[3];
+    for (int c = 0; c < 3; ++c)
+    {
+        float spec = m.color2[c] * m.scale2;
+        float schlick = spec + (1.0f - spec) * fr;
+        out[c] = (schlick * nfactor) * lobe;
+    }
+    return { out[0], out[1], out[2] };
+}
+
+// blinn::pdf (brdf.h:182-190)
+__device__ __forceinline__ float blinn_pdf(gbrt_material const& m, v3 n, v3 wo, v3 wi)
+{
+    const float pi = 3.14159265358979323846264338328e+00f;
+    v3 h = normalize3(wi + wo);
+    float costheta = dot3(n, h);
+    float vdoth = dot3(wo, h);
+    return ((m.exponent + 1.0f) * pow_d(costheta, m.exponent)) / (2.0f * pi * 4.0f * vdoth);
+}
 
 struct camera_basis
 {
@@ -98,21 +133,28 @@ enum : uint32_t
     kVertexMatte = 2,
     kVertexEnd = 3,   // matte with a zero pdf: the path stops without contributing
     kVertexSpecular = 4,   // mirror / glass: next throughput = thr * spec (not differentiated)
+    kVertexPlastic = 5,    // plastic: thr * spec as specular, NEE = w * thr * gnee * lint
 };
 
 struct vertex_rec
 {
     uint32_t kind, geom, lgeom, nee;
-    v3 thr;
-    float sigma;      // matte: next throughput = thr * albedo * sigma
-    float mis;        // emission: contribution = thr * mis * emission * scale
-    float escale;     // emission: material scale (ls)
-    float kfac;       // NEE: contribution = w * thr * albedo * lint * kfac
+    v3 thr;           // throughput entering the vertex
+    float rr;         // Russian roulette normaliser (0: none)
     float w, x, b0;   // NEE: w = power_heuristic(x, b0 * max(thr))
     float kl;         // NEE: lint = emission[lgeom] * kl
     v3 lint;
-    float rr;         // Russian roulette normaliser (0: none)
-    v3 spec;          // specular: next throughput = thr * spec (then / rr)
+    v3 gnee;          // NEE: contribution = w * thr * albedo * gnee * lint (matte),
+                      //      w * thr * gnee * lint (plastic)
+    union
+    {
+        v3 spec;      // specular, plastic: next throughput = thr * spec (then / rr)
+        float sigma;  // matte: next throughput = thr * albedo * sigma (then / rr)
+        struct
+        {
+            float mis, scale;   // emission: contribution = thr * mis * emission * scale
+        } emit;
+    } f;
 };
 
 struct vertex_out
@@ -127,11 +169,179 @@ struct vertex_out
 
 __device__ __forceinline__ v3 param3(const float* a, uint32_t i) { return { a[3 * i], a[3 * i + 1], a[3 * i + 2] }; }
 
+struct lobe_sample
+{
+    v3 refl, src;
+    float pdf;
+    uint32_t k;        // the random-number counter after the draws
+    uint32_t glossy;   // the Blinn lobe was sampled (inter = GlossyReflection)
+};
+
+// plastic::sample (detail/material/plastic.inl:42-95) on the faceforwarded normal nn:
+// one draw picks the lobe by the mean reflectances, and the pdf returned is the chosen
+// lobe's alone.  Out of line, like plastic_nee below: the double-precision pow, cos and
+// sin would otherwise raise the register pressure of every kernel that shades.
+__device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restrict__ mp, v3 nn, v3 view,
+                                                   uint32_t frame, uint32_t p, uint32_t sample, uint32_t k)
+{
+    const float inv_pi = 3.18309886183790691216444201928e-01f;
+    const float pi = 3.14159265358979323846264338328e+00f;
+    const float two_pi = 6.28318530717958623199592693709e+00f;
+    const gbrt_material m = *mp;
+    lobe_sample out;
+    float prob_diff = ((m.color[0] + m.color[1]) + m.color[2]) / 3.0f * m.scale;
+    float prob_spec = ((m.color2[0] + m.color2[1]) + m.color2[2]) / 3.0f * m.scale2;
+    const bool all_zero = prob_diff == 0.0f && prob_spec == 0.0f;
+    prob_diff = all_zero ? 0.5f : prob_diff;
+    prob_spec = all_zero ? 0.5f : prob_spec;
+    prob_diff = prob_diff / (prob_diff + prob_spec);
+    const float u = gbrt_rng_u01(frame, p, sample, k++);
+    v3 w = nn;
+    v3 v = fabsf(w.x) > fabsf(w.y) ? normalize3(v3{ -w.z, 0.0f, w.x }) : normalize3(v3{ 0.0f, w.z, -w.y });
+    v3 uu = cross3(v, w);
+    if (u < prob_diff)
+    {
+        // lambertian::sample_f as for matte (second argument drawn first)
+        float u2 = gbrt_rng_u01(frame, p, sample, k++);
+        float u1 = gbrt_rng_u01(frame, p, sample, k++);
+        float r = sqrtf(u1);
+        float theta = two_pi * u2;
+        v3 s3 = { r * cos_d(theta), r * sin_d(theta), sqrtf(1.0f - u1) };
+        out.refl = normalize3(uu * s3.x + v * s3.y + w * s3.z);
+        out.pdf = dot3(nn, out.refl) * inv_pi;
+        out.src = (v3{ m.color[0], m.color[1], m.color[2] } * m.scale) * inv_pi;
+        out.glossy = 0u;
+    }
+    else
+    {
+        // blinn::sample_f (brdf.h:143-180): half vector around n, wi = reflect(wo, h)
+        float u1 = gbrt_rng_u01(frame, p, sample, k++);
+        float u2 = gbrt_rng_u01(frame, p, sample, k++);
+        float costheta = pow_d(u1, 1.0f / (m.exponent + 1.0f));
+        float sintheta = sqrtf(fmaxf(0.0f, 1.0f - costheta * costheta));
+        float phi = u2 * two_pi;
+        v3 h = normalize3(uu * (sintheta * cos_d(phi)) + v * (sintheta * sin_d(phi)) + w * costheta);
+        out.refl = h * (2.0f * dot3(h, view)) - view;
+        float vdoth = dot3(view, h);
+        out.pdf = ((m.exponent + 1.0f) * pow_d(costheta, m.exponent)) / (2.0f * pi * 4.0f * vdoth);
+        out.src = blinn_f(m, nn, view, out.refl);
+        out.glossy = 1u;
+    }
+    out.k = k;
+    return out;
+}
+
+// mirror::sample and glass::sample on the unflipped shading normal sn (out of line,
+// as sample_plastic).
+__device__ __noinline__ lobe_sample sample_specular(const gbrt_material* __restrict__ mp, v3 sn, v3 view,
+                                                    uint32_t frame, uint32_t p, uint32_t sample, uint32_t k)
+{
+    const gbrt_material m = *mp;
+    lobe_sample out;
+    out.glossy = 0u;
+    if (m.kind == GBRT_MATERIAL_MIRROR)
+    {
+        // mirror::sample -> specular_reflection::sample_f(sr.normal, view) (brdf.h:317-340):
+        // wi = reflect(wo, n), pdf 1, conductor Fresnel (fresnel.h:18-35) * cr * kr / |n.wi|
+        const v3 wo = view;
+        out.refl = sn * (2.0f * dot3(sn, wo)) - wo;
+        out.pdf = 1.0f;
+        const float cosi = fabsf(dot3(sn, wo));
+        const float cr[3] = { m.color[0], m.color[1], m.color[2] };
+        float f[3];
+        for (int c = 0; c < 3; ++c)
+        {
+            const float eta = m.ior[c], kap = m.absorption[c];
+            const float a = eta * eta + kap * kap;
+            const float rs2 = ((a - 2.0f * eta * cosi) + cosi * cosi) / ((a + 2.0f * eta * cosi) + cosi * cosi);
+            const float rp2 = ((a * cosi * cosi - 2.0f * eta * cosi) + 1.0f) / ((a * cosi * cosi + 2.0f * eta * cosi) + 1.0f);
+            f[c] = ((rs2 + rp2) / 2.0f) * (cr[c] * m.scale);
+        }
+        const float dn = fabsf(dot3(sn, out.refl));
+        out.src = { f[0] / dn, f[1] / dn, f[2] / dn };
+    }
+    else
+    {
+        // glass::sample -> specular_transmission::sample_f(sr.normal, view) (brdf.h:385-456)
+        const v3 wo = view;
+        float cosi = dot3(sn, wo);
+        cosi = cosi < 1.0f ? cosi : 1.0f;          // clamp(x, -1, 1) = max(-1, min(x, 1))
+        cosi = -1.0f < cosi ? cosi : -1.0f;
+        const bool entering = cosi > 0.0f;
+        const v3 N = entering ? sn : -sn;
+        const float ior1[3] = { 1.0f, 1.0f, 1.0f }, ior2[3] = { m.ior[0], m.ior[1], m.ior[2] };
+        const float etai0 = entering ? ior1[0] : ior2[0], etat0 = entering ? ior2[0] : ior1[0];
+        if (!entering) cosi = fabsf(cosi);
+        const float eta = etai0 / etat0;
+        const float sini = sqrtf(fmaxf(0.0f, 1.0f - cosi * cosi));
+        const float sint = eta * sini;
+        const float cost = sqrtf(fmaxf(0.0f, 1.0f - sint * sint));
+        // fresnel_reflectance(dielectric_tag, ior1, ior2, cosi, cost) (fresnel.h:37-56)
+        float R[3];
+        for (int c = 0; c < 3; ++c)
+        {
+            const float rs = (ior1[c] * cosi - ior2[c] * cost) / (ior1[c] * cosi + ior2[c] * cost);
+            const float rp = (ior2[c] * cosi - ior1[c] * cost) / (ior2[c] * cosi + ior1[c] * cost);
+            R[c] = (rs * rs + rp * rp) / 2.0f;
+        }
+        if (sint >= 1.0f) R[0] = R[1] = R[2] = 1.0f;   // total internal reflection
+        // refract(wo, N, eta) (vector.inl:695-707; not normalised) and reflect(wo, N)
+        const float rc = dot3(N, wo);
+        const float rsin = fmaxf(0.0f, 1.0f - rc * rc);
+        const float rsint = eta * eta * rsin;
+        const v3 refracted = rsint >= 1.0f ? v3{ 0.0f, 0.0f, 0.0f } : (-wo) * eta + N * (eta * rc - sqrtf(1.0f - rsint));
+        const v3 reflected = N * (2.0f * dot3(N, wo)) - wo;
+        const float u = gbrt_rng_u01(frame, p, sample, k++);
+        float val[3];
+        if (u < R[0])
+        {
+            out.refl = reflected;
+            out.pdf = R[0];
+            const float cr[3] = { m.color2[0], m.color2[1], m.color2[2] };
+            for (int c = 0; c < 3; ++c) val[c] = R[c] * (cr[c] * m.scale2);
+        }
+        else
+        {
+            out.refl = normalize3(refracted);
+            out.pdf = 1.0f - R[0];
+            const float ct[3] = { m.color[0], m.color[1], m.color[2] };
+            for (int c = 0; c < 3; ++c) val[c] = (1.0f - R[c]) * (ct[c] * m.scale);
+        }
+        const float dn = dot3(N, out.refl);
+        out.src = { val[0] / dn, val[1] / dn, val[2] / dn };
+    }
+    out.k = k;
+    return out;
+}
+
+struct nee_terms
+{
+    v3 brdf;     // (diffuse + Blinn) reflectance toward L
+    float pdf;   // surf.pdf(view, L, inter)
+};
+
+// A plastic surface's next-event terms toward L: plastic::pdf (plastic.inl:97-110,
+// the sampled lobe's) and the reflectance inside plastic::shade (plastic.inl:20-39)
+// added to the diffuse term cd.
+__device__ __noinline__ nee_terms plastic_nee(const gbrt_material* __restrict__ mp, v3 nn, v3 view, v3 L, v3 cd,
+                                              uint32_t glossy)
+{
+    const float inv_pi = 3.18309886183790691216444201928e-01f;
+    const gbrt_material m = *mp;
+    nee_terms out;
+    out.pdf = glossy ? blinn_pdf(m, nn, view, L) : dot3(nn, L) * inv_pi;
+    out.brdf = cd + blinn_f(m, nn, view, L);
+    return out;
+}
+
 // One bounce of pathtracing::kernel::operator() (detail/pathtracing.inl:65-221) for one
 // path whose ray (ori, dir) hit triangle `tri` at `t` (tri < 0: missed).  Updates the
 // path state, adds emission / ambient to st.rad, and returns the next ray and the NEE
 // shadow ray with its unoccluded contribution.  Shared by the wavefront shade kernel
 // and the adjoint's replay, so both compute bit-identical paths.
+// Extended = false compiles out the mirror, glass and plastic branches, for scenes
+// whose materials are all matte or emissive (any other kind then shades as matte).
+template <bool Extended = true>
 __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p, uint32_t bounce, v3 ori, v3 dir,
                                              float tmin, float tmax, int tri, float t, path_state& st,
                                              vertex_out& out, uint32_t* __restrict__ status)
@@ -177,86 +387,33 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         geom = 0;
     }
     bool emission = m.kind == GBRT_MATERIAL_EMISSIVE;
-    const bool mirror = m.kind == GBRT_MATERIAL_MIRROR, glass = m.kind == GBRT_MATERIAL_GLASS;
-    const bool specular = mirror || glass;
+    const bool specular = Extended && (m.kind == GBRT_MATERIAL_MIRROR || m.kind == GBRT_MATERIAL_GLASS);
+    const bool plastic = Extended && m.kind == GBRT_MATERIAL_PLASTIC;
+    bool glossy = false;   // plastic: the Blinn lobe was sampled (inter = GlossyReflection)
     v3 mcol = { m.color[0], m.color[1], m.color[2] };
-    if (!emission && !specular && sp.albedo) mcol = param3(sp.albedo, geom);
+    if (!emission && !specular && !plastic && sp.albedo) mcol = param3(sp.albedo, geom);
     if (emission && sp.emission) mcol = param3(sp.emission, geom);
     rec.geom = geom;
 
     v3 refl = { 0.0f, 0.0f, 0.0f };
     float brdf_pdf;
     v3 src;
-    if (mirror)
+    if (specular)
     {
-        // mirror::sample -> specular_reflection::sample_f(sr.normal, view) (brdf.h:317-340):
-        // wi = reflect(wo, n), pdf 1, conductor Fresnel (fresnel.h:18-35) * cr * kr / |n.wi|
-        const v3 wo = view;
-        refl = sn * (2.0f * dot3(sn, wo)) - wo;
-        brdf_pdf = 1.0f;
-        const float cosi = fabsf(dot3(sn, wo));
-        const float cr[3] = { mcol.x, mcol.y, mcol.z };
-        float f[3];
-        for (int c = 0; c < 3; ++c)
-        {
-            const float eta = m.ior[c], k = m.absorption[c];
-            const float a = eta * eta + k * k;
-            const float rs2 = ((a - 2.0f * eta * cosi) + cosi * cosi) / ((a + 2.0f * eta * cosi) + cosi * cosi);
-            const float rp2 = ((a * cosi * cosi - 2.0f * eta * cosi) + 1.0f) / ((a * cosi * cosi + 2.0f * eta * cosi) + 1.0f);
-            f[c] = ((rs2 + rp2) / 2.0f) * (cr[c] * m.scale);
-        }
-        const float dn = fabsf(dot3(sn, refl));
-        src = { f[0] / dn, f[1] / dn, f[2] / dn };
+        lobe_sample ls = sample_specular(sp.materials + geom, sn, view, sp.frame, p, sp.sample, st.k);
+        refl = ls.refl;
+        brdf_pdf = ls.pdf;
+        src = ls.src;
+        st.k = ls.k;
     }
-    else if (glass)
+    else if (plastic)
     {
-        // glass::sample -> specular_transmission::sample_f(sr.normal, view) (brdf.h:385-456)
-        const v3 wo = view;
-        float cosi = dot3(sn, wo);
-        cosi = cosi < 1.0f ? cosi : 1.0f;          // clamp(x, -1, 1) = max(-1, min(x, 1))
-        cosi = -1.0f < cosi ? cosi : -1.0f;
-        const bool entering = cosi > 0.0f;
-        const v3 N = entering ? sn : -sn;
-        const float ior1[3] = { 1.0f, 1.0f, 1.0f }, ior2[3] = { m.ior[0], m.ior[1], m.ior[2] };
-        const float etai0 = entering ? ior1[0] : ior2[0], etat0 = entering ? ior2[0] : ior1[0];
-        if (!entering) cosi = fabsf(cosi);
-        const float eta = etai0 / etat0;
-        const float sini = sqrtf(fmaxf(0.0f, 1.0f - cosi * cosi));
-        const float sint = eta * sini;
-        const float cost = sqrtf(fmaxf(0.0f, 1.0f - sint * sint));
-        // fresnel_reflectance(dielectric_tag, ior1, ior2, cosi, cost) (fresnel.h:37-56)
-        float R[3];
-        for (int c = 0; c < 3; ++c)
-        {
-            const float rs = (ior1[c] * cosi - ior2[c] * cost) / (ior1[c] * cosi + ior2[c] * cost);
-            const float rp = (ior2[c] * cosi - ior1[c] * cost) / (ior2[c] * cosi + ior1[c] * cost);
-            R[c] = (rs * rs + rp * rp) / 2.0f;
-        }
-        if (sint >= 1.0f) R[0] = R[1] = R[2] = 1.0f;   // total internal reflection
-        // refract(wo, N, eta) (vector.inl:695-707; not normalised) and reflect(wo, N)
-        const float rc = dot3(N, wo);
-        const float rsin = fmaxf(0.0f, 1.0f - rc * rc);
-        const float rsint = eta * eta * rsin;
-        const v3 refracted = rsint >= 1.0f ? v3{ 0.0f, 0.0f, 0.0f } : (-wo) * eta + N * (eta * rc - sqrtf(1.0f - rsint));
-        const v3 reflected = N * (2.0f * dot3(N, wo)) - wo;
-        const float u = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
-        float val[3];
-        if (u < R[0])
-        {
-            refl = reflected;
-            brdf_pdf = R[0];
-            const float cr[3] = { m.color2[0], m.color2[1], m.color2[2] };
-            for (int c = 0; c < 3; ++c) val[c] = R[c] * (cr[c] * m.scale2);
-        }
-        else
-        {
-            refl = normalize3(refracted);
-            brdf_pdf = 1.0f - R[0];
-            const float ct[3] = { mcol.x, mcol.y, mcol.z };
-            for (int c = 0; c < 3; ++c) val[c] = (1.0f - R[c]) * (ct[c] * m.scale);
-        }
-        const float dn = dot3(N, refl);
-        src = { val[0] / dn, val[1] / dn, val[2] / dn };
+        lobe_sample ls = sample_plastic(sp.materials + geom, faceforward3(sn, view, gn), view, sp.frame, p, sp.sample, st.k);
+        refl = ls.refl;
+        brdf_pdf = ls.pdf;
+        src = ls.src;
+        glossy = ls.glossy != 0u;
+        st.k = ls.k;
     }
     else if (!emission)
     {
@@ -303,8 +460,8 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
     {
         st.rad = st.rad + (st.thr * mis) * src;
         rec.kind = kVertexEmission;
-        rec.mis = mis;
-        rec.escale = m.scale;
+        rec.f.emit.mis = mis;
+        rec.f.emit.scale = m.scale;
         return;
     }
     if (zero_pdf)
@@ -312,7 +469,7 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         rec.kind = kVertexEnd;
         return;
     }
-    rec.kind = specular ? kVertexSpecular : kVertexMatte;
+    rec.kind = specular ? kVertexSpecular : (plastic ? kVertexPlastic : kVertexMatte);
     v3 nn = faceforward3(sn, view, gn);
     if (sp.num_lights > 0 && specular)
     {
@@ -349,10 +506,18 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         float ldotn = dot3(L, nn);
         float ldotln = fabsf(dot3(-L, ln));
         float bpdf0 = dot3(nn, L) * inv_pi;
+        v3 cd = (mcol * m.scale) * inv_pi;
+        v3 brdf = cd;
+        if (plastic)
+        {
+            nee_terms nt = plastic_nee(sp.materials + geom, nn, view, L, cd, glossy ? 1u : 0u);
+            bpdf0 = nt.pdf;
+            brdf = nt.brdf;
+        }
         float bpdf = bpdf0 * max_elem(st.thr);
         float ndotl = fmaxf(0.0f, dot3(nn, L));
-        v3 cd = (mcol * m.scale) * inv_pi;
-        v3 shade = ((cd * pi) * lint) * ndotl;
+        // (plastic::shade, plastic.inl:20-39: (diffuse + Blinn) * pi * intensity * n.l)
+        v3 shade = ((brdf * pi) * lint) * ndotl;
         v3 src2 = (shade * inv_pi) / ldotn;
         float x = lpdf / float(sp.num_lights);
         float mis2 = power_heuristic(x, bpdf);
@@ -370,14 +535,24 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
             rec.w = mis2;
             rec.x = x;
             rec.b0 = bpdf0;
-            // contribution = w * thr * albedo * lint * kfac
-            rec.kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
+            // contribution = w * thr * albedo * lint * kfac (matte), w * thr * gnee * lint (plastic)
+            if (plastic)
+            {
+                rec.gnee = brdf * (pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights));
+            }
+            else
+            {
+                const float kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
+                rec.gnee = { kfac, kfac, kfac };
+            }
         }
     }
     float cosp = dot3(nn, refl) / brdf_pdf;
-    rec.spec = src * cosp;
+    if (specular || plastic)
+        rec.f.spec = src * cosp;
+    else
+        rec.f.sigma = m.scale * inv_pi * cosp;
     st.thr = st.thr * (src * cosp);
-    rec.sigma = m.scale * inv_pi * cosp;
     bool terminate = false;
     if (bounce >= 2 && !(sp.flags & GBRT_PT_NO_RUSSIAN_ROULETTE))
     {

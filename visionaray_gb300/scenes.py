@@ -104,30 +104,58 @@ def box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
     return tris, mats, lights
 
 
-def specular_box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
-    """box_scene with every third blob a gold-like mirror (conductor Fresnel: ior
-    (0.27, 0.42, 1.35), absorption (3.4, 2.3, 1.8)) and every third, from the third on,
-    clear glass (ior 1.5, transmission and reflection colors 1): the specular materials
-    on closed, noisy surfaces, so paths refract in and out and meet total internal
-    reflection.  Returns (triangles, materials per geom_id, area lights)."""
-    from .types import GLASS, MIRROR
+def specular_box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0, cycle=None):
+    """box_scene whose blobs take their material kinds from `cycle` in turn (default
+    matte, mirror, glass): a gold-like mirror (conductor Fresnel: ior (0.27, 0.42, 1.35),
+    absorption (3.4, 2.3, 1.8)), clear glass (ior 1.5, transmission and reflection
+    colors 1), a red plastic (cd (0.7, 0.2, 0.15), cs 0.4 white, exponent 32) or the blob's
+    matte albedo: the specular and glossy materials on closed, noisy surfaces, so paths
+    refract in and out and meet total internal reflection.  Returns (triangles,
+    materials per geom_id, area lights)."""
+    from .types import GLASS, MATTE, MIRROR, PLASTIC
+    cycle = (MATTE, MIRROR, GLASS) if cycle is None else tuple(cycle)
     tris, mats, lights = box_scene(n_blobs, subdiv, seed, light_y, emission)
     per = 20 * subdiv * subdiv
     for b in range(n_blobs):
         sl = slice(14 + b * per, 14 + (b + 1) * per)
-        if b % 3 == 1:
+        kind = cycle[b % len(cycle)]
+        if kind == PLASTIC:
+            mats["kind"][sl] = PLASTIC
+            mats["color"][sl] = (0.7, 0.2, 0.15)
+            mats["scale"][sl] = 1.0
+            mats["color2"][sl] = (0.4, 0.4, 0.4)
+            mats["scale2"][sl] = 1.0
+            mats["exponent"][sl] = 32.0
+        elif kind == MIRROR:
             mats["kind"][sl] = MIRROR
             mats["color"][sl] = (0.95, 0.9, 0.8)
             mats["scale"][sl] = 1.0
             mats["ior"][sl] = (0.27, 0.42, 1.35)
             mats["absorption"][sl] = (3.4, 2.3, 1.8)
-        elif b % 3 == 2:
+        elif kind == GLASS:
             mats["kind"][sl] = GLASS
             mats["color"][sl] = (1.0, 1.0, 1.0)
             mats["scale"][sl] = 1.0
             mats["color2"][sl] = (1.0, 1.0, 1.0)
             mats["scale2"][sl] = 1.0
             mats["ior"][sl] = (1.5, 1.5, 1.5)
+    return tris, mats, lights
+
+
+def glossy_box_scene(n_blobs=10, subdiv=8, seed=1, light_y=0.999, emission=15.0):
+    """specular_box_scene with blobs cycling matte, plastic, mirror, plastic, glass and
+    the box's walls (its first 12 triangles) a white plastic (cd 0.8, cs 0.25, exponent
+    16): glossy next-event estimation and Blinn sampling over most of the image."""
+    from .types import GLASS, MATTE, MIRROR, PLASTIC
+    tris, mats, lights = specular_box_scene(n_blobs, subdiv, seed, light_y, emission,
+                                            cycle=(MATTE, PLASTIC, MIRROR, PLASTIC, GLASS))
+    walls = slice(0, 12)
+    mats["kind"][walls] = PLASTIC
+    mats["color"][walls] = (0.8, 0.8, 0.8)
+    mats["scale"][walls] = 1.0
+    mats["color2"][walls] = (0.25, 0.25, 0.25)
+    mats["scale2"][walls] = 1.0
+    mats["exponent"][walls] = 16.0
     return tris, mats, lights
 
 

@@ -19,7 +19,7 @@ BVH_NODE = np.dtype([("bbox_min", "<f4", (3,)), ("bbox_max", "<f4", (3,)),
 # path tracing (gbrt.h): gbrt_material, gbrt_area_light, gbrt_camera, gbrt_pt_params
 MATERIAL = np.dtype([("kind", "<u4"), ("color", "<f4", (3,)), ("scale", "<f4"), ("ior", "<f4", (3,)),
                      ("absorption", "<f4", (3,)), ("color2", "<f4", (3,)), ("scale2", "<f4"),
-                     ("reserved", "<u4")])
+                     ("exponent", "<f4")])
 AREA_LIGHT = np.dtype([("geometry", TRIANGLE), ("cl", "<f4", (3,)), ("kl", "<f4")])
 CAMERA = np.dtype([("eye", "<f4", (3,)), ("center", "<f4", (3,)), ("up", "<f4", (3,)),
                    ("fovy_degrees", "<f4")])
@@ -30,7 +30,7 @@ INSTANCE = np.dtype([("blas", "<u8"), ("transform", "<f4", (12,))])
 HIT_INST = np.dtype([("prim_id", "<u4"), ("inst_id", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),
                      ("geom_id", "<u4"), ("reserved", "<u4", (2,))])
 BATCH_LAUNCH = np.dtype([("block", "<u4"), ("tile", "<u4"), ("stack", "<u4"), ("order", "<u4")])
-MATTE, EMISSIVE, MIRROR, GLASS = 0, 1, 2, 3
+MATTE, EMISSIVE, MIRROR, GLASS, PLASTIC = 0, 1, 2, 3, 4
 BATCH_ORDER_ROWS, BATCH_ORDER_BLOCKS = 0, 1
 PT_SHADOW_RANGE_FIX = 1
 PT_NO_RUSSIAN_ROULETTE = 2
