@@ -270,6 +270,38 @@ typedef struct gbrt_area_light
     float         kl;
 } gbrt_area_light;
 
+/* One member of visionaray's generic_light<area_light, point_light, spot_light>
+ * (generic_light.h) for next-event estimation:
+ *   area  (detail/area_light.inl:27-53): geometry, cl, kl -- as gbrt_area_light
+ *   point (detail/point_light.inl:16-56): position, cl, kl and the constant, linear
+ *         and quadratic attenuation.  Its sample is a delta light of pdf 1 whose
+ *         intensity is cl * kl * pi / constant attenuation: point_light::sample
+ *         evaluates the attenuation at the light's own position (distance 0), so
+ *         there is no distance falloff; it draws three random numbers (an unused
+ *         normal)
+ *   spot  (detail/spot_light.inl): as point plus spot_direction, spot_cutoff
+ *         (radians) and spot_exponent.  spot_light::sample evaluates the cone at the
+ *         light's own position too: normalize(0) is NaN, the cone test fails and the
+ *         sample's intensity is 0 -- a spot light takes its share of the light picks
+ *         and adds nothing, as in the reference
+ * A light's draw count (1 pick + 2 for an area light, 1 + 3 for a point or spot
+ * light) follows the reference's, so random streams stay matched.                  */
+#define GBRT_LIGHT_AREA  0u
+#define GBRT_LIGHT_POINT 1u
+#define GBRT_LIGHT_SPOT  2u
+typedef struct gbrt_light
+{
+    uint32_t      kind;
+    float         cl[3];
+    float         kl;
+    gbrt_triangle geometry;
+    float         position[3];
+    float         attenuation[3];   /* constant, linear, quadratic */
+    float         spot_direction[3];
+    float         spot_cutoff;
+    float         spot_exponent;
+} gbrt_light;
+
 /* pinhole_camera after look_at(eye, center, up) and perspective(fovy, w / h, ...)
  * (pinhole_camera.h, detail/pinhole_camera.inl:87-120).                            */
 typedef struct gbrt_camera
@@ -337,6 +369,13 @@ gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* bvh,
                                  gbrt_material const* h_materials, uint32_t num_materials,
                                  gbrt_area_light const* h_lights, uint32_t num_lights,
                                  gbrt_pt_scene** out);
+/* As gbrt_pt_scene_create with a generic_light<area_light, point_light, spot_light>
+ * list (make_kernel_params over generic lights, kernels.h:136-188; the light is
+ * picked uniformly, sampling.h:195-213).                                          */
+gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                        gbrt_material const* h_materials, uint32_t num_materials,
+                                        gbrt_light const* h_lights, uint32_t num_lights,
+                                        gbrt_pt_scene** out);
 gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene);
 
 /* Renders one frame: cuda_sched<basic_ray<float>>::frame(pathtracing::kernel{params},

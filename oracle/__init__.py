@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from visionaray_gb300.types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, MATERIAL, PT_PARAMS
+from visionaray_gb300.types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, LIGHT, MATERIAL, PT_PARAMS, lights_of_area_lights
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")
@@ -44,6 +44,13 @@ class Tree:
                 f = int(self.nodes["first"][i])
                 st += [(f, d + 1), (f + 1, d + 1)]
         return best
+
+
+def _as_lights(lights):
+    """LIGHT records (area, point, spot); AREA_LIGHT records are converted."""
+    if np.asarray(lights).dtype == LIGHT:
+        return np.ascontiguousarray(lights, LIGHT)
+    return lights_of_area_lights(lights)
 
 
 class Oracle:
@@ -149,7 +156,7 @@ class Oracle:
         PT_DOUBLE (the FP64 oracle), PT_FLOAT_TRIG_DOUBLE (the CUDA path's)."""
         tris = np.ascontiguousarray(tris)
         materials = np.ascontiguousarray(materials, MATERIAL)
-        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        lights = _as_lights(lights)
         camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
         params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
         w, h = int(params["width"][0]), int(params["height"][0])
@@ -166,7 +173,7 @@ class Oracle:
         (img_adj (h, w, 4)) at the gbrt_rng.h stream, in double (fp64) or float."""
         tris = np.ascontiguousarray(tris)
         materials = np.ascontiguousarray(materials, MATERIAL)
-        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        lights = _as_lights(lights)
         camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
         params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
         w, h = int(params["width"][0]), int(params["height"][0])
@@ -329,7 +336,7 @@ class Reference:
         (height, width, 4) float32."""
         tris = np.ascontiguousarray(tris)
         materials = np.ascontiguousarray(materials, MATERIAL)
-        lights = np.ascontiguousarray(lights, AREA_LIGHT)
+        lights = _as_lights(lights)
         camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
         params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
         w, h = int(params["width"][0]), int(params["height"][0])

@@ -105,11 +105,12 @@ void orc_trace_linear(const gbrt_triangle* tris, uint32_t ntris, const gbrt_ray*
  * reference build's arithmetic); 1: double (the FP64 oracle); 2: float with the
  * hemisphere sample's cos/sin evaluated in double and rounded once (the CUDA path's
  * arithmetic); mode | 4: the hemisphere sample's two draws in argument order (the
- * order visionaray's device build evaluates them in).  counters (may be NULL)
- * receives {closest rays, shadow rays, box tests, triangle tests}.                 */
+ * order visionaray's device build evaluates them in).  lights: area, point and spot
+ * lights (gbrt_light).  counters (may be NULL) receives {closest rays, shadow rays,
+ * box tests, triangle tests}.                                                        */
 void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                    const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
-                   const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                   const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                    const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba,
                    uint64_t* counters);
 
@@ -121,7 +122,7 @@ void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32
  * adjoint); else float with the CUDA path's cos/sin.                               */
 void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                            const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
-                           const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                           const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                            const gbrt_pt_params* p, const float* albedo, const float* emission,
                            const double* img_adj, int fp64, int nthreads, double* grad_albedo,
                            double* grad_emission, double* image);

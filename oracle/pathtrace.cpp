@@ -251,7 +251,7 @@ T blinn_pdf(gbrt_material const& m, vec<T> n, vec<T> wo, vec<T> wi, bool trig_do
 }
 
 template <typename T>
-vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_light const* lights,
                 uint32_t nl, gbrt_pt_params const& p, vec<T> ori, vec<T> dir, T tmin, T tmax,
                 gbrt_sample_generator& gen, bool& first_hit, pt_counters& cnt, bool trig_double,
                 pt_params_ext const& ext = {}, vrec<T>* recs = nullptr, int* nrec = nullptr)
@@ -485,31 +485,63 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         vec<T> n = faceforward(sn, view_dir, gn);
         if (nl > 0)
         {
-            // sample_random_light + area_light::sample + sample_surface
+            // sample_random_light (sampling.h:195-213) + the light's sample
             T ul = T(gen.next());
             int light_id = static_cast<int>(float(ul) * float(nl));
             if (light_id >= int(nl)) light_id = int(nl) - 1;
-            tri_t<T> lt = load_tri<T>(lights[light_id].geometry);
-            T s1 = T(gen.next());
-            T s2 = T(gen.next());
-            vec<T> lv1 = lt.v1, lv2 = lt.v1 + lt.e1, lv3 = lt.v1 + lt.e2;
-            T sq = std::sqrt(s1);
-            vec<T> pos = lv1 * (T(1.0) - sq) + lv2 * sq * (T(1.0) - s2) + lv3 * sq * s2;
-            vec<T> ldir = pos - isect;
-            T dist = length(ldir);
-            vec<T> lint = { T(lights[light_id].cl[0]) * T(lights[light_id].kl),
-                            T(lights[light_id].cl[1]) * T(lights[light_id].kl),
-                            T(lights[light_id].cl[2]) * T(lights[light_id].kl) };
-            uint32_t lgeom = lights[light_id].geometry.geom_id;
-            if (ext.emission && lgeom < nmat) lint = load<T>(ext.emission + 3 * lgeom) * T(lights[light_id].kl);
-            vec<T> lnormal = normalize(cross(lt.e1, lt.e2));
-            T larea = T(0.5) * length(cross(lt.e1, lt.e2));
-            T ldotln0 = std::abs(dot(-normalize(ldir), lnormal));
-            T solid_angle = (ldotln0 * larea) / (dist * dist);
-            T lpdf = T(1.0) / solid_angle;
-
-            vec<T> L = normalize(ldir);
-            vec<T> ln = faceforward(lnormal, -L, lnormal);
+            gbrt_light const& lsrc = lights[light_id];
+            vec<T> ldir, lint, L, ln;
+            T dist, lpdf;
+            uint32_t lgeom = 0xFFFFFFFFu;
+            if (lsrc.kind == GBRT_LIGHT_AREA)
+            {
+                // area_light::sample + sample_surface (area_light.inl:27-53, triangle.inl:69-83)
+                tri_t<T> lt = load_tri<T>(lsrc.geometry);
+                T s1 = T(gen.next());
+                T s2 = T(gen.next());
+                vec<T> lv1 = lt.v1, lv2 = lt.v1 + lt.e1, lv3 = lt.v1 + lt.e2;
+                T sq = std::sqrt(s1);
+                vec<T> pos = lv1 * (T(1.0) - sq) + lv2 * sq * (T(1.0) - s2) + lv3 * sq * s2;
+                ldir = pos - isect;
+                dist = length(ldir);
+                lint = { T(lsrc.cl[0]) * T(lsrc.kl), T(lsrc.cl[1]) * T(lsrc.kl), T(lsrc.cl[2]) * T(lsrc.kl) };
+                lgeom = lsrc.geometry.geom_id;
+                if (ext.emission && lgeom < nmat) lint = load<T>(ext.emission + 3 * lgeom) * T(lsrc.kl);
+                vec<T> lnormal = normalize(cross(lt.e1, lt.e2));
+                T larea = T(0.5) * length(cross(lt.e1, lt.e2));
+                T ldotln0 = std::abs(dot(-normalize(ldir), lnormal));
+                T solid_angle = (ldotln0 * larea) / (dist * dist);
+                lpdf = T(1.0) / solid_angle;
+                L = normalize(ldir);
+                ln = faceforward(lnormal, -L, lnormal);
+                if (!ext.emission) lgeom = 0xFFFFFFFFu;
+            }
+            else
+            {
+                // point_light::sample / spot_light::sample (point_light.inl:16-56,
+                // spot_light.inl:14-62): intensity(pos) * pi at pos = the light's own
+                // position, three draws for an unused normal, a delta light of pdf 1
+                vec<T> pos = load<T>(lsrc.position);
+                ldir = pos - isect;
+                dist = length(ldir);
+                vec<T> dd = pos - pos;
+                T d = length(dd);
+                T att = T(1.0 / (T(lsrc.attenuation[0]) + T(lsrc.attenuation[1]) * d + T(lsrc.attenuation[2]) * d * d));
+                vec<T> in = vec<T>{ T(lsrc.cl[0]) * T(lsrc.kl), T(lsrc.cl[1]) * T(lsrc.kl), T(lsrc.cl[2]) * T(lsrc.kl) } * att;
+                if (lsrc.kind == GBRT_LIGHT_SPOT)
+                {
+                    T c = dot(load<T>(lsrc.spot_direction), normalize(-dd));
+                    T spot = c > T(std::cos(lsrc.spot_cutoff)) ? std::pow(c, T(lsrc.spot_exponent)) : T(0.0);
+                    in = in * spot;
+                }
+                lint = in * pi;
+                gen.next();
+                gen.next();
+                gen.next();
+                lpdf = T(1.0);
+                L = normalize(ldir);
+                ln = faceforward(-L, -L, -L);
+            }
             T ldotn = dot(L, n);
             T ldotln = std::abs(dot(-L, ln));
             // shadow ray (pathtracing.inl:171-176); GBRT_PT_SHADOW_RANGE_FIX ends it one
@@ -537,8 +569,8 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
                 {
                     intensity = intensity + (((throughput * mis2) * src2) * (ldotn / lpdf)) * T(float(nl));
                     rec.nee = 1;
-                    rec.lgeom = ext.emission ? lgeom : 0xFFFFFFFFu;
-                    rec.kl = T(lights[light_id].kl);
+                    rec.lgeom = lgeom;
+                    rec.kl = T(lsrc.kl);
                     rec.lint = lint;
                     rec.w = mis2;
                     rec.x = lpdf / T(float(nl));
@@ -577,7 +609,7 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
 }
 
 template <typename T>
-void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_light const* lights,
             uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, int nthreads, double* out,
             pt_counters& total, bool trig_double, pt_params_ext const& ext = {})
 {
@@ -772,7 +804,7 @@ void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats,
 }
 
 template <typename T>
-void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_area_light const* lights,
+void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_light const* lights,
              uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, pt_params_ext const& ext,
              const double* img_adj, int nthreads, double* grad_albedo, double* grad_emission, double* image)
 {
@@ -849,7 +881,7 @@ void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gb
 
 extern "C" void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                                       const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
-                                      const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                                      const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                                       const gbrt_pt_params* p, const float* albedo, const float* emission,
                                       const double* img_adj, int fp64, int nthreads, double* grad_albedo,
                                       double* grad_emission, double* image)
@@ -866,7 +898,7 @@ extern "C" void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_
 
 extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                               const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
-                              const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam,
+                              const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                               const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba, uint64_t* counters)
 {
     scene_arrays s{ tris, nodes, num_nodes, indices };

@@ -17,11 +17,14 @@
 
 #include <visionaray/area_light.h>
 #include <visionaray/bvh.h>
+#include <visionaray/generic_light.h>
 #include <visionaray/generic_material.h>
 #include <visionaray/kernels.h>
 #include <visionaray/material.h>
 #include <visionaray/math/math.h>
 #include <visionaray/pinhole_camera.h>
+#include <visionaray/point_light.h>
+#include <visionaray/spot_light.h>
 #include <visionaray/traverse.h>
 #include <visionaray/detail/bvh/refit.h>
 #include <visionaray/detail/bvh/statistics.h>
@@ -252,17 +255,21 @@ void ref_trace_instances(uint32_t num_meshes, const gbrt_triangle* const* mesh_t
 }
 
 // visionaray's pathtracing::kernel (detail/pathtracing.inl:42-233) over a binned-SAH
-// index_bvh, generic_material<matte, emissive, mirror, glass, plastic> per geom_id and triangle area lights,
+} // extern "C"
+
+namespace {
+
+// index_bvh, generic_material<matte, emissive, mirror, glass, plastic> per geom_id and the lights `al`,
 // driven per (pixel, sample) by the gbrt_rng.h stream: the jittered primary ray
 // (sched_common.h:209-233, jitter x drawn before y) through visionaray's own
 // pinhole_camera, samples averaged and blended into accum as sample_pixel_impl does
 // (sched_common.h:427-526).  accum is RGBA32F, read and written.
-void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
-                   const gbrt_area_light* lights, uint32_t nl, const gbrt_camera* cam, const gbrt_pt_params* p,
-                   float* accum, int nthreads)
+template <typename Light>
+void render_reference(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
+                      std::vector<Light> const& al, const gbrt_camera* cam, const gbrt_pt_params* p, float* accum,
+                      int nthreads)
 {
     using mat_t = generic_material<matte<float>, emissive<float>, mirror<float>, glass<float>, plastic<float>>;
-    using light_t = area_light<float, triangle_t>;
     auto prims = to_prims(tris, n);
     binned_sah_builder builder;
     auto tree = builder.build(index_bvh<triangle_t>{}, prims.data(), prims.size());
@@ -320,16 +327,6 @@ void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* m
             materials[i] = m;
         }
     }
-    std::vector<light_t> al;
-    for (uint32_t i = 0; i < nl; ++i)
-    {
-        triangle_t g;
-        std::memcpy(&g, &lights[i].geometry, sizeof(g));
-        light_t l(g);
-        l.set_cl(vec3(lights[i].cl[0], lights[i].cl[1], lights[i].cl[2]));
-        l.set_kl(lights[i].kl);
-        al.push_back(l);
-    }
     auto kp = make_kernel_params(refs.data(), refs.data() + 1, materials.data(), al.data(), al.data() + al.size(),
                                  p->num_bounces, p->epsilon,
                                  vec4(p->background[0], p->background[1], p->background[2], p->background[3]),
@@ -382,4 +379,70 @@ void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* m
     for (auto& th : pool) th.join();
 }
 
-} // extern "C"
+
+area_light<float, triangle_t> area_of(gbrt_light const& l)
+{
+    triangle_t g;
+    std::memcpy(&g, &l.geometry, sizeof(g));
+    area_light<float, triangle_t> a(g);
+    a.set_cl(vec3(l.cl[0], l.cl[1], l.cl[2]));
+    a.set_kl(l.kl);
+    return a;
+}
+
+} // namespace
+
+// Lights all area lights: area_light<float, basic_triangle> as the path-tracing
+// configurations use; otherwise generic_light<area_light, point_light, spot_light>.
+extern "C" void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
+                              const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
+                              const gbrt_pt_params* p, float* accum, int nthreads)
+{
+    bool all_area = true;
+    for (uint32_t i = 0; i < nl; ++i) all_area = all_area && lights[i].kind == GBRT_LIGHT_AREA;
+    if (all_area)
+    {
+        std::vector<area_light<float, triangle_t>> al;
+        for (uint32_t i = 0; i < nl; ++i) al.push_back(area_of(lights[i]));
+        render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads);
+        return;
+    }
+    using light_t = generic_light<area_light<float, triangle_t>, point_light<float>, spot_light<float>>;
+    std::vector<light_t> al;
+    for (uint32_t i = 0; i < nl; ++i)
+    {
+        gbrt_light const& l = lights[i];
+        vec3 cl(l.cl[0], l.cl[1], l.cl[2]), pos(l.position[0], l.position[1], l.position[2]);
+        if (l.kind == GBRT_LIGHT_POINT)
+        {
+            point_light<float> pl;
+            pl.set_cl(cl);
+            pl.set_kl(l.kl);
+            pl.set_position(pos);
+            pl.set_constant_attenuation(l.attenuation[0]);
+            pl.set_linear_attenuation(l.attenuation[1]);
+            pl.set_quadratic_attenuation(l.attenuation[2]);
+            al.push_back(pl);
+        }
+        else if (l.kind == GBRT_LIGHT_SPOT)
+        {
+            spot_light<float> sl;
+            sl.set_cl(cl);
+            sl.set_kl(l.kl);
+            sl.set_position(pos);
+            sl.set_spot_direction(vec3(l.spot_direction[0], l.spot_direction[1], l.spot_direction[2]));
+            sl.set_spot_cutoff(l.spot_cutoff);
+            sl.set_spot_exponent(l.spot_exponent);
+            sl.set_constant_attenuation(l.attenuation[0]);
+            sl.set_linear_attenuation(l.attenuation[1]);
+            sl.set_quadratic_attenuation(l.attenuation[2]);
+            al.push_back(sl);
+        }
+        else
+        {
+            al.push_back(area_of(l));
+        }
+    }
+    render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads);
+}
+

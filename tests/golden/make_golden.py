@@ -129,6 +129,21 @@ def material_pathtrace_case(ref, samples, kind, frame_id):
             "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
 
 
+def lights_pathtrace_case(ref, samples):
+    """scenes.glossy_box_scene lit by scenes.mixed_lights (area, point and spot lights)."""
+    tris, mats, area = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+    lights = scenes.mixed_lights(area)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(64, 48, 4, num_bounces=8, epsilon=1e-4, frame_id=7)
+    img = ref.pathtrace(tris, mats, lights, cam, params)
+    samples["pt_lights_image"] = img
+    return {"scene": {"kind": "glossy_box", "n_blobs": 10, "subdiv": 8, "seed": 1, "lights": "mixed_lights"},
+            "camera": "scenes.box_camera()", "params": {"width": 64, "height": 48, "spp": 4, "num_bounces": 8,
+                                                        "epsilon": 1e-4, "frame_id": 7, "flags": 0},
+            "triangles_sha256": digest(tris), "materials_sha256": digest(mats), "lights_sha256": digest(lights),
+            "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
+
+
 def main():
     if not Reference.available():
         raise SystemExit("oracle/_ref/libvsnray_ref.so is missing: build it where the visionaray "
@@ -141,7 +156,8 @@ def main():
            "heightfield": heightfield_case(ref, samples),
            "pathtrace": pathtrace_case(ref, samples),
            "pathtrace_specular": material_pathtrace_case(ref, samples, "specular_box", 5),
-           "pathtrace_glossy": material_pathtrace_case(ref, samples, "glossy_box", 6)}
+           "pathtrace_glossy": material_pathtrace_case(ref, samples, "glossy_box", 6),
+           "pathtrace_lights": lights_pathtrace_case(ref, samples)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "golden_samples.npz"), **samples)

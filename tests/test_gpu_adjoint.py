@@ -84,12 +84,15 @@ def test_inverse_albedo_reduces_the_loss():
     assert res["bwd_ms"] > 0 and res["fwd_ms"] > 0
 
 
-def test_adjoint_through_specular_and_plastic_vertices(oracle):
+@pytest.mark.parametrize("light_set", ["area", "mixed"])
+def test_adjoint_through_specular_and_plastic_vertices(oracle, light_set):
     """Mirror, glass and plastic blobs and plastic walls: the reverse sweep carries the
     adjoint through each specular or plastic vertex's fixed factor and a plastic
     vertex's next-event term; against the FP32 and FP64 host adjoints."""
     ctx = vg.Context(0)
     tris, mats, lights = scenes.glossy_box_scene(n_blobs=5, subdiv=4, seed=1)
+    if light_set == "mixed":
+        lights = scenes.mixed_lights(lights)
     bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
     scene = vg.PTScene(bvh, mats, lights)
     albedo = torch.from_numpy(np.ascontiguousarray(mats["color"], np.float32)).cuda()

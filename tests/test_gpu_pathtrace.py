@@ -150,16 +150,31 @@ def test_sorted_queues_equal_unsorted(small_box, flags):
     assert out[0].tobytes() == out[1].tobytes()
 
 
-@pytest.fixture(scope="module", params=["specular", "glossy"])
+@pytest.fixture(scope="module", params=["specular", "glossy", "lights"])
 def material_box(request):
     """Mirror and glass blobs (conductor and dielectric Fresnel, refraction, total
-    internal reflection), or those plus plastic blobs and walls (lobe choice, Blinn
-    sampling, glossy next-event estimation)."""
+    internal reflection); those plus plastic blobs and walls (lobe choice, Blinn
+    sampling, glossy next-event estimation); or the latter lit by area, point and spot
+    lights (generic lights, delta-light sampling)."""
     if request.param == "specular":
         tris, mats, lights = scenes.specular_box_scene(n_blobs=8, subdiv=8, seed=1)
     else:
         tris, mats, lights = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+        if request.param == "lights":
+            lights = scenes.mixed_lights(lights)
     return tris, mats, lights, scenes.box_camera()
+
+
+def test_unknown_light_kind_is_rejected():
+    from visionaray_gb300.types import LIGHT
+    tris, mats, area = scenes.box_scene(n_blobs=1, subdiv=4, seed=1)
+    lights = scenes.mixed_lights(area)
+    lights["kind"][2] = 7
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    from visionaray_gb300.runtime import GbrtError
+    with pytest.raises(GbrtError, match="unknown light kind"):
+        vg.PTScene(bvh, mats, lights)
+    assert np.asarray(lights).dtype == LIGHT
 
 
 def test_materials_reference_mode_matches_fp32_oracle(oracle, material_box):

@@ -77,6 +77,61 @@ def test_golden_material_images(oracle, golden, name):
         assert (np.abs(img - ref).max(axis=2) == 0).mean() > 0.5
 
 
+def test_golden_point_and_spot_lights(oracle, golden):
+    """Area, point and spot lights (generic_light) against the reference kernel's image."""
+    meta, samples = golden
+    g = meta["pathtrace_lights"]
+    tris, mats, area = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+    lights = scenes.mixed_lights(area)
+    assert digest(lights) == g["lights_sha256"] and digest(mats) == g["materials_sha256"]
+    pr = g["params"]
+    params = scenes.pt_params(pr["width"], pr["height"], pr["spp"], num_bounces=pr["num_bounces"],
+                              epsilon=pr["epsilon"], frame_id=pr["frame_id"])
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, scenes.box_camera(), params,
+                              mode=Oracle.PT_FLOAT)
+    img = img.astype(np.float32)
+    ref = samples["pt_lights_image"]
+    if Reference.available():
+        assert np.array_equal(img, ref)
+    else:
+        assert np.allclose(img.reshape(-1, 4).mean(0), ref.reshape(-1, 4).mean(0), rtol=0.03)
+        assert (np.abs(img - ref).max(axis=2) == 0).mean() > 0.5
+
+
+@pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+@pytest.mark.parametrize("frame,spp,bounces", [(0, 2, 8), (5, 3, 3), (9, 1, 1)])
+def test_fp32_oracle_is_the_reference_kernel_lights(oracle, frame, spp, bounces):
+    tris, mats, area = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+    lights = scenes.mixed_lights(area)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(40, 24, spp, num_bounces=bounces, frame_id=frame)
+    ref = Reference().pathtrace(tris, mats, lights, cam, params)
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT)
+    assert np.array_equal(img.astype(np.float32), ref)
+
+
+@pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+def test_reference_spot_light_adds_nothing(oracle):
+    """spot_light::sample evaluates its cone at its own position (normalize(0) = NaN):
+    the reference's image does not change with the spot light's power or position,
+    and neither does the oracle's."""
+    from visionaray_gb300.types import LIGHT_SPOT
+    tris, mats, area = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+    lights = scenes.mixed_lights(area)
+    other = lights.copy()
+    spot = other["kind"] == LIGHT_SPOT
+    other["kl"][spot] = 100.0
+    other["position"][spot] = (0.5, 0.5, 0.5)
+    params = scenes.pt_params(32, 16, 2, num_bounces=4, frame_id=3)
+    cam = scenes.box_camera()
+    a = Reference().pathtrace(tris, mats, lights, cam, params)
+    assert np.array_equal(a, Reference().pathtrace(tris, mats, other, cam, params))
+    tree = oracle.build_sah(tris)
+    o1, _ = oracle.pathtrace(tree, tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT)
+    o2, _ = oracle.pathtrace(tree, tris, mats, other, cam, params, mode=Oracle.PT_FLOAT)
+    assert np.array_equal(o1, o2)
+
+
 @pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
 @pytest.mark.parametrize("name", sorted(MATERIAL_SCENES))
 @pytest.mark.parametrize("frame,spp,bounces", [(0, 2, 8), (5, 3, 3), (9, 1, 1)])
@@ -143,7 +198,8 @@ def test_shadow_range_fix_makes_fp32_and_fp64_agree(oracle, small_box):
     assert cnt[0] > 48 * 32 * 4 and cnt[1] > 0
 
 
-def test_oracle_adjoint_through_specular_vertices(oracle):
+@pytest.mark.parametrize("light_set", ["area", "mixed"])
+def test_oracle_adjoint_through_specular_vertices(oracle, light_set):
     """The FP64 host adjoint on a box with mirror, glass and plastic blobs and plastic
     walls against central differences of the FP64 forward pass at common random
     numbers (roulette off, shadow range fixed, so the image is smooth in the albedos):
@@ -151,6 +207,8 @@ def test_oracle_adjoint_through_specular_vertices(oracle):
     plastic vertex's next-event term through its MIS weight and the light's emission."""
     from visionaray_gb300 import inverse
     tris, mats, lights = scenes.glossy_box_scene(n_blobs=5, subdiv=4, seed=1)
+    if light_set == "mixed":
+        lights = scenes.mixed_lights(lights)   # point and spot lights: no emission parameter
     cam = scenes.box_camera()
     params = scenes.pt_params(32, 24, 2, num_bounces=6, frame_id=7, flags=inverse.FLAGS)
     tree = oracle.build_sah(tris)

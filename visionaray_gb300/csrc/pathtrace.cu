@@ -22,6 +22,8 @@
 
 #include "pt_shade.cuh"
 
+#include <cmath>
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -636,22 +638,62 @@ gbrt_status frame_buffers_for(gbrt_context* ctx, uint32_t n, frame_buffers& fb)
 
 using namespace gbrt;
 
-extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_material const* h_materials,
-                                            uint32_t num_materials, gbrt_area_light const* h_lights,
-                                            uint32_t num_lights, gbrt_pt_scene** out)
+namespace gbrt {
+namespace {
+
+// The device record of an area light: 4 float4 = v1 (w: the triangle's geom_id bits),
+// e1 (w: 0), e2, intensity cl * kl (w: kl), as area_light::intensity
+// (area_light.inl:22-25).
+void area_record(gbrt_triangle const& t, const float cl[3], float kl, float4* r)
 {
-    if (!ctx) return GBRT_ERR_INVALID_ARG;
-    if (!out || !bvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null bvh or output");
-    *out = nullptr;
-    if ((num_materials && !h_materials) || (num_lights && !h_lights))
-        return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null material or light array");
+    uint32_t lg = t.geom_id;
+    r[0] = make_float4(t.v1[0], t.v1[1], t.v1[2], 0.0f);
+    memcpy(&r[0].w, &lg, 4);
+    r[1] = make_float4(t.e1[0], t.e1[1], t.e1[2], 0.0f);
+    r[2] = make_float4(t.e2[0], t.e2[1], t.e2[2], 0.0f);
+    r[3] = make_float4(cl[0] * kl, cl[1] * kl, cl[2] * kl, kl);
+}
+
+// The device record of a point or spot light: position (w: no geom_id), e1.w = 1
+// marks a delta light, and the sample's intensity: intensity(pos) * pi evaluated, as
+// point_light::sample and spot_light::sample do, at pos = the light's own position
+// (point_light.inl:16-56, spot_light.inl:14-62), in the reference's float arithmetic.
+void delta_record(gbrt_light const& l, float4* r)
+{
+    const float pi = 3.14159265358979323846264338328e+00f;
+    const float d[3] = { l.position[0] - l.position[0], l.position[1] - l.position[1], l.position[2] - l.position[2] };
+    const float dist = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const float att = float(1.0 / (l.attenuation[0] + l.attenuation[1] * dist + l.attenuation[2] * dist * dist));
+    float spot = 1.0f;
+    if (l.kind == GBRT_LIGHT_SPOT)
+    {
+        // light_dir = position - pos = 0: normalize(-light_dir) = 0 * (1 / sqrt(0))
+        const float nd[3] = { -d[0], -d[1], -d[2] };
+        const float inv = 1.0f / std::sqrt(nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2]);
+        const float c = l.spot_direction[0] * (nd[0] * inv) + l.spot_direction[1] * (nd[1] * inv) +
+                        l.spot_direction[2] * (nd[2] * inv);
+        spot = c > std::cos(l.spot_cutoff) ? std::pow(c, l.spot_exponent) : 0.0f;
+    }
+    float in[3];
+    for (int c = 0; c < 3; ++c) in[c] = ((l.cl[c] * l.kl) * att * spot) * pi;
+    const uint32_t none = 0xFFFFFFFFu;
+    r[0] = make_float4(l.position[0], l.position[1], l.position[2], 0.0f);
+    memcpy(&r[0].w, &none, 4);
+    r[1] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    r[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    r[3] = make_float4(in[0], in[1], in[2], l.kl);
+}
+
+gbrt_status create_scene(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_material const* h_materials,
+                         uint32_t num_materials, std::vector<float4> const& light_records, gbrt_pt_scene** out)
+{
     device_guard g(ctx->device);
     auto* sc = new (std::nothrow) gbrt_pt_scene;
     if (!sc) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "pt_scene_create: host allocation");
     sc->bvh = bvh;
     sc->device = ctx->device;
     sc->num_materials = num_materials;
-    sc->num_lights = num_lights;
+    sc->num_lights = uint32_t(light_records.size() / 4);
     for (uint32_t k = 0; k < num_materials; ++k)
     {
         const uint32_t kind = h_materials[k].kind;
@@ -674,23 +716,12 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
             return check_cuda(ctx, e, "pt_scene_create: materials");
         }
     }
-    if (num_lights)
+    if (!light_records.empty())
     {
-        std::vector<float4> l(size_t(num_lights) * 4);
-        for (uint32_t k = 0; k < num_lights; ++k)
-        {
-            gbrt_triangle const& t = h_lights[k].geometry;
-            uint32_t lg = t.geom_id;
-            l[4 * k + 0] = make_float4(t.v1[0], t.v1[1], t.v1[2], 0.0f);
-            memcpy(&l[4 * k + 0].w, &lg, 4);
-            l[4 * k + 1] = make_float4(t.e1[0], t.e1[1], t.e1[2], 0.0f);
-            l[4 * k + 2] = make_float4(t.e2[0], t.e2[1], t.e2[2], 0.0f);
-            // area_light::intensity = cl * kl (area_light.inl:22-25)
-            l[4 * k + 3] = make_float4(h_lights[k].cl[0] * h_lights[k].kl, h_lights[k].cl[1] * h_lights[k].kl,
-                                       h_lights[k].cl[2] * h_lights[k].kl, h_lights[k].kl);
-        }
-        cudaError_t e = cudaMalloc(&sc->lights, l.size() * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMemcpy(sc->lights, l.data(), l.size() * sizeof(float4), cudaMemcpyHostToDevice);
+        cudaError_t e = cudaMalloc(&sc->lights, light_records.size() * sizeof(float4));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sc->lights, light_records.data(), light_records.size() * sizeof(float4),
+                           cudaMemcpyHostToDevice);
         if (e != cudaSuccess)
         {
             cleanup();
@@ -699,6 +730,48 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
     }
     *out = sc;
     return GBRT_OK;
+}
+
+} // namespace
+} // namespace gbrt
+
+extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_material const* h_materials,
+                                            uint32_t num_materials, gbrt_area_light const* h_lights,
+                                            uint32_t num_lights, gbrt_pt_scene** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out || !bvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null bvh or output");
+    *out = nullptr;
+    if ((num_materials && !h_materials) || (num_lights && !h_lights))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null material or light array");
+    std::vector<float4> rec(size_t(num_lights) * 4);
+    for (uint32_t k = 0; k < num_lights; ++k)
+        area_record(h_lights[k].geometry, h_lights[k].cl, h_lights[k].kl, &rec[4 * k]);
+    return create_scene(ctx, bvh, h_materials, num_materials, rec, out);
+}
+
+extern "C" gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh const* bvh,
+                                                   gbrt_material const* h_materials, uint32_t num_materials,
+                                                   gbrt_light const* h_lights, uint32_t num_lights,
+                                                   gbrt_pt_scene** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out || !bvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: null bvh or output");
+    *out = nullptr;
+    if ((num_materials && !h_materials) || (num_lights && !h_lights))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: null material or light array");
+    std::vector<float4> rec(size_t(num_lights) * 4);
+    for (uint32_t k = 0; k < num_lights; ++k)
+    {
+        gbrt_light const& l = h_lights[k];
+        if (l.kind == GBRT_LIGHT_AREA)
+            area_record(l.geometry, l.cl, l.kl, &rec[4 * k]);
+        else if (l.kind == GBRT_LIGHT_POINT || l.kind == GBRT_LIGHT_SPOT)
+            delta_record(l, &rec[4 * k]);
+        else
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: unknown light kind");
+    }
+    return create_scene(ctx, bvh, h_materials, num_materials, rec, out);
 }
 
 extern "C" gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint32_t width, uint32_t height, float* out)

@@ -471,79 +471,99 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
     }
     rec.kind = specular ? kVertexSpecular : (plastic ? kVertexPlastic : kVertexMatte);
     v3 nn = faceforward3(sn, view, gn);
-    if (sp.num_lights > 0 && specular)
+    if (sp.num_lights > 0)
     {
-        // the reference samples a light here too (three draws) but a specular
-        // surface's shade() is 0, so the next-event contribution is zero
-        st.k += 3;
-    }
-    else if (sp.num_lights > 0)
-    {
-        // sample_random_light + area_light::sample + sample_surface
-        // (sampling.h:195-213, area_light.inl:27-53, triangle.inl:69-83)
+        // sample_random_light (sampling.h:195-213) and the light's sample: an area light
+        // (area_light.inl:27-53, sample_surface triangle.inl:69-83) draws two numbers, a
+        // point or spot light (point_light.inl:35-56) three for a normal it does not use
         float ul = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
         int lid = int(ul * float(sp.num_lights));
         if (lid >= int(sp.num_lights)) lid = int(sp.num_lights) - 1;
         const float4* lp = sp.lights + 4 * lid;
-        float4 l0 = lp[0], l3 = lp[3];
-        v3 lv1 = xyz(l0), le1 = xyz(lp[1]), le2 = xyz(lp[2]), lint = xyz(l3);
-        uint32_t lgeom = __float_as_uint(l0.w);
-        if (sp.emission && lgeom < sp.num_materials) lint = param3(sp.emission, lgeom) * l3.w;
-        float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
-        float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
-        v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
-        float sq = sqrtf(s1);
-        v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
-        v3 ldir = pos - isect;
-        float dist = length3(ldir);
-        v3 lnormal = normalize3(cross3(le1, le2));
-        float larea = 0.5f * length3(cross3(le1, le2));
-        float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
-        float lsolid = (ldotln0 * larea) / (dist * dist);
-        float lpdf = 1.0f / lsolid;
-        v3 L = normalize3(ldir);
-        v3 ln = faceforward3(lnormal, -L, lnormal);
-        float ldotn = dot3(L, nn);
-        float ldotln = fabsf(dot3(-L, ln));
-        float bpdf0 = dot3(nn, L) * inv_pi;
-        v3 cd = (mcol * m.scale) * inv_pi;
-        v3 brdf = cd;
-        if (plastic)
+        const float4 l0 = lp[0], l1 = lp[1], l3 = lp[3];
+        const bool delta = l1.w != 0.0f;
+        if (specular)
         {
-            nee_terms nt = plastic_nee(sp.materials + geom, nn, view, L, cd, glossy ? 1u : 0u);
-            bpdf0 = nt.pdf;
-            brdf = nt.brdf;
+            // a specular surface's shade() is 0: the light is sampled (its draws taken)
+            // but the next-event contribution is zero
+            st.k += delta ? 3u : 2u;
         }
-        float bpdf = bpdf0 * max_elem(st.thr);
-        float ndotl = fmaxf(0.0f, dot3(nn, L));
-        // (plastic::shade, plastic.inl:20-39: (diffuse + Blinn) * pi * intensity * n.l)
-        v3 shade = ((brdf * pi) * lint) * ndotl;
-        v3 src2 = (shade * inv_pi) / ldotn;
-        float x = lpdf / float(sp.num_lights);
-        float mis2 = power_heuristic(x, bpdf);
-        if (ldotn > 0.0f && ldotln > 0.0f)
+        else
         {
-            out.contrib = (((st.thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
-            out.shadow = true;
-            out.sh_o = isect + L * sp.epsilon;
-            out.sh_d = L;
-            out.sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon : dist - sp.epsilon;
-            rec.nee = 1;
-            rec.lgeom = sp.emission ? lgeom : 0xFFFFFFFFu;
-            rec.kl = l3.w;
-            rec.lint = lint;
-            rec.w = mis2;
-            rec.x = x;
-            rec.b0 = bpdf0;
-            // contribution = w * thr * albedo * lint * kfac (matte), w * thr * gnee * lint (plastic)
-            if (plastic)
+            v3 lint = xyz(l3);
+            uint32_t lgeom = __float_as_uint(l0.w);
+            if (sp.emission && lgeom < sp.num_materials) lint = param3(sp.emission, lgeom) * l3.w;
+            v3 ldir, L, ln;
+            float dist, lpdf;
+            if (delta)
             {
-                rec.gnee = brdf * (pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights));
+                st.k += 3;
+                ldir = xyz(l0) - isect;
+                dist = length3(ldir);
+                lpdf = 1.0f;
+                L = normalize3(ldir);
+                ln = faceforward3(-L, -L, -L);   // select(delta_light, -L, normal), faceforwarded
             }
             else
             {
-                const float kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
-                rec.gnee = { kfac, kfac, kfac };
+                v3 lv1 = xyz(l0), le1 = xyz(l1), le2 = xyz(lp[2]);
+                float s1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+                float s2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
+                v3 lv2 = lv1 + le1, lv3 = lv1 + le2;
+                float sq = sqrtf(s1);
+                v3 pos = lv1 * (1.0f - sq) + lv2 * sq * (1.0f - s2) + lv3 * sq * s2;
+                ldir = pos - isect;
+                dist = length3(ldir);
+                v3 lnormal = normalize3(cross3(le1, le2));
+                float larea = 0.5f * length3(cross3(le1, le2));
+                float ldotln0 = fabsf(dot3(-normalize3(ldir), lnormal));
+                float lsolid = (ldotln0 * larea) / (dist * dist);
+                lpdf = 1.0f / lsolid;
+                L = normalize3(ldir);
+                ln = faceforward3(lnormal, -L, lnormal);
+            }
+            float ldotn = dot3(L, nn);
+            float ldotln = fabsf(dot3(-L, ln));
+            float bpdf0 = dot3(nn, L) * inv_pi;
+            v3 cd = (mcol * m.scale) * inv_pi;
+            v3 brdf = cd;
+            if (plastic)
+            {
+                nee_terms nt = plastic_nee(sp.materials + geom, nn, view, L, cd, glossy ? 1u : 0u);
+                bpdf0 = nt.pdf;
+                brdf = nt.brdf;
+            }
+            float bpdf = bpdf0 * max_elem(st.thr);
+            float ndotl = fmaxf(0.0f, dot3(nn, L));
+            // (plastic::shade, plastic.inl:20-39: (diffuse + Blinn) * pi * intensity * n.l)
+            v3 shade = ((brdf * pi) * lint) * ndotl;
+            v3 src2 = (shade * inv_pi) / ldotn;
+            float x = lpdf / float(sp.num_lights);
+            float mis2 = power_heuristic(x, bpdf);
+            if (ldotn > 0.0f && ldotln > 0.0f)
+            {
+                out.contrib = (((st.thr * mis2) * src2) * (ldotn / lpdf)) * float(sp.num_lights);
+                out.shadow = true;
+                out.sh_o = isect + L * sp.epsilon;
+                out.sh_d = L;
+                out.sh_tmax = (sp.flags & GBRT_PT_SHADOW_RANGE_FIX) ? dist - sp.epsilon - sp.epsilon : dist - sp.epsilon;
+                rec.nee = 1;
+                rec.lgeom = sp.emission ? lgeom : 0xFFFFFFFFu;
+                rec.kl = l3.w;
+                rec.lint = lint;
+                rec.w = mis2;
+                rec.x = x;
+                rec.b0 = bpdf0;
+                // contribution = w * thr * albedo * lint * kfac (matte), w * thr * gnee * lint (plastic)
+                if (plastic)
+                {
+                    rec.gnee = brdf * (pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights));
+                }
+                else
+                {
+                    const float kfac = m.scale * inv_pi * pi * ndotl * inv_pi / ldotn * (ldotn / lpdf) * float(sp.num_lights);
+                    rec.gnee = { kfac, kfac, kfac };
+                }
             }
         }
     }

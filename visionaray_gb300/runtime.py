@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, HIT_INST, INSTANCE, MATERIAL, PT_PARAMS, RAY,
+from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, HIT_INST, INSTANCE, LIGHT, MATERIAL, PT_PARAMS, RAY,
                     TRIANGLE)
 
 LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
@@ -51,6 +51,7 @@ SIGNATURES = {
     "gbrt_trace_closest_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_trace_any_hit_host": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_pt_scene_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
+    "gbrt_pt_scene_create_lights": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_pt_scene_destroy": (_i32, [_vp]),
     "gbrt_pinhole_camera_basis": (_i32, [_vp, _u32, _u32, _vp]),
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
@@ -318,15 +319,20 @@ def any_hit(rays, bvh, out=None):
 
 class PTScene:
     """make_kernel_params(prims, materials, lights, ...) counterpart: a BVH with its
-    materials (one per geom_id) and area lights, ready for pathtrace_frame."""
+    materials (one per geom_id) and lights -- AREA_LIGHT records, or LIGHT records
+    (area, point and spot lights) -- ready for pathtrace_frame."""
 
     def __init__(self, bvh, materials, lights):
         self.bvh, self.ctx = bvh, bvh.ctx
         mats = np.ascontiguousarray(materials, MATERIAL)
-        lts = np.ascontiguousarray(lights, AREA_LIGHT)
         h = ctypes.c_void_p()
-        self.ctx.check(self.ctx.lib.gbrt_pt_scene_create(self.ctx.h, bvh.h, _hptr(mats), len(mats), _hptr(lts),
-                                                         len(lts), ctypes.byref(h)))
+        if np.asarray(lights).dtype == LIGHT:
+            lts = np.ascontiguousarray(lights, LIGHT)
+            create = self.ctx.lib.gbrt_pt_scene_create_lights
+        else:
+            lts = np.ascontiguousarray(lights, AREA_LIGHT)
+            create = self.ctx.lib.gbrt_pt_scene_create
+        self.ctx.check(create(self.ctx.h, bvh.h, _hptr(mats), len(mats), _hptr(lts), len(lts), ctypes.byref(h)))
         self.h = h
 
     def close(self):

@@ -159,6 +159,26 @@ def glossy_box_scene(n_blobs=10, subdiv=8, seed=1, light_y=0.999, emission=15.0)
     return tris, mats, lights
 
 
+def mixed_lights(area_lights):
+    """The box's area lights plus two point lights and a spot light (LIGHT records):
+    a warm point light at (0.3, 0.7, 0.5) with attenuation (1, 0.5, 0.25), a green one
+    at (0.6, 0.3, 0.7) with (2, 0, 1), and a blue spot at (0.7, 0.6, 0.4) aimed down
+    (cutoff 0.8 rad, exponent 4), which the reference's sampling leaves dark."""
+    from .types import LIGHT, LIGHT_POINT, LIGHT_SPOT, lights_of_area_lights
+    area = lights_of_area_lights(area_lights)
+    out = np.zeros(len(area) + 3, LIGHT)
+    out[:len(area)] = area
+    pt, sp, pt2 = out[len(area)], out[len(area) + 1], out[len(area) + 2]
+    pt["kind"], pt["cl"], pt["kl"], pt["position"], pt["attenuation"] = (
+        LIGHT_POINT, (1.0, 0.8, 0.6), 0.4, (0.3, 0.7, 0.5), (1.0, 0.5, 0.25))
+    sp["kind"], sp["cl"], sp["kl"], sp["position"], sp["attenuation"] = (
+        LIGHT_SPOT, (0.5, 0.5, 1.0), 2.0, (0.7, 0.6, 0.4), (1.0, 0.0, 0.0))
+    sp["spot_direction"], sp["spot_cutoff"], sp["spot_exponent"] = (0.0, -1.0, 0.0), 0.8, 4.0
+    pt2["kind"], pt2["cl"], pt2["kl"], pt2["position"], pt2["attenuation"] = (
+        LIGHT_POINT, (0.2, 1.0, 0.3), 1.0, (0.6, 0.3, 0.7), (2.0, 0.0, 1.0))
+    return out
+
+
 def box_camera(eye=(0.5, 0.5, 0.02), center=(0.5, 0.5, 1.0), up=(0.0, 1.0, 0.0), fovy_degrees=60.0):
     """Camera inside the closed box, near the front wall, looking at the back wall."""
     from .types import CAMERA

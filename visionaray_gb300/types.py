@@ -21,6 +21,21 @@ MATERIAL = np.dtype([("kind", "<u4"), ("color", "<f4", (3,)), ("scale", "<f4"), 
                      ("absorption", "<f4", (3,)), ("color2", "<f4", (3,)), ("scale2", "<f4"),
                      ("exponent", "<f4")])
 AREA_LIGHT = np.dtype([("geometry", TRIANGLE), ("cl", "<f4", (3,)), ("kl", "<f4")])
+LIGHT = np.dtype([("kind", "<u4"), ("cl", "<f4", (3,)), ("kl", "<f4"), ("geometry", TRIANGLE),
+                  ("position", "<f4", (3,)), ("attenuation", "<f4", (3,)), ("spot_direction", "<f4", (3,)),
+                  ("spot_cutoff", "<f4"), ("spot_exponent", "<f4")])
+LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT = 0, 1, 2
+
+
+def lights_of_area_lights(area_lights):
+    """AREA_LIGHT records as LIGHT records of kind LIGHT_AREA."""
+    a = np.asarray(area_lights, AREA_LIGHT).reshape(-1)
+    out = np.zeros(len(a), LIGHT)
+    out["kind"] = LIGHT_AREA
+    out["geometry"], out["cl"], out["kl"] = a["geometry"], a["cl"], a["kl"]
+    return out
+
+
 CAMERA = np.dtype([("eye", "<f4", (3,)), ("center", "<f4", (3,)), ("up", "<f4", (3,)),
                    ("fovy_degrees", "<f4")])
 PT_PARAMS = np.dtype([("width", "<u4"), ("height", "<u4"), ("spp", "<u4"), ("num_bounces", "<u4"),
