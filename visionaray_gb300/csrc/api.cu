@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <new>
+#include <vector>
 
 namespace gbrt {
 
@@ -98,14 +99,46 @@ gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
     return GBRT_OK;
 }
 
+// The chunk sizes of a host-buffer query of n rays with full chunks of c: a quarter
+// chunk first and last (the copy-in before the first traversal and the copy-out after
+// the last one overlap nothing), full chunks between.  Queries of at most 2c rays are
+// split into a quarter, the middle and a quarter.
+std::vector<size_t> host_chunks(size_t n, size_t c)
+{
+    std::vector<size_t> out;
+    const size_t q = c / 4;
+    if (n <= 2 * q)
+    {
+        out.push_back(n);
+        return out;
+    }
+    out.push_back(q);
+    size_t rest = n - q;
+    while (rest > c + q)
+    {
+        out.push_back(c);
+        rest -= c;
+    }
+    if (rest > q)
+    {
+        out.push_back(rest - q);
+        out.push_back(q);
+    }
+    else
+    {
+        out.push_back(rest);
+    }
+    return out;
+}
+
 // Host-buffer trace: chunks alternate between the slots, each on its own stream, so
 // the copy-in of one chunk overlaps the traversal and copy-out of the others.
-constexpr int kHostChunkLog2 = 22;   // 4M rays (128 MB) per chunk
 gbrt_status trace_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h_rays, uint32_t n, gbrt_hit* h_hits,
                        bool any_hit)
 {
     if (n == 0) return GBRT_OK;
-    const size_t chunk = std::min<size_t>(n, size_t(1) << kHostChunkLog2);   // rays per slot
+    const std::vector<size_t> sizes = host_chunks(n, ctx->host_chunk);
+    const size_t chunk = *std::max_element(sizes.begin(), sizes.end());   // rays per slot
     gbrt_status st = ensure_slots(ctx, chunk);
     if (st != GBRT_OK) return st;
     // work queued on the context stream (e.g. the build) must finish first
@@ -113,12 +146,12 @@ gbrt_status trace_host(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* h
     GBRT_CUDA(ctx, cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     GBRT_CUDA(ctx, cudaEventRecord(ready, ctx->stream));
     for (int k = 0; k < gbrt_context::kSlots; ++k) GBRT_CUDA(ctx, cudaStreamWaitEvent(ctx->slot_stream[k], ready, 0));
-    int c = 0;
-    for (size_t b = 0; b < n; b += chunk, ++c)
+    size_t b = 0;
+    for (size_t c = 0; c < sizes.size(); b += sizes[c], ++c)
     {
-        int k = c % gbrt_context::kSlots;
+        int k = int(c % gbrt_context::kSlots);
         cudaStream_t s = ctx->slot_stream[k];
-        uint32_t m = uint32_t(std::min<size_t>(chunk, n - b));
+        uint32_t m = uint32_t(sizes[c]);
         GBRT_CUDA(ctx, cudaMemcpyAsync(ctx->slot_rays[k], h_rays + b, size_t(m) * sizeof(gbrt_ray),
                                        cudaMemcpyHostToDevice, s));
         st = trace(ctx, bvh, static_cast<gbrt_ray*>(ctx->slot_rays[k]), m, static_cast<gbrt_hit*>(ctx->slot_hits[k]),
@@ -214,6 +247,15 @@ gbrt_status gbrt_context_set_trace_refill(gbrt_context* ctx, uint32_t min_idle_l
     if (min_idle_lanes < 1 || min_idle_lanes > 32)
         return fail(ctx, GBRT_ERR_INVALID_ARG, "set_trace_refill: 1 to 32 lanes");
     ctx->trace_refill = min_idle_lanes;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_set_host_chunk(gbrt_context* ctx, uint32_t rays)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (rays < (1u << 16) || rays > (1u << 26))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_host_chunk: 2^16 to 2^26 rays");
+    ctx->host_chunk = rays;
     return GBRT_OK;
 }
 

@@ -36,6 +36,7 @@ SIGNATURES = {
     "gbrt_kernel_launch_count": (_u64, [_vp]),
     "gbrt_context_set_trace_flags": (_i32, [_vp, _u32]),
     "gbrt_context_set_trace_refill": (_i32, [_vp, _u32]),
+    "gbrt_context_set_host_chunk": (_i32, [_vp, _u32]),
     "gbrt_bvh_build_lbvh": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_build_lbvh_host": (_i32, [_vp, _vp, _u32, _pp]),
     "gbrt_bvh_build_ploc": (_i32, [_vp, _vp, _u32, _pp]),
@@ -148,6 +149,10 @@ class Context:
     def set_trace_refill(self, min_idle_lanes):
         """Persistent traversal: idle lanes of a warp that trigger a refill (1..32)."""
         self.check(self.lib.gbrt_context_set_trace_refill(self.h, int(min_idle_lanes)))
+
+    def set_host_chunk(self, rays):
+        """Rays per chunk of the host-buffer queries (2^16 .. 2^26, default 2^22)."""
+        self.check(self.lib.gbrt_context_set_host_chunk(self.h, int(rays)))
 
     @property
     def launches(self):
