@@ -65,6 +65,24 @@ def test_host_buffer_path_equals_device_path(soup_case):
     assert ((host_any["prim_id"] != NO_HIT) == (trace(bvh, rays, True)["prim_id"] != NO_HIT)).all()
 
 
+@pytest.mark.parametrize("chunk", [1 << 16, 1 << 17])
+def test_host_buffer_path_in_chunks(soup_case, chunk):
+    """Small host chunks: the query runs as a quarter chunk, full chunks, the rest and
+    a quarter chunk on alternating slots; hits equal the device path's bit for bit."""
+    tris, rays, _, _, _ = soup_case
+    ctx = vg.Context(0)
+    ctx.set_host_chunk(chunk)
+    bvh = vg.lbvh_builder(ctx).build(tris)
+    dev = trace(bvh, rays)
+    assert len(rays) > 4 * chunk
+    host = vg.closest_hit(rays, bvh)
+    assert host.tobytes() == dev.tobytes()
+    odd = rays[: 2 * chunk + 12345]
+    assert vg.closest_hit(odd, bvh).tobytes() == dev[: len(odd)].tobytes()
+    with pytest.raises(vg.runtime.GbrtError):
+        ctx.set_host_chunk(1000)
+
+
 @pytest.mark.parametrize("grid", [64, 512])
 def test_heightfield_secondary_and_ao(oracle, grid):
     tris = scenes.heightfield(grid=grid, seed=1)

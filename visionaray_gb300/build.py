@@ -82,7 +82,7 @@ def build(verbose=False, with_reference=True):
         objs.append(o)
         if _stale(o, [s] + headers):
             jobs.append((src, [NVCC] + NVCC_FLAGS + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o]))
-    scenes_srcs = [os.path.join(CSRC, "scenes.cpp"), os.path.join(CSRC, "obj.cpp")]
+    scenes_srcs = [os.path.join(CSRC, "scenes.cpp"), os.path.join(CSRC, "obj.cpp"), os.path.join(CSRC, "ply.cpp")]
     if _stale(LIBSCENES, scenes_srcs + [os.path.join(CSRC, "scenes.h")]):
         jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
                                 "-ffp-contract=off", "-Wall"] + scenes_srcs + ["-o", LIBSCENES]))

@@ -73,6 +73,15 @@ int64_t gbrt_obj_load(const char* path, gbrt_triangle* out, uint64_t capacity);
  * count, -1 when the file cannot be read.                                          */
 int64_t gbrt_obj_materials(const char* path, gbrt_material* out, uint64_t capacity);
 
+/* Stanford PLY ingestion (the reference viewer's load_ply, src/common/
+ * ply_loader.cpp): the vertex element's x, y, z and the face element's
+ * vertex_indices, triangles (v1, e1, e2) without a degeneracy test, prim_id = running
+ * index, geom_id = 0; faces of more than three vertices as fans.  ascii and binary
+ * (either byte order) bodies.  Writes up to `capacity` triangles to out (may be NULL)
+ * and returns the triangle count, -1 when the file cannot be read or is malformed
+ * (including a face index outside the vertex list).                               */
+int64_t gbrt_ply_load(const char* path, gbrt_triangle* out, uint64_t capacity);
+
 /* Uniform float in [0,1) of the counter-based generator used above (exposed so that
  * tests can reproduce any value).                                                  */
 float gbrt_scene_u01(uint64_t seed, uint64_t stream, uint64_t index);

@@ -240,6 +240,25 @@ def batch_workload(num_scenes=512, seed=3, n_min=1000, n_max=1_000_000, spp=1, n
     return tris, offsets, cams, params, mats
 
 
+def load_ply(path):
+    """Triangles of a Stanford PLY file (ascii or binary), as the reference viewer's
+    loader reads them: the vertex element's x, y, z and the face element's
+    vertex_indices, geom_id 0, faces of more than three vertices as fans.  Raises
+    ValueError for an unreadable or malformed file."""
+    lib = _load()
+    if not hasattr(lib.gbrt_ply_load, "_typed"):
+        lib.gbrt_ply_load.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64]
+        lib.gbrt_ply_load.restype = ctypes.c_int64
+        lib.gbrt_ply_load._typed = True
+    p = str(path).encode()
+    n = lib.gbrt_ply_load(p, None, 0)
+    if n < 0:
+        raise ValueError(f"cannot read PLY file {path}")
+    tris = np.empty(n, TRIANGLE)
+    lib.gbrt_ply_load(p, _ptr(tris), n)
+    return tris
+
+
 def load_obj(path):
     """(triangles, materials) of a Wavefront OBJ file, as the reference viewer's loader
     reads its geometry (fans, negative indices, degenerate faces dropped, geom_id per
