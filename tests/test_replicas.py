@@ -66,6 +66,42 @@ def test_two_gloo_ranks():
     mp.spawn(_rank_main, args=(2, _free_port(), costs), nprocs=2, join=True)
 
 
+def test_split_samples():
+    assert replicas.split_samples(16, 1) == [16]
+    assert replicas.split_samples(16, 3) == [6, 5, 5]
+    assert replicas.split_samples(7, 7) == [1] * 7
+    assert sum(replicas.split_samples(256, 8)) == 256
+    with pytest.raises(ValueError):
+        replicas.split_samples(2, 3)
+
+
+def _samples_rank(rank, world, port, samples, grads):
+    """Each rank holds the per-sample images of its share of the samples and a partial
+    gradient; the all-rank mean image and summed gradient equal the single-process ones."""
+    os.environ.update({"WORLD_SIZE": str(world), "RANK": str(rank), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    import torch
+    import torch.distributed as dist
+    replicas.init("gloo")
+    counts = replicas.split_samples(len(samples), world)
+    first = sum(counts[:rank])
+    f64 = torch.float64
+    mine = torch.tensor(samples[first:first + counts[rank]], dtype=f64).mean(0)
+    image = replicas.mean_image_(mine.clone(), counts[rank], len(samples))
+    assert torch.allclose(image, torch.tensor(samples, dtype=f64).mean(0), rtol=1e-12, atol=1e-12)
+    g = replicas.all_reduce_sum_(torch.tensor(grads[rank], dtype=f64))
+    assert torch.allclose(g, torch.tensor(grads, dtype=f64).sum(0), rtol=1e-12, atol=1e-12)
+    dist.destroy_process_group()
+
+
+def test_sample_parallel_reductions_two_gloo_ranks():
+    import torch.multiprocessing as mp
+    rng = np.random.default_rng(11)
+    samples = rng.normal(size=(7, 3, 4, 4)).tolist()   # 7 samples of a 3x4 RGBA image
+    grads = rng.normal(size=(2, 5, 3)).tolist()
+    mp.spawn(_samples_rank, args=(2, _free_port(), samples, grads), nprocs=2, join=True)
+
+
 def test_reference_arm_other_ranks_exit_quietly():
     """Under torchrun the reference arm runs on rank 0 only; rank 1 exits 0 at once."""
     env = dict(os.environ, WORLD_SIZE="2", RANK="1", LOCAL_RANK="1", MASTER_ADDR="127.0.0.1")

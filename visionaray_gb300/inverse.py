@@ -46,8 +46,21 @@ def l2_adjoint(image, target):
 def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_spp=256, ctx=None, log=None,
              extra_flags=0, builder="lbvh"):
     """Adam on the albedos.  Returns a dict with the loss history, the parameter error
-    and the mean forward / backward times (CUDA events)."""
+    and the mean forward / backward times (CUDA events).
+
+    Under torch.distributed with N > 1 ranks (one GPU each) the step is data-parallel
+    over samples: rank r renders its replicas.split_samples(spp, N)[r] samples per
+    pixel with frame_id = step * N + r, the images are averaged by an all-reduce, every
+    rank back-propagates the common loss through its own samples, and the gradients
+    are summed by an all-reduce, so all ranks take the same Adam step.  With one rank
+    this is the single-GPU step (frame_id = step)."""
     import torch
+    import torch.distributed as dist
+
+    from . import replicas
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    rank = dist.get_rank() if world > 1 else 0
+    my_spp = replicas.split_samples(spp, world)[rank]
     ctx = ctx or rt.default_context()
     scene, tris, mats, lights, hidden, emission = setup(ctx=ctx, builder=builder)
     cam = scenes.box_camera()
@@ -61,11 +74,17 @@ def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_
     fwd_ms, bwd_ms, losses = [], [], []
     image = None
     for it in range(steps):
-        params = scenes.pt_params(width, height, spp, num_bounces=depth, frame_id=it, flags=FLAGS | extra_flags)
+        params = scenes.pt_params(width, height, my_spp, num_bounces=depth, frame_id=it * world + rank,
+                                  flags=FLAGS | extra_flags)
         ev[0].record(ctx.stream)
         image = rt.pathtrace_forward(scene, cam, params, albedo, emission, image=image)
         ev[1].record(ctx.stream)
+        if world > 1:
+            torch.cuda.synchronize()   # the collective runs on torch's stream
+            replicas.mean_image_(image, my_spp, spp)
         loss, adj = l2_adjoint(image, target)
+        if world > 1:
+            adj.mul_(float(my_spp) / float(spp))   # this rank's share of the mean image
         grad_a = torch.zeros_like(albedo)
         grad_e = torch.zeros_like(emission)
         ev[2].record(ctx.stream)
@@ -73,6 +92,9 @@ def optimize(steps=200, lr=0.02, width=512, height=512, spp=16, depth=6, target_
         rt.pathtrace_backward(scene, cam, params, albedo, emission, adj, grad_a, grad_e)
         e3.record(ctx.stream)
         torch.cuda.synchronize()
+        if world > 1:
+            replicas.all_reduce_sum_(grad_a)
+            replicas.all_reduce_sum_(grad_e)
         fwd_ms.append(ev[0].elapsed_time(ev[1]))
         bwd_ms.append(ev[2].elapsed_time(e3))
         losses.append(loss)

@@ -1,15 +1,17 @@
-"""Multi-GPU host logic of the benchmark: one process per GPU, no collective on the data
-path.
+"""Multi-GPU host logic: one process per GPU.
 
 Rays, pixels and whole scenes are independent (visionaray's schedulers hand every
 pixel to its own thread, detail/cuda_sched.inl:43-49), so nothing is exchanged between
-GPUs while tracing.  Two ways of using N GPUs follow from that:
+GPUs while tracing.  Three ways of using N GPUs follow:
   replicas   every rank runs the whole workload (the heightfield traversal, weak
              scaling); the job's rate is N x work / the slowest rank's time
   scenes     a batch of independent scenes is partitioned across ranks by cost
              (longest-processing-time greedy), each rank builds and renders its share
              (strong scaling of a fixed batch)
-The only collectives are on timings (a max over ranks), run outside the timed work.
+  samples    inverse rendering splits each step's samples per pixel across ranks
+             (split_samples); the one real exchange is an all-reduce of the rendered
+             image (weighted by samples) and of the parameter gradients per step
+Timings are reduced with a max over ranks, outside the timed work.
 Rendezvous: MASTER_ADDR defaults to 127.0.0.1.
 """
 import os
@@ -75,3 +77,27 @@ def scene_costs(offsets, params):
         work = int(p["width"]) * int(p["height"]) * int(p["spp"]) * max(int(p["num_bounces"]), 1)
         costs.append(tris + 4 * work)
     return costs
+
+
+def split_samples(spp, world):
+    """Samples per pixel of each rank when `spp` are split across `world` ranks: the
+    first spp % world ranks take one more.  Every rank computes the same list."""
+    if world < 1 or spp < world:
+        raise ValueError("need 1 <= world <= spp")
+    return [spp // world + (1 if r < spp % world else 0) for r in range(world)]
+
+
+def all_reduce_sum_(tensor):
+    """In-place sum of a tensor over all ranks (nothing on one rank)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(tensor, op=dist.ReduceOp.SUM)
+    return tensor
+
+
+def mean_image_(image, my_spp, total_spp):
+    """The all-rank image of a frame whose samples are split across ranks: each rank's
+    per-pixel mean over its `my_spp` samples, weighted by my_spp / total_spp and summed
+    in place (alpha included)."""
+    image.mul_(float(my_spp) / float(total_spp))
+    return all_reduce_sum_(image)
