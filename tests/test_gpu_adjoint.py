@@ -61,7 +61,11 @@ def test_adjoint_matches_central_differences(setup):
         a_m, e_m = (minus, emission) if kind == "a" else (albedo, minus)
         fd = (loss_of(scene, cam, params, a_p, e_p, adj) - loss_of(scene, cam, params, a_m, e_m, adj)) / step
         g = float((ga if kind == "a" else ge)[slot, c])
-        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6 * np.abs(ga).max(), (kind, slot, c, g, fd)
+        # 1e-3 relative, plus an absolute floor for the FP32 forward's rounding: each
+        # loss sums ~6,000 float32 pixel terms, whose rounding noise (~1e-7 relative
+        # each) divided by the 2e-3 step is ~5e-4 in the quotient, i.e. 1e-4 of the
+        # largest gradient (15) here
+        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-4 * np.abs(ga).max(), (kind, slot, c, g, fd)
 
 
 def test_adjoint_matches_host_adjoints(setup, oracle):

@@ -116,6 +116,7 @@ struct gbrt_batch
     uint32_t frames_set = 0;        // scenes whose frames are on the device (0 or num_scenes)
     gbrt_material* d_materials = nullptr;
     uint32_t num_materials = 0;
+    bool extended_materials = false;   // some material is a mirror, glass or plastic
     uint32_t* d_work = nullptr;     // persistent-kernel work counter
     gbrt_batch_launch launch = { 128, 32, 64, GBRT_BATCH_ORDER_ROWS };
     // the captured build + frame

@@ -61,7 +61,9 @@ constexpr int kBatchSharedStack = 8;
 // spill traffic, bounds it.
 constexpr int kBatchWarpsPerSM = 64;
 
-template <int Block, int Stack>
+// Extended = false: a material table of matte and emissive slots only (the other
+// materials' branches compiled out, as for the adjoint).
+template <int Block, int Stack, bool Extended>
 __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt(batch_args a)
 {
     const uint32_t full = 0xFFFFFFFFu;
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
                                                               a.total_tris, { o.x, o.y, o.z }, { d.x, d.y, d.z }, 0.0f,
                                                               FLT_MAX, a.status);
                     vertex_out out;
-                    shade_vertex(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, a.status);
+                    shade_vertex<Extended>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, a.status);
                     if (!out.cont) break;
                     o = out.next_o;
                     d = out.next_d;
@@ -139,33 +141,39 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
 
 using batch_kernel = void (*)(batch_args);
 
-template <int Block>
+template <int Block, bool Extended>
 batch_kernel pick_stack(uint32_t stack)
 {
     switch (stack)
     {
-    case 16: return batch_pt<Block, 16>;
-    case 24: return batch_pt<Block, 24>;
-    case 32: return batch_pt<Block, 32>;
-    case 64: return batch_pt<Block, 64>;
+    case 16: return batch_pt<Block, 16, Extended>;
+    case 24: return batch_pt<Block, 24, Extended>;
+    case 32: return batch_pt<Block, 32, Extended>;
+    case 64: return batch_pt<Block, 64, Extended>;
     default: return nullptr;
     }
 }
 
-batch_kernel pick_kernel(gbrt_batch_launch const& l)
+template <bool Extended>
+batch_kernel pick_block(gbrt_batch_launch const& l)
 {
     switch (l.block)
     {
-    case 128: return pick_stack<128>(l.stack);
-    case 256: return pick_stack<256>(l.stack);
-    case 512: return pick_stack<512>(l.stack);
+    case 128: return pick_stack<128, Extended>(l.stack);
+    case 256: return pick_stack<256, Extended>(l.stack);
+    case 512: return pick_stack<512, Extended>(l.stack);
     default: return nullptr;
     }
+}
+
+batch_kernel pick_kernel(gbrt_batch_launch const& l, bool extended)
+{
+    return extended ? pick_block<true>(l) : pick_block<false>(l);
 }
 
 bool launch_valid(gbrt_batch_launch const& l)
 {
-    return pick_kernel(l) != nullptr && (l.tile == 32 || l.tile == 64) &&
+    return pick_kernel(l, false) != nullptr && (l.tile == 32 || l.tile == 64) &&
            (l.order == GBRT_BATCH_ORDER_ROWS || l.order == GBRT_BATCH_ORDER_BLOCKS);
 }
 
@@ -176,7 +184,7 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     if (b->frames_set != b->num_scenes) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: frames not set");
     if (!d_images || (reinterpret_cast<uintptr_t>(d_images) & 15u))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: images null or not 16-byte aligned");
-    batch_kernel kernel = pick_kernel(b->launch);
+    batch_kernel kernel = pick_kernel(b->launch, b->extended_materials);
     if (!kernel) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: bad launch shape");
     int per_sm = 0;
     GBRT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, int(b->launch.block), 0));
@@ -266,6 +274,13 @@ extern "C" gbrt_status gbrt_batch_set_frames(gbrt_context* ctx, gbrt_batch* batc
         GBRT_CUDA(ctx, cudaMemcpy(batch->d_materials, h_materials, size_t(num_materials) * sizeof(gbrt_material),
                                   cudaMemcpyHostToDevice));
     batch->num_materials = num_materials;
+    batch->extended_materials = false;
+    for (uint32_t k = 0; k < num_materials; ++k)
+    {
+        const uint32_t kind = h_materials[k].kind;
+        batch->extended_materials |=
+            kind == GBRT_MATERIAL_MIRROR || kind == GBRT_MATERIAL_GLASS || kind == GBRT_MATERIAL_PLASTIC;
+    }
     batch->total_pixels = uint32_t(total);
     batch->frames_set = ns;
     batch->graph_dirty = true;
