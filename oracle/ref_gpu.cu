@@ -10,7 +10,9 @@
 //   closest_hit / any_hit over an index_bvh_ref_t (detail/traverse_linear.inl:156-225,
 //     whose device branch is the short-stack traversal of detail/bvh/intersect.inl:166-356)
 //   pathtracing::kernel::operator() (detail/pathtracing.inl:42-233) with
-//     generic_material<matte, emissive> per geom_id and triangle area lights, one thread
+//     generic_material<matte, emissive> per geom_id and triangle area lights (and an
+//     extended instantiation: generic_material<matte, emissive, mirror, glass, plastic>
+//     and generic_light<area_light, point_light, spot_light>), one thread
 //     per pixel as cuda_sched's render kernel runs it (detail/cuda_sched.inl:32-69),
 //     samples averaged and blended as sample_pixel_impl does (sched_common.h:427-526)
 // Host-side helpers of visionaray (make_kernel_params, area_light's constructor,
@@ -26,10 +28,13 @@
 
 #include <visionaray/area_light.h>
 #include <visionaray/bvh.h>
+#include <visionaray/generic_light.h>
 #include <visionaray/generic_material.h>
 #include <visionaray/kernels.h>
 #include <visionaray/material.h>
 #include <visionaray/math/math.h>
+#include <visionaray/point_light.h>
+#include <visionaray/spot_light.h>
 #include <visionaray/traverse.h>
 
 #include "../include/visionaray_gb300/gbrt.h"
@@ -41,9 +46,13 @@ using triangle_t = basic_triangle<3, float, unsigned>;
 using tree_ref_t = index_bvh_ref_t<triangle_t>;
 using mat_t = generic_material<matte<float>, emissive<float>>;
 using light_t = area_light<float, triangle_t>;
-using kparams_t = decltype(make_kernel_params(std::declval<tree_ref_t const*>(), std::declval<tree_ref_t const*>(),
-                                              std::declval<mat_t const*>(), std::declval<light_t const*>(),
-                                              std::declval<light_t const*>(), 0u, 0.0f, vec4(), vec4()));
+// the extended instantiation: every material kind and generic lights
+using mat_ext_t = generic_material<matte<float>, emissive<float>, mirror<float>, glass<float>, plastic<float>>;
+using light_ext_t = generic_light<area_light<float, triangle_t>, point_light<float>, spot_light<float>>;
+template <typename Mat, typename Light>
+using kparams_of = decltype(make_kernel_params(std::declval<tree_ref_t const*>(), std::declval<tree_ref_t const*>(),
+                                               std::declval<Mat const*>(), std::declval<Light const*>(),
+                                               std::declval<Light const*>(), 0u, 0.0f, vec4(), vec4()));
 
 static_assert(sizeof(triangle_t) == sizeof(gbrt_triangle), "triangle layout");
 static_assert(sizeof(bvh_node) == sizeof(gbrt_bvh_node), "node layout");
@@ -131,6 +140,109 @@ extern "C" __global__ void vsnray_ref_pt_setup(ref_ptrs tree, tree_ref_t* refs, 
     }
 }
 
+// The extended instantiation's materials (all five kinds) and lights (area, point,
+// spot), with the field mapping of gbrt.h.
+extern "C" __global__ void vsnray_ref_pt_setup_ext(ref_ptrs tree, tree_ref_t* refs, const gbrt_material* in_m,
+                                                   unsigned nm, mat_ext_t* mats, const gbrt_light* in_l, unsigned nl,
+                                                   light_ext_t* lights)
+{
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) refs[0] = make_ref(tree);
+    if (i < nm)
+    {
+        gbrt_material const& g = in_m[i];
+        vec3 c(g.color[0], g.color[1], g.color[2]), c2(g.color2[0], g.color2[1], g.color2[2]);
+        vec3 ior(g.ior[0], g.ior[1], g.ior[2]), ab(g.absorption[0], g.absorption[1], g.absorption[2]);
+        auto& dst = static_cast<mat_ext_t::base_type&>(mats[i]);
+        if (g.kind == GBRT_MATERIAL_EMISSIVE)
+        {
+            emissive<float> e;
+            e.ce() = from_rgb(c);
+            e.ls() = g.scale;
+            dst = e;
+        }
+        else if (g.kind == GBRT_MATERIAL_MIRROR)
+        {
+            mirror<float> m;
+            m.cr() = from_rgb(c);
+            m.kr() = g.scale;
+            m.ior() = from_rgb(ior);
+            m.absorption() = from_rgb(ab);
+            dst = m;
+        }
+        else if (g.kind == GBRT_MATERIAL_GLASS)
+        {
+            glass<float> m;
+            m.ct() = from_rgb(c);
+            m.kt() = g.scale;
+            m.cr() = from_rgb(c2);
+            m.kr() = g.scale2;
+            m.ior() = from_rgb(ior);
+            dst = m;
+        }
+        else if (g.kind == GBRT_MATERIAL_PLASTIC)
+        {
+            plastic<float> m;
+            m.ca() = from_rgb(vec3(0.0f));
+            m.ka() = 0.0f;
+            m.cd() = from_rgb(c);
+            m.kd() = g.scale;
+            m.cs() = from_rgb(c2);
+            m.ks() = g.scale2;
+            m.specular_exp() = g.exponent;
+            dst = m;
+        }
+        else
+        {
+            matte<float> m;
+            m.ca() = from_rgb(vec3(0.0f));
+            m.ka() = 0.0f;
+            m.cd() = from_rgb(c);
+            m.kd() = g.scale;
+            dst = m;
+        }
+    }
+    if (i < nl)
+    {
+        gbrt_light const& g = in_l[i];
+        vec3 cl(g.cl[0], g.cl[1], g.cl[2]), pos(g.position[0], g.position[1], g.position[2]);
+        auto& dst = static_cast<light_ext_t::base_type&>(lights[i]);
+        if (g.kind == GBRT_LIGHT_POINT)
+        {
+            point_light<float> l;
+            l.set_cl(cl);
+            l.set_kl(g.kl);
+            l.set_position(pos);
+            l.set_constant_attenuation(g.attenuation[0]);
+            l.set_linear_attenuation(g.attenuation[1]);
+            l.set_quadratic_attenuation(g.attenuation[2]);
+            dst = l;
+        }
+        else if (g.kind == GBRT_LIGHT_SPOT)
+        {
+            spot_light<float> l;
+            l.set_cl(cl);
+            l.set_kl(g.kl);
+            l.set_position(pos);
+            l.set_spot_direction(vec3(g.spot_direction[0], g.spot_direction[1], g.spot_direction[2]));
+            l.set_spot_cutoff(g.spot_cutoff);
+            l.set_spot_exponent(g.spot_exponent);
+            l.set_constant_attenuation(g.attenuation[0]);
+            l.set_linear_attenuation(g.attenuation[1]);
+            l.set_quadratic_attenuation(g.attenuation[2]);
+            dst = l;
+        }
+        else
+        {
+            area_light<float, triangle_t> l;
+            memcpy(static_cast<void*>(&l.geometry()), &g.geometry, sizeof(triangle_t));
+            l.set_cl(cl);
+            l.set_kl(g.kl);
+            dst = l;
+        }
+    }
+}
+
 struct camera_basis
 {
     float eye[3], U[3], V[3], W[3];
@@ -139,9 +251,11 @@ struct camera_basis
 // One frame: thread (x, y) runs the pixel's spp samples through pathtracing::kernel with
 // the gbrt_rng.h stream (jitter x drawn before y), averages them and blends
 // accum = avg * sfactor + accum * dfactor.
-extern "C" __global__ void vsnray_ref_pathtrace(const tree_ref_t* refs, const mat_t* mats, const light_t* lights,
-                                                unsigned nl, camera_basis cam, gbrt_pt_params p, float* accum)
+template <typename Mat, typename Light>
+__device__ void pathtrace_pixel(const tree_ref_t* refs, const Mat* mats, const Light* lights, unsigned nl,
+                                camera_basis const& cam, gbrt_pt_params const& p, float* accum)
 {
+    using kparams_t = kparams_of<Mat, Light>;
     unsigned x = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= p.width || y >= p.height) return;
@@ -194,6 +308,19 @@ extern "C" __global__ void vsnray_ref_pathtrace(const tree_ref_t* refs, const ma
     a[3] = out.w;
 }
 
+extern "C" __global__ void vsnray_ref_pathtrace(const tree_ref_t* refs, const mat_t* mats, const light_t* lights,
+                                                unsigned nl, camera_basis cam, gbrt_pt_params p, float* accum)
+{
+    pathtrace_pixel(refs, mats, lights, nl, cam, p, accum);
+}
+
+extern "C" __global__ void vsnray_ref_pathtrace_ext(const tree_ref_t* refs, const mat_ext_t* mats,
+                                                    const light_ext_t* lights, unsigned nl, camera_basis cam,
+                                                    gbrt_pt_params p, float* accum)
+{
+    pathtrace_pixel(refs, mats, lights, nl, cam, p, accum);
+}
+
 // sizeof of the visionaray objects the host allocates arrays of: tree ref, material,
 // light.
 extern "C" __global__ void vsnray_ref_sizes(unsigned* out)
@@ -201,4 +328,6 @@ extern "C" __global__ void vsnray_ref_sizes(unsigned* out)
     out[0] = unsigned(sizeof(tree_ref_t));
     out[1] = unsigned(sizeof(mat_t));
     out[2] = unsigned(sizeof(light_t));
+    out[3] = unsigned(sizeof(mat_ext_t));
+    out[4] = unsigned(sizeof(light_ext_t));
 }

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CUBIN = os.path.join(HERE, "_ref", "vsnray_ref_gpu.cubin")               # nvcc defaults
 CUBIN_EXACT = os.path.join(HERE, "_ref", "vsnray_ref_gpu_exact.cubin")   # --fmad=false
 KERNELS = ("vsnray_ref_closest_hit", "vsnray_ref_any_hit", "vsnray_ref_pt_setup", "vsnray_ref_pathtrace",
-           "vsnray_ref_sizes")
+           "vsnray_ref_pt_setup_ext", "vsnray_ref_pathtrace_ext", "vsnray_ref_sizes")
 
 
 def available(exact=False):
@@ -79,10 +79,11 @@ class ReferenceGPU:
             f = vp()
             self._check(cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
             self.fn[name] = f
-        sizes = torch.zeros(4, dtype=torch.int32, device=self.dev)
+        sizes = torch.zeros(8, dtype=torch.int32, device=self.dev)
         self._launch("vsnray_ref_sizes", (1, 1, 1), (1, 1, 1), [vp(sizes.data_ptr())])
         torch.cuda.synchronize()
-        self.size_ref, self.size_mat, self.size_light = (int(x) for x in sizes.tolist()[:3])
+        self.size_ref, self.size_mat, self.size_light, self.size_mat_ext, self.size_light_ext = (
+            int(x) for x in sizes.tolist()[:5])
 
     def _check(self, err, what):
         if err != 0:
@@ -121,22 +122,33 @@ class ReferenceGPU:
 
     def pt_scene(self, tree, materials, lights):
         """Device arrays of visionaray objects for pathtrace(): the tree ref, one
-        generic_material<matte, emissive> per material slot, the area lights."""
+        material per slot and the lights.  Matte / emissive slots with area lights
+        (AREA_LIGHT records) use generic_material<matte, emissive> and area_light;
+        otherwise (a mirror, glass or plastic slot, or LIGHT records) the extended
+        instantiation: generic_material<matte, emissive, mirror, glass, plastic> and
+        generic_light<area_light, point_light, spot_light>."""
         torch = self.torch
         from visionaray_gb300.runtime import as_device_bytes
-        m = as_device_bytes(np.ascontiguousarray(materials))
-        l_ = as_device_bytes(np.ascontiguousarray(lights)) if len(lights) else torch.zeros(64, dtype=torch.uint8,
+        from visionaray_gb300.types import LIGHT, MATTE, EMISSIVE, lights_of_area_lights
+        materials = np.ascontiguousarray(materials)
+        ext = np.asarray(lights).dtype == LIGHT or bool(np.isin(materials["kind"], (MATTE, EMISSIVE), invert=True).any())
+        if ext and np.asarray(lights).dtype != LIGHT:
+            lights = lights_of_area_lights(lights)
+        m = as_device_bytes(materials)
+        l_ = as_device_bytes(np.ascontiguousarray(lights)) if len(lights) else torch.zeros(128, dtype=torch.uint8,
                                                                                          device=self.dev)
         nm, nl = len(materials), len(lights)
+        size_mat = self.size_mat_ext if ext else self.size_mat
+        size_light = self.size_light_ext if ext else self.size_light
         refs = torch.zeros(self.size_ref, dtype=torch.uint8, device=self.dev)
-        mats = torch.zeros(max(nm, 1) * self.size_mat, dtype=torch.uint8, device=self.dev)
-        lts = torch.zeros(max(nl, 1) * self.size_light, dtype=torch.uint8, device=self.dev)
+        mats = torch.zeros(max(nm, 1) * size_mat, dtype=torch.uint8, device=self.dev)
+        lts = torch.zeros(max(nl, 1) * size_light, dtype=torch.uint8, device=self.dev)
         items = max(nm, nl, 1)
         vp = ctypes.c_void_p
-        self._launch("vsnray_ref_pt_setup", ((items + 127) // 128, 1, 1), (128, 1, 1),
-                     [tree.ptrs, vp(refs.data_ptr()), vp(m.data_ptr()), ctypes.c_uint(nm), vp(mats.data_ptr()),
-                      vp(l_.data_ptr()), ctypes.c_uint(nl), vp(lts.data_ptr())])
-        return {"refs": refs, "mats": mats, "lights": lts, "nl": nl, "keep": (m, l_, tree)}
+        self._launch("vsnray_ref_pt_setup_ext" if ext else "vsnray_ref_pt_setup", ((items + 127) // 128, 1, 1),
+                     (128, 1, 1), [tree.ptrs, vp(refs.data_ptr()), vp(m.data_ptr()), ctypes.c_uint(nm),
+                                   vp(mats.data_ptr()), vp(l_.data_ptr()), ctypes.c_uint(nl), vp(lts.data_ptr())])
+        return {"refs": refs, "mats": mats, "lights": lts, "nl": nl, "ext": ext, "keep": (m, l_, tree)}
 
     def pathtrace(self, scene, camera, params, accum, block=(16, 16)):
         """One frame of pathtracing::kernel, one thread per pixel (cuda_sched's 16 x 16
@@ -148,7 +160,8 @@ class ReferenceGPU:
         par = (ctypes.c_char * p.dtype.itemsize).from_buffer_copy(p.tobytes())
         vp = ctypes.c_void_p
         grid = ((w + block[0] - 1) // block[0], (h + block[1] - 1) // block[1], 1)
-        self._launch("vsnray_ref_pathtrace", grid, (block[0], block[1], 1),
+        self._launch("vsnray_ref_pathtrace_ext" if scene["ext"] else "vsnray_ref_pathtrace", grid,
+                     (block[0], block[1], 1),
                      [vp(scene["refs"].data_ptr()), vp(scene["mats"].data_ptr()), vp(scene["lights"].data_ptr()),
                       ctypes.c_uint(scene["nl"]), cam, par, vp(accum.data_ptr())])
         return accum

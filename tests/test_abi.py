@@ -60,6 +60,7 @@ def test_abi_version_and_struct_sizes():
     assert types.HIT.itemsize == 16 and types.BVH_NODE.itemsize == 32
     assert types.MATERIAL.itemsize == 64 and types.AREA_LIGHT.itemsize == 60
     assert types.INSTANCE.itemsize == 56 and types.HIT_INST.itemsize == 32
+    assert types.LIGHT.itemsize == 108
 
 
 def test_null_context_is_rejected_without_touching_the_gpu():

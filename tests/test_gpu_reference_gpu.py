@@ -112,3 +112,68 @@ def test_reference_gpu_pathtracer_closed_box():
         s = render_pair(exact, tris, mats, lights, cam, params)
         print(exact, s)
         assert np.isclose(s["mean"][0], s["mean"][1], rtol=0.1), s
+
+
+def material_soup(n=20000, seed=4):
+    """A soup whose triangles cycle matte, mirror, glass and plastic slots."""
+    from visionaray_gb300.types import GLASS, MATERIAL, MIRROR, PLASTIC
+    tris = scenes.soup(n, seed=seed, offset=0.5 / n ** (1 / 3))
+    tris["geom_id"] = tris["prim_id"] % 4
+    mats = np.zeros(4, MATERIAL)
+    mats["kind"] = (0, MIRROR, GLASS, PLASTIC)
+    mats["color"] = ((0.7, 0.6, 0.5), (0.9, 0.9, 0.8), (1.0, 1.0, 1.0), (0.2, 0.5, 0.7))
+    mats["scale"] = 1.0
+    mats["ior"] = ((1.0, 1.0, 1.0), (0.27, 0.42, 1.35), (1.5, 1.5, 1.5), (1.0, 1.0, 1.0))
+    mats["absorption"][1] = (3.4, 2.3, 1.8)
+    mats["color2"][2], mats["scale2"][2] = (1.0, 1.0, 1.0), 1.0
+    mats["color2"][3], mats["scale2"][3], mats["exponent"][3] = (0.5, 0.5, 0.5), 1.0, 24.0
+    return tris, mats
+
+
+@pytest.mark.skipif(not ref_gpu.available(exact=True), reason="exact reference cubin not built")
+def test_reference_gpu_materials_and_point_light_open_scene():
+    """Mirror, glass and plastic slots and a point light through the reference's
+    generic_material / generic_light instantiation on the GPU: the device build (first
+    hemisphere draw first, rsqrtf normalisation) against the oracle with the device
+    build's draw order; and the product's mean against it."""
+    from oracle import Oracle
+    from visionaray_gb300.types import LIGHT, LIGHT_POINT
+    tris, mats = material_soup()
+    lights = np.zeros(1, LIGHT)
+    lights["kind"], lights["cl"], lights["kl"] = LIGHT_POINT, (1.0, 0.9, 0.8), 0.5
+    lights["position"], lights["attenuation"] = (0.5, 1.6, -0.4), (1.0, 0.0, 0.0)
+    cam = scenes.box_camera(eye=(0.5, 0.5, -1.2), center=(0.5, 0.5, 0.5), fovy_degrees=50.0)
+    params = scenes.pt_params(96, 64, 4, num_bounces=4, frame_id=3, ambient=(0.5, 0.6, 0.7))
+    s = render_pair(True, tris, mats, lights, cam, params)
+    print(s)
+    assert abs(s["mean"][0] - s["mean"][1]) <= 0.03 * s["mean"][1], s
+    orc = Oracle()
+    ref = ref_gpu.ReferenceGPU(0, exact=True)
+    d_tris = vg.as_device_bytes(tris)
+    bvh = vg.lbvh_builder().build(d_tris)
+    theirs = torch.zeros((64, 96, 4), dtype=torch.float32, device="cuda:0")
+    rscene = ref.pt_scene(ref.tree(d_tris, bvh), mats, lights)
+    assert rscene["ext"]
+    ref.pathtrace(rscene, cam, params, theirs)
+    torch.cuda.synchronize()
+    img, _ = orc.pathtrace(orc.build_sah(tris), tris, mats, lights, cam, params,
+                           mode=Oracle.PT_FLOAT | Oracle.PT_DRAWS_IN_ORDER)
+    b = theirs.cpu().numpy()[..., :3].astype(np.float64)
+    d = np.abs(img[..., :3] - b).max(axis=2)
+    close = float((d <= 1e-4 * b.max()).mean())
+    print("device build vs oracle (draws in order):", close, float(np.sqrt((d ** 2).mean())))
+    assert close >= 0.9, close
+
+
+@pytest.mark.skipif(not ref_gpu.available(exact=True), reason="exact reference cubin not built")
+def test_reference_gpu_glossy_box_mixed_lights():
+    """The glossy box lit by area, point and spot lights: means agree (closed box, see
+    test_reference_gpu_pathtracer_closed_box)."""
+    tris, mats, area = scenes.glossy_box_scene(n_blobs=10, subdiv=8, seed=1)
+    lights = scenes.mixed_lights(area)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(192, 128, 8, num_bounces=8, frame_id=12)
+    for exact in (True, False):
+        s = render_pair(exact, tris, mats, lights, cam, params)
+        print(exact, s)
+        assert np.isclose(s["mean"][0], s["mean"][1], rtol=0.1), s

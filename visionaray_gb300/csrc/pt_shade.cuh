@@ -43,8 +43,29 @@ __device__ __forceinline__ float max_elem(v3 v)
 }
 __device__ __forceinline__ float power_heuristic(float p1, float p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
 __device__ __forceinline__ v3 xyz(float4 a) { return { a.x, a.y, a.z }; }
-// pow, cos and sin evaluated in double and rounded once to float
-__device__ __forceinline__ float pow_d(float x, float y) { return float(pow(double(x), double(y))); }
+// pow, cos and sin evaluated in double and rounded once to float.  pow with a
+// non-negative integer exponent up to 1024 (the Blinn exponents of typical scenes and
+// Schlick's fifth power) is binary exponentiation in double: at most 2 log2(y) roundings
+// of 2^-53 each, so the float result is the double pow's except for values within about
+// 2^-27 of a float rounding boundary, at a few multiplications instead of the double
+// pow's log and exp (FP64 issue is slow on this GPU: the general pow made the Blinn
+// lobe 40 % of a glossy frame).
+__device__ __forceinline__ float pow_d(float x, float y)
+{
+    if (y >= 0.0f && y <= 1024.0f && y == truncf(y))
+    {
+        unsigned n = unsigned(y);
+        double b = double(x), r = 1.0;
+        while (n)
+        {
+            if (n & 1u) r *= b;
+            n >>= 1;
+            if (n) b *= b;
+        }
+        return float(r);
+    }
+    return float(pow(double(x), double(y)));
+}
 __device__ __forceinline__ float cos_d(float x) { return float(cos(double(x))); }
 __device__ __forceinline__ float sin_d(float x) { return float(sin(double(x))); }
 
