@@ -10,11 +10,20 @@
 //   closest_hit(ray, refs, refs + 1)  (per ray,         visionaray_gb300::closest_hit(ctx, bvh, d_rays, n, d_hits)
 //   traverse_linear.inl:192-225)                        (batched: a device functor cannot cross a C ABI)
 //   any_hit(ray, refs, refs + 1)  (:156-189)            visionaray_gb300::any_hit(ctx, bvh, d_rays, n, d_hits)
+//   auto kp = make_kernel_params(prims, materials,      auto kp = visionaray_gb300::make_kernel_params(ctx, bvh,
+//       lights, bounces, eps, bg, ambient)                  materials, lights, bounces, eps, bg, ambient)
+//   (kernels.h:136-188)
+//   pathtracing::kernel<decltype(kp)> k; k.params = kp; visionaray_gb300::pathtracing::kernel<...> k; k.params = &kp;
+//   cuda_sched<R>(8, 8).frame(k, make_sched_params(     visionaray_gb300::cuda_sched(ctx).frame(k,
+//       jittered_blend, cam, rt))                           sched_params{camera, width, height, spp, ...})
+//   (detail/cuda_sched.inl:226-246)                     (the built-in path tracer only: a user lambda is device
+//                                                        code that cannot cross a C ABI)
 //
 // Errors: the reference prints through CUDA_SAFE_CALL (cuda/safe_call.h:18-23) and
 // carries on; the shim throws visionaray_gb300::error carrying the gbrt_status.
 #pragma once
 
+#include <array>
 #include <cstddef>
 #include <stdexcept>
 #include <string>
@@ -149,6 +158,28 @@ private:
     context* ctx_;
 };
 
+// Parallel locally-ordered clustering build (no visionaray counterpart; a tree of
+// lower SAH cost than the LBVH over the same Morton order).  P as for lbvh_builder.
+struct ploc_builder
+{
+    explicit ploc_builder(context& ctx) : ctx_(&ctx) {}
+
+    template <typename P>
+    cuda_index_bvh build(cuda_index_bvh /* tag */, P const* d_primitives, size_t num_prims)
+    {
+        static_assert(sizeof(P) == sizeof(gbrt_triangle), "P must be laid out as basic_triangle<3, float, unsigned>");
+        if (num_prims > 0xFFFFFFFFu) throw error(GBRT_ERR_TOO_LARGE, "ploc_builder::build: too many primitives");
+        gbrt_bvh* h = nullptr;
+        check(gbrt_bvh_build_ploc(ctx_->get(), reinterpret_cast<gbrt_triangle const*>(d_primitives),
+                                  uint32_t(num_prims), &h),
+              ctx_->get(), "gbrt_bvh_build_ploc");
+        return cuda_index_bvh(*ctx_, h);
+    }
+
+private:
+    context* ctx_;
+};
+
 // bvh_refitter (detail/bvh/refit.h:25-117), GPU refit of an LBVH-built tree to new
 // positions of its primitives (device, the build's order).
 struct bvh_refitter
@@ -181,5 +212,132 @@ inline void any_hit(context& ctx, cuda_index_bvh const& bvh, gbrt_ray const* d_r
 {
     check(gbrt_trace_any_hit(ctx.get(), bvh.get(), d_rays, uint32_t(n), d_hits), ctx.get(), "gbrt_trace_any_hit");
 }
+
+// make_kernel_params(prims, materials, lights, num_bounces, epsilon, bg_color,
+// ambient_color) (kernels.h:136-188) for the built-in path tracer: the scene (a BVH
+// that must outlive it, materials indexed by geom_id, lights; host arrays, copied)
+// and the per-frame constants.  Move-only.
+class kernel_params
+{
+public:
+    kernel_params(context& ctx, cuda_index_bvh const& bvh, std::vector<gbrt_material> const& materials,
+                  std::vector<gbrt_light> const& lights, unsigned num_bounces, float epsilon,
+                  std::array<float, 4> background, std::array<float, 3> ambient)
+        : ctx_(&ctx), num_bounces(num_bounces), epsilon(epsilon), background(background), ambient(ambient)
+    {
+        check(gbrt_pt_scene_create_lights(ctx.get(), bvh.get(), materials.data(), uint32_t(materials.size()),
+                                          lights.data(), uint32_t(lights.size()), &scene_),
+              ctx.get(), "gbrt_pt_scene_create_lights");
+    }
+    ~kernel_params()
+    {
+        if (scene_) gbrt_pt_scene_destroy(scene_);
+    }
+    kernel_params(kernel_params&& o) noexcept
+        : ctx_(o.ctx_), scene_(std::exchange(o.scene_, nullptr)), num_bounces(o.num_bounces), epsilon(o.epsilon),
+          background(o.background), ambient(o.ambient)
+    {
+    }
+    kernel_params(kernel_params const&) = delete;
+    kernel_params& operator=(kernel_params const&) = delete;
+    kernel_params& operator=(kernel_params&&) = delete;
+
+    gbrt_pt_scene* scene() const { return scene_; }
+    context& ctx() const { return *ctx_; }
+
+private:
+    context* ctx_;
+    gbrt_pt_scene* scene_ = nullptr;
+
+public:
+    unsigned num_bounces;
+    float epsilon;
+    std::array<float, 4> background;
+    std::array<float, 3> ambient;
+};
+
+inline kernel_params make_kernel_params(context& ctx, cuda_index_bvh const& bvh,
+                                        std::vector<gbrt_material> const& materials,
+                                        std::vector<gbrt_light> const& lights, unsigned num_bounces, float epsilon,
+                                        std::array<float, 4> background, std::array<float, 3> ambient)
+{
+    return kernel_params(ctx, bvh, materials, lights, num_bounces, epsilon, background, ambient);
+}
+
+// The same with area_light<float, basic_triangle> records.
+inline kernel_params make_kernel_params(context& ctx, cuda_index_bvh const& bvh,
+                                        std::vector<gbrt_material> const& materials,
+                                        std::vector<gbrt_area_light> const& area_lights, unsigned num_bounces,
+                                        float epsilon, std::array<float, 4> background, std::array<float, 3> ambient)
+{
+    std::vector<gbrt_light> lights(area_lights.size());
+    for (size_t i = 0; i < area_lights.size(); ++i)
+    {
+        lights[i] = gbrt_light{};
+        lights[i].kind = GBRT_LIGHT_AREA;
+        lights[i].geometry = area_lights[i].geometry;
+        for (int c = 0; c < 3; ++c) lights[i].cl[c] = area_lights[i].cl[c];
+        lights[i].kl = area_lights[i].kl;
+    }
+    return kernel_params(ctx, bvh, materials, lights, num_bounces, epsilon, background, ambient);
+}
+
+namespace pathtracing {
+
+// pathtracing::kernel<Params> (detail/pathtracing.inl:33-233): holds the parameters it
+// renders with (by pointer here: kernel_params owns device memory).
+template <typename Params>
+struct kernel
+{
+    Params const* params = nullptr;
+};
+
+} // namespace pathtracing
+
+// What make_sched_params(pixel_sampler::jittered_blend_type, camera, render_target)
+// carries for one frame (detail/sched_common.h:427-526): the pinhole camera, the image
+// size, samples per pixel, the blend accum = sfactor * frame + dfactor * accum, the
+// frame number that seeds the random stream, and the render target (RGBA32F device
+// images; d_color may be null).
+struct sched_params
+{
+    gbrt_camera camera;
+    uint32_t width = 0, height = 0, spp = 1, frame_id = 0;
+    float sfactor = 1.0f, dfactor = 0.0f;
+    float* d_accum = nullptr;
+    float* d_color = nullptr;
+    uint32_t flags = 0;   // GBRT_PT_* bits
+};
+
+// cuda_sched<R>::frame (detail/cuda_sched.inl:226-246) for the built-in path tracer:
+// asynchronous on the context stream.
+class cuda_sched
+{
+public:
+    explicit cuda_sched(context& ctx) : ctx_(&ctx) {}
+
+    void frame(pathtracing::kernel<kernel_params> const& k, sched_params const& sp)
+    {
+        if (!k.params) throw error(GBRT_ERR_INVALID_ARG, "cuda_sched::frame: kernel without params");
+        kernel_params const& kp = *k.params;
+        gbrt_pt_params p{};
+        p.width = sp.width;
+        p.height = sp.height;
+        p.spp = sp.spp;
+        p.num_bounces = kp.num_bounces;
+        p.epsilon = kp.epsilon;
+        p.frame_id = sp.frame_id;
+        p.sfactor = sp.sfactor;
+        p.dfactor = sp.dfactor;
+        for (int c = 0; c < 4; ++c) p.background[c] = kp.background[size_t(c)];
+        for (int c = 0; c < 3; ++c) p.ambient[c] = kp.ambient[size_t(c)];
+        p.flags = sp.flags;
+        check(gbrt_pathtrace_frame(ctx_->get(), kp.scene(), &sp.camera, &p, sp.d_accum, sp.d_color), ctx_->get(),
+              "gbrt_pathtrace_frame");
+    }
+
+private:
+    context* ctx_;
+};
 
 } // namespace visionaray_gb300
