@@ -248,7 +248,8 @@ gbrt_status gbrt_trace_any_hit_host(gbrt_context* ctx, gbrt_bvh const* bvh,
  *   plastic  (detail/material/plastic.inl, lambertian + blinn brdf.h:26-84, 118-191):
  *            cd = color, kd = scale, cs = color2, ks = scale2,
  *            specular_exp = exponent
- * (the path-tracing configurations use matte and emissive).                       */
+ * (the path-tracing configurations use matte and emissive).  Scene creation and
+ * gbrt_batch_set_frames reject any other kind with GBRT_ERR_INVALID_ARG.            */
 #define GBRT_MATERIAL_MATTE    0u
 #define GBRT_MATERIAL_EMISSIVE 1u
 #define GBRT_MATERIAL_MIRROR   2u

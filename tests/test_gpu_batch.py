@@ -240,3 +240,13 @@ def test_batch_rejects_bad_arguments():
         batch.launch = (100, 32, 64, 0)
     with pytest.raises(vg.GbrtError):
         batch.pathtrace(torch.empty((4, 4), dtype=torch.float32, device="cuda:0"))   # frames not set
+
+
+def test_batch_rejects_unknown_material_kind():
+    from visionaray_gb300.runtime import GbrtError
+    tris, offsets, cams, params, mats = make_batch_inputs([50, 60])
+    batch = vg.Batch(offsets)
+    batch.build(vg.as_device_bytes(tris))
+    mats["kind"][0] = 5
+    with pytest.raises(GbrtError, match="unknown material kind"):
+        batch.set_frames(cams, params, mats)

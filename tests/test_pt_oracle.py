@@ -180,6 +180,19 @@ def test_reference_blend_and_background(oracle, small_box):
     assert (c.reshape(-1, 4) == np.array([0.5, 1.0, 2.0, 1.0], np.float32)).all(axis=1).any()
 
 
+@pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+@pytest.mark.parametrize("frame,spp,bounces", [(1, 2, 8), (4, 2, 3)])
+def test_fp32_oracle_is_the_reference_kernel_edge_materials(oracle, frame, spp, bounces):
+    from .materials import edge_material_box
+    tris, mats, lights = edge_material_box()
+    cam = scenes.box_camera()
+    params = scenes.pt_params(40, 24, spp, num_bounces=bounces, frame_id=frame)
+    ref = Reference().pathtrace(tris, mats, lights, cam, params)
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT)
+    assert np.isfinite(ref).all()
+    assert np.array_equal(img.astype(np.float32), ref)
+
+
 def test_shadow_range_fix_makes_fp32_and_fp64_agree(oracle, small_box):
     tris, mats, lights, cam = small_box
     tree = oracle.build_sah(tris)

@@ -228,6 +228,9 @@ extern "C" gbrt_status gbrt_batch_set_frames(gbrt_context* ctx, gbrt_batch* batc
     if (!ctx) return GBRT_ERR_INVALID_ARG;
     if (!batch || !h_cameras || !h_params || (num_materials && !h_materials))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_frames: null argument");
+    for (uint32_t k = 0; k < num_materials; ++k)
+        if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_frames: unknown material kind");
     const uint32_t ns = batch->num_scenes;
     std::vector<batch_frame> frames(ns);
     std::vector<uint32_t> offs(ns + 1);

@@ -744,6 +744,9 @@ extern "C" gbrt_status gbrt_pt_scene_create(gbrt_context* ctx, gbrt_bvh const* b
     *out = nullptr;
     if ((num_materials && !h_materials) || (num_lights && !h_lights))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: null material or light array");
+    for (uint32_t k = 0; k < num_materials; ++k)
+        if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create: unknown material kind");
     std::vector<float4> rec(size_t(num_lights) * 4);
     for (uint32_t k = 0; k < num_lights; ++k)
         area_record(h_lights[k].geometry, h_lights[k].cl, h_lights[k].kl, &rec[4 * k]);
@@ -760,6 +763,9 @@ extern "C" gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh c
     *out = nullptr;
     if ((num_materials && !h_materials) || (num_lights && !h_lights))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: null material or light array");
+    for (uint32_t k = 0; k < num_materials; ++k)
+        if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: unknown material kind");
     std::vector<float4> rec(size_t(num_lights) * 4);
     for (uint32_t k = 0; k < num_lights; ++k)
     {
