@@ -183,11 +183,21 @@ PT_WORKLOAD = ("path tracing: closed unit box + 0.25^2 ceiling light (emission 1
                "Russian roulette from depth 3")
 
 
-def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc"):
-    """Msamples/s of the path-tracing workload (one frame = 1920x1080 x 64 spp)."""
+PT_GLOSSY_WORKLOAD = ("path tracing: the same box, its 256 blobs cycling matte / plastic / mirror / plastic / glass "
+                      "and plastic walls, lit by the ceiling light, two point lights and a spot light, 1920x1080, "
+                      "64 spp, depth 8, Russian roulette from depth 3")
+
+
+def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc", scene_kind="box"):
+    """Msamples/s of the path-tracing workload (one frame = 1920x1080 x 64 spp);
+    scene_kind "glossy": the materials-and-lights variant of the same box."""
     import torch
     from visionaray_gb300 import scenes
-    tris, mats, lights = scenes.box_scene()
+    if scene_kind == "glossy":
+        tris, mats, area = scenes.glossy_box_scene(n_blobs=256, subdiv=22, seed=1)
+        lights = scenes.mixed_lights(area)
+    else:
+        tris, mats, lights = scenes.box_scene()
     make = vg.ploc_builder if builder == "ploc" else vg.lbvh_builder
     bvh = make(ctx).build(vg.as_device_bytes(tris, ctx.device))
     scene = vg.PTScene(bvh, mats, lights)
@@ -210,7 +220,8 @@ def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc"):
     ms = ev[0].elapsed_time(ev[1]) / frames
     samples = PT_WIDTH * PT_HEIGHT * PT_SPP
     mean = accum[..., :3].mean().item()
-    return {"workload": PT_WORKLOAD, "flags": flags, "builder": builder, "frames": frames, "ms_per_frame": round(ms, 2),
+    return {"workload": PT_GLOSSY_WORKLOAD if scene_kind == "glossy" else PT_WORKLOAD, "flags": flags,
+            "builder": builder, "frames": frames, "ms_per_frame": round(ms, 2),
             "msamples_s": round(samples / (ms * 1e-3) / 1e6, 2), "image_mean": round(mean, 5),
             "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
 
@@ -507,7 +518,7 @@ def run_ours(args):
 
     pt = None
     if args.pt_frames > 0:
-        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint, args.pt_builder)
+        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint, args.pt_builder, args.pt_scene)
 
     batched = None
     if args.batch_steps > 0:
@@ -557,6 +568,8 @@ def main():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pt-frames", type=int, default=2, help="timed path-tracing frames (0: skip)")
+    p.add_argument("--pt-scene", choices=("box", "glossy"), default="box",
+                   help="path-tracing scene: the matte box of the workload, or its materials-and-lights variant")
     p.add_argument("--no-ploc", action="store_true", help="skip the traversal through the PLOC tree")
     p.add_argument("--builder", choices=["lbvh", "ploc"], default="lbvh",
                    help="tree of the traversal leg: the LBVH (the workload's builder) or the PLOC build")
