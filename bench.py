@@ -45,7 +45,7 @@ N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
 # of the full-size workload with the default ray order; profiles/
 # trace_rays_permuted_heightfield_2048_dram.md).
-TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.37e9 + 0.154e9, 2.60e9 + 0.526e9
+TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.375e9 + 0.153e9, 2.620e9 + 0.530e9
 
 
 def b_ray(n_node, n_tri):

@@ -126,7 +126,7 @@ gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
 gbrt_status gbrt_context_set_trace_refill(gbrt_context* ctx, uint32_t min_idle_lanes);
 
 /* Host-buffer queries (gbrt_trace_*_host) move rays and hits in chunks of this many
- * rays (2^16 .. 2^26, default 2^22), alternating between two device slots so one
+ * rays (2^16 .. 2^26, default 2^23), alternating between two device slots so one
  * chunk's copies overlap another's traversal.                                      */
 gbrt_status gbrt_context_set_host_chunk(gbrt_context* ctx, uint32_t rays);
 

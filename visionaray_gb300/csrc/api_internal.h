@@ -50,7 +50,7 @@ struct gbrt_context
     // and of each host-path slot.
     uint32_t trace_flags = 0;
     uint32_t trace_refill = 8;   // persistent traversal: idle lanes that trigger a refill
-    uint32_t host_chunk = 1u << 22;   // host-buffer queries: rays per chunk (128 MB of rays)
+    uint32_t host_chunk = 1u << 23;   // host-buffer queries: rays per chunk (256 MB of rays)
     void* trace_scratch = nullptr;
     size_t trace_scratch_bytes = 0;
     void* slot_trace_scratch[kSlots] = { nullptr, nullptr };

@@ -151,7 +151,7 @@ class Context:
         self.check(self.lib.gbrt_context_set_trace_refill(self.h, int(min_idle_lanes)))
 
     def set_host_chunk(self, rays):
-        """Rays per chunk of the host-buffer queries (2^16 .. 2^26, default 2^22)."""
+        """Rays per chunk of the host-buffer queries (2^16 .. 2^26, default 2^23)."""
         self.check(self.lib.gbrt_context_set_host_chunk(self.h, int(rays)))
 
     @property
