@@ -71,9 +71,11 @@ def workload(rank_print=print, grid=GRID, origins=ORIGINS):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 25 ms with timestamps from
+    before the warm-up on, summarised over the samples inside the marked (timed) region
+    (the nearest one if the region is shorter than the sampling period)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -81,12 +83,13 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "25"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=self._read, daemon=True)
             self.reader.start()
         except Exception:
@@ -97,6 +100,12 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -106,23 +115,33 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        import datetime
+        rows = []
         for line in self.lines:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx = float(parts[2])
+                t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((t, float(parts[2]), float(parts[3]), parts[6:10]))
             except ValueError:
                 continue
-            for name, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        if not sm:
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        t0 = self.t0 if self.t0 is not None else rows[0][0]
+        t1 = self.t1 if self.t1 is not None else rows[-1][0]
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        nearest = not inside
+        if nearest:
+            mid = 0.5 * (t0 + t1)
+            inside = [min(rows, key=lambda r: abs(r[0] - mid))]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {n for r in inside for n, v in zip(names, r[3]) if v.lower() == "active"}
+        out = {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": inside[-1][2],
+               "reasons": sorted(reasons), "samples": len(inside)}
+        if nearest:
+            out["nearest_sample"] = True
+        return out
 
 
 def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=8, repeats=1):
@@ -410,28 +429,31 @@ def run_ours(args):
         if ev:
             ev[2].record(stream)
 
-    # warm-up: at least W steps and at least 1.5 s of them (a GPU fresh out of idle runs
-    # its first second slower while its clocks and power state settle)
-    t_warm = time.perf_counter()
-    done = 0
-    while done < args.warmup or time.perf_counter() - t_warm < 1.5:
-        step()
-        done += 1
-        if done % 8 == 0:
-            ctx.synchronize()
-    ctx.synchronize()
-
+    # the clock sampler runs from before the warm-up (nvidia-smi takes a moment to
+    # start); only its samples inside the timed region count
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches0 = ctx.launches
-    replicas.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        # warm-up: at least W steps and at least 1.5 s of them (a GPU fresh out of idle
+        # runs its first second slower while its clocks and power state settle)
+        t_warm = time.perf_counter()
+        done = 0
+        while done < args.warmup or time.perf_counter() - t_warm < 1.5:
+            step()
+            done += 1
+            if done % 8 == 0:
+                ctx.synchronize()
+        ctx.synchronize()
+        launches0 = ctx.launches
+        replicas.barrier()
+        torch.cuda.synchronize()
+        clocks.mark_start()
         start.record(stream)
         for k in range(args.steps):
             step(events[k])
         stop.record(stream)
         torch.cuda.synchronize()
+        clocks.mark_end()
     replicas.barrier()
     gpu_launches = ctx.launches - launches0
     ctx.synchronize()   # raises on a flagged stack overflow / bad index
