@@ -226,6 +226,7 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
         cudaFree(ctx->trace_scratch);
         cudaFree(ctx->scratch);
         cudaFree(ctx->pt_scratch);
+        cudaFree(ctx->d_trig);
         cudaFree(ctx->d_status);
     }
     delete ctx;

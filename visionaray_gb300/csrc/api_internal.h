@@ -45,6 +45,10 @@ struct gbrt_context
     // Path-tracer wavefront state (grown on demand, freed with the context).
     void* pt_scratch = nullptr;
     size_t pt_scratch_bytes = 0;
+    // The path tracer's sample angles: cos and sin (rounded once from double) of
+    // 2 pi u for each of the 2^24 values u = k / 2^24 a random draw takes (float2 per
+    // k, 128 MB), filled once by ensure_trig_table (pathtrace.cu).
+    float2* d_trig = nullptr;
 
     // Ray queries: GBRT_TRACE_* flags and the ray-order scratch of the context stream
     // and of each host-path slot.
@@ -251,3 +255,8 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
         cudaError_t e_ = (call);                                                           \
         if (e_ != cudaSuccess) return gbrt::check_cuda((ctx), e_, #call);                  \
     } while (0)
+
+namespace gbrt {
+// Allocates and fills gbrt_context::d_trig if it is not there yet (pathtrace.cu).
+gbrt_status ensure_trig_table(gbrt_context* ctx);
+} // namespace gbrt

@@ -47,6 +47,7 @@ struct batch_args
     int32_t total_inner, total_tris;
     const gbrt_material* materials;
     uint32_t num_materials;
+    const float2* trig;
     uint32_t* work;
     float4* images;
     uint32_t* status;
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
     sp.num_tris = a.total_tris;
     sp.albedo = nullptr;
     sp.emission = nullptr;
+    sp.trig = a.trig;
     sp.bounce = 0;
     for (;;)
     {
@@ -208,6 +210,8 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     a.total_tris = int32_t(b->total);
     a.materials = b->d_materials;
     a.num_materials = b->num_materials;
+    if (!ctx->d_trig) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: frames not set on this context");
+    a.trig = ctx->d_trig;
     a.work = b->d_work;
     a.images = reinterpret_cast<float4*>(d_images);
     a.status = ctx->d_status;
@@ -231,6 +235,9 @@ extern "C" gbrt_status gbrt_batch_set_frames(gbrt_context* ctx, gbrt_batch* batc
     for (uint32_t k = 0; k < num_materials; ++k)
         if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
             return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_frames: unknown material kind");
+    // the sample-angle table, allocated here so that a captured frame allocates nothing
+    gbrt_status tst = ensure_trig_table(ctx);
+    if (tst != GBRT_OK) return tst;
     const uint32_t ns = batch->num_scenes;
     std::vector<batch_frame> frames(ns);
     std::vector<uint32_t> offs(ns + 1);

@@ -641,6 +641,33 @@ using namespace gbrt;
 namespace gbrt {
 namespace {
 
+// Fills the sample-angle table: entry k holds cos and sin of theta = two_pi * u with
+// u = k / 2^24, exactly as the shading code forms u (gbrt_rng_u01) and theta, each
+// evaluated in double and rounded once to float.
+__global__ void __launch_bounds__(kBlock) fill_trig(float2* __restrict__ table)
+{
+    const float two_pi = 6.28318530717958623199592693709e+00f;
+    uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= (1u << 24)) return;
+    float u = float(k) * (1.0f / 16777216.0f);
+    float theta = two_pi * u;
+    table[k] = make_float2(float(cos(double(theta))), float(sin(double(theta))));
+}
+
+} // namespace
+
+gbrt_status ensure_trig_table(gbrt_context* ctx)
+{
+    if (ctx->d_trig) return GBRT_OK;
+    device_guard g(ctx->device);
+    GBRT_CUDA(ctx, cudaMalloc(&ctx->d_trig, (size_t(1) << 24) * sizeof(float2)));
+    fill_trig<<<(1u << 24) / kBlock, kBlock, 0, ctx->stream>>>(ctx->d_trig);
+    GBRT_LAUNCH_CHECK(ctx, "fill_trig");
+    return GBRT_OK;
+}
+
+namespace {
+
 // The device record of an area light: 4 float4 = v1 (w: the triangle's geom_id bits),
 // e1 (w: 0), e2, intensity cl * kl (w: kl), as area_light::intensity
 // (area_light.inl:22-25).
@@ -688,6 +715,8 @@ gbrt_status create_scene(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_material c
                          uint32_t num_materials, std::vector<float4> const& light_records, gbrt_pt_scene** out)
 {
     device_guard g(ctx->device);
+    gbrt_status tst = ensure_trig_table(ctx);   // once per context, here rather than in a frame
+    if (tst != GBRT_OK) return tst;
     auto* sc = new (std::nothrow) gbrt_pt_scene;
     if (!sc) return fail(ctx, GBRT_ERR_OUT_OF_MEMORY, "pt_scene_create: host allocation");
     sc->bvh = bvh;
@@ -819,10 +848,11 @@ gbrt_status check_frame_args(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt
     return GBRT_OK;
 }
 
-shade_params shade_params_for(gbrt_pt_scene const* scene, gbrt_pt_params const& p, const float* albedo,
-                              const float* emission)
+shade_params shade_params_for(gbrt_context const* ctx, gbrt_pt_scene const* scene, gbrt_pt_params const& p,
+                              const float* albedo, const float* emission)
 {
     shade_params sp;
+    sp.trig = ctx->d_trig;
     sp.materials = scene->materials;
     sp.num_materials = scene->num_materials;
     sp.lights = scene->lights;
@@ -850,7 +880,9 @@ gbrt_status render_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_cam
     const uint32_t n = p.width * p.height;
     camera_basis cam = camera_for(camera, p.width, p.height);
     gbrt_bvh const* bvh = scene->bvh;
-    shade_params sp = shade_params_for(scene, p, albedo, emission);
+    gbrt_status tst = ensure_trig_table(ctx);   // a no-op unless the scene came from another context
+    if (tst != GBRT_OK) return tst;
+    shade_params sp = shade_params_for(ctx, scene, p, albedo, emission);
     // background: ambient_light(bg.xyz, bg.w).intensity with alpha 1 (kernels.h:172-174,
     // pathtracing.inl:62)
     float4 bg = make_float4(p.background[0] * p.background[3], p.background[1] * p.background[3],
@@ -1001,7 +1033,9 @@ extern "C" gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene 
     if (bvh->num_prims == 0 || scene->num_materials == 0) return GBRT_OK;   // nothing to differentiate
     device_guard g(ctx->device);
     camera_basis cam = camera_for(*camera, p.width, p.height);
-    shade_params sp = shade_params_for(scene, p, d_albedo, d_emission);
+    gbrt_status tst = ensure_trig_table(ctx);
+    if (tst != GBRT_OK) return tst;
+    shade_params sp = shade_params_for(ctx, scene, p, d_albedo, d_emission);
     const uint64_t paths = uint64_t(p.width) * p.height * p.spp;
     if (paths > (1ull << 31)) return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_backward: more than 2^31 paths");
     const uint32_t blocks = uint32_t((paths + kBlock - 1) / kBlock);

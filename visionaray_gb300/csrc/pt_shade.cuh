@@ -43,7 +43,7 @@ __device__ __forceinline__ float max_elem(v3 v)
 }
 __device__ __forceinline__ float power_heuristic(float p1, float p2) { return (p1 * p1) / (p1 * p1 + p2 * p2); }
 __device__ __forceinline__ v3 xyz(float4 a) { return { a.x, a.y, a.z }; }
-// pow, cos and sin evaluated in double and rounded once to float.  pow with a
+// pow evaluated in double and rounded once to float.  pow with a
 // non-negative integer exponent up to 1024 (the Blinn exponents of typical scenes and
 // Schlick's fifth power) is binary exponentiation in double: at most 2 log2(y) roundings
 // of 2^-53 each, so the float result is the double pow's except for values within about
@@ -66,8 +66,6 @@ __device__ __forceinline__ float pow_d(float x, float y)
     }
     return float(pow(double(x), double(y)));
 }
-__device__ __forceinline__ float cos_d(float x) { return float(cos(double(x))); }
-__device__ __forceinline__ float sin_d(float x) { return float(sin(double(x))); }
 
 // blinn::f (brdf.h:128-141): Schlick's Fresnel term on cs * ks and the normalised
 // Blinn-Phong lobe
@@ -137,7 +135,18 @@ struct shade_params
     // slot) replacing the materials' own; light intensity = emission[geom] * kl
     const float* albedo;
     const float* emission;
+    // (cos, sin) of 2 pi u for the 2^24 values of a draw u (gbrt_context::d_trig)
+    const float2* trig;
 };
+
+// cos and sin of the float angle 2 pi u (u a draw of gbrt_rng_u01, a multiple of
+// 2^-24), each evaluated in double and rounded once to float -- looked up: the table
+// holds exactly those values for every u, computed once, so the shading kernels
+// issue no double-precision trigonometry (FP64 issue is slow on this GPU).
+__device__ __forceinline__ float2 trig_of(const float2* __restrict__ table, float u)
+{
+    return __ldg(&table[uint32_t(u * 16777216.0f) & 0xFFFFFFu]);
+}
 
 struct path_state
 {
@@ -202,12 +211,12 @@ struct lobe_sample
 // one draw picks the lobe by the mean reflectances, and the pdf returned is the chosen
 // lobe's alone.  Out of line, like plastic_nee below: the double-precision pow, cos and
 // sin would otherwise raise the register pressure of every kernel that shades.
-__device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restrict__ mp, v3 nn, v3 view,
+__device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restrict__ mp,
+                                                   const float2* __restrict__ trig, v3 nn, v3 view,
                                                    uint32_t frame, uint32_t p, uint32_t sample, uint32_t k)
 {
     const float inv_pi = 3.18309886183790691216444201928e-01f;
     const float pi = 3.14159265358979323846264338328e+00f;
-    const float two_pi = 6.28318530717958623199592693709e+00f;
     const gbrt_material m = *mp;
     lobe_sample out;
     float prob_diff = ((m.color[0] + m.color[1]) + m.color[2]) / 3.0f * m.scale;
@@ -226,8 +235,8 @@ __device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restri
         float u2 = gbrt_rng_u01(frame, p, sample, k++);
         float u1 = gbrt_rng_u01(frame, p, sample, k++);
         float r = sqrtf(u1);
-        float theta = two_pi * u2;
-        v3 s3 = { r * cos_d(theta), r * sin_d(theta), sqrtf(1.0f - u1) };
+        const float2 cs = trig_of(trig, u2);   // theta = two_pi * u2
+        v3 s3 = { r * cs.x, r * cs.y, sqrtf(1.0f - u1) };
         out.refl = normalize3(uu * s3.x + v * s3.y + w * s3.z);
         out.pdf = dot3(nn, out.refl) * inv_pi;
         out.src = (v3{ m.color[0], m.color[1], m.color[2] } * m.scale) * inv_pi;
@@ -243,8 +252,8 @@ __device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restri
         // except within ~2^-25 of a rounding boundary; cheaper than the double pow
         float costheta = float(exp2(double(1.0f / (m.exponent + 1.0f)) * log2(double(u1))));
         float sintheta = sqrtf(fmaxf(0.0f, 1.0f - costheta * costheta));
-        float phi = u2 * two_pi;
-        v3 h = normalize3(uu * (sintheta * cos_d(phi)) + v * (sintheta * sin_d(phi)) + w * costheta);
+        const float2 cs = trig_of(trig, u2);   // phi = u2 * two_pi
+        v3 h = normalize3(uu * (sintheta * cs.x) + v * (sintheta * cs.y) + w * costheta);
         out.refl = h * (2.0f * dot3(h, view)) - view;
         float vdoth = dot3(view, h);
         out.pdf = ((m.exponent + 1.0f) * pow_d(costheta, m.exponent)) / (2.0f * pi * 4.0f * vdoth);
@@ -372,7 +381,6 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
 {
     const float inv_pi = 3.18309886183790691216444201928e-01f;
     const float pi = 3.14159265358979323846264338328e+00f;
-    const float two_pi = 6.28318530717958623199592693709e+00f;
     out.cont = false;
     out.shadow = false;
     vertex_rec& rec = out.rec;
@@ -432,7 +440,8 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
     }
     else if (plastic)
     {
-        lobe_sample ls = sample_plastic(sp.materials + geom, faceforward3(sn, view, gn), view, sp.frame, p, sp.sample, st.k);
+        lobe_sample ls = sample_plastic(sp.materials + geom, sp.trig, faceforward3(sn, view, gn), view, sp.frame, p,
+                                        sp.sample, st.k);
         refl = ls.refl;
         brdf_pdf = ls.pdf;
         src = ls.src;
@@ -451,11 +460,9 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
         float u2 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
         float u1 = gbrt_rng_u01(sp.frame, p, sp.sample, st.k++);
         float r = sqrtf(u1);
-        float theta = two_pi * u2;
-        // cos and sin evaluated in double and rounded once to float
-        float ct = float(cos(double(theta)));
-        float sth = float(sin(double(theta)));
-        v3 s3 = { r * ct, r * sth, sqrtf(1.0f - u1) };
+        // theta = two_pi * u2; its cos and sin evaluated in double, rounded once to float
+        const float2 cs = trig_of(sp.trig, u2);
+        v3 s3 = { r * cs.x, r * cs.y, sqrtf(1.0f - u1) };
         refl = normalize3(u * s3.x + v * s3.y + w * s3.z);
         brdf_pdf = dot3(nn, refl) * inv_pi;
         src = (mcol * m.scale) * inv_pi;
