@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from visionaray_gb300.types import AREA_LIGHT, BVH_NODE, CAMERA, HIT, LIGHT, MATERIAL, PT_PARAMS, lights_of_area_lights
+from visionaray_gb300.types import BVH_NODE, CAMERA, HIT, LIGHT, MATERIAL, PT_PARAMS, lights_of_area_lights
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")

@@ -3,7 +3,6 @@ whose blobs cycle a plastic with zero reflectances (the lobe choice falls back t
 1/2 : 1/2), a plastic with exponent 0 and one with a non-integer exponent (7.5), glass
 of index 1 (no bending, no reflection) and of index 2.4 (more total internal
 reflection), and a mirror of index 1 without absorption."""
-import numpy as np
 
 from visionaray_gb300 import scenes
 from visionaray_gb300.types import GLASS, MIRROR, PLASTIC

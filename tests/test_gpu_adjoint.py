@@ -8,7 +8,6 @@ import pytest
 import torch
 
 import visionaray_gb300 as vg
-from oracle import Oracle
 from visionaray_gb300 import inverse, scenes
 
 pytestmark = pytest.mark.gpu

@@ -11,7 +11,7 @@ import torch
 
 import visionaray_gb300 as vg
 from visionaray_gb300 import scenes
-from visionaray_gb300.types import BATCH_ORDER_BLOCKS, BATCH_ORDER_ROWS, HIT, TRIANGLE
+from visionaray_gb300.types import BATCH_ORDER_BLOCKS, BATCH_ORDER_ROWS, TRIANGLE
 
 from .parity import compare_closest
 

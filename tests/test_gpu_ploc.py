@@ -7,7 +7,6 @@ import pytest
 import visionaray_gb300 as vg
 from oracle import Tree
 from visionaray_gb300 import scenes
-from visionaray_gb300.types import NO_HIT
 
 from .parity import compare_any, compare_closest
 

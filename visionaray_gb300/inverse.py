@@ -6,8 +6,6 @@ uniform start, each step a forward frame, the L2 image loss and the backward pas
 (gbrt_pathtrace_forward / gbrt_pathtrace_backward).  Random numbers are common
 (frame_id fixed) between the forward and backward pass of a step.
 """
-import time
-
 import numpy as np
 
 from . import runtime as rt
