@@ -1,0 +1,45 @@
+"""bench.py's JSON line on a reduced workload: every key of the benchmark contract is
+present and consistent (value = rays per step / time, e2e on the host path giving the
+device path's hits, a roofline fraction, clock samples taken inside the timed region,
+counted kernel launches)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(*args):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                         timeout=900, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [line for line in out.stdout.splitlines() if line.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+def test_bench_line_has_the_contract_keys():
+    d = run_bench("--steps", "3", "--warmup", "3", "--grid", "256", "--origins", "16384", "--pt-frames", "1",
+                  "--batch-steps", "1", "--batch-scenes", "8", "--batch-max-tris", "20000", "--adjoint-steps", "3",
+                  "--no-cpu-baseline")
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "roofline", "e2e", "gpu_launches", "clocks"):
+        assert key in d, key
+    assert d["n_gpus"] == 1 and d["steps"] == 3 and d["warmup"] == 3 and d["higher_is_better"] is True
+    rays = d["config"]["rays_per_step"]
+    assert d["value"] == pytest.approx(rays / (d["ms_per_step"] * 1e-3) / 1e6, rel=1e-2)
+    r = d["roofline"]
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-3)
+    e = d["e2e"]
+    assert e["value"] > 0 and e["h2d_bytes_per_step"] == 32 * rays and e["d2h_bytes_per_step"] == 16 * rays
+    assert e["matches_device_path"] is True
+    assert d["gpu_launches"] > 0
+    assert d["clocks"]["samples"] >= 1
+    assert d["pathtrace"]["msamples_s"] > 0 and d["batched_pathtrace"]["images_bit_identical"] is True
+    assert d["adjoint"]["bwd_ms"] > 0
+
