@@ -119,6 +119,12 @@ int         gbrt_abi_version(void);
  * with new rays from an atomic counter instead of idling until their slowest ray ends
  * (node pairs only; hits identical bit for bit).                                     */
 #define GBRT_TRACE_PERSISTENT 4u
+/* With this flag set when gbrt_bvh_build_lbvh runs, the 4-wide nodes are also stored
+ * quantised to 64 bytes in the layout of visionaray's bvh_compressed_node<4> (bvh.h:
+ * 319-426; 8-bit offsets in power-of-two units, rounded outward), and ray queries on a
+ * context with the flag traverse those.  Implies the 4-wide collapse.  Path tracing
+ * keeps the node pairs (or the 4-wide nodes).                                         */
+#define GBRT_TRACE_COMPRESSED_NODES 8u
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
 
 /* Persistent traversal: a warp refills once at least min_idle_lanes (1..32, default 8)

@@ -89,6 +89,7 @@ struct gbrt_bvh
     gbrt::bvh4_node* nodes4 = nullptr;
     uint32_t num_nodes4 = 0;
     uint32_t leaf_max4 = 0;
+    gbrt::bvh4q_node* nodes4q = nullptr;   // the same nodes quantised (GBRT_TRACE_COMPRESSED_NODES)
 };
 
 // Many scenes built and traced as one arena (batch.cu, batch_pt.cu).  Scene s owns

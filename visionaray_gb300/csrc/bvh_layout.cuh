@@ -56,6 +56,24 @@ struct __align__(16) bvh4_node
 };
 static_assert(sizeof(bvh4_node) == 128, "4-wide node is 128 bytes");
 
+// Quantised 4-wide node (64 bytes = four 128-bit loads) in the byte layout of
+// visionaray's bvh_compressed_node<4> (bvh.h:319-426): the children's boxes as 8-bit
+// offsets from the node's origin in units of 2^e per axis (24 bytes, lo x/y/z then
+// hi x/y/z, four children each), the children as packed {int id; short count} (24
+// bytes), the origin (12 bytes) and the three exponents (3 bytes).  count > 0: leaf of
+// count triangles from id; 0: inner child, id indexes these nodes; -1: empty slot.
+// The quantisation rounds outward and the traversal decodes with directed rounding, so
+// every decoded box contains its child's true box.
+struct __align__(16) bvh4q_node
+{
+    unsigned char q[24];         // lo.x[4] lo.y[4] lo.z[4] hi.x[4] hi.y[4] hi.z[4]
+    unsigned char children[24];  // 4 x {int32 id; int16 count}, packed
+    float origin[3];
+    signed char e[3];
+    unsigned char pad;
+};
+static_assert(sizeof(bvh4q_node) == 64, "quantised 4-wide node is 64 bytes");
+
 constexpr int kStack4 = 96;        // 4-wide traversal stack entries (up to 3 per level)
 constexpr int kLeafMax4 = 4;       // triangles per 4-wide leaf (default)
 

@@ -200,6 +200,74 @@ __global__ void __launch_bounds__(kBlock) refit_and_emit(gbrt_triangle const* __
     atomicOr(status, kStatusBadIndex);
 }
 
+// bvh_compressed_node<4>::init (bvh.h:350-393) on the GPU, rounding outward: origin =
+// the node box's low corner, per axis the exponent e of the smallest power of two with
+// 255 * 2^e >= the box's extent (rounded up), and per child
+// lo = floor(round_down(lo - origin) / 2^e), hi = ceil(round_up(hi - origin) / 2^e);
+// the division by 2^e is exact.  Decoding origin + q * 2^e rounded down (lo) or up (hi)
+// then never shrinks a box.
+__device__ __forceinline__ int quant_exponent(float extent)
+{
+    float t = __fdiv_ru(extent, 255.0f);
+    if (!(t > 0.0f)) return -126;   // flat (or degenerate) axis: every offset is 0
+    int ex;
+    float m = frexpf(t, &ex);       // t = m * 2^ex, m in [0.5, 1)
+    int e = m == 0.5f ? ex - 1 : ex;
+    return e < -126 ? -126 : (e > 126 ? 126 : e);
+}
+
+__global__ void __launch_bounds__(kBlock) quantize_nodes4(const bvh4_node* __restrict__ nodes4, uint32_t count,
+                                                          bvh4q_node* __restrict__ out)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= count) return;
+    bvh4_node nd = nodes4[i];
+    const float lo[3][4] = { { nd.lox.x, nd.lox.y, nd.lox.z, nd.lox.w },
+                             { nd.loy.x, nd.loy.y, nd.loy.z, nd.loy.w },
+                             { nd.loz.x, nd.loz.y, nd.loz.z, nd.loz.w } };
+    const float hi[3][4] = { { nd.hix.x, nd.hix.y, nd.hix.z, nd.hix.w },
+                             { nd.hiy.x, nd.hiy.y, nd.hiy.z, nd.hiy.w },
+                             { nd.hiz.x, nd.hiz.y, nd.hiz.z, nd.hiz.w } };
+    const int ch[4] = { nd.child.x, nd.child.y, nd.child.z, nd.child.w };
+    const int ct[4] = { nd.count.x, nd.count.y, nd.count.z, nd.count.w };
+    bvh4q_node q;
+    for (int a = 0; a < 3; ++a)
+    {
+        float mn = FLT_MAX, mx = -FLT_MAX;
+        for (int k = 0; k < 4; ++k)
+        {
+            if (ct[k] < 0) continue;
+            mn = fminf(mn, lo[a][k]);
+            mx = fmaxf(mx, hi[a][k]);
+        }
+        if (mn > mx) mn = mx = 0.0f;   // no child (cannot happen for an emitted node)
+        const int e = quant_exponent(__fsub_ru(mx, mn));
+        const float inv = __int_as_float((127 - e) << 23);   // 2^-e, e in [-126, 126]
+        q.origin[a] = mn;
+        q.e[a] = (signed char)e;
+        for (int k = 0; k < 4; ++k)
+        {
+            float ql = 0.0f, qh = 0.0f;
+            if (ct[k] >= 0)
+            {
+                ql = floorf(__fsub_rd(lo[a][k], mn) * inv);
+                qh = ceilf(__fsub_ru(hi[a][k], mn) * inv);
+            }
+            q.q[a * 4 + k] = (unsigned char)fminf(fmaxf(ql, 0.0f), 255.0f);
+            q.q[12 + a * 4 + k] = (unsigned char)fminf(fmaxf(qh, 0.0f), 255.0f);
+        }
+    }
+    for (int k = 0; k < 4; ++k)
+    {
+        int32_t id = ct[k] < 0 ? -1 : ch[k];
+        int16_t c = ct[k] < 0 ? int16_t(-1) : int16_t(ct[k]);
+        memcpy(&q.children[6 * k], &id, 4);
+        memcpy(&q.children[6 * k + 4], &c, 2);
+    }
+    q.pad = 0;
+    out[i] = q;
+}
+
 // One level of the collapse into 4-wide nodes: every queued (pair node, 4-wide node)
 // item opens the pair node's two children and keeps opening the inner child of largest
 // surface area until four children are reached; children with at most leaf_max
@@ -603,7 +671,7 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
         // scene bounds: the union of the root's two child boxes
         set_scene_box(bvh, root);
 
-        if (ctx->trace_flags & GBRT_TRACE_WIDE_NODES)
+        if (ctx->trace_flags & (GBRT_TRACE_WIDE_NODES | GBRT_TRACE_COMPRESSED_NODES))
         {
             // collapse into 4-wide nodes (on request), one level per launch; the pair tree
             // has h inner levels, so h levels drain every queue
@@ -632,6 +700,13 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
             GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4, size_t(bvh->num_nodes4) * sizeof(bvh4_node)));
             GBRT_CUDA(ctx, cudaMemcpyAsync(bvh->nodes4, nodes4_tmp, size_t(bvh->num_nodes4) * sizeof(bvh4_node),
                                            cudaMemcpyDeviceToDevice, s));
+            if (ctx->trace_flags & GBRT_TRACE_COMPRESSED_NODES)
+            {
+                GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4q, size_t(bvh->num_nodes4) * sizeof(bvh4q_node)));
+                quantize_nodes4<<<blocks_for(bvh->num_nodes4), kBlock, 0, s>>>(bvh->nodes4, bvh->num_nodes4,
+                                                                                bvh->nodes4q);
+                GBRT_LAUNCH_CHECK(ctx, "quantize_nodes4");
+            }
         }
     }
     else
@@ -662,6 +737,8 @@ gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_
         cudaFree(bvh->nodes4);
         bvh->nodes4 = nullptr;
         bvh->num_nodes4 = 0;
+        cudaFree(bvh->nodes4q);
+        bvh->nodes4q = nullptr;
     }
     if (n == 1)
     {

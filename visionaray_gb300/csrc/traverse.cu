@@ -22,14 +22,27 @@ constexpr int kSharedStack = 16;
 constexpr int kMinBlocksAny = 12, kMinBlocksClosest = 12;
 
 // One ray through the node pairs (stack top in shared memory) or the 4-wide nodes.
-template <bool AnyHit, bool Wide>
+// Node layouts of the ray queries: the node pairs, the 4-wide nodes, the quantised
+// 4-wide nodes.
+enum : int
+{
+    kNodesPairs = 0,
+    kNodesWide = 1,
+    kNodesCompressed = 2,
+};
+
+template <bool AnyHit, int Nodes>
 __device__ __forceinline__ trace_result trace_one(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
                                                   uint32_t* __restrict__ status)
 {
-    return traverse_view_shared<AnyHit, Wide, kTraceBlock, kSharedStack>(v, o, d, tmin, tmax, status);
+    if constexpr (Nodes == kNodesCompressed)
+        return traverse_bvh4<AnyHit>(v.nodes4q, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
+    else
+        return traverse_view_shared<AnyHit, Nodes == kNodesWide, kTraceBlock, kSharedStack>(v, o, d, tmin, tmax,
+                                                                                              status);
 }
 
-template <bool AnyHit, bool Wide>
+template <bool AnyHit, int Nodes>
 __global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBlocksClosest) trace_rays(bvh_view v, const gbrt_ray* __restrict__ rays, uint32_t n,
                                                           gbrt_hit* __restrict__ hits,
                                                           uint32_t* __restrict__ status)
@@ -39,14 +52,14 @@ __global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBloc
 
     float4 r0 = ldg4(&rays[i]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
-    trace_result h = trace_one<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = trace_one<AnyHit, Nodes>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[i] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
 }
 
 // Rays in the order perm[0..n): ray j = perm[i] writes hit j.
-template <bool AnyHit, bool Wide>
+template <bool AnyHit, int Nodes>
 __global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBlocksClosest) trace_rays_permuted(bvh_view v, const gbrt_ray* __restrict__ rays,
                                                                    uint32_t n, const uint32_t* __restrict__ perm,
                                                                    gbrt_hit* __restrict__ hits,
@@ -62,7 +75,7 @@ __global__ void __launch_bounds__(kTraceBlock, AnyHit ? kMinBlocksAny : kMinBloc
     }
     float4 r0 = ldg4(&rays[j]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[j]) + 1);
-    trace_result h = trace_one<AnyHit, Wide>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    trace_result h = trace_one<AnyHit, Nodes>(v, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     uint32_t prim = h.tri >= 0 ? __float_as_uint(ldg4(&v.tris[h.tri].t0).w) : GBRT_NO_HIT;
     reinterpret_cast<uint4*>(hits)[j] =
         make_uint4(prim, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
@@ -300,9 +313,10 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         return GBRT_OK;
     }
     const bvh_view v = view_of(bvh);
-    const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
+    const bool compressed = bvh->nodes4q != nullptr && (ctx->trace_flags & GBRT_TRACE_COMPRESSED_NODES);
+    const bool wide = !compressed && bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     const bool have_scratch = scratch && scratch_bytes >= trace_scratch_bytes(n);
-    const bool persistent = (ctx->trace_flags & GBRT_TRACE_PERSISTENT) && !wide && have_scratch;
+    const bool persistent = (ctx->trace_flags & GBRT_TRACE_PERSISTENT) && !wide && !compressed && have_scratch;
     const uint32_t* perm = nullptr;
     if ((ctx->trace_flags & GBRT_TRACE_SORT_RAYS) && n >= kSortMinRays && have_scratch)
     {
@@ -328,10 +342,14 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         {
             auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
                                                                                         ctx->d_status); };
-            if (wide)
-                any_hit ? launch(trace_rays_permuted<true, true>) : launch(trace_rays_permuted<false, true>);
+            if (compressed)
+                any_hit ? launch(trace_rays_permuted<true, kNodesCompressed>)
+                        : launch(trace_rays_permuted<false, kNodesCompressed>);
+            else if (wide)
+                any_hit ? launch(trace_rays_permuted<true, kNodesWide>) : launch(trace_rays_permuted<false, kNodesWide>);
             else
-                any_hit ? launch(trace_rays_permuted<true, false>) : launch(trace_rays_permuted<false, false>);
+                any_hit ? launch(trace_rays_permuted<true, kNodesPairs>)
+                        : launch(trace_rays_permuted<false, kNodesPairs>);
             GBRT_LAUNCH_CHECK(ctx, "trace_rays_permuted");
             return GBRT_OK;
         }
@@ -351,10 +369,12 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         return GBRT_OK;
     }
     auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, d_hits, ctx->d_status); };
-    if (wide)
-        any_hit ? launch(trace_rays<true, true>) : launch(trace_rays<false, true>);
+    if (compressed)
+        any_hit ? launch(trace_rays<true, kNodesCompressed>) : launch(trace_rays<false, kNodesCompressed>);
+    else if (wide)
+        any_hit ? launch(trace_rays<true, kNodesWide>) : launch(trace_rays<false, kNodesWide>);
     else
-        any_hit ? launch(trace_rays<true, false>) : launch(trace_rays<false, false>);
+        any_hit ? launch(trace_rays<true, kNodesPairs>) : launch(trace_rays<false, kNodesPairs>);
     GBRT_LAUNCH_CHECK(ctx, "trace_rays");
     return GBRT_OK;
 }

@@ -163,13 +163,66 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
     return traverse_bvh_with<AnyHit>(stack, nodes, tris, root, num_inner, num_tris, o, d, tmin, tmax, status);
 }
 
-// The same query over the 4-wide nodes (bvh_layout.cuh): one eight-load node fetch
-// tests four boxes; hit leaves are tested at once (so best.t shrinks before the
+// The four child boxes and links of a 4-wide node: eight loads of the plain node ...
+__device__ __forceinline__ void decode4(const bvh4_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
+                                        float hy[4], float lz[4], float hz[4], int ch[4], int ct[4])
+{
+    float4 lox = ldg4(&np->lox), hix = ldg4(&np->hix);
+    float4 loy = ldg4(&np->loy), hiy = ldg4(&np->hiy);
+    float4 loz = ldg4(&np->loz), hiz = ldg4(&np->hiz);
+    int4 ch4 = __ldg(&np->child);
+    int4 ct4 = __ldg(&np->count);
+    lx[0] = lox.x, lx[1] = lox.y, lx[2] = lox.z, lx[3] = lox.w;
+    hx[0] = hix.x, hx[1] = hix.y, hx[2] = hix.z, hx[3] = hix.w;
+    ly[0] = loy.x, ly[1] = loy.y, ly[2] = loy.z, ly[3] = loy.w;
+    hy[0] = hiy.x, hy[1] = hiy.y, hy[2] = hiy.z, hy[3] = hiy.w;
+    lz[0] = loz.x, lz[1] = loz.y, lz[2] = loz.z, lz[3] = loz.w;
+    hz[0] = hiz.x, hz[1] = hiz.y, hz[2] = hiz.z, hz[3] = hiz.w;
+    ch[0] = ch4.x, ch[1] = ch4.y, ch[2] = ch4.z, ch[3] = ch4.w;
+    ct[0] = ct4.x, ct[1] = ct4.y, ct[2] = ct4.z, ct[3] = ct4.w;
+}
+
+// ... or four loads of the quantised node, decoded as origin + q * 2^e rounded down for
+// the low and up for the high planes (q * 2^e is exact), so no box shrinks.
+__device__ __forceinline__ void decode4(const bvh4q_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
+                                        float hy[4], float lz[4], float hz[4], int ch[4], int ct[4])
+{
+    const uint4* w = reinterpret_cast<const uint4*>(np);
+    const uint4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2), w3 = __ldg(w + 3);
+    const float ox = __uint_as_float(w3.x), oy = __uint_as_float(w3.y), oz = __uint_as_float(w3.z);
+    const int ex = int(int8_t(w3.w & 0xFFu)), ey = int(int8_t((w3.w >> 8) & 0xFFu)),
+              ez = int(int8_t((w3.w >> 16) & 0xFFu));
+    const float sx = __int_as_float((ex + 127) << 23), sy = __int_as_float((ey + 127) << 23),
+                sz = __int_as_float((ez + 127) << 23);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const int sh = 8 * k;
+        lx[k] = __fmaf_rd(float((w0.x >> sh) & 0xFFu), sx, ox);
+        ly[k] = __fmaf_rd(float((w0.y >> sh) & 0xFFu), sy, oy);
+        lz[k] = __fmaf_rd(float((w0.z >> sh) & 0xFFu), sz, oz);
+        hx[k] = __fmaf_ru(float((w0.w >> sh) & 0xFFu), sx, ox);
+        hy[k] = __fmaf_ru(float((w1.x >> sh) & 0xFFu), sy, oy);
+        hz[k] = __fmaf_ru(float((w1.y >> sh) & 0xFFu), sz, oz);
+    }
+    // children: {int32 id; int16 count} packed at bytes 24 + 6k
+    ch[0] = int(w1.z);
+    ct[0] = int(int16_t(w1.w & 0xFFFFu));
+    ch[1] = int(__byte_perm(w1.w, w2.x, 0x5432));
+    ct[1] = int(int16_t(w2.x >> 16));
+    ch[2] = int(w2.y);
+    ct[2] = int(int16_t(w2.z & 0xFFFFu));
+    ch[3] = int(__byte_perm(w2.z, w2.w, 0x5432));
+    ct[3] = int(int16_t(w2.w >> 16));
+}
+
+// The same query over 4-wide nodes (bvh_layout.cuh, plain or quantised): one node
+// fetch tests four boxes; hit leaves are tested at once (so best.t shrinks before the
 // inner children are ordered), the hit inner children are visited nearest first and
 // the others pushed with their entry distance, so a popped entry already beyond the
 // best hit is dropped without a fetch.
-template <bool AnyHit>
-__device__ __forceinline__ trace_result traverse_bvh4(const bvh4_node* __restrict__ nodes4, int32_t num_nodes4,
+template <bool AnyHit, typename Node4>
+__device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ nodes4, int32_t num_nodes4,
                                                       const tri48* __restrict__ tris, int32_t num_tris, f3 o, f3 d,
                                                       float tmin, float tmax, uint32_t* __restrict__ status)
 {
@@ -187,17 +240,9 @@ __device__ __forceinline__ trace_result traverse_bvh4(const bvh4_node* __restric
             atomicOr(status, kStatusBadIndex);
             break;
         }
-        const bvh4_node* np = nodes4 + node;
-        float4 lox = ldg4(&np->lox), hix = ldg4(&np->hix);
-        float4 loy = ldg4(&np->loy), hiy = ldg4(&np->hiy);
-        float4 loz = ldg4(&np->loz), hiz = ldg4(&np->hiz);
-        int4 ch4 = __ldg(&np->child);
-        int4 ct4 = __ldg(&np->count);
-        const float lx[4] = { lox.x, lox.y, lox.z, lox.w }, hx[4] = { hix.x, hix.y, hix.z, hix.w };
-        const float ly[4] = { loy.x, loy.y, loy.z, loy.w }, hy[4] = { hiy.x, hiy.y, hiy.z, hiy.w };
-        const float lz[4] = { loz.x, loz.y, loz.z, loz.w }, hz[4] = { hiz.x, hiz.y, hiz.z, hiz.w };
-        const int ch[4] = { ch4.x, ch4.y, ch4.z, ch4.w };
-        const int ct[4] = { ct4.x, ct4.y, ct4.z, ct4.w };
+        float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
+        int ch[4], ct[4];
+        decode4(nodes4 + node, lx, hx, ly, hy, lz, hz, ch, ct);
         float tn[4];
         bool hit[4];
 #pragma unroll
@@ -310,13 +355,14 @@ struct bvh_view
 {
     const bvh2_node* nodes;
     const bvh4_node* nodes4;
+    const bvh4q_node* nodes4q;
     const tri48* tris;
     int32_t root, num_inner, num_nodes4, num_tris;
 };
 
 inline bvh_view view_of(gbrt_bvh const* b)
 {
-    return { b->nodes, b->nodes4, b->tris, b->root, int32_t(b->num_inner), int32_t(b->num_nodes4),
+    return { b->nodes, b->nodes4, b->nodes4q, b->tris, b->root, int32_t(b->num_inner), int32_t(b->num_nodes4),
              int32_t(b->num_prims) };
 }
 

@@ -141,6 +141,7 @@ class Context:
     TRACE_SORT_RAYS = 1
     TRACE_WIDE_NODES = 2
     TRACE_PERSISTENT = 4
+    TRACE_COMPRESSED_NODES = 8
 
     def set_trace_flags(self, flags):
         """GBRT_TRACE_* options of the ray queries (TRACE_SORT_RAYS: coherent order)."""
