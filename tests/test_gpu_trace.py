@@ -68,7 +68,8 @@ def test_host_buffer_path_equals_device_path(soup_case):
 @pytest.mark.parametrize("chunk", [1 << 16, 1 << 17])
 def test_host_buffer_path_in_chunks(soup_case, chunk):
     """Small host chunks: the query runs as a quarter chunk, full chunks, the rest and
-    a quarter chunk on alternating slots; hits equal the device path's bit for bit."""
+    a quarter chunk on alternating slots (a query of at most one chunk as a quarter, a
+    half and a quarter of itself); hits equal the device path's bit for bit."""
     tris, rays, _, _, _ = soup_case
     ctx = vg.Context(0)
     ctx.set_host_chunk(chunk)
@@ -79,6 +80,8 @@ def test_host_buffer_path_in_chunks(soup_case, chunk):
     assert host.tobytes() == dev.tobytes()
     odd = rays[: 2 * chunk + 12345]
     assert vg.closest_hit(odd, bvh).tobytes() == dev[: len(odd)].tobytes()
+    small = rays[: chunk - 7]   # a quarter, a half and a quarter of itself
+    assert vg.closest_hit(small, bvh).tobytes() == dev[: len(small)].tobytes()
     with pytest.raises(vg.runtime.GbrtError):
         ctx.set_host_chunk(1000)
 

@@ -103,15 +103,24 @@ gbrt_status ensure_slots(gbrt_context* ctx, size_t rays_per_slot)
 
 // The chunk sizes of a host-buffer query of n rays with full chunks of c: a quarter
 // chunk first and last (the copy-in before the first traversal and the copy-out after
-// the last one overlap nothing), full chunks between.  Queries of at most 2c rays are
-// split into a quarter, the middle and a quarter.
+// the last one overlap nothing), full chunks between.  Queries of at most c rays are
+// split into a quarter, a half and a quarter of themselves; at most c / 4 rays, one
+// chunk.
 std::vector<size_t> host_chunks(size_t n, size_t c)
 {
     std::vector<size_t> out;
     const size_t q = c / 4;
-    if (n <= 2 * q)
+    if (n <= q)
     {
         out.push_back(n);
+        return out;
+    }
+    if (n <= c)
+    {
+        const size_t a = n / 4;
+        out.push_back(a);
+        out.push_back(n - 2 * a);
+        out.push_back(a);
         return out;
     }
     out.push_back(q);
