@@ -209,8 +209,8 @@ struct lobe_sample
 
 // plastic::sample (detail/material/plastic.inl:42-95) on the faceforwarded normal nn:
 // one draw picks the lobe by the mean reflectances, and the pdf returned is the chosen
-// lobe's alone.  Out of line, like plastic_nee below: the double-precision pow, cos and
-// sin would otherwise raise the register pressure of every kernel that shades.
+// lobe's alone.  Out of line, like plastic_nee below: the double-precision pow and
+// exp2 / log2 would otherwise raise the register pressure of every kernel that shades.
 __device__ __noinline__ lobe_sample sample_plastic(const gbrt_material* __restrict__ mp,
                                                    const float2* __restrict__ trig, v3 nn, v3 view,
                                                    uint32_t frame, uint32_t p, uint32_t sample, uint32_t k)
