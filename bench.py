@@ -510,6 +510,12 @@ def run_ours(args):
                             if (args.grid, args.origins, args.trace_flags) == (GRID, ORIGINS, 1) else None),
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size capture",
                 "peak_source": f"{peak_kind} hbm_gbs"}
+    # the pure-I/O floor (48 B per ray: the ray in, the hit out) and the DRAM bandwidth
+    # the launch actually drew (its ncu traffic over its event time)
+    io_gbs = d["rays"] * 48 / (d["ms_per_launch"] * 1e-3) / 1e9
+    roofline["io_floor"] = {"bytes_per_ray": 48, "achieved_gbs": round(io_gbs, 1), "frac": round(io_gbs / peak, 4)}
+    if roofline["traffic"]:
+        roofline["dram_gbs"] = round(roofline["traffic"] / (d["ms_per_launch"] * 1e-3) / 1e9, 1)
 
     # the same rays through the PLOC tree (a higher-quality GPU build; the workload's
     # builder is the LBVH, so this is reported beside the line's value, not as it)
