@@ -35,6 +35,7 @@ def test_bench_line_has_the_contract_keys():
     assert d["value"] == pytest.approx(rays / (d["ms_per_step"] * 1e-3) / 1e6, rel=1e-2)
     r = d["roofline"]
     assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-3)
+    assert r["io_floor"]["bytes_per_ray"] == 48 and 0 < r["io_floor"]["frac"] < r["frac"]
     e = d["e2e"]
     assert e["value"] > 0 and e["h2d_bytes_per_step"] == 32 * rays and e["d2h_bytes_per_step"] == 16 * rays
     assert e["matches_device_path"] is True
