@@ -79,6 +79,31 @@ inline box combine(box a, box const& b)
     return a;
 }
 
+// The GPU builder's float atomicMin / atomicMax (detail/bvh/lbvh.h:63-91): a compare-
+// and-swap loop from +FLT_MAX / -FLT_MAX that stores a value only when it lies below
+// (above) the current one, so NaN, +Inf into a minimum and -Inf into a maximum never
+// land.  Folding cas_lo / cas_hi of each value gives those bounds in any order.
+inline float cas_lo(float x) { return x < FLT_MAX ? x : FLT_MAX; }
+inline float cas_hi(float x) { return x > -FLT_MAX ? x : -FLT_MAX; }
+
+inline void atomic_insert(box& b, v3 p)
+{
+    b.lo = { vmin(b.lo.x, cas_lo(p.x)), vmin(b.lo.y, cas_lo(p.y)), vmin(b.lo.z, cas_lo(p.z)) };
+    b.hi = { vmax(b.hi.x, cas_hi(p.x)), vmax(b.hi.y, cas_hi(p.y)), vmax(b.hi.z, cas_hi(p.z)) };
+}
+
+// assign_node_bounds (lbvh.h:332-372): an inner box is the atomic fold of the leaf boxes
+// below it.
+inline box atomic_combine(box const& a, box const& b)
+{
+    box r;
+    r.lo = { vmin(cas_lo(a.lo.x), cas_lo(b.lo.x)), vmin(cas_lo(a.lo.y), cas_lo(b.lo.y)),
+             vmin(cas_lo(a.lo.z), cas_lo(b.lo.z)) };
+    r.hi = { vmax(cas_hi(a.hi.x), cas_hi(b.hi.x)), vmax(cas_hi(a.hi.y), cas_hi(b.hi.y)),
+             vmax(cas_hi(a.hi.z), cas_hi(b.hi.z)) };
+    return r;
+}
+
 inline float safe_half_surface_area(box const& b)
 {
     v3 s = b.size();
@@ -755,7 +780,7 @@ extern "C" void orc_morton_codes(const gbrt_triangle* tris, uint32_t n, uint32_t
     for (uint32_t i = 0; i < n; ++i)
     {
         cen[i] = tri_bounds(tris[i]).center();
-        cb.insert(cen[i]);
+        atomic_insert(cb, cen[i]);   // lbvh.h:233-238
     }
     for (uint32_t i = 0; i < n; ++i) codes[i] = quantise_centroid(cen[i], cb);
 }
@@ -786,7 +811,7 @@ extern "C" orc_bvh* orc_build_karras(const gbrt_triangle* tris, uint32_t n)
     {
         pb[i] = tri_bounds(tris[i]);
         cen[i] = pb[i].center();
-        cb.insert(cen[i]);
+        atomic_insert(cb, cen[i]);   // lbvh.h:233-238
     }
     struct ref
     {
@@ -828,7 +853,7 @@ extern "C" orc_bvh* orc_build_karras(const gbrt_triangle* tris, uint32_t n)
             st.pop_back();
             if (expanded)
             {
-                inner_box[size_t(i)] = combine(child_box(left[size_t(i)]), child_box(right[size_t(i)]));
+                inner_box[size_t(i)] = atomic_combine(child_box(left[size_t(i)]), child_box(right[size_t(i)]));
                 continue;
             }
             st.push_back({ i, true });

@@ -62,3 +62,27 @@ def compare_any(got, ref, rays, tris_by_prim, oracle):
         assert hit and rec["t"] == got["t"][i], i
         assert rays["tmin"][i] <= got["t"][i] <= rays["tmax"][i], i
     return {"rays": int(len(rays)), "occluded": int(g_occ.sum())}
+
+
+def non_finite_soup(n_good=20000, seed=9):
+    """A triangle soup with 20 zero-area, 20 NaN-vertex and 20 Inf-vertex triangles
+    inserted after the first half (prim ids = positions; the bad ones are
+    n_good // 2 .. n_good // 2 + 59)."""
+    from visionaray_gb300 import scenes
+    good = scenes.soup(n_good, seed=seed)
+    bad = np.zeros(60, good.dtype)
+    rng = np.random.default_rng(2)
+    bad["v1"] = rng.uniform(0, 1, size=(60, 3))
+    bad["e1"][:20] = (0.1, 0.0, 0.0)   # zero area: e2 parallel to e1
+    bad["e2"][:20] = (0.2, 0.0, 0.0)
+    bad["v1"][20:40, 1] = np.nan
+    bad["e1"][20:40] = (0.05, 0.0, 0.0)
+    bad["e2"][20:40] = (0.0, 0.05, 0.0)
+    bad["v1"][40:] = (np.inf, 0.5, 0.5)
+    bad["e1"][40:] = (0.05, 0.0, 0.0)
+    bad["e2"][40:] = (0.0, 0.05, 0.0)
+    h = n_good // 2
+    tris = np.concatenate([good[:h], bad, good[h:]])
+    tris["prim_id"] = np.arange(len(tris))
+    tris["geom_id"] = 0
+    return tris

@@ -11,7 +11,7 @@ import visionaray_gb300 as vg
 from visionaray_gb300 import scenes
 from visionaray_gb300.types import NO_HIT, RAY, TRIANGLE
 
-from .parity import compare_any, compare_closest
+from .parity import compare_any, compare_closest, non_finite_soup
 
 pytestmark = pytest.mark.gpu
 
@@ -250,3 +250,22 @@ def test_compressed_nodes_agree(oracle, grid, sort):
     got = trace(bvh2, rays)
     ref = oracle.trace(oracle.build_sah(soup), soup, rays)
     compare_closest(got, ref, rays, soup, oracle)
+
+
+def test_degenerate_and_non_finite_triangles(oracle):
+    """Zero-area, NaN and Inf triangles: the build and the queries complete without a
+    flagged fault, no ray hits a bad triangle, and the tree is the reference GPU
+    builder's for the same input (the oracle's restatement, traversed on the CPU): its
+    atomic bottom-up bounds skip NaN, so every ray's closest hit is the brute-force one."""
+    tris = non_finite_soup()
+    rays = scenes.pinhole_rays(256, 256)
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    got = trace(bvh, rays)
+    got_any = trace(bvh, rays, any_hit=True)
+    ref = oracle.trace(oracle.build_karras(tris), tris, rays)
+    compare_closest(got, ref, rays, tris, oracle)
+    hit = got["prim_id"] != NO_HIT
+    assert (got["prim_id"][hit] < 10000).sum() + (got["prim_id"][hit] >= 10060).sum() == hit.sum()
+    assert ((got_any["prim_id"] != NO_HIT) == hit).all()
+    lin = oracle.trace_linear(tris, rays)
+    compare_closest(got, lin, rays, tris, oracle)

@@ -90,3 +90,24 @@ def test_lbvh_cpu_rejects_max_leaf_one(oracle):
     # lbvh.h:505-508 + :633-645 recurse forever for max_leaf_size = 1 with equal codes
     with pytest.raises(ValueError):
         oracle.build_lbvh_cpu(four_tris(), max_leaf=1)
+
+
+def test_karras_bounds_skip_non_finite(oracle):
+    """The GPU builder's bounds are float atomicMin / atomicMax by compare-and-swap from
+    (+FLT_MAX, -FLT_MAX) (detail/bvh/lbvh.h:63-91, 233-238, 332-372), which never store
+    NaN, nor +Inf into a minimum or -Inf into a maximum: in the restated tree only the
+    NaN triangles' own leaves carry NaN, no inner box does, and the closest hits over
+    the tree are the brute-force ones."""
+    from visionaray_gb300 import scenes
+
+    from .parity import compare_closest, non_finite_soup
+    tris = non_finite_soup(4000, seed=4)
+    tree = oracle.build_karras(tris)
+    inner = tree.nodes["num_prims"] == 0
+    boxes = np.concatenate([tree.nodes["bbox_min"], tree.nodes["bbox_max"]], axis=1)
+    assert not np.isnan(boxes[inner]).any()
+    nan_leaves = np.isnan(boxes[~inner]).any(axis=1).sum()
+    assert nan_leaves == 20
+    assert (tree.nodes["bbox_min"][inner] < np.float32(np.inf)).all()
+    rays = scenes.pinhole_rays(64, 64)
+    compare_closest(oracle.trace(tree, tris, rays), oracle.trace_linear(tris, rays), rays, tris, oracle)

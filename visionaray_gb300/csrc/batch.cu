@@ -54,15 +54,16 @@ __global__ void __launch_bounds__(kBlock) batch_centroids(gbrt_triangle const* _
     uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
     if (!active) return;
     uint32_t peers = __match_any_sync(mask, s);
-    float mn[3] = { c.x, c.y, c.z }, mx[3] = { c.x, c.y, c.z };
+    // the reference's atomic fold (lbvh.h:233-238) skips NaN and outward infinities
+    float mn[3] = { cas_lo(c.x), cas_lo(c.y), cas_lo(c.z) }, mx[3] = { cas_hi(c.x), cas_hi(c.y), cas_hi(c.z) };
     for (uint32_t m = peers; m; m &= m - 1)
     {
         int src = __ffs(m) - 1;
         for (int a = 0; a < 3; ++a)
         {
             float v = __shfl_sync(peers, a == 0 ? c.x : (a == 1 ? c.y : c.z), src);
-            mn[a] = ref_min(mn[a], v);
-            mx[a] = ref_max(mx[a], v);
+            mn[a] = ref_min(mn[a], cas_lo(v));
+            mx[a] = ref_max(mx[a], cas_hi(v));
         }
     }
     if ((threadIdx.x & 31) == __ffs(peers) - 1)
@@ -282,12 +283,7 @@ __global__ void __launch_bounds__(kBlock) batch_export(const bvh2_node* __restri
     }
     if (i == 0)
     {
-        box3 r;
-        r.lo = { ref_min(cbox[0].lo.x, cbox[1].lo.x), ref_min(cbox[0].lo.y, cbox[1].lo.y),
-                 ref_min(cbox[0].lo.z, cbox[1].lo.z) };
-        r.hi = { ref_max(cbox[0].hi.x, cbox[1].hi.x), ref_max(cbox[0].hi.y, cbox[1].hi.y),
-                 ref_max(cbox[0].hi.z, cbox[1].hi.z) };
-        put(out[0], r, 1u, 0);
+        put(out[0], box_union_cas(cbox[0], cbox[1]), 1u, 0);
     }
 }
 

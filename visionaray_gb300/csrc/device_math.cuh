@@ -19,6 +19,14 @@ namespace gbrt {
 __device__ __forceinline__ float ref_min(float x, float y) { return x < y ? x : y; }
 __device__ __forceinline__ float ref_max(float x, float y) { return x < y ? y : x; }
 
+// The reference's float atomicMin / atomicMax (detail/bvh/lbvh.h:63-91) is a
+// compare-and-swap loop from +FLT_MAX / -FLT_MAX that stores a value only when it lies
+// below (above) the current one: NaN, +Inf into a minimum and -Inf into a maximum are
+// never stored.  ref_min / ref_max over cas_lo / cas_hi of the arguments give those
+// bounds in any order of arrival (signed zeros aside).
+__device__ __forceinline__ float cas_lo(float x) { return x < FLT_MAX ? x : FLT_MAX; }
+__device__ __forceinline__ float cas_hi(float x) { return x > -FLT_MAX ? x : -FLT_MAX; }
+
 struct f3
 {
     float x, y, z;

@@ -42,12 +42,13 @@ __global__ void __launch_bounds__(kBlock) centroid_bounds(gbrt_triangle const* _
         box3 b = tri_box(load_tri(tris, i));
         f3 c = box_center(b);
         centroids[i] = make_float4(c.x, c.y, c.z, 0.0f);
-        mn[0] = ref_min(mn[0], c.x);
-        mn[1] = ref_min(mn[1], c.y);
-        mn[2] = ref_min(mn[2], c.z);
-        mx[0] = ref_max(mx[0], c.x);
-        mx[1] = ref_max(mx[1], c.y);
-        mx[2] = ref_max(mx[2], c.z);
+        // the reference's atomic fold (lbvh.h:233-238) skips NaN and outward infinities
+        mn[0] = ref_min(mn[0], cas_lo(c.x));
+        mn[1] = ref_min(mn[1], cas_lo(c.y));
+        mn[2] = ref_min(mn[2], cas_lo(c.z));
+        mx[0] = ref_max(mx[0], cas_hi(c.x));
+        mx[1] = ref_max(mx[1], cas_hi(c.y));
+        mx[2] = ref_max(mx[2], cas_hi(c.z));
     }
     __shared__ float red[kBlock / 32][6];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -448,12 +449,7 @@ __global__ void __launch_bounds__(kBlock) export_collapse(const bvh2_node* __res
     }
     if (i == 0)
     {
-        box3 r;
-        r.lo = { ref_min(cbox[0].lo.x, cbox[1].lo.x), ref_min(cbox[0].lo.y, cbox[1].lo.y),
-                 ref_min(cbox[0].lo.z, cbox[1].lo.z) };
-        r.hi = { ref_max(cbox[0].hi.x, cbox[1].hi.x), ref_max(cbox[0].hi.y, cbox[1].hi.y),
-                 ref_max(cbox[0].hi.z, cbox[1].hi.z) };
-        put(out[0], r, 1u, 0);
+        put(out[0], box_union_cas(cbox[0], cbox[1]), 1u, 0);
     }
 }
 

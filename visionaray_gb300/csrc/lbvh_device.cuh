@@ -127,8 +127,20 @@ __device__ __forceinline__ box3 load_union_cg(bvh2_node* node)
     float4 b = __ldcg(&node->xy1);
     float4 z = __ldcg(&node->z01);
     box3 r;
-    r.lo = { ref_min(a.x, b.x), ref_min(a.z, b.z), ref_min(z.x, z.z) };
-    r.hi = { ref_max(a.y, b.y), ref_max(a.w, b.w), ref_max(z.y, z.w) };
+    r.lo = { ref_min(cas_lo(a.x), cas_lo(b.x)), ref_min(cas_lo(a.z), cas_lo(b.z)), ref_min(cas_lo(z.x), cas_lo(z.z)) };
+    r.hi = { ref_max(cas_hi(a.y), cas_hi(b.y)), ref_max(cas_hi(a.w), cas_hi(b.w)), ref_max(cas_hi(z.y), cas_hi(z.w)) };
+    return r;
+}
+
+// An inner node's box as the reference's assign_node_bounds leaves it (lbvh.h:332-372):
+// the atomic fold of every leaf box below it, NaN and outward infinities skipped.
+__device__ __forceinline__ box3 box_union_cas(box3 const& a, box3 const& b)
+{
+    box3 r;
+    r.lo = { ref_min(cas_lo(a.lo.x), cas_lo(b.lo.x)), ref_min(cas_lo(a.lo.y), cas_lo(b.lo.y)),
+             ref_min(cas_lo(a.lo.z), cas_lo(b.lo.z)) };
+    r.hi = { ref_max(cas_hi(a.hi.x), cas_hi(b.hi.x)), ref_max(cas_hi(a.hi.y), cas_hi(b.hi.y)),
+             ref_max(cas_hi(a.hi.z), cas_hi(b.hi.z)) };
     return r;
 }
 

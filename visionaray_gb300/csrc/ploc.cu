@@ -239,8 +239,11 @@ __global__ void __launch_bounds__(kBlock) ploc_merge(const float4* __restrict__ 
         nodes[node] = nd;
         if (ca >= 0) nodes[ca].link.w = int(node << 1) | 0;
         if (cb >= 0) nodes[cb].link.w = int(node << 1) | 1;
-        alo = make_float4(ref_min(alo.x, blo.x), ref_min(alo.y, blo.y), ref_min(alo.z, blo.z), __int_as_float(int(node)));
-        ahi = make_float4(ref_max(ahi.x, bhi.x), ref_max(ahi.y, bhi.y), ref_max(ahi.z, bhi.z), __int_as_float(height));
+        // merged as the LBVH merges (NaN and outward infinities of a leaf box skipped)
+        alo = make_float4(ref_min(cas_lo(alo.x), cas_lo(blo.x)), ref_min(cas_lo(alo.y), cas_lo(blo.y)),
+                          ref_min(cas_lo(alo.z), cas_lo(blo.z)), __int_as_float(int(node)));
+        ahi = make_float4(ref_max(cas_hi(ahi.x), cas_hi(bhi.x)), ref_max(cas_hi(ahi.y), cas_hi(bhi.y)),
+                          ref_max(cas_hi(ahi.z), cas_hi(bhi.z)), __int_as_float(height));
     }
     out_lo[dst] = alo;
     out_hi[dst] = ahi;
