@@ -390,6 +390,39 @@ gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh const* bvh,
                                         gbrt_pt_scene** out);
 gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene);
 
+/* An environment light in place of the constant ambient light: the kernel's amb_light
+ * as environment_light<float, texture_ref<vec4, 2>> (environment_light.h:22-58,
+ * detail/environment_light.inl:18-34).  A ray that leaves the scene adds
+ * tex2D(texture, (u, v)).xyz * scale * throughput, where d = world_to_light * (dir, 0),
+ * u = atan2(d.x, d.z) / 2 pi (+1 below 0) and v = acos(d.y) / pi; world_to_light is
+ * the inverse of light_to_world computed as the reference's float cofactor inverse
+ * (math/detail/matrix4.inl:353-388).  The texture is d_texels: width * height RGBA32F
+ * texels in device memory, texel (x, y) at offset y * width + x, 16-byte aligned, read
+ * through the CPU texture's filters (texture/detail/filter/nearest.h, linear.h) and
+ * address modes (texture/detail/texture_common.h:91-126).  The scene keeps the pointer:
+ * the texels stay valid and unchanged while the scene renders with them.           */
+#define GBRT_FILTER_NEAREST 0u
+#define GBRT_FILTER_LINEAR  1u
+#define GBRT_ADDRESS_WRAP   0u
+#define GBRT_ADDRESS_MIRROR 1u
+#define GBRT_ADDRESS_CLAMP  2u
+typedef struct gbrt_environment
+{
+    const float* d_texels;
+    uint32_t     width;
+    uint32_t     height;
+    uint32_t     filter;              /* GBRT_FILTER_*                                */
+    uint32_t     address;             /* GBRT_ADDRESS_*, both texture axes            */
+    float        scale[3];
+    float        light_to_world[16];  /* 4x4, column-major (visionaray's mat4)        */
+} gbrt_environment;
+
+/* Sets (env != NULL) or removes (NULL: the params' ambient light again) the scene's
+ * environment light (environment_light::texture / scale / set_light_to_world_transform).
+ * Bad sizes, modes, a null or misaligned texel pointer, or a singular transform are
+ * GBRT_ERR_INVALID_ARG.  The batched renderer keeps the constant ambient light.    */
+gbrt_status gbrt_pt_scene_set_environment(gbrt_context* ctx, gbrt_pt_scene* scene, gbrt_environment const* env);
+
 /* Renders one frame: cuda_sched<basic_ray<float>>::frame(pathtracing::kernel{params},
  * make_sched_params(jittered_blend, cam, rt)) (detail/cuda_sched.inl:226-246) as a
  * wavefront path tracer.  d_accum and d_color are RGBA32F device images of

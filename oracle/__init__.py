@@ -11,7 +11,8 @@ import os
 
 import numpy as np
 
-from visionaray_gb300.types import BVH_NODE, CAMERA, HIT, LIGHT, MATERIAL, PT_PARAMS, lights_of_area_lights
+from visionaray_gb300.types import (ADDRESS_CLAMP, BVH_NODE, CAMERA, FILTER_LINEAR, HIT, LIGHT, MATERIAL, PT_PARAMS,
+                                    environment, lights_of_area_lights)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")
@@ -44,6 +45,21 @@ class Tree:
                 f = int(self.nodes["first"][i])
                 st += [(f, d + 1), (f + 1, d + 1)]
         return best
+
+
+class env_light:
+    """An environment light for the host renderers: texels (h, w, 4) float32 (texel
+    (x, y) at [y, x]), FILTER_* / ADDRESS_* modes, scale and a 4x4 light_to_world."""
+
+    def __init__(self, texels, filter=FILTER_LINEAR, address=ADDRESS_CLAMP, scale=(1.0, 1.0, 1.0),
+                 light_to_world=None):
+        self.texels = np.ascontiguousarray(texels, np.float32)
+        h, w = self.texels.shape[:2]
+        self.record = environment(self.texels.ctypes.data, w, h, filter, address, scale, light_to_world)
+
+
+def _env_p(env):
+    return None if env is None else env.record.ctypes.data
 
 
 def _as_lights(lights):
@@ -81,9 +97,9 @@ class Oracle:
         L.orc_trace.argtypes = [_vp, _u32, _vp, _vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.orc_trace.restype = _i32
         L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
-        L.orc_pathtrace.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp, _vp]
+        L.orc_pathtrace.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp, _vp, _vp]
         L.orc_pathtrace_adjoint.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _vp, _vp,
-                                            _i32, _i32, _vp, _vp, _vp]
+                                            _i32, _i32, _vp, _vp, _vp, _vp]
         self.L = L
 
     def _tree(self, h):
@@ -150,10 +166,11 @@ class Oracle:
     # visionaray's device build evaluates them (its CPU build draws the second first)
     PT_DRAWS_IN_ORDER = 4
 
-    def pathtrace(self, tree, tris, materials, lights, camera, params, mode=1, nthreads=0):
+    def pathtrace(self, tree, tris, materials, lights, camera, params, mode=1, nthreads=0, env=None):
         """Per-pixel average RGBA (height, width, 4) of one frame, and the counters
         {closest, shadow, boxes, tris}.  mode: PT_FLOAT (the reference's arithmetic),
-        PT_DOUBLE (the FP64 oracle), PT_FLOAT_TRIG_DOUBLE (the CUDA path's)."""
+        PT_DOUBLE (the FP64 oracle), PT_FLOAT_TRIG_DOUBLE (the CUDA path's).  env: an
+        environment light (env_light()) in place of the ambient light."""
         tris = np.ascontiguousarray(tris)
         materials = np.ascontiguousarray(materials, MATERIAL)
         lights = _as_lights(lights)
@@ -164,11 +181,11 @@ class Oracle:
         cnt = np.zeros(4, np.uint64)
         self.L.orc_pathtrace(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
                              len(materials), _p(lights), len(lights), _p(camera), _p(params), int(mode), nthreads,
-                             _p(out), _p(cnt))
+                             _p(out), _p(cnt), _env_p(env))
         return out, cnt
 
     def pathtrace_adjoint(self, tree, tris, materials, lights, camera, params, albedo, emission, img_adj,
-                          fp64=True, nthreads=0):
+                          fp64=True, nthreads=0, env=None):
         """(grad_albedo, grad_emission, image): the path-replay adjoint of sum(I * img_adj)
         (img_adj (h, w, 4)) at the gbrt_rng.h stream, in double (fp64) or float."""
         tris = np.ascontiguousarray(tris)
@@ -185,7 +202,7 @@ class Oracle:
         img = np.zeros((h, w, 4), np.float64)
         self.L.orc_pathtrace_adjoint(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
                                      len(materials), _p(lights), len(lights), _p(camera), _p(params), _p(a), _p(e),
-                                     _p(adj), int(fp64), nthreads, _p(ga), _p(ge), _p(img))
+                                     _p(adj), int(fp64), nthreads, _p(ga), _p(ge), _p(img), _env_p(env))
         return ga, ge, img
 
     def refit(self, tree, tris):
@@ -258,7 +275,7 @@ class Reference:
         L.ref_karras_children.argtypes = [_vp, _u32, _vp, _vp]
         L.ref_trace.argtypes = [_vp, _vp, _u64, _i32, _i32, _vp, _vp]
         L.ref_trace.restype = _i32
-        L.ref_pathtrace.argtypes = [_vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _i32]
+        L.ref_pathtrace.argtypes = [_vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _i32, _vp]
         L.ref_refit.argtypes = [_vp, _vp, _u32]
         L.ref_trace_instances.argtypes = [_u32, _vp, _vp, _u32, _vp, _vp, _vp, _u64, _i32, _vp]
         self.L = L
@@ -331,9 +348,9 @@ class Reference:
         self.L.ref_karras_children(_p(c), n, _p(left), _p(right))
         return left, right
 
-    def pathtrace(self, tris, materials, lights, camera, params, accum=None, nthreads=0):
+    def pathtrace(self, tris, materials, lights, camera, params, accum=None, nthreads=0, env=None):
         """visionaray's pathtracing::kernel (its SAH tree), one frame blended into accum
-        (height, width, 4) float32."""
+        (height, width, 4) float32; env (env_light): environment_light as amb_light."""
         tris = np.ascontiguousarray(tris)
         materials = np.ascontiguousarray(materials, MATERIAL)
         lights = _as_lights(lights)
@@ -342,5 +359,5 @@ class Reference:
         w, h = int(params["width"][0]), int(params["height"][0])
         acc = np.zeros((h, w, 4), np.float32) if accum is None else np.ascontiguousarray(accum, np.float32)
         self.L.ref_pathtrace(_p(tris), len(tris), _p(materials), len(materials), _p(lights), len(lights),
-                             _p(camera), _p(params), _p(acc), nthreads)
+                             _p(camera), _p(params), _p(acc), nthreads, _env_p(env))
         return acc

@@ -107,12 +107,13 @@ void orc_trace_linear(const gbrt_triangle* tris, uint32_t ntris, const gbrt_ray*
  * arithmetic); mode | 4: the hemisphere sample's two draws in argument order (the
  * order visionaray's device build evaluates them in).  lights: area, point and spot
  * lights (gbrt_light).  counters (may be NULL) receives {closest rays, shadow rays,
- * box tests, triangle tests}.                                                        */
+ * box tests, triangle tests}.  env (may be NULL): an environment light in place of the
+ * ambient light, its d_texels a HOST pointer here.                                   */
 void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                    const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
                    const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                    const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba,
-                   uint64_t* counters);
+                   uint64_t* counters, const gbrt_environment* env);
 
 /* Path-replay adjoint of the path tracer at the gbrt_rng.h stream: per-slot gradients
  * of sum(I * img_adj) w.r.t. the albedo / emission parameters (3 per material slot;
@@ -125,7 +126,7 @@ void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_node* nodes
                            const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                            const gbrt_pt_params* p, const float* albedo, const float* emission,
                            const double* img_adj, int fp64, int nthreads, double* grad_albedo,
-                           double* grad_emission, double* image);
+                           double* grad_emission, double* image, const gbrt_environment* env);
 
 #ifdef __cplusplus
 }

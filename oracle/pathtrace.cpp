@@ -185,7 +185,105 @@ struct pt_params_ext
     // of the two draws is unspecified C++; visionaray's CPU build (g++) draws the second
     // argument first, its device build (nvcc) the first argument first
     bool draws_in_order = false;
+    // environment_light in place of the ambient light (null: ambient); env_m = rows 0-2
+    // of world_to_light
+    const gbrt_environment* env = nullptr;
+    float env_m[12] = {};
 };
+
+// Rows 0-2 of the inverse of the column-major 4x4 `a` by the reference's float cofactor
+// expansion (math/detail/matrix4.inl:353-388; m(r, c) = a[4c + r], out[4r + c]).
+void inverse_rows(const float a[16], float out[12])
+{
+    auto m = [&](int r, int c) { return a[4 * c + r]; };
+    auto det2 = [](float m00, float m01, float m10, float m11) { return m00 * m11 - m10 * m01; };
+    float s0 = det2(m(0, 0), m(0, 1), m(1, 0), m(1, 1)), s1 = det2(m(0, 0), m(0, 2), m(1, 0), m(1, 2));
+    float s2 = det2(m(0, 0), m(0, 3), m(1, 0), m(1, 3)), s3 = det2(m(0, 1), m(0, 2), m(1, 1), m(1, 2));
+    float s4 = det2(m(0, 1), m(0, 3), m(1, 1), m(1, 3)), s5 = det2(m(0, 2), m(0, 3), m(1, 2), m(1, 3));
+    float c5 = det2(m(2, 2), m(2, 3), m(3, 2), m(3, 3)), c4 = det2(m(2, 1), m(2, 3), m(3, 1), m(3, 3));
+    float c3 = det2(m(2, 1), m(2, 2), m(3, 1), m(3, 2)), c2 = det2(m(2, 0), m(2, 3), m(3, 0), m(3, 3));
+    float c1 = det2(m(2, 0), m(2, 2), m(3, 0), m(3, 2)), c0 = det2(m(2, 0), m(2, 1), m(3, 0), m(3, 1));
+    float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    out[0] = (+m(1, 1) * c5 - m(1, 2) * c4 + m(1, 3) * c3) / det;
+    out[4] = (-m(1, 0) * c5 + m(1, 2) * c2 + m(1, 3) * c1) / det;
+    out[8] = (+m(1, 0) * c4 - m(1, 1) * c2 + m(1, 3) * c0) / det;
+    out[1] = (-m(0, 1) * c5 + m(0, 2) * c4 - m(0, 3) * c3) / det;
+    out[5] = (+m(0, 0) * c5 - m(0, 2) * c2 + m(0, 3) * c1) / det;
+    out[9] = (-m(0, 0) * c4 + m(0, 1) * c2 - m(0, 3) * c0) / det;
+    out[2] = (+m(3, 1) * s5 - m(3, 2) * s4 + m(3, 3) * s3) / det;
+    out[6] = (-m(3, 0) * s5 + m(3, 2) * s2 - m(3, 3) * s1) / det;
+    out[10] = (+m(3, 0) * s4 - m(3, 1) * s2 + m(3, 3) * s0) / det;
+    out[3] = (-m(2, 1) * s5 + m(2, 2) * s4 - m(2, 3) * s3) / det;
+    out[7] = (+m(2, 0) * s5 - m(2, 2) * s2 + m(2, 3) * s1) / det;
+    out[11] = (-m(2, 0) * s4 + m(2, 1) * s2 - m(2, 3) * s0) / det;
+}
+
+// remap_texture_coordinate (texture/detail/texture_common.h:91-126) for one axis of n
+// texels; clamp(x, a, b) = max(a, min(x, b)) (math/detail/math.h:530-533).
+template <typename T>
+T tex_remap(T c, uint32_t n, uint32_t address)
+{
+    const T fn = T(int(n));
+    if (address == GBRT_ADDRESS_WRAP) return c - std::floor(c);
+    if (address == GBRT_ADDRESS_MIRROR)
+    {
+        T f = std::floor(c);
+        return (int(f) & 1) == 1 ? T(int(n) - 1) / fn - (c - f) : c - f;
+    }
+    T lo = c < T(1.0) - T(1.0) / fn ? c : T(1.0) - T(1.0) / fn;
+    return T(0.0) < lo ? lo : T(0.0);
+}
+
+// convert_to_int of coord * size; an index outside the texture (the reference reads out
+// of bounds there) is clamped to the edge.
+template <typename T>
+int tex_index(T c, uint32_t n)
+{
+    T x = c * T(int(n));
+    int i = x != x ? 0 : (x >= T(2147483647.0) ? int(n) - 1 : (x <= T(-2147483648.0) ? 0 : int(x)));
+    return std::min(std::max(i, 0), int(n) - 1);
+}
+
+// environment_light::intensity (detail/environment_light.inl:18-34) with tex2D's CPU
+// nearest / linear filter (texture/detail/filter/nearest.h:44-66, linear.h:56-96;
+// lerp_r(a, b, x) = (1 - x) a + x b, math/detail/math.h:550-555), in T.
+template <typename T>
+vec<T> env_intensity(pt_params_ext const& ext, vec<T> dir)
+{
+    gbrt_environment const& e = *ext.env;
+    const float* m = ext.env_m;
+    const T two_pi = T(6.28318530717958647692528676656e+00);
+    const T inv_pi = T(3.18309886183790691216444201928e-01);
+    T dx = T(m[0]) * dir.x + T(m[1]) * dir.y + T(m[2]) * dir.z + T(m[3]) * T(0.0);
+    T dy = T(m[4]) * dir.x + T(m[5]) * dir.y + T(m[6]) * dir.z + T(m[7]) * T(0.0);
+    T dz = T(m[8]) * dir.x + T(m[9]) * dir.y + T(m[10]) * dir.z + T(m[11]) * T(0.0);
+    T x = std::atan2(dx, dz);
+    x = x < T(0.0) ? x + two_pi : x;
+    T y = std::acos(dy);
+    T u = x / two_pi, v = y * inv_pi;
+    auto texel = [&](int ix, int iy) {
+        const float* t = e.d_texels + 4 * (size_t(iy) * e.width + size_t(ix));
+        return vec<T>{ T(t[0]), T(t[1]), T(t[2]) };
+    };
+    vec<T> c;
+    if (e.filter == GBRT_FILTER_NEAREST)
+    {
+        c = texel(tex_index(tex_remap(u, e.width, e.address), e.width),
+                  tex_index(tex_remap(v, e.height, e.address), e.height));
+    }
+    else
+    {
+        const T fw = T(int(e.width)), fh = T(int(e.height));
+        T c1x = tex_remap(u - T(0.5) / fw, e.width, e.address), c1y = tex_remap(v - T(0.5) / fh, e.height, e.address);
+        T c2x = tex_remap(u + T(0.5) / fw, e.width, e.address), c2y = tex_remap(v + T(0.5) / fh, e.height, e.address);
+        int lx = tex_index(c1x, e.width), ly = tex_index(c1y, e.height);
+        int hx = tex_index(c2x, e.width), hy = tex_index(c2y, e.height);
+        T ux = c1x * fw - T(lx), uy = c1y * fh - T(ly);
+        auto lerp = [](vec<T> a, vec<T> b, T t) { return (T(1.0) - t) * a + t * b; };
+        c = lerp(lerp(texel(lx, ly), texel(hx, ly), ux), lerp(texel(lx, hy), texel(hx, hy), ux), uy);
+    }
+    return { c.x * T(e.scale[0]), c.y * T(e.scale[1]), c.z * T(e.scale[2]) };
+}
 
 enum : uint32_t
 {
@@ -274,7 +372,11 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
         ++cnt.closest;
         vrec<T> rec;
         rec.thr = throughput;
-        if (active && !hr.hit) intensity = intensity + ambient * throughput;
+        if (active && !hr.hit)
+        {
+            rec.spec = ext.env ? env_intensity<T>(ext, dir) : ambient;
+            intensity = intensity + rec.spec * throughput;
+        }
         active = active && hr.hit;
         if (!active)
         {
@@ -690,7 +792,7 @@ void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbr
 // w.r.t. albedo and emission, roulette and geometry decisions held fixed).
 template <typename T>
 void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats, pt_params_ext const& ext,
-           vec<T> ambient, double* ga, double* ge)
+           double* ga, double* ge)
 {
     vec<T> tbar = { 0, 0, 0 };
     for (int k = nrec - 1; k >= 0; --k)
@@ -699,7 +801,7 @@ void sweep(vrec<T> const* recs, int nrec, vec<T> adj, gbrt_material const* mats,
         gbrt_material const& m = mats[r.geom];
         if (r.kind == kMiss)
         {
-            tbar = adj * ambient;
+            tbar = adj * r.spec;   // the ambient or environment light the ray left into
         }
         else if (r.kind == kEnd)
         {
@@ -816,7 +918,6 @@ void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gb
     T aspect = T(p.width) / T(p.height);
     T th = std::tan(fovy / T(2.0));
     vec<T> U = sv * th * aspect, V = uv * th, W = -f;
-    const vec<T> ambient = { T(p.ambient[0]), T(p.ambient[1]), T(p.ambient[2]) };
     uint64_t npix = uint64_t(p.width) * p.height;
     if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
     std::vector<std::vector<double>> ga(static_cast<size_t>(nthreads), std::vector<double>(3 * size_t(nmat), 0.0));
@@ -849,7 +950,7 @@ void adjoint(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gb
                     sum = sum + c;
                     vec<T> adj = { T(img_adj[4 * pix + 0]) / T(float(p.spp)), T(img_adj[4 * pix + 1]) / T(float(p.spp)),
                                    T(img_adj[4 * pix + 2]) / T(float(p.spp)) };
-                    sweep<T>(recs, nrec, adj, mats, ext, ambient, ga[size_t(tid)].data(), ge[size_t(tid)].data());
+                    sweep<T>(recs, nrec, adj, mats, ext, ga[size_t(tid)].data(), ge[size_t(tid)].data());
                 }
                 if (image)
                 {
@@ -884,12 +985,14 @@ extern "C" void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_
                                       const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
                                       const gbrt_pt_params* p, const float* albedo, const float* emission,
                                       const double* img_adj, int fp64, int nthreads, double* grad_albedo,
-                                      double* grad_emission, double* image)
+                                      double* grad_emission, double* image, const gbrt_environment* env)
 {
     scene_arrays s{ tris, nodes, num_nodes, indices };
     pt_params_ext ext;
     ext.albedo = albedo;
     ext.emission = emission;
+    ext.env = env;
+    if (env) inverse_rows(env->light_to_world, ext.env_m);
     if (fp64)
         adjoint<double>(s, mats, nmat, lights, nl, *cam, *p, ext, img_adj, nthreads, grad_albedo, grad_emission, image);
     else
@@ -899,11 +1002,14 @@ extern "C" void orc_pathtrace_adjoint(const gbrt_triangle* tris, const gbrt_bvh_
 extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
                               const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
                               const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
-                              const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba, uint64_t* counters)
+                              const gbrt_pt_params* p, int mode, int nthreads, double* out_rgba, uint64_t* counters,
+                              const gbrt_environment* env)
 {
     scene_arrays s{ tris, nodes, num_nodes, indices };
     pt_counters c;
     pt_params_ext ext;
+    ext.env = env;
+    if (env) inverse_rows(env->light_to_world, ext.env_m);
     ext.draws_in_order = (mode & 4) != 0;   // the device build's draw order
     mode &= 3;
     if (mode == 1)

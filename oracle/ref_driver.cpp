@@ -16,6 +16,8 @@
 #include <vector>
 
 #include <visionaray/area_light.h>
+#include <visionaray/environment_light.h>
+#include <visionaray/texture/texture.h>
 #include <visionaray/bvh.h>
 #include <visionaray/generic_light.h>
 #include <visionaray/generic_material.h>
@@ -264,10 +266,20 @@ namespace {
 // (sched_common.h:209-233, jitter x drawn before y) through visionaray's own
 // pinhole_camera, samples averaged and blended into accum as sample_pixel_impl does
 // (sched_common.h:427-526).  accum is RGBA32F, read and written.
+// kernel_params KP with its ambient light type replaced by Amb (kernels.h:20-66).
+template <typename KP, typename Amb>
+struct with_ambient;
+template <typename NB, typename CB, typename P, typename N, typename TC, typename M, typename C, typename Tx,
+          typename L, typename BG, typename A, typename Amb>
+struct with_ambient<kernel_params<NB, CB, P, N, TC, M, C, Tx, L, BG, A>, Amb>
+{
+    using type = kernel_params<NB, CB, P, N, TC, M, C, Tx, L, BG, Amb>;
+};
+
 template <typename Light>
 void render_reference(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
                       std::vector<Light> const& al, const gbrt_camera* cam, const gbrt_pt_params* p, float* accum,
-                      int nthreads)
+                      int nthreads, const gbrt_environment* env)
 {
     using mat_t = generic_material<matte<float>, emissive<float>, mirror<float>, glass<float>, plastic<float>>;
     auto prims = to_prims(tris, n);
@@ -331,8 +343,6 @@ void render_reference(const gbrt_triangle* tris, uint32_t n, const gbrt_material
                                  p->num_bounces, p->epsilon,
                                  vec4(p->background[0], p->background[1], p->background[2], p->background[3]),
                                  vec4(p->ambient[0], p->ambient[1], p->ambient[2], 1.0f));
-    pathtracing::kernel<decltype(kp)> kernel;
-    kernel.params = kp;
 
     pinhole_camera c;
     float fovy = cam->fovy_degrees * constants::degrees_to_radians<float>();
@@ -343,6 +353,9 @@ void render_reference(const gbrt_triangle* tris, uint32_t n, const gbrt_material
 
     uint64_t npix = uint64_t(p->width) * p->height;
     if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+    auto run = [&](auto const& params) {
+    pathtracing::kernel<std::decay_t<decltype(params)>> kernel;
+    kernel.params = params;
     std::atomic<uint64_t> next{ 0 };
     auto worker = [&]() {
         for (;;)
@@ -377,6 +390,28 @@ void render_reference(const gbrt_triangle* tris, uint32_t n, const gbrt_material
     std::vector<std::thread> pool;
     for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
     for (auto& th : pool) th.join();
+    };
+    if (!env)
+    {
+        run(kp);
+        return;
+    }
+    // environment_light<float, texture_ref<vec4, 2>> as the viewer sets it up
+    // (src/viewer/viewer.cpp:1480-1492): a host texture, its modes, scale and transform
+    texture<vec4, 2> tex(env->width, env->height);
+    tex.reset(reinterpret_cast<vec4 const*>(env->d_texels));
+    tex.set_address_mode(env->address == GBRT_ADDRESS_WRAP ? Wrap : (env->address == GBRT_ADDRESS_MIRROR ? Mirror : Clamp));
+    tex.set_filter_mode(env->filter == GBRT_FILTER_NEAREST ? Nearest : Linear);
+    environment_light<float, texture_ref<vec4, 2>> el;
+    el.texture() = texture_ref<vec4, 2>(tex);
+    el.scale() = from_rgb(vec3(env->scale[0], env->scale[1], env->scale[2]));
+    const float* a = env->light_to_world;
+    el.set_light_to_world_transform(mat4(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10], a[11],
+                                         a[12], a[13], a[14], a[15]));
+    typename with_ambient<decltype(kp), decltype(el)>::type kp2{
+        { kp.prims.begin, kp.prims.end }, kp.geometric_normals, kp.shading_normals, kp.tex_coords, kp.materials,
+        kp.colors, kp.textures, { kp.lights.begin, kp.lights.end }, kp.num_bounces, kp.epsilon, kp.background, el };
+    run(kp2);
 }
 
 
@@ -396,7 +431,7 @@ area_light<float, triangle_t> area_of(gbrt_light const& l)
 // configurations use; otherwise generic_light<area_light, point_light, spot_light>.
 extern "C" void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_material* mats, uint32_t nmat,
                               const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
-                              const gbrt_pt_params* p, float* accum, int nthreads)
+                              const gbrt_pt_params* p, float* accum, int nthreads, const gbrt_environment* env)
 {
     bool all_area = true;
     for (uint32_t i = 0; i < nl; ++i) all_area = all_area && lights[i].kind == GBRT_LIGHT_AREA;
@@ -404,7 +439,7 @@ extern "C" void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_
     {
         std::vector<area_light<float, triangle_t>> al;
         for (uint32_t i = 0; i < nl; ++i) al.push_back(area_of(lights[i]));
-        render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads);
+        render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads, env);
         return;
     }
     using light_t = generic_light<area_light<float, triangle_t>, point_light<float>, spot_light<float>>;
@@ -443,6 +478,6 @@ extern "C" void ref_pathtrace(const gbrt_triangle* tris, uint32_t n, const gbrt_
             al.push_back(area_of(l));
         }
     }
-    render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads);
+    render_reference(tris, n, mats, nmat, al, cam, p, accum, nthreads, env);
 }
 

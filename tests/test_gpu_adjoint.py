@@ -116,3 +116,37 @@ def test_adjoint_through_specular_and_plastic_vertices(oracle, light_set):
         rel_a = np.linalg.norm(ga - ha) / np.linalg.norm(ha)
         rel_e = np.linalg.norm(ge - he) / np.linalg.norm(he)
         assert rel_a <= tol and rel_e <= tol, (fp64, rel_a, rel_e)
+
+
+def test_adjoint_with_an_environment_light(oracle):
+    """Paths that leave into an environment light: the replay's miss vertex carries the
+    lat-long lookup, against the FP32 and FP64 host adjoints (the lookup's atan2 / acos
+    are CUDA's there and the C library's here: a few ulps apart)."""
+    from oracle import env_light
+
+    from .materials import ENV_TRANSFORMS, env_texels, open_blob_scene
+    ctx = vg.Context(0)
+    tris, mats, lights, cam = open_blob_scene(n_blobs=5, subdiv=4)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    scene = vg.PTScene(bvh, mats, lights)
+    tex = env_texels(32, 16)
+    scene.set_environment(torch.from_numpy(tex).cuda(), light_to_world=ENV_TRANSFORMS["rotation"])
+    albedo = torch.from_numpy(np.ascontiguousarray(mats["color"], np.float32)).cuda()
+    emission = albedo.clone()
+    adj = torch.from_numpy(np.random.default_rng(3).normal(size=(32, 48, 4)).astype(np.float32)).cuda()
+    adj[..., 3] = 0
+    params = scenes.pt_params(48, 32, 4, num_bounces=5, frame_id=4, flags=inverse.FLAGS)
+    img = vg.pathtrace_forward(scene, cam, params, albedo, emission)
+    assert torch.equal(img, vg.pathtrace_frame(scene, cam, params))
+    ga, ge = vg.pathtrace_backward(scene, cam, params, albedo, emission, adj)
+    ctx.synchronize()
+    ga, ge = ga.cpu().numpy().astype(np.float64), ge.cpu().numpy().astype(np.float64)
+    tree = oracle.build_sah(tris)
+    env = env_light(tex, light_to_world=ENV_TRANSFORMS["rotation"])
+    a_np, e_np, adj_np = albedo.cpu().numpy(), emission.cpu().numpy(), adj.cpu().numpy()
+    for fp64, tol in ((False, 1e-3), (True, 3e-3)):
+        ha, he, _ = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, a_np, e_np, adj_np, fp64=fp64,
+                                             env=env)
+        rel_a = np.linalg.norm(ga - ha) / np.linalg.norm(ha)
+        rel_e = np.linalg.norm(ge - he) / np.linalg.norm(he)
+        assert rel_a <= tol and rel_e <= tol, (fp64, rel_a, rel_e)

@@ -242,3 +242,47 @@ def test_unknown_material_kind_is_rejected():
         vg.PTScene(bvh, mats, lights)
     with pytest.raises(GbrtError, match="unknown material kind"):
         vg.PTScene(bvh, mats, scenes.mixed_lights(lights))
+
+
+@pytest.mark.parametrize("filt,address,transform", [("linear", "clamp", "identity"), ("linear", "wrap", "rotation"),
+                                                    ("nearest", "mirror", "quarter_turn")])
+def test_environment_light_matches_fp32_oracle(oracle, filt, address, transform):
+    """gbrt_pt_scene_set_environment against the FP32 oracle (itself bit-exact against
+    visionaray's kernel with environment_light).  atan2 / acos are CUDA's here and the
+    C library's in the oracle, a few ulps apart: a lookup can land on a neighbouring
+    texel (nearest) or weight (linear), so pixels are compared by error, not bits."""
+    from oracle import env_light
+    from visionaray_gb300 import types
+
+    from .materials import ENV_TRANSFORMS, env_texels, open_blob_scene
+    tris, mats, lights, cam = open_blob_scene()
+    tex = env_texels()
+    kw = dict(filter=getattr(types, "FILTER_" + filt.upper()), address=getattr(types, "ADDRESS_" + address.upper()),
+              scale=(1.5, 1.0, 0.75), light_to_world=ENV_TRANSFORMS[transform])
+    params = scenes.pt_params(96, 64, 4, num_bounces=6, frame_id=7)
+    bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
+    scene = vg.PTScene(bvh, mats, lights)
+    scene.set_environment(torch.from_numpy(tex).cuda(), **kw)
+    gpu = vg.pathtrace_frame(scene, cam, params).cpu().numpy().astype(np.float64)
+    ref, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params,
+                              mode=Oracle.PT_FLOAT_TRIG_DOUBLE, env=env_light(tex, **kw))
+    s = stats(gpu, ref)
+    assert s["exact"] >= 0.5, s
+    assert s["rmse"] <= 0.02 * s["mean"], s
+    # removing it restores the ambient light
+    scene.set_environment(None)
+    plain = vg.pathtrace_frame(scene, cam, params).cpu().numpy()
+    again, _, _ = render(tris, mats, lights, cam, params)
+    assert np.array_equal(plain, again.astype(np.float32))
+
+
+def test_environment_arguments_are_checked():
+    from visionaray_gb300.runtime import GbrtError
+    tris, mats, lights = scenes.box_scene(n_blobs=2, subdiv=2, seed=1)
+    scene = vg.PTScene(vg.lbvh_builder().build(vg.as_device_bytes(tris)), mats, lights)
+    tex = torch.ones((4, 8, 4), dtype=torch.float32, device="cuda:0")
+    for kw in (dict(filter=2), dict(address=3), dict(light_to_world=np.zeros((4, 4), np.float32))):
+        with pytest.raises(GbrtError):
+            scene.set_environment(tex, **kw)
+    with pytest.raises(ValueError):
+        scene.set_environment(tex[..., :3])

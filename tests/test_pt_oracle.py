@@ -255,3 +255,77 @@ def test_oracle_adjoint_through_specular_vertices(oracle, light_set):
         # the image is a polynomial in the albedos (a slot met twice on a path enters
         # squared): central differences carry an O(h^2) term, 1e-4 relative bounds it
         assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(ga).max(), (kind, slot, c, g, fd)
+
+
+ENV_MODES = [("linear", "clamp", "identity"), ("linear", "wrap", "rotation"), ("nearest", "mirror", "quarter_turn"),
+             ("nearest", "wrap", "rotation")]
+
+
+@pytest.mark.skipif(not Reference.available(), reason="visionaray sources not built here")
+@pytest.mark.parametrize("filt,address,transform", ENV_MODES)
+def test_fp32_oracle_is_the_reference_kernel_environment(oracle, filt, address, transform):
+    """environment_light<float, texture_ref<vec4, 2>> as the kernel's amb_light: the
+    FP32 oracle's lat-long lookup, texture filters, address modes and float inverse
+    transform are the reference's, bit for bit."""
+    from oracle import env_light
+    from visionaray_gb300 import types
+
+    from .materials import ENV_TRANSFORMS, env_texels, open_blob_scene
+    tris, mats, lights, cam = open_blob_scene()
+    env = env_light(env_texels(), filter=getattr(types, "FILTER_" + filt.upper()),
+                    address=getattr(types, "ADDRESS_" + address.upper()), scale=(1.5, 1.0, 0.75),
+                    light_to_world=ENV_TRANSFORMS[transform])
+    params = scenes.pt_params(40, 24, 2, num_bounces=4, frame_id=3)
+    ref = Reference().pathtrace(tris, mats, lights, cam, params, env=env)
+    img, _ = oracle.pathtrace(oracle.build_sah(tris), tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT, env=env)
+    assert np.array_equal(img.astype(np.float32), ref)
+    plain = Reference().pathtrace(tris, mats, lights, cam, params)
+    assert not np.array_equal(plain, ref)   # the environment is seen
+
+
+def test_constant_nearest_environment_is_the_ambient_light(oracle):
+    """A constant texture under the nearest filter and unit scale returns the texel
+    itself, so the image equals the one with that ambient light (any transform)."""
+    from oracle import env_light
+    from visionaray_gb300 import types
+
+    from .materials import ENV_TRANSFORMS, open_blob_scene
+    tris, mats, lights, cam = open_blob_scene()
+    c = np.array([0.3, 0.6, 0.9, 1.0], np.float32)
+    env = env_light(np.broadcast_to(c, (8, 16, 4)), filter=types.FILTER_NEAREST, address=types.ADDRESS_WRAP,
+                    light_to_world=ENV_TRANSFORMS["rotation"])
+    tree = oracle.build_sah(tris)
+    params = scenes.pt_params(24, 16, 2, num_bounces=3, frame_id=2)
+    a, _ = oracle.pathtrace(tree, tris, mats, lights, cam, params, mode=Oracle.PT_FLOAT, env=env)
+    b, _ = oracle.pathtrace(tree, tris, mats, lights, cam, scenes.pt_params(24, 16, 2, num_bounces=3, frame_id=2,
+                                                                            ambient=tuple(c[:3])),
+                            mode=Oracle.PT_FLOAT)
+    assert np.array_equal(a, b)
+
+
+def test_adjoint_with_an_environment_matches_finite_differences(oracle):
+    """The path-replay adjoint carries the environment radiance of each escaped path
+    (FP64 oracle, central differences of the albedo)."""
+    from oracle import env_light
+
+    from .materials import ENV_TRANSFORMS, env_texels, open_blob_scene
+    tris, mats, lights, cam = open_blob_scene(n_blobs=4, subdiv=6)
+    env = env_light(env_texels(32, 16), light_to_world=ENV_TRANSFORMS["rotation"])
+    tree = oracle.build_sah(tris)
+    params = scenes.pt_params(16, 12, 2, num_bounces=4, frame_id=1)
+    albedo = np.ascontiguousarray(mats["color"], np.float32)
+    adj = np.zeros((12, 16, 4))
+    adj[..., :3] = 1.0
+    ga, _, _ = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, albedo, None, adj, env=env)
+    assert np.abs(ga).max() > 0
+    g = int(np.argmax(np.abs(ga).max(axis=1)))
+    h = 1e-3
+    for ch in range(3):
+        vals = []
+        for sgn in (1, -1):
+            a2 = albedo.copy()
+            a2[g, ch] += sgn * h
+            _, _, img = oracle.pathtrace_adjoint(tree, tris, mats, lights, cam, params, a2, None, adj, env=env)
+            vals.append(img[..., :3].sum())
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert fd == pytest.approx(ga[g, ch], rel=1e-3, abs=1e-6 * np.abs(ga).max())

@@ -36,6 +36,7 @@ struct gbrt_pt_scene
     float4* lights = nullptr;   // 4 float4 per light: v1, e1, e2, intensity (cl * kl)
     uint32_t num_lights = 0;
     bool extended = false;      // some material is a mirror, glass or plastic
+    gbrt::env_view* env = nullptr;   // device copy; null: the params' constant ambient light
 };
 
 namespace gbrt {
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
             geom = r.geom;
             if (r.kind == kVertexMiss)
             {
-                tbar = adj * v3{ sp.ambient.x, sp.ambient.y, sp.ambient.z };
+                tbar = adj * r.f.spec;   // the ambient or environment light the ray left into
             }
             else if (r.kind == kVertexEnd)
             {
@@ -823,12 +824,93 @@ extern "C" gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint
     return GBRT_OK;
 }
 
+namespace gbrt {
+namespace {
+
+// Rows 0-2 of the inverse of the column-major 4x4 `a`, as the reference's float inverse
+// forms it (math/detail/matrix4.inl:353-388): the 2x2 minors of rows 0-1 (s0..s5) and
+// rows 2-3 (c0..c5), the determinant from them, each cofactor sum over it.  m(r, c) =
+// a[4c + r]; out[4r + c] = inverse(r, c).  False for a zero or non-finite determinant.
+bool inverse_rows(const float a[16], float out[12])
+{
+    auto m = [&](int r, int c) { return a[4 * c + r]; };
+    auto det2 = [](float m00, float m01, float m10, float m11) { return m00 * m11 - m10 * m01; };
+    const float s0 = det2(m(0, 0), m(0, 1), m(1, 0), m(1, 1));
+    const float s1 = det2(m(0, 0), m(0, 2), m(1, 0), m(1, 2));
+    const float s2 = det2(m(0, 0), m(0, 3), m(1, 0), m(1, 3));
+    const float s3 = det2(m(0, 1), m(0, 2), m(1, 1), m(1, 2));
+    const float s4 = det2(m(0, 1), m(0, 3), m(1, 1), m(1, 3));
+    const float s5 = det2(m(0, 2), m(0, 3), m(1, 2), m(1, 3));
+    const float c5 = det2(m(2, 2), m(2, 3), m(3, 2), m(3, 3));
+    const float c4 = det2(m(2, 1), m(2, 3), m(3, 1), m(3, 3));
+    const float c3 = det2(m(2, 1), m(2, 2), m(3, 1), m(3, 2));
+    const float c2 = det2(m(2, 0), m(2, 3), m(3, 0), m(3, 3));
+    const float c1 = det2(m(2, 0), m(2, 2), m(3, 0), m(3, 2));
+    const float c0 = det2(m(2, 0), m(2, 1), m(3, 0), m(3, 1));
+    const float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    if (!(det != 0.0f) || !std::isfinite(det)) return false;
+    out[0] = (m(1, 1) * c5 - m(1, 2) * c4 + m(1, 3) * c3) / det;
+    out[4] = (-m(1, 0) * c5 + m(1, 2) * c2 + m(1, 3) * c1) / det;
+    out[8] = (m(1, 0) * c4 - m(1, 1) * c2 + m(1, 3) * c0) / det;
+    out[1] = (-m(0, 1) * c5 + m(0, 2) * c4 - m(0, 3) * c3) / det;
+    out[5] = (m(0, 0) * c5 - m(0, 2) * c2 + m(0, 3) * c1) / det;
+    out[9] = (-m(0, 0) * c4 + m(0, 1) * c2 - m(0, 3) * c0) / det;
+    out[2] = (m(3, 1) * s5 - m(3, 2) * s4 + m(3, 3) * s3) / det;
+    out[6] = (-m(3, 0) * s5 + m(3, 2) * s2 - m(3, 3) * s1) / det;
+    out[10] = (m(3, 0) * s4 - m(3, 1) * s2 + m(3, 3) * s0) / det;
+    out[3] = (-m(2, 1) * s5 + m(2, 2) * s4 - m(2, 3) * s3) / det;
+    out[7] = (m(2, 0) * s5 - m(2, 2) * s2 + m(2, 3) * s1) / det;
+    out[11] = (-m(2, 0) * s4 + m(2, 1) * s2 - m(2, 3) * s0) / det;
+    return true;
+}
+
+} // namespace
+} // namespace gbrt
+
+extern "C" gbrt_status gbrt_pt_scene_set_environment(gbrt_context* ctx, gbrt_pt_scene* scene,
+                                                     gbrt_environment const* env)
+{
+    using namespace gbrt;
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!scene) return fail(ctx, GBRT_ERR_INVALID_ARG, "set_environment: null scene");
+    device_guard g(scene->device);
+    if (!env)
+    {
+        // the stream may still render with the old record: free it after the stream drains
+        GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(scene->env);
+        scene->env = nullptr;
+        return GBRT_OK;
+    }
+    if (!env->d_texels || (reinterpret_cast<uintptr_t>(env->d_texels) & 15u))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_environment: texels must be a 16-byte aligned device pointer");
+    if (env->width == 0 || env->height == 0 || env->width > (1u << 16) || env->height > (1u << 16))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_environment: width and height must be 1 .. 65536");
+    if (env->filter > GBRT_FILTER_LINEAR || env->address > GBRT_ADDRESS_CLAMP)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_environment: unknown filter or address mode");
+    env_view v;
+    if (!inverse_rows(env->light_to_world, v.m))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "set_environment: light_to_world is singular");
+    v.texels = reinterpret_cast<const float4*>(env->d_texels);
+    v.width = env->width;
+    v.height = env->height;
+    v.filter = env->filter;
+    v.address = env->address;
+    for (int k = 0; k < 3; ++k) v.scale[k] = env->scale[k];
+    // frames already enqueued read the previous record: replace it once they are done
+    GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!scene->env) GBRT_CUDA(ctx, cudaMalloc(&scene->env, sizeof(env_view)));
+    GBRT_CUDA(ctx, cudaMemcpy(scene->env, &v, sizeof(env_view), cudaMemcpyHostToDevice));
+    return GBRT_OK;
+}
+
 extern "C" gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene)
 {
     if (!scene) return GBRT_ERR_INVALID_ARG;
     device_guard g(scene->device);
     cudaFree(scene->materials);
     cudaFree(scene->lights);
+    cudaFree(scene->env);
     delete scene;
     return GBRT_OK;
 }
@@ -867,6 +949,7 @@ shade_params shade_params_for(gbrt_context const* ctx, gbrt_pt_scene const* scen
     sp.flags = p.flags;
     sp.albedo = albedo;
     sp.emission = emission;
+    sp.env = scene->env;
     return sp;
 }
 

@@ -120,6 +120,16 @@ __device__ __forceinline__ v3 primary_dir(camera_basis const& cam, uint32_t widt
     return normalize3(U * u + V * v + W);
 }
 
+// environment_light<float, texture_ref<vec4, 2>> (environment_light.h:22-58): the
+// texture, the scale and rows 0-2 of world_to_light (4 columns each).
+struct env_view
+{
+    const float4* texels = nullptr;   // null: the constant ambient light
+    uint32_t width = 0, height = 0, filter = 0, address = 0;
+    float scale[3] = { 0.0f, 0.0f, 0.0f };
+    float m[12] = {};
+};
+
 struct shade_params
 {
     const gbrt_material* materials;
@@ -137,7 +147,81 @@ struct shade_params
     const float* emission;
     // (cos, sin) of 2 pi u for the 2^24 values of a draw u (gbrt_context::d_trig)
     const float2* trig;
+    const env_view* env = nullptr;   // device record; null: the constant ambient light
 };
+
+// remap_texture_coordinate (texture/detail/texture_common.h:91-126) for one axis of n
+// texels; clamp(x, a, b) = max(a, min(x, b)) (math/detail/math.h:530-533).
+__device__ __forceinline__ float tex_remap(float c, uint32_t n, uint32_t address)
+{
+    const float fn = float(int(n));
+    if (address == GBRT_ADDRESS_WRAP) return c - floorf(c);
+    if (address == GBRT_ADDRESS_MIRROR)
+    {
+        float f = floorf(c);
+        return (int(f) & 1) == 1 ? float(int(n) - 1) / fn - (c - f) : c - f;
+    }
+    return ref_max(0.0f, ref_min(c, 1.0f - 1.0f / fn));
+}
+
+// A texel index: convert_to_int (truncation) as the filters take it, kept inside the
+// row (an index the reference would read outside the texture, from a coordinate that
+// rounds to 1.0 under Wrap or from NaN, reads the edge texel here).
+__device__ __forceinline__ int tex_index(float c, uint32_t n)
+{
+    int i = int(c * float(int(n)));
+    return min(max(i, 0), int(n) - 1);
+}
+
+__device__ __forceinline__ float4 tex_lerp(float4 a, float4 b, float x)
+{
+    // lerp_r(a, b, x) = (1 - x) * a + x * b (math/detail/math.h:550-555)
+    const float w = 1.0f - x;
+    return make_float4(w * a.x + x * b.x, w * a.y + x * b.y, w * a.z + x * b.z, w * a.w + x * b.w);
+}
+
+// environment_light::intensity (detail/environment_light.inl:18-34): the direction in
+// light space, its lat-long coordinates and tex2D (filter/nearest.h:44-66, filter/
+// linear.h:56-96) times the scale.  Off the shading path's common case: not inlined.
+__device__ __noinline__ v3 env_intensity(const env_view* __restrict__ ev, v3 dir)
+{
+    const env_view e = *ev;
+    const float two_pi = 6.28318530717958647692528676656e+00f;
+    const float inv_pi = 3.18309886183790691216444201928e-01f;
+    const float dx = e.m[0] * dir.x + e.m[1] * dir.y + e.m[2] * dir.z + e.m[3] * 0.0f;
+    const float dy = e.m[4] * dir.x + e.m[5] * dir.y + e.m[6] * dir.z + e.m[7] * 0.0f;
+    const float dz = e.m[8] * dir.x + e.m[9] * dir.y + e.m[10] * dir.z + e.m[11] * 0.0f;
+    float x = atan2f(dx, dz);
+    x = x < 0.0f ? x + two_pi : x;
+    const float y = acosf(dy);
+    const float u = x / two_pi;
+    const float v = y * inv_pi;
+    float4 t;
+    if (e.filter == GBRT_FILTER_NEAREST)
+    {
+        const int ix = tex_index(tex_remap(u, e.width, e.address), e.width);
+        const int iy = tex_index(tex_remap(v, e.height, e.address), e.height);
+        t = __ldg(&e.texels[size_t(iy) * e.width + ix]);
+    }
+    else
+    {
+        const float fw = float(int(e.width)), fh = float(int(e.height));
+        const float c1x = tex_remap(u - 0.5f / fw, e.width, e.address);
+        const float c1y = tex_remap(v - 0.5f / fh, e.height, e.address);
+        const float c2x = tex_remap(u + 0.5f / fw, e.width, e.address);
+        const float c2y = tex_remap(v + 0.5f / fh, e.height, e.address);
+        const int lx = tex_index(c1x, e.width), ly = tex_index(c1y, e.height);
+        const int hx = tex_index(c2x, e.width), hy = tex_index(c2y, e.height);
+        const float4 s0 = __ldg(&e.texels[size_t(ly) * e.width + lx]);
+        const float4 s1 = __ldg(&e.texels[size_t(ly) * e.width + hx]);
+        const float4 s2 = __ldg(&e.texels[size_t(hy) * e.width + lx]);
+        const float4 s3 = __ldg(&e.texels[size_t(hy) * e.width + hx]);
+        const float ux = c1x * fw - float(lx);
+        const float uy = c1y * fh - float(ly);
+        t = tex_lerp(tex_lerp(s0, s1, ux), tex_lerp(s2, s3, ux), uy);
+    }
+    return v3{ t.x * e.scale[0], t.y * e.scale[1], t.z * e.scale[2] };
+}
 
 // cos and sin of the float angle 2 pi u (u a draw of gbrt_rng_u01, a multiple of
 // 2^-24), each evaluated in double and rounded once to float -- looked up: the table
@@ -178,7 +262,7 @@ struct vertex_rec
                       //      w * thr * gnee * lint (plastic)
     union
     {
-        v3 spec;      // specular, plastic: next throughput = thr * spec (then / rr)
+        v3 spec;      // specular, plastic: next throughput = thr * spec (then / rr); miss: the light seen
         float sigma;  // matte: next throughput = thr * albedo * sigma (then / rr)
         struct
         {
@@ -393,8 +477,9 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
 
     if (tri < 0 || tri >= sp.num_tris)
     {
-        // the ray left the scene: ambient light (pathtracing.inl:71-79)
-        v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
+        // the ray left the scene: ambient or environment light (pathtracing.inl:71-79)
+        v3 amb = sp.env ? env_intensity(sp.env, dir) : v3{ sp.ambient.x, sp.ambient.y, sp.ambient.z };
+        rec.f.spec = amb;
         st.rad = st.rad + amb * st.thr;
         return;
     }

@@ -15,8 +15,8 @@ import os
 
 import numpy as np
 
-from .types import (AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, HIT, HIT_INST, INSTANCE, LIGHT, MATERIAL, PT_PARAMS, RAY,
-                    TRIANGLE)
+from .types import (ADDRESS_CLAMP, AREA_LIGHT, BATCH_LAUNCH, BVH_NODE, CAMERA, FILTER_LINEAR, HIT, HIT_INST, INSTANCE,
+                    LIGHT, MATERIAL, PT_PARAMS, RAY, TRIANGLE, environment)
 
 LIBGBRT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libgbrt.so")
 
@@ -54,6 +54,7 @@ SIGNATURES = {
     "gbrt_pt_scene_create": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_pt_scene_create_lights": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _pp]),
     "gbrt_pt_scene_destroy": (_i32, [_vp]),
+    "gbrt_pt_scene_set_environment": (_i32, [_vp, _vp, _vp]),
     "gbrt_pinhole_camera_basis": (_i32, [_vp, _u32, _u32, _vp]),
     "gbrt_pathtrace_frame": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gbrt_pathtrace_forward": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -340,6 +341,23 @@ class PTScene:
             create = self.ctx.lib.gbrt_pt_scene_create
         self.ctx.check(create(self.ctx.h, bvh.h, _hptr(mats), len(mats), _hptr(lts), len(lts), ctypes.byref(h)))
         self.h = h
+        self._env = None
+
+    def set_environment(self, texels, filter=FILTER_LINEAR, address=ADDRESS_CLAMP, scale=(1.0, 1.0, 1.0),
+                        light_to_world=None):
+        """environment_light in place of the ambient light: texels is an (h, w, 4)
+        float32 CUDA tensor (texel (x, y) at [y, x]), kept alive by the scene; None
+        removes it."""
+        if texels is None:
+            self.ctx.check(self.ctx.lib.gbrt_pt_scene_set_environment(self.ctx.h, self.h, None))
+            self._env = None
+            return
+        t = texels.contiguous()
+        if t.dim() != 3 or t.shape[2] != 4 or t.dtype != _torch().float32 or not t.is_cuda:
+            raise ValueError("texels must be an (h, w, 4) float32 CUDA tensor")
+        e = environment(t.data_ptr(), t.shape[1], t.shape[0], filter, address, scale, light_to_world)
+        self.ctx.check(self.ctx.lib.gbrt_pt_scene_set_environment(self.ctx.h, self.h, _hptr(e)))
+        self._env = t
 
     def close(self):
         if getattr(self, "h", None):

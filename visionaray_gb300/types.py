@@ -26,6 +26,25 @@ LIGHT = np.dtype([("kind", "<u4"), ("cl", "<f4", (3,)), ("kl", "<f4"), ("geometr
                   ("spot_cutoff", "<f4"), ("spot_exponent", "<f4")])
 LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT = 0, 1, 2
 
+# gbrt_environment: the texel pointer (device for the product, host for the oracle),
+# texture size, filter and address mode, scale and the column-major light_to_world.
+ENVIRONMENT = np.dtype([("texels", "<u8"), ("width", "<u4"), ("height", "<u4"), ("filter", "<u4"),
+                        ("address", "<u4"), ("scale", "<f4", (3,)), ("light_to_world", "<f4", (16,))], align=True)
+FILTER_NEAREST, FILTER_LINEAR = 0, 1
+ADDRESS_WRAP, ADDRESS_MIRROR, ADDRESS_CLAMP = 0, 1, 2
+
+
+def environment(texels_ptr, width, height, filter=FILTER_LINEAR, address=ADDRESS_CLAMP, scale=(1.0, 1.0, 1.0),
+                light_to_world=None):
+    """One ENVIRONMENT record; light_to_world is a 4x4 (row, column) matrix, stored
+    column-major (identity when None)."""
+    e = np.zeros(1, ENVIRONMENT)
+    e["texels"], e["width"], e["height"] = texels_ptr, width, height
+    e["filter"], e["address"], e["scale"] = filter, address, scale
+    m = np.eye(4, dtype=np.float32) if light_to_world is None else np.asarray(light_to_world, np.float32)
+    e["light_to_world"] = m.T.reshape(16)
+    return e
+
 
 def lights_of_area_lights(area_lights):
     """AREA_LIGHT records as LIGHT records of kind LIGHT_AREA."""
