@@ -182,8 +182,9 @@ __device__ __forceinline__ float4 tex_lerp(float4 a, float4 b, float x)
 
 // environment_light::intensity (detail/environment_light.inl:18-34): the direction in
 // light space, its lat-long coordinates and tex2D (filter/nearest.h:44-66, filter/
-// linear.h:56-96) times the scale.  Off the shading path's common case: not inlined.
-__device__ __noinline__ v3 env_intensity(const env_view* __restrict__ ev, v3 dir)
+// linear.h:56-96) times the scale.  Inlined: a call would give every kernel that
+// shades a call frame (measured slower on the adjoint's replay).
+__device__ __forceinline__ v3 env_intensity(const env_view* __restrict__ ev, v3 dir)
 {
     const env_view e = *ev;
     const float two_pi = 6.28318530717958647692528676656e+00f;
