@@ -144,6 +144,26 @@ def lights_pathtrace_case(ref, samples):
             "image_sha256": digest(img), "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
 
 
+def environment_pathtrace_case(ref, samples):
+    """The open blob scene (box walls removed) under an environment light: the seeded
+    lat-long map of tests/materials.py, bilinear, Wrap, rotated."""
+    from oracle import env_light
+    from tests.materials import ENV_TRANSFORMS, env_texels, open_blob_scene
+    from visionaray_gb300 import types
+    tris, mats, lights, cam = open_blob_scene()
+    tex = env_texels()
+    env = env_light(tex, filter=types.FILTER_LINEAR, address=types.ADDRESS_WRAP, scale=(1.5, 1.0, 0.75),
+                    light_to_world=ENV_TRANSFORMS["rotation"])
+    params = scenes.pt_params(64, 48, 4, num_bounces=6, frame_id=8)
+    img = ref.pathtrace(tris, mats, lights, cam, params, env=env)
+    samples["pt_env_image"] = img
+    return {"scene": "tests.materials.open_blob_scene()", "environment": {"texels": "env_texels()",
+            "filter": "linear", "address": "wrap", "scale": [1.5, 1.0, 0.75], "light_to_world": "rotation"},
+            "params": {"width": 64, "height": 48, "spp": 4, "num_bounces": 6, "frame_id": 8},
+            "texels_sha256": digest(tex), "triangles_sha256": digest(tris), "image_sha256": digest(img),
+            "mean_rgb": [float(v) for v in img.reshape(-1, 4).mean(0)[:3]]}
+
+
 def main():
     if not Reference.available():
         raise SystemExit("oracle/_ref/libvsnray_ref.so is missing: build it where the visionaray "
@@ -157,7 +177,8 @@ def main():
            "pathtrace": pathtrace_case(ref, samples),
            "pathtrace_specular": material_pathtrace_case(ref, samples, "specular_box", 5),
            "pathtrace_glossy": material_pathtrace_case(ref, samples, "glossy_box", 6),
-           "pathtrace_lights": lights_pathtrace_case(ref, samples)}
+           "pathtrace_lights": lights_pathtrace_case(ref, samples),
+           "pathtrace_environment": environment_pathtrace_case(ref, samples)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "golden_samples.npz"), **samples)
