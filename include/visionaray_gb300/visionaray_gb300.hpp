@@ -213,6 +213,23 @@ inline void any_hit(context& ctx, cuda_index_bvh const& bvh, gbrt_ray const* d_r
     check(gbrt_trace_any_hit(ctx.get(), bvh.get(), d_rays, uint32_t(n), d_hits), ctx.get(), "gbrt_trace_any_hit");
 }
 
+// environment_light<float, texture_ref<vec4, 2>> (environment_light.h:22-58): a
+// device RGBA32F lat-long texture (width * height texels, row-major; it must outlive
+// the kernel_params it is set on), the texture's filter and address modes, the scale
+// and light_to_world (column-major).  kernel_params::set_environment puts it in place
+// of the ambient light.
+struct environment_light
+{
+    const float* d_texels = nullptr;
+    unsigned width = 0, height = 0;
+    unsigned filter = GBRT_FILTER_LINEAR, address = GBRT_ADDRESS_CLAMP;
+    std::array<float, 3> scale{ { 1.0f, 1.0f, 1.0f } };
+    std::array<float, 16> light_to_world{ { 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f,
+                                            0.0f, 0.0f, 0.0f, 1.0f } };
+
+    void set_light_to_world_transform(std::array<float, 16> const& m) { light_to_world = m; }
+};
+
 // make_kernel_params(prims, materials, lights, num_bounces, epsilon, bg_color,
 // ambient_color) (kernels.h:136-188) for the built-in path tracer: the scene (a BVH
 // that must outlive it, materials indexed by geom_id, lights; host arrays, copied)
@@ -244,6 +261,20 @@ public:
 
     gbrt_pt_scene* scene() const { return scene_; }
     context& ctx() const { return *ctx_; }
+
+    // amb_light = env (kernels.h:423-424 with an environment_light)
+    void set_environment(environment_light const& env)
+    {
+        gbrt_environment e{};
+        e.d_texels = env.d_texels;
+        e.width = env.width;
+        e.height = env.height;
+        e.filter = env.filter;
+        e.address = env.address;
+        for (int c = 0; c < 3; ++c) e.scale[c] = env.scale[size_t(c)];
+        for (int k = 0; k < 16; ++k) e.light_to_world[k] = env.light_to_world[size_t(k)];
+        check(gbrt_pt_scene_set_environment(ctx_->get(), scene_, &e), ctx_->get(), "gbrt_pt_scene_set_environment");
+    }
 
 private:
     context* ctx_;

@@ -93,7 +93,26 @@ int main()
         sp.spp = 4;
         sp.d_accum = d_accum;
         vg::cuda_sched(ctx).frame(k, sp);
+        // a second frame under a 2x1 environment light, blended in
+        std::vector<float> texels = { 0.2f, 0.4f, 0.8f, 1.0f, 0.9f, 0.7f, 0.3f, 1.0f };
+        float* d_texels = nullptr;
+        if (cudaMalloc(reinterpret_cast<void**>(&d_texels), texels.size() * sizeof(float)) != cudaSuccess)
+        {
+            std::printf("cuda alloc failed\n");
+            return 1;
+        }
+        cudaMemcpy(d_texels, texels.data(), texels.size() * sizeof(float), cudaMemcpyHostToDevice);
+        vg::environment_light env;
+        env.d_texels = d_texels;
+        env.width = 2;
+        env.height = 1;
+        env.address = GBRT_ADDRESS_WRAP;
+        kp.set_environment(env);
+        sp.sfactor = 0.5f;
+        sp.dfactor = 0.5f;
+        vg::cuda_sched(ctx).frame(k, sp);
         ctx.synchronize();
+        cudaFree(d_texels);
         std::vector<float> img(size_t(w) * hgt * 4);
         cudaMemcpy(img.data(), d_accum, img.size() * sizeof(float), cudaMemcpyDeviceToHost);
         double sum = 0.0;   // of the color channels (alpha is 1 wherever a ray hit)
