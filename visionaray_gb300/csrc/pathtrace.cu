@@ -458,7 +458,7 @@ __device__ __forceinline__ v3 nee_throughput_adjoint(vertex_rec const& r, v3 adj
 // of every emissive vertex and sampled light.  Memory stays O(pixels): nothing of the
 // forward frame is stored.  Geometry, visibility and the Russian-roulette decision are
 // not differentiated (the roulette's 1 / p weight is).
-template <bool Wide, bool Extended>
+template <bool Wide, bool Extended, bool Env>
 __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view v, shade_params sp, camera_basis cam, uint32_t width,
                                                      uint32_t height, uint32_t spp, uint32_t num_bounces,
                                                      const float4* __restrict__ img_adj, float* __restrict__ grad_albedo,
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
         {
             trace_result h = traverse_view<false, Wide>(v, { o.x, o.y, o.z }, { d.x, d.y, d.z }, 0.0f, FLT_MAX, status);
             vertex_out out;
-            shade_vertex<Extended>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, status);
+            shade_vertex<Extended, Env>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, status);
             if (out.shadow)
             {
                 trace_result sh = traverse_view<true, Wide>(v, { out.sh_o.x, out.sh_o.y, out.sh_o.z },
@@ -518,7 +518,8 @@ __global__ void __launch_bounds__(kBlock, kAdjointMinBlocks) pt_adjoint(bvh_view
             geom = r.geom;
             if (r.kind == kVertexMiss)
             {
-                tbar = adj * r.f.spec;   // the ambient or environment light the ray left into
+                // the ambient or environment light the ray left into
+                tbar = adj * (Env ? r.f.spec : v3{ sp.ambient.x, sp.ambient.y, sp.ambient.z });
             }
             else if (r.kind == kVertexEnd)
             {
@@ -1125,8 +1126,10 @@ extern "C" gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene 
     const bvh_view v = view_of(bvh);
     const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     // matte / emissive scenes get the replay without the other materials' branches
-    auto kernel = wide ? (scene->extended ? pt_adjoint<true, true> : pt_adjoint<true, false>)
-                       : (scene->extended ? pt_adjoint<false, true> : pt_adjoint<false, false>);
+    // (an environment light takes the full replay)
+    auto kernel = scene->env ? (wide ? pt_adjoint<true, true, true> : pt_adjoint<false, true, true>)
+                  : wide     ? (scene->extended ? pt_adjoint<true, true, false> : pt_adjoint<true, false, false>)
+                             : (scene->extended ? pt_adjoint<false, true, false> : pt_adjoint<false, false, false>);
     kernel<<<blocks, kBlock, 0, ctx->stream>>>(v, sp, cam, p.width, p.height, p.spp, p.num_bounces,
                                                reinterpret_cast<const float4*>(d_image_adjoint), d_grad_albedo,
                                                d_grad_emission, ctx->d_status);

@@ -459,7 +459,9 @@ __device__ __noinline__ nee_terms plastic_nee(const gbrt_material* __restrict__ 
 // and the adjoint's replay, so both compute bit-identical paths.
 // Extended = false compiles out the mirror, glass and plastic branches, for scenes
 // whose materials are all matte or emissive (any other kind then shades as matte).
-template <bool Extended = true>
+// Env = false compiles out the environment light (the adjoint's replay of scenes
+// without one: the miss record then carries nothing and the sweep reads the ambient).
+template <bool Extended = true, bool Env = true>
 __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p, uint32_t bounce, v3 ori, v3 dir,
                                              float tmin, float tmax, int tri, float t, path_state& st,
                                              vertex_out& out, uint32_t* __restrict__ status)
@@ -479,8 +481,12 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
     if (tri < 0 || tri >= sp.num_tris)
     {
         // the ray left the scene: ambient or environment light (pathtracing.inl:71-79)
-        v3 amb = sp.env ? env_intensity(sp.env, dir) : v3{ sp.ambient.x, sp.ambient.y, sp.ambient.z };
-        rec.f.spec = amb;
+        v3 amb = { sp.ambient.x, sp.ambient.y, sp.ambient.z };
+        if (Env)
+        {
+            if (sp.env) amb = env_intensity(sp.env, dir);
+            rec.f.spec = amb;
+        }
         st.rad = st.rad + amb * st.thr;
         return;
     }
