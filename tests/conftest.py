@@ -15,8 +15,10 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def _native_build():
     """Builds the native libraries once per session (no-op when up to date)."""
+    from oracle import build as oracle_build
     from visionaray_gb300 import build
     build.build()
+    oracle_build.build()
 
 
 @pytest.fixture(scope="session")

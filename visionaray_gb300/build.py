@@ -1,15 +1,11 @@
-"""In-tree build of the native parts (no cmake, no pip): run `python -m visionaray_gb300.build`.
+"""In-tree build of the product's native parts (no cmake, no pip): run
+`python -m visionaray_gb300.build`.
 
-Products, all git-ignored and rebuilt on every machine (x86-64 here, AArch64 on the
+Products, both git-ignored and rebuilt on every machine (x86-64 here, AArch64 on the
 GPU host):
   visionaray_gb300/_lib/libgbrt.so         CUDA kernels + C ABI (sm_103a only)
   visionaray_gb300/_lib/libgbrt_scenes.so  deterministic synthetic workloads (host)
-  oracle/_build/liboracle.so               CPU oracle (test infrastructure)
-  oracle/_ref/libvsnray_ref.so             visionaray's own CPU code, only where its
-                                           headers are present (test infrastructure)
-  oracle/_ref/vsnray_ref_gpu.cubin         visionaray's own GPU traversal and path tracer
-                                           (device code, sm_103a), only where its headers
-                                           are present (benchmark infrastructure)
+The oracle (test infrastructure) has its own recipe, oracle/build.py.
 Translation units compile in parallel; an up-to-date output is not rebuilt.
 """
 import os
@@ -21,8 +17,6 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "_lib")
-ORACLE = os.path.join(ROOT, "oracle")
-REFERENCE_INCLUDE = os.environ.get("VSNRAY_INCLUDE", "/root/reference/include")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -42,10 +36,6 @@ PER_FILE_FLAGS = {"pathtrace.cu": ["--fmad=false"], "batch_pt.cu": ["--fmad=fals
 
 LIBGBRT = os.path.join(LIB, "libgbrt.so")
 LIBSCENES = os.path.join(LIB, "libgbrt_scenes.so")
-LIBORACLE = os.path.join(ORACLE, "_build", "liboracle.so")
-LIBREF = os.path.join(ORACLE, "_ref", "libvsnray_ref.so")
-REFCUBIN = os.path.join(ORACLE, "_ref", "vsnray_ref_gpu.cubin")
-REFCUBIN_EXACT = os.path.join(ORACLE, "_ref", "vsnray_ref_gpu_exact.cubin")
 
 
 def _stale(out, deps):
@@ -68,7 +58,7 @@ def _run_all(jobs):
         raise RuntimeError(f"native build failed:\n{msg}")
 
 
-def build(verbose=False, with_reference=True):
+def build(verbose=False):
     os.makedirs(LIB, exist_ok=True)
     os.makedirs(os.path.join(LIB, "obj"), exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in CU_HEADERS] + [
@@ -86,34 +76,6 @@ def build(verbose=False, with_reference=True):
     if _stale(LIBSCENES, scenes_srcs + [os.path.join(CSRC, "scenes.h")]):
         jobs.append(("scenes", ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
                                 "-ffp-contract=off", "-Wall"] + scenes_srcs + ["-o", LIBSCENES]))
-    # the oracle flags are those of oracle/Makefile (kept for manual builds)
-    oracle_flags = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"]
-    oracle_srcs = [os.path.join(ORACLE, f) for f in ("oracle.cpp", "pathtrace.cpp")]
-    oracle_deps = oracle_srcs + [os.path.join(ORACLE, "oracle.h"),
-                                 os.path.join(ROOT, "include", "visionaray_gb300", "gbrt_rng.h"),
-                                 os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h")]
-    if _stale(LIBORACLE, oracle_deps):
-        os.makedirs(os.path.dirname(LIBORACLE), exist_ok=True)
-        jobs.append(("oracle", oracle_flags + ["-o", LIBORACLE] + oracle_srcs + ["-lpthread"]))
-    have_ref = with_reference and os.path.isdir(os.path.join(REFERENCE_INCLUDE, "visionaray"))
-    ref_src = os.path.join(ORACLE, "ref_driver.cpp")
-    if have_ref and _stale(LIBREF, oracle_deps + [ref_src]):
-        os.makedirs(os.path.dirname(LIBREF), exist_ok=True)
-        jobs.append(("reference", oracle_flags + ["-w", "-DNDEBUG", "-I" + REFERENCE_INCLUDE, "-o", LIBREF,
-                                                  ref_src, "-lpthread"]))
-    # visionaray's own GPU traversal and path-tracing kernel as device code only (a cubin
-    # runs on the GPU host whatever its CPU); built only where the headers are
-    # (default nvcc contraction, as visionaray's own build; and a --fmad=false twin whose
-    # arithmetic is the CPU reference's, for parity checks)
-    ref_gpu_src = os.path.join(ORACLE, "ref_gpu.cu")
-    ref_gpu_deps = [ref_gpu_src, os.path.join(ROOT, "include", "visionaray_gb300", "gbrt.h"),
-                    os.path.join(ROOT, "include", "visionaray_gb300", "gbrt_rng.h")]
-    for cubin, extra in ((REFCUBIN, []), (REFCUBIN_EXACT, ["--fmad=false"])):
-        if have_ref and _stale(cubin, ref_gpu_deps):
-            os.makedirs(os.path.dirname(cubin), exist_ok=True)
-            jobs.append(("reference-gpu", [NVCC, "-cubin"] + ARCH + extra + [
-                "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-w", "-I" + REFERENCE_INCLUDE, ref_gpu_src,
-                "-o", cubin]))
     if verbose:
         for n, c in jobs:
             print(n, " ".join(c))

@@ -42,6 +42,33 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 std::mutex g_setup_mutex;
 void* g_scratch_address[kMaxDevices] = {};
 
+// Makes ctx->device current for its lifetime and restores the caller's device; both
+// switches are checked, so a failure is reported instead of running on another device.
+struct checked_device
+{
+    int prev = -1;
+    bool switched = false;
+    cudaError_t error = cudaSuccess;
+
+    explicit checked_device(int dev)
+    {
+        error = cudaGetDevice(&prev);
+        if (error == cudaSuccess && prev != dev)
+        {
+            error = cudaSetDevice(dev);
+            switched = error == cudaSuccess;
+        }
+    }
+    // Restores the caller's device; the status of that switch back.
+    cudaError_t restore()
+    {
+        if (!switched) return cudaSuccess;
+        switched = false;
+        return cudaSetDevice(prev);
+    }
+    ~checked_device() { restore(); }
+};
+
 // Once per device, with that device current: the array's device address.
 gbrt_status scratch_address(gbrt_context* ctx, void** out)
 {
@@ -50,18 +77,13 @@ gbrt_status scratch_address(gbrt_context* ctx, void** out)
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_address[ctx->device])
     {
-        int prev = -1;
-        cudaError_t e = cudaGetDevice(&prev);
-        if (e != cudaSuccess) return check_cuda(ctx, e, "build_lbvh_noalloc: cudaGetDevice");
-        if (prev != ctx->device)
-        {
-            e = cudaSetDevice(ctx->device);
-            if (e != cudaSuccess) return check_cuda(ctx, e, "build_lbvh_noalloc: cudaSetDevice");
-        }
+        checked_device dev(ctx->device);
+        if (dev.error != cudaSuccess) return check_cuda(ctx, dev.error, "build_lbvh_noalloc: selecting the device");
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (prev != ctx->device) cudaSetDevice(prev);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return check_cuda(ctx, e, "build_lbvh_noalloc: cudaGetSymbolAddress");
+        e = dev.restore();
+        if (e != cudaSuccess) return check_cuda(ctx, e, "build_lbvh_noalloc: restoring the caller's device");
         g_scratch_address[ctx->device] = p;
     }
     *out = g_scratch_address[ctx->device];
@@ -89,9 +111,11 @@ extern "C" gbrt_status gbrt_bvh_build_lbvh_noalloc(gbrt_context* ctx, gbrt_trian
     void* scratch = nullptr;
     gbrt_status st = scratch_address(ctx, &scratch);
     if (st != GBRT_OK) return st;
-    int prev = -1;
-    if (cudaGetDevice(&prev) == cudaSuccess && prev != ctx->device) cudaSetDevice(ctx->device);
+    checked_device dev(ctx->device);
+    if (dev.error != cudaSuccess) return check_cuda(ctx, dev.error, "build_lbvh_noalloc: selecting the device");
     st = build_lbvh_in_scratch(ctx, d_tris, n, scratch, kNoAllocScratchBytes, d_nodes, d_indices);
-    if (prev >= 0 && prev != ctx->device) cudaSetDevice(prev);
+    cudaError_t e = dev.restore();
+    if (st == GBRT_OK && e != cudaSuccess)
+        return check_cuda(ctx, e, "build_lbvh_noalloc: restoring the caller's device");
     return st;
 }
