@@ -98,6 +98,8 @@ class Oracle:
         L.orc_trace.restype = _i32
         L.orc_trace_linear.argtypes = [_vp, _u32, _vp, _u64, _i32, _i32, _vp]
         L.orc_pathtrace.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp, _vp, _vp]
+        L.orc_pathtrace_pixels.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _i32, _i32, _vp,
+                                           _u64, _vp, _vp, _vp]
         L.orc_pathtrace_adjoint.argtypes = [_vp, _vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _vp, _vp,
                                             _i32, _i32, _vp, _vp, _vp, _vp]
         self.L = L
@@ -182,6 +184,26 @@ class Oracle:
         self.L.orc_pathtrace(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
                              len(materials), _p(lights), len(lights), _p(camera), _p(params), int(mode), nthreads,
                              _p(out), _p(cnt), _env_p(env))
+        return out, cnt
+
+    def pathtrace_pixels(self, tree, tris, materials, lights, camera, params, pixels, mode=1, nthreads=0, env=None):
+        """`pathtrace` on the listed pixels only (row-major indices < width * height):
+        RGBA (len(pixels), 4) and the counters {closest, shadow, boxes, tris} of those
+        pixels' paths."""
+        tris = np.ascontiguousarray(tris)
+        materials = np.ascontiguousarray(materials, MATERIAL)
+        lights = _as_lights(lights)
+        camera = np.ascontiguousarray(np.asarray(camera, CAMERA).reshape(1))
+        params = np.ascontiguousarray(np.asarray(params, PT_PARAMS).reshape(1))
+        pix = np.ascontiguousarray(pixels, np.uint32)
+        npix = int(params["width"][0]) * int(params["height"][0])
+        if len(pix) and int(pix.max()) >= npix:
+            raise ValueError("pixel index outside the frame")
+        out = np.zeros((len(pix), 4), np.float64)
+        cnt = np.zeros(4, np.uint64)
+        self.L.orc_pathtrace_pixels(_p(tris), _p(tree.nodes), len(tree.nodes), _p(tree.indices), _p(materials),
+                                    len(materials), _p(lights), len(lights), _p(camera), _p(params), int(mode),
+                                    nthreads, _p(pix), len(pix), _p(out), _p(cnt), _env_p(env))
         return out, cnt
 
     def pathtrace_adjoint(self, tree, tris, materials, lights, camera, params, albedo, emission, img_adj,

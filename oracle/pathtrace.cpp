@@ -713,8 +713,10 @@ vec<T> radiance(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat,
 template <typename T>
 void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbrt_light const* lights,
             uint32_t nl, gbrt_camera const& cam, gbrt_pt_params const& p, int nthreads, double* out,
-            pt_counters& total, bool trig_double, pt_params_ext const& ext = {})
+            pt_counters& total, bool trig_double, pt_params_ext const& ext = {}, const uint32_t* plist = nullptr,
+            uint64_t nlist = 0)
 {
+    // plist: render only these pixels (row-major indices), out[4 k ...] for plist[k]
     // pinhole_camera::begin_frame (detail/pinhole_camera.inl:87-97) in T
     vec<T> eye = load<T>(cam.eye), center = load<T>(cam.center), up = load<T>(cam.up);
     vec<T> f = normalize(eye - center);
@@ -727,17 +729,18 @@ void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbr
     vec<T> V = uv * th;
     vec<T> W = -f;
 
-    uint64_t npix = uint64_t(p.width) * p.height;
+    uint64_t npix = plist ? nlist : uint64_t(p.width) * p.height;
     if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
     std::atomic<uint64_t> next{ 0 };
     std::vector<pt_counters> per(static_cast<size_t>(nthreads));
     auto worker = [&](int tid) {
         for (;;)
         {
-            uint64_t b = next.fetch_add(64);
+            uint64_t b = next.fetch_add(plist ? 1 : 64);
             if (b >= npix) break;
-            for (uint64_t pix = b; pix < std::min(npix, b + 64); ++pix)
+            for (uint64_t k = b; k < std::min(npix, b + (plist ? 1 : 64)); ++k)
             {
+                uint64_t pix = plist ? plist[k] : k;
                 T x = T(pix % p.width), y = T(pix / p.width);
                 vec<T> sum = { 0, 0, 0 };
                 T alpha = 0;
@@ -769,10 +772,10 @@ void render(scene_arrays const& s, gbrt_material const* mats, uint32_t nmat, gbr
                     }
                 }
                 T inv = T(float(p.spp));
-                out[4 * pix + 0] = double(sum.x / inv);
-                out[4 * pix + 1] = double(sum.y / inv);
-                out[4 * pix + 2] = double(sum.z / inv);
-                out[4 * pix + 3] = double(alpha / inv);
+                out[4 * k + 0] = double(sum.x / inv);
+                out[4 * k + 1] = double(sum.y / inv);
+                out[4 * k + 2] = double(sum.z / inv);
+                out[4 * k + 3] = double(alpha / inv);
             }
         }
     };
@@ -1016,6 +1019,35 @@ extern "C" void orc_pathtrace(const gbrt_triangle* tris, const gbrt_bvh_node* no
         render<double>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, false, ext);
     else
         render<float>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, mode == 2, ext);
+    if (counters)
+    {
+        counters[0] = c.closest;
+        counters[1] = c.shadow;
+        counters[2] = c.boxes;
+        counters[3] = c.tris;
+    }
+}
+
+// orc_pathtrace on the listed pixels only (row-major indices into the width x height
+// frame, each < width * height): out_rgba[4 k ...] is pixel plist[k]'s average.
+extern "C" void orc_pathtrace_pixels(const gbrt_triangle* tris, const gbrt_bvh_node* nodes, uint32_t num_nodes,
+                                     const uint32_t* indices, const gbrt_material* mats, uint32_t nmat,
+                                     const gbrt_light* lights, uint32_t nl, const gbrt_camera* cam,
+                                     const gbrt_pt_params* p, int mode, int nthreads, const uint32_t* plist,
+                                     uint64_t nlist, double* out_rgba, uint64_t* counters,
+                                     const gbrt_environment* env)
+{
+    scene_arrays s{ tris, nodes, num_nodes, indices };
+    pt_counters c;
+    pt_params_ext ext;
+    ext.env = env;
+    if (env) inverse_rows(env->light_to_world, ext.env_m);
+    ext.draws_in_order = (mode & 4) != 0;
+    mode &= 3;
+    if (mode == 1)
+        render<double>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, false, ext, plist, nlist);
+    else
+        render<float>(s, mats, nmat, lights, nl, *cam, *p, nthreads, out_rgba, c, mode == 2, ext, plist, nlist);
     if (counters)
     {
         counters[0] = c.closest;
