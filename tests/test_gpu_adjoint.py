@@ -81,9 +81,13 @@ def test_adjoint_matches_host_adjoints(setup, oracle):
         assert rel_a <= tol and rel_e <= tol, (fp64, rel_a, rel_e)
 
 
-def test_inverse_albedo_reduces_the_loss():
-    res = inverse.optimize(steps=12, width=128, height=128, spp=4, target_spp=32)
-    assert res["losses"][-1] < 0.7 * res["losses"][0]
+def test_inverse_albedo_recovers_the_seen_albedos():
+    """A short run at reduced size: the albedo error of the slots the camera sees, on
+    the same slots at the start and the end, falls (the decorrelated estimator)."""
+    res = inverse.optimize(steps=40, width=128, height=128, spp=8, target_spp=64, min_pixels=16)
+    start, end = res["errors_start"], res["errors_end"]
+    assert end["coverage_weighted"] < 0.8 * start["coverage_weighted"], (start, end)
+    assert res["losses"][-1] < res["losses"][0]
     assert res["bwd_ms"] > 0 and res["fwd_ms"] > 0
 
 
