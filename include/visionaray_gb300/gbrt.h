@@ -33,7 +33,8 @@ typedef enum gbrt_status
     GBRT_ERR_INVALID_ARG    = 1,  /* null pointer, bad size, bad enum                  */
     GBRT_ERR_OUT_OF_MEMORY  = 2,  /* device allocation failed                           */
     GBRT_ERR_CUDA           = 3,  /* a CUDA runtime call or kernel launch failed        */
-    GBRT_ERR_WATCHDOG       = 4,  /* a bounded device-side wait gave up                 */
+    GBRT_ERR_WATCHDOG       = 4,  /* reserved, never returned: no kernel of this library
+                                   * waits on a flag, a peer or a barrier             */
     GBRT_ERR_STACK_OVERFLOW = 5,  /* traversal stack exceeded (tree deeper than limit)  */
     GBRT_ERR_TOO_LARGE      = 6   /* input larger than a documented maximum             */
 } gbrt_status;
@@ -187,6 +188,15 @@ gbrt_status gbrt_bvh_build_ploc(gbrt_context* ctx, gbrt_triangle const* d_tris, 
  * Only for trees built by gbrt_bvh_build_lbvh.                                    */
 gbrt_status gbrt_bvh_export_bvh2(gbrt_context* ctx, gbrt_bvh const* bvh,
                                  gbrt_bvh_node* d_nodes, uint32_t* d_indices);
+
+/* lbvh_builder::build (detail/bvh/lbvh.h:681-844) into an existing tree: the full
+ * GPU LBVH build of n triangles (device, the same count the tree was built with, any
+ * positions) written into the tree's own arrays, so a scene whose geometry changes
+ * every frame is rebuilt without device allocations (a 4-wide collapse, if the
+ * context asks for one, is still allocated anew).  The result equals
+ * gbrt_bvh_build_lbvh's for the same triangles.  Path-tracing scenes made from the
+ * tree see the new tree.  Synchronises the context stream (the tree height).        */
+gbrt_status gbrt_bvh_rebuild_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris, uint32_t n);
 
 /* bvh_refitter::refit(tree, prims, n) (detail/bvh/refit.h:25-117) on the GPU: new
  * positions of the same n triangles (device, the build's input order); the tree keeps
@@ -567,10 +577,19 @@ gbrt_status gbrt_batch_height(gbrt_context* ctx, gbrt_batch const* batch, uint32
 /* One frame of every scene in a single persistent launch: warps take tiles of pixels of
  * any scene from one atomic work queue and run the path tracer (the same shading as
  * gbrt_pathtrace_frame, so scene s's image equals the one gbrt_pathtrace_frame
- * renders with its camera and params).  d_images: RGBA32F, 16-byte aligned, scene s at
- * pixel offset sum_{t<s} width_t * height_t.  Area lights are not supported here
- * (ambient light only).  Enqueue only.                                             */
+ * renders with its camera, params and lights).  d_images: RGBA32F, 16-byte aligned,
+ * scene s at pixel offset sum_{t<s} width_t * height_t.  Enqueue only.              */
 gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch const* batch, float* d_images);
+
+/* The lights of each scene of a batch (make_kernel_params' light list per scene,
+ * pathtracing.inl:42-233 next-event estimation): h_lights (host, area / point / spot
+ * records as for gbrt_pt_scene_create_lights), scene s sampling
+ * h_lights[h_light_offsets[s] .. h_light_offsets[s + 1]) (num_scenes + 1 host
+ * entries from 0 to num_lights; null when num_lights is 0).  Replaces earlier lights;
+ * scenes without lights keep the params' ambient light only.  Synchronises the
+ * context stream.                                                                   */
+gbrt_status gbrt_batch_set_lights(gbrt_context* ctx, gbrt_batch* batch, gbrt_light const* h_lights,
+                                  uint32_t num_lights, uint32_t const* h_light_offsets);
 
 /* gbrt_batch_build + gbrt_batch_pathtrace captured once into a CUDA graph and
  * replayed on the context stream on every call (re-captured when d_tris, d_images,
@@ -589,6 +608,16 @@ gbrt_status gbrt_batch_autotune(gbrt_context* ctx, gbrt_batch* batch, float* d_i
 /* Number of kernels the library launched on this context since creation (the
  * count covers every kernel of every call).                                        */
 uint64_t gbrt_kernel_launch_count(gbrt_context const* ctx);
+
+/* Instrumentation (no visionaray counterpart: the reference times nothing itself).
+ * While enabled, every ray query (gbrt_trace_*) records a CUDA event pair around its
+ * traversal kernel -- after the ray order is computed -- on the stream it runs on, in
+ * a ring of the 256 most recent queries.  gbrt_context_kernel_times waits for the
+ * recorded events, writes the durations (ms) of the most recent min(recorded, max,
+ * 256) queries, oldest first, to out_ms, their number to *count, and clears the
+ * record.  Enabling also clears it.                                                */
+gbrt_status gbrt_context_set_kernel_timing(gbrt_context* ctx, int enable);
+gbrt_status gbrt_context_kernel_times(gbrt_context* ctx, float* out_ms, uint32_t max, uint32_t* count);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -250,3 +250,54 @@ def test_batch_rejects_unknown_material_kind():
     mats["kind"][0] = 5
     with pytest.raises(GbrtError, match="unknown material kind"):
         batch.set_frames(cams, params, mats)
+
+
+def test_lit_batch_equals_per_scene_frames():
+    """Scenes with area lights: five box scenes of different seeds in one batch, one
+    material table for all (each scene's geom_ids offset into it), scene s sampling its
+    own two ceiling lights -- scene 3 has none and keeps the ambient light.  Each
+    scene's batched image equals gbrt_pathtrace_frame's with that scene's lights, bit
+    for bit, under two launch shapes."""
+    parts, mat_parts, light_parts, light_offsets = [], [], [], [0]
+    slot = 0
+    for s in range(5):
+        t, m, lights = scenes.box_scene(n_blobs=2 + s, subdiv=3, seed=10 + s)
+        t = t.copy()
+        t["geom_id"] += slot
+        lights = lights.copy()
+        lights["geometry"]["geom_id"] += slot
+        if s == 3:
+            lights = lights[:0]
+        parts.append(t)
+        mat_parts.append(m)
+        light_parts.append(lights)
+        light_offsets.append(light_offsets[-1] + len(lights))
+        slot += len(m)
+    tris = np.concatenate(parts)
+    mats = np.concatenate(mat_parts)
+    lights = np.concatenate(light_parts)
+    offsets = np.zeros(len(parts) + 1, np.uint32)
+    offsets[1:] = np.cumsum([len(p) for p in parts])
+    cam = scenes.box_camera()
+    cams = np.array([cam] * len(parts))
+    params = np.array([scenes.pt_params(32 + 8 * s, 24 + 4 * s, 2, num_bounces=5, frame_id=3 + s,
+                                        ambient=(0.2, 0.2, 0.2)) for s in range(len(parts))])
+    batch = vg.Batch(offsets)
+    batch.build(vg.as_device_bytes(tris))
+    batch.set_frames(cams, params, mats)
+    batch.set_lights(lights, light_offsets)
+    want = []
+    for s, t in enumerate(parts):
+        bvh = vg.lbvh_builder().build(vg.as_device_bytes(t))
+        img = vg.pathtrace_frame(vg.PTScene(bvh, mats, light_parts[s]), cam, params[s])
+        bvh.ctx.synchronize()
+        want.append(img.cpu().numpy())
+    for launch in [(128, 32, 64, BATCH_ORDER_ROWS), (256, 64, 32, BATCH_ORDER_BLOCKS)]:
+        batch.launch = launch
+        images = batch.pathtrace()
+        batch.ctx.synchronize()
+        for s in range(len(parts)):
+            got = batch.image(images, s, params).cpu().numpy()
+            assert got.tobytes() == want[s].tobytes(), (launch, s)
+    lit = [float(w[..., :3].mean()) for w in want]
+    assert min(lit[s] for s in (0, 1, 2, 4)) > lit[3]   # next-event estimation lights the lit scenes

@@ -117,3 +117,54 @@ def test_refit_rejects_other_counts():
     bvh = vg.lbvh_builder().build(vg.as_device_bytes(tris))
     with pytest.raises(vg.GbrtError):
         bvh.refit(vg.as_device_bytes(tris[:99]))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5000, 120000])
+def test_rebuild_equals_fresh_build(oracle, n):
+    """gbrt_bvh_rebuild_lbvh: a full rebuild of new positions of the same number of
+    triangles, written into the tree's own arrays; the result equals a fresh build of
+    those triangles and the oracle's restatement of visionaray's GPU builder, and a
+    rebuild after the first allocates no device memory."""
+    import torch
+    a = scenes.soup(n, seed=50 + n)
+    b = scenes.soup(n, seed=90 + n, offset=0.05)
+    bvh = gpu_build(a)
+    d_b = vg.as_device_bytes(b)
+    bvh.rebuild(d_b)
+    nodes, idx = bvh.export_bvh2()
+    fresh = gpu_build(b).export_bvh2()
+    assert nodes.tobytes() == fresh[0].tobytes() and np.array_equal(idx, fresh[1])
+    assert_same_tree(nodes, idx, oracle.build_karras(b))
+    d_a = vg.as_device_bytes(a)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    bvh.rebuild(d_a)
+    bvh.ctx.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert_same_tree(*bvh.export_bvh2(), oracle.build_karras(a))
+
+
+def test_rebuild_is_seen_by_a_path_tracing_scene():
+    from visionaray_gb300.types import AREA_LIGHT, MATERIAL
+    a, b = scenes.soup(3000, seed=61, offset=0.03), scenes.soup(3000, seed=62, offset=0.03)
+    mats = np.zeros(1, MATERIAL)
+    mats["color"], mats["scale"] = (0.6, 0.7, 0.8), 1.0
+    cam = scenes.box_camera(eye=(0.5, 0.5, -1.0), center=(0.5, 0.5, 0.5), fovy_degrees=45.0)
+    params = scenes.pt_params(40, 32, 2, num_bounces=3, ambient=(1.0, 1.0, 1.0))
+    bvh = gpu_build(a)
+    scene = vg.PTScene(bvh, mats, np.zeros(0, AREA_LIGHT))
+    bvh.rebuild(vg.as_device_bytes(b))
+    got = vg.pathtrace_frame(scene, cam, params).cpu().numpy()
+    other = gpu_build(b)
+    want = vg.pathtrace_frame(vg.PTScene(other, mats, np.zeros(0, AREA_LIGHT)), cam, params).cpu().numpy()
+    assert got.tobytes() == want.tobytes()
+
+
+def test_rebuild_rejects_other_counts_and_trees():
+    tris = scenes.soup(100, seed=2)
+    bvh = gpu_build(tris)
+    with pytest.raises(vg.GbrtError):
+        bvh.rebuild(vg.as_device_bytes(tris[:99]))
+    ploc = vg.ploc_builder().build(vg.as_device_bytes(tris))
+    with pytest.raises(vg.GbrtError):
+        ploc.rebuild(vg.as_device_bytes(tris))

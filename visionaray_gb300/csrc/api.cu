@@ -234,6 +234,8 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
             cudaFree(ctx->slot_hits[k]);
             cudaFree(ctx->slot_trace_scratch[k]);
         }
+        for (cudaEvent_t& e : ctx->timing_events)
+            if (e) cudaEventDestroy(e);
         cudaFree(ctx->trace_scratch);
         cudaFree(ctx->scratch);
         cudaFree(ctx->pt_scratch);
@@ -293,8 +295,38 @@ gbrt_status gbrt_context_synchronize(gbrt_context* ctx)
             return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "a traversal stack overflowed; results are incomplete");
         if (status & kStatusBadIndex)
             return fail(ctx, GBRT_ERR_CUDA, "a kernel met an out-of-range node or triangle index and skipped it");
-        return fail(ctx, GBRT_ERR_WATCHDOG, "a bounded device-side wait gave up");
+        return fail(ctx, GBRT_ERR_CUDA, "a kernel reported unknown status bits " + std::to_string(status));
     }
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_set_kernel_timing(gbrt_context* ctx, int enable)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    device_guard g(ctx->device);
+    if (enable && !ctx->timing_events[0])
+        for (cudaEvent_t& e : ctx->timing_events)
+            GBRT_CUDA(ctx, cudaEventCreate(&e));
+    ctx->kernel_timing = enable != 0;
+    ctx->timing_count = 0;
+    return GBRT_OK;
+}
+
+gbrt_status gbrt_context_kernel_times(gbrt_context* ctx, float* out_ms, uint32_t max, uint32_t* count)
+{
+    if (!ctx || !count || (max > 0 && !out_ms)) return GBRT_ERR_INVALID_ARG;
+    device_guard g(ctx->device);
+    const uint32_t ring = gbrt_context::kTimingRing;
+    uint32_t m = ctx->timing_count < ring ? ctx->timing_count : ring;
+    if (m > max) m = max;
+    for (uint32_t j = 0; j < m; ++j)
+    {
+        const uint32_t k = (ctx->timing_count - m + j) % ring;
+        GBRT_CUDA(ctx, cudaEventSynchronize(ctx->timing_events[2 * k + 1]));
+        GBRT_CUDA(ctx, cudaEventElapsedTime(&out_ms[j], ctx->timing_events[2 * k], ctx->timing_events[2 * k + 1]));
+    }
+    *count = m;
+    ctx->timing_count = 0;
     return GBRT_OK;
 }
 
@@ -419,6 +451,20 @@ gbrt_status gbrt_bvh_counts(gbrt_bvh const* bvh, uint32_t* num_prims, uint32_t* 
     if (num_bvh2_nodes) *num_bvh2_nodes = bvh->num_prims > 0 ? 2 * bvh->num_prims - 1 : 0;
     if (depth_bound) *depth_bound = bvh->height;
     return GBRT_OK;
+}
+
+gbrt_status gbrt_bvh_rebuild_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris, uint32_t n)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!bvh || (n > 0 && !d_tris)) return fail(ctx, GBRT_ERR_INVALID_ARG, "rebuild_lbvh: null argument");
+    if (bvh->kind != bvh_kind::lbvh) return fail(ctx, GBRT_ERR_INVALID_ARG, "rebuild_lbvh: not an LBVH");
+    if (n != bvh->num_prims)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "rebuild_lbvh: triangle count differs from the tree's");
+    if (bvh->device != ctx->device) return fail(ctx, GBRT_ERR_INVALID_ARG, "rebuild_lbvh: tree on another device");
+    if ((reinterpret_cast<uintptr_t>(d_tris) & 3u) != 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "rebuild_lbvh: triangles not 4-byte aligned");
+    device_guard g(ctx->device);
+    return build_lbvh(ctx, d_tris, n, bvh);
 }
 
 gbrt_status gbrt_bvh_refit(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_tris, uint32_t n)

@@ -16,7 +16,6 @@
 enum : uint32_t
 {
     kStatusStackOverflow = 1u << 0,
-    kStatusWatchdog      = 1u << 1,
     kStatusBadIndex      = 1u << 2,   // a node/triangle index outside its array was skipped
 };
 
@@ -59,7 +58,37 @@ struct gbrt_context
     size_t trace_scratch_bytes = 0;
     void* slot_trace_scratch[kSlots] = { nullptr, nullptr };
     size_t slot_trace_scratch_bytes = 0;
+
+    // Kernel timing (gbrt_context_set_kernel_timing): a CUDA event pair around the
+    // traversal kernel of each ray query, in a ring of kTimingRing pairs
+    // (timing_events[2k] start, [2k + 1] stop); timing_count queries recorded so far.
+    static constexpr uint32_t kTimingRing = 256;
+    bool kernel_timing = false;
+    cudaEvent_t timing_events[2 * kTimingRing] = {};
+    uint32_t timing_count = 0;
 };
+
+namespace gbrt {
+// Records the start event of the next ring slot on `stream` when kernel timing is on,
+// and its stop event when it goes out of scope: wraps one traversal kernel launch.
+struct kernel_timer
+{
+    cudaStream_t stream;
+    cudaEvent_t stop = nullptr;
+    kernel_timer(gbrt_context* ctx, cudaStream_t s) : stream(s)
+    {
+        if (!ctx->kernel_timing) return;
+        const uint32_t k = ctx->timing_count % gbrt_context::kTimingRing;
+        cudaEventRecord(ctx->timing_events[2 * k], s);
+        stop = ctx->timing_events[2 * k + 1];
+        ++ctx->timing_count;
+    }
+    ~kernel_timer()
+    {
+        if (stop) cudaEventRecord(stop, stream);
+    }
+};
+} // namespace gbrt
 
 enum class bvh_kind
 {
@@ -123,6 +152,11 @@ struct gbrt_batch
     uint32_t num_materials = 0;
     bool extended_materials = false;   // some material is a mirror, glass or plastic
     uint32_t* d_work = nullptr;     // persistent-kernel work counter
+    // lights (gbrt_batch_set_lights): 4 float4 per light, scene s's lights at
+    // [light_offsets[s], light_offsets[s + 1])
+    float4* d_lights = nullptr;
+    uint32_t* d_light_offsets = nullptr;
+    uint32_t num_lights = 0;
     gbrt_batch_launch launch = { 128, 32, 64, GBRT_BATCH_ORDER_ROWS };
     // the captured build + frame
     cudaStream_t capture_stream = nullptr;
@@ -156,6 +190,11 @@ gbrt_status fail(gbrt_context* ctx, gbrt_status st, std::string const& what);
 gbrt_status check_cuda(gbrt_context* ctx, cudaError_t err, const char* where);
 // Grows the context scratch to at least `bytes`.
 gbrt_status ensure_scratch(gbrt_context* ctx, size_t bytes);
+
+// pathtrace.cu: the device records (4 float4 each) of area, point and spot lights, as
+// path-tracing scenes hold them; fails on an unknown light kind.
+gbrt_status light_records(gbrt_context* ctx, gbrt_light const* h_lights, uint32_t num_lights,
+                          std::vector<float4>& out, const char* who);
 
 // lbvh.cu
 gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t n, gbrt_bvh* bvh);

@@ -336,6 +336,8 @@ void free_batch(gbrt_batch* b)
     cudaFree(b->d_pixel_offsets);
     cudaFree(b->d_materials);
     cudaFree(b->d_work);
+    cudaFree(b->d_lights);
+    cudaFree(b->d_light_offsets);
 }
 
 } // namespace

@@ -11,8 +11,10 @@
 // search over the pixel offsets, and run each pixel's samples and bounces in-thread:
 // traversal of the scene's tree in the shared arena (traverse_bvh from the scene's
 // root) and the same shade_vertex as the wavefront renderer (pt_shade.cuh), so scene
-// s's image equals gbrt_pathtrace_frame's bit for bit.  This unit is compiled with
-// --fmad=false like pathtrace.cu.
+// s's image equals gbrt_pathtrace_frame's bit for bit.  Scenes with lights
+// (gbrt_batch_set_lights) sample them as the megakernel renderer does: the light
+// sample's shadow ray is an any-hit query through the scene's tree right after the
+// vertex is shaded.  This unit is compiled with --fmad=false like pathtrace.cu.
 
 #include "pt_shade.cuh"
 
@@ -47,6 +49,8 @@ struct batch_args
     int32_t total_inner, total_tris;
     const gbrt_material* materials;
     uint32_t num_materials;
+    const float4* lights;            // 4 float4 per light
+    const uint32_t* light_offsets;   // scene s: lights [light_offsets[s], light_offsets[s + 1])
     const float2* trig;
     uint32_t* work;
     float4* images;
@@ -63,8 +67,9 @@ constexpr int kBatchSharedStack = 8;
 constexpr int kBatchWarpsPerSM = 64;
 
 // Extended = false: a material table of matte and emissive slots only (the other
-// materials' branches compiled out, as for the adjoint).
-template <int Block, int Stack, bool Extended>
+// materials' branches compiled out, as for the adjoint).  Lit = false: no scene has
+// lights (the next-event path compiled out).
+template <int Block, int Stack, bool Extended, bool Lit>
 __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt(batch_args a)
 {
     const uint32_t full = 0xFFFFFFFFu;
@@ -103,6 +108,12 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
                 uint32_t blk = local >> 5, w = local & 31u, bw = f.width >> 3;
                 pixel = ((blk / bw) * 4u + (w >> 3)) * f.width + (blk % bw) * 8u + (w & 7u);
             }
+            if constexpr (Lit)
+            {
+                const uint32_t l0 = __ldg(&a.light_offsets[s]);
+                sp.lights = a.lights + 4 * uint64_t(l0);
+                sp.num_lights = __ldg(&a.light_offsets[s + 1]) - l0;
+            }
             sp.epsilon = f.epsilon;
             sp.ambient = f.ambient;
             sp.frame = f.frame_id;
@@ -122,6 +133,19 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
                                                               FLT_MAX, a.status);
                     vertex_out out;
                     shade_vertex<Extended>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, a.status);
+                    if constexpr (Lit)
+                    {
+                        if (out.shadow)
+                        {
+                            trace_result sh = traverse_bvh_with<true>(
+                                stack, a.nodes, a.tris, f.root, a.total_inner, a.total_tris,
+                                { out.sh_o.x, out.sh_o.y, out.sh_o.z }, { out.sh_d.x, out.sh_d.y, out.sh_d.z },
+                                sp.epsilon, out.sh_tmax, a.status);
+                            if (sh.tri < 0)
+                                st.rad = { st.rad.x + out.contrib.x, st.rad.y + out.contrib.y,
+                                           st.rad.z + out.contrib.z };
+                        }
+                    }
                     if (!out.cont) break;
                     o = out.next_o;
                     d = out.next_d;
@@ -143,39 +167,40 @@ __global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt
 
 using batch_kernel = void (*)(batch_args);
 
-template <int Block, bool Extended>
+template <int Block, bool Extended, bool Lit>
 batch_kernel pick_stack(uint32_t stack)
 {
     switch (stack)
     {
-    case 16: return batch_pt<Block, 16, Extended>;
-    case 24: return batch_pt<Block, 24, Extended>;
-    case 32: return batch_pt<Block, 32, Extended>;
-    case 64: return batch_pt<Block, 64, Extended>;
+    case 16: return batch_pt<Block, 16, Extended, Lit>;
+    case 24: return batch_pt<Block, 24, Extended, Lit>;
+    case 32: return batch_pt<Block, 32, Extended, Lit>;
+    case 64: return batch_pt<Block, 64, Extended, Lit>;
     default: return nullptr;
     }
 }
 
-template <bool Extended>
+template <bool Extended, bool Lit>
 batch_kernel pick_block(gbrt_batch_launch const& l)
 {
     switch (l.block)
     {
-    case 128: return pick_stack<128, Extended>(l.stack);
-    case 256: return pick_stack<256, Extended>(l.stack);
-    case 512: return pick_stack<512, Extended>(l.stack);
+    case 128: return pick_stack<128, Extended, Lit>(l.stack);
+    case 256: return pick_stack<256, Extended, Lit>(l.stack);
+    case 512: return pick_stack<512, Extended, Lit>(l.stack);
     default: return nullptr;
     }
 }
 
-batch_kernel pick_kernel(gbrt_batch_launch const& l, bool extended)
+batch_kernel pick_kernel(gbrt_batch_launch const& l, bool extended, bool lit)
 {
-    return extended ? pick_block<true>(l) : pick_block<false>(l);
+    if (lit) return extended ? pick_block<true, true>(l) : pick_block<false, true>(l);
+    return extended ? pick_block<true, false>(l) : pick_block<false, false>(l);
 }
 
 bool launch_valid(gbrt_batch_launch const& l)
 {
-    return pick_kernel(l, false) != nullptr && (l.tile == 32 || l.tile == 64) &&
+    return pick_kernel(l, false, false) != nullptr && (l.tile == 32 || l.tile == 64) &&
            (l.order == GBRT_BATCH_ORDER_ROWS || l.order == GBRT_BATCH_ORDER_BLOCKS);
 }
 
@@ -186,7 +211,7 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     if (b->frames_set != b->num_scenes) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: frames not set");
     if (!d_images || (reinterpret_cast<uintptr_t>(d_images) & 15u))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: images null or not 16-byte aligned");
-    batch_kernel kernel = pick_kernel(b->launch, b->extended_materials);
+    batch_kernel kernel = pick_kernel(b->launch, b->extended_materials, b->num_lights > 0);
     if (!kernel) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: bad launch shape");
     int per_sm = 0;
     GBRT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, int(b->launch.block), 0));
@@ -210,6 +235,8 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     a.total_tris = int32_t(b->total);
     a.materials = b->d_materials;
     a.num_materials = b->num_materials;
+    a.lights = b->d_lights;
+    a.light_offsets = b->d_light_offsets;
     if (!ctx->d_trig) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: frames not set on this context");
     a.trig = ctx->d_trig;
     a.work = b->d_work;
@@ -294,6 +321,42 @@ extern "C" gbrt_status gbrt_batch_set_frames(gbrt_context* ctx, gbrt_batch* batc
     batch->total_pixels = uint32_t(total);
     batch->frames_set = ns;
     batch->graph_dirty = true;
+    return GBRT_OK;
+}
+
+extern "C" gbrt_status gbrt_batch_set_lights(gbrt_context* ctx, gbrt_batch* batch, gbrt_light const* h_lights,
+                                             uint32_t num_lights, uint32_t const* h_light_offsets)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!batch || (num_lights && (!h_lights || !h_light_offsets)))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_lights: null argument");
+    const uint32_t ns = batch->num_scenes;
+    if (num_lights)
+    {
+        if (h_light_offsets[0] != 0 || h_light_offsets[ns] != num_lights)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_lights: offsets must run from 0 to num_lights");
+        for (uint32_t s = 0; s < ns; ++s)
+            if (h_light_offsets[s + 1] < h_light_offsets[s])
+                return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_set_lights: offsets decrease");
+    }
+    std::vector<float4> rec;
+    gbrt_status st = light_records(ctx, h_lights, num_lights, rec, "batch_set_lights");
+    if (st != GBRT_OK) return st;
+    device_guard g(ctx->device);
+    // the previous frame may still read these buffers
+    GBRT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(batch->d_lights);
+    cudaFree(batch->d_light_offsets);
+    batch->d_lights = nullptr;
+    batch->d_light_offsets = nullptr;
+    batch->num_lights = 0;
+    batch->graph_dirty = true;
+    if (num_lights == 0) return GBRT_OK;
+    GBRT_CUDA(ctx, cudaMalloc(&batch->d_lights, rec.size() * sizeof(float4)));
+    GBRT_CUDA(ctx, cudaMalloc(&batch->d_light_offsets, size_t(ns + 1) * 4));
+    GBRT_CUDA(ctx, cudaMemcpy(batch->d_lights, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    GBRT_CUDA(ctx, cudaMemcpy(batch->d_light_offsets, h_light_offsets, size_t(ns + 1) * 4, cudaMemcpyHostToDevice));
+    batch->num_lights = num_lights;
     return GBRT_OK;
 }
 

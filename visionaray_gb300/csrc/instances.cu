@@ -203,9 +203,9 @@ __global__ void __launch_bounds__(kBlock) tlas_trace(tlas_view tv, const gbrt_ra
                 node = kEmptyLink;
                 break;
             }
-            const bvh2_node* np = tv.nodes + node;
-            float4 a = ldg4(&np->xy0), b = ldg4(&np->xy1), z = ldg4(&np->z01);
-            int4 link = __ldg(&np->link);
+            float4 a, b, z;
+            int4 link;
+            load_pair(tv.nodes + node, a, b, z, link);
             float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
             float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
             float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;

@@ -580,10 +580,22 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
     if (n == 0) return GBRT_OK;
 
     cudaStream_t s = ctx->stream;
-    GBRT_CUDA(ctx, cudaMalloc(&bvh->tris, size_t(n) * sizeof(tri48)));
-    GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_codes, size_t(n) * 4));
-    GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_ids, size_t(n) * 4));
-    if (bvh->num_inner > 0) GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes, size_t(bvh->num_inner) * sizeof(bvh2_node)));
+    // a rebuild (gbrt_bvh_rebuild_lbvh) of a tree of the same size writes into its arrays
+    if (!bvh->tris) GBRT_CUDA(ctx, cudaMalloc(&bvh->tris, size_t(n) * sizeof(tri48)));
+    if (!bvh->sorted_codes) GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_codes, size_t(n) * 4));
+    if (!bvh->sorted_ids) GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_ids, size_t(n) * 4));
+    if (bvh->num_inner > 0 && !bvh->nodes)
+        GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes, size_t(bvh->num_inner) * sizeof(bvh2_node)));
+    if (bvh->nodes4)
+    {
+        // a rebuild with a 4-wide collapse from the previous build: its size may change
+        GBRT_CUDA(ctx, cudaStreamSynchronize(s));
+        cudaFree(bvh->nodes4);
+        bvh->nodes4 = nullptr;
+        bvh->num_nodes4 = 0;
+        cudaFree(bvh->nodes4q);
+        bvh->nodes4q = nullptr;
+    }
 
     // scratch: centroids | keys_alt | vals_alt | leaf_parent | arrivals | cb(6) | height | sort
     size_t off_centroids = 0;

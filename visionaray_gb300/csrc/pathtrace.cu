@@ -797,18 +797,27 @@ extern "C" gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh c
     for (uint32_t k = 0; k < num_materials; ++k)
         if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
             return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: unknown material kind");
-    std::vector<float4> rec(size_t(num_lights) * 4);
+    std::vector<float4> rec;
+    gbrt_status st = light_records(ctx, h_lights, num_lights, rec, "pt_scene_create_lights");
+    if (st != GBRT_OK) return st;
+    return create_scene(ctx, bvh, h_materials, num_materials, rec, out);
+}
+
+gbrt_status gbrt::light_records(gbrt_context* ctx, gbrt_light const* h_lights, uint32_t num_lights,
+                                std::vector<float4>& out, const char* who)
+{
+    out.assign(size_t(num_lights) * 4, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (uint32_t k = 0; k < num_lights; ++k)
     {
         gbrt_light const& l = h_lights[k];
         if (l.kind == GBRT_LIGHT_AREA)
-            area_record(l.geometry, l.cl, l.kl, &rec[4 * k]);
+            area_record(l.geometry, l.cl, l.kl, &out[4 * k]);
         else if (l.kind == GBRT_LIGHT_POINT || l.kind == GBRT_LIGHT_SPOT)
-            delta_record(l, &rec[4 * k]);
+            delta_record(l, &out[4 * k]);
         else
-            return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_lights: unknown light kind");
+            return fail(ctx, GBRT_ERR_INVALID_ARG, std::string(who) + ": unknown light kind");
     }
-    return create_scene(ctx, bvh, h_materials, num_materials, rec, out);
+    return GBRT_OK;
 }
 
 extern "C" gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint32_t width, uint32_t height, float* out)

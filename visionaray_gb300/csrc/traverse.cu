@@ -163,11 +163,9 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_dynamic(bvh_view v, co
                 node = kEmptyLink;
                 break;
             }
-            const bvh2_node* np = v.nodes + node;
-            float4 a = ldg4(&np->xy0);
-            float4 b = ldg4(&np->xy1);
-            float4 z = ldg4(&np->z01);
-            int4 link = __ldg(&np->link);
+            float4 a, b, z;
+            int4 link;
+            load_pair(v.nodes + node, a, b, z, link);
             float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
             float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
             float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;
@@ -340,6 +338,7 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         perm = vals;   // radix_sort_pairs leaves the result in (keys, values)
         if (!persistent)
         {
+            kernel_timer timer(ctx, stream);
             auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
                                                                                         ctx->d_status); };
             if (compressed)
@@ -363,11 +362,13 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         uint32_t grid = uint32_t(ctx->num_sms) * uint32_t(per_sm > 0 ? per_sm : 1);
         if (grid > blocks) grid = blocks;
         GBRT_CUDA(ctx, cudaMemsetAsync(counter, 0, 4, stream));
+        kernel_timer timer(ctx, stream);
         kernel<<<grid, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits, counter, ctx->trace_refill,
                                                  ctx->d_status);
         GBRT_LAUNCH_CHECK(ctx, "trace_rays_dynamic");
         return GBRT_OK;
     }
+    kernel_timer timer(ctx, stream);
     auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, d_hits, ctx->d_status); };
     if (compressed)
         any_hit ? launch(trace_rays<true, kNodesCompressed>) : launch(trace_rays<false, kNodesCompressed>);

@@ -4,7 +4,7 @@
 // Replaces the device branch of visionaray's intersect<Traversal>(ray, bvh, isect)
 // (detail/bvh/intersect.inl:166-356), which visits BVH2 nodes one 32-byte box at a
 // time with a 5-entry stack and a restart trail.  Here each step fetches one 64-byte
-// record (four 128-bit read-only loads) holding both children's boxes, tests both,
+// record (two 256-bit read-only loads) holding both children's boxes, tests both,
 // descends into the nearer hit child and pushes the farther one on a per-thread stack
 // (Aila & Laine 2009 "while-while" form).  Leaves are contiguous runs of 48-byte
 // triangles tested with the reference's exact ray/triangle arithmetic
@@ -58,6 +58,32 @@ struct shared_stack
     __device__ __forceinline__ int get(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
 };
 
+// The next stack entry to visit, kEmptyLink when the stack is empty.
+template <class StackT>
+__device__ __forceinline__ int pop_entry(StackT const& stack, int& sp)
+{
+    return sp > 0 ? stack.get(--sp) : kEmptyLink;
+}
+
+// One node pair as two 256-bit read-only loads (ld.global.nc.v8.f32, sm_100 and later;
+// records are 64-byte aligned): half the load instructions of four 128-bit loads.
+// Measured on the heightfield workload (kernel alone, same rays and hits): closest hit
+// 3.754 -> 3.669 ms, AO any hit 16.63 -> 16.19 ms per launch.
+__device__ __forceinline__ void load_pair(const bvh2_node* np, float4& a, float4& b, float4& z, int4& link)
+{
+    float r[16];
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7])
+                 : "l"(np));
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r[8]), "=f"(r[9]), "=f"(r[10]), "=f"(r[11]), "=f"(r[12]), "=f"(r[13]), "=f"(r[14]), "=f"(r[15])
+                 : "l"(reinterpret_cast<const char*>(np) + 32));
+    a = make_float4(r[0], r[1], r[2], r[3]);
+    b = make_float4(r[4], r[5], r[6], r[7]);
+    z = make_float4(r[8], r[9], r[10], r[11]);
+    link = make_int4(__float_as_int(r[12]), __float_as_int(r[13]), __float_as_int(r[14]), __float_as_int(r[15]));
+}
+
 // A tree taller than the stack's capacity sets kStatusStackOverflow and skips the
 // subtrees that did not fit.  t_best: a hit must be strictly closer than this (a
 // closer hit found elsewhere, e.g. in another instance); the result's t is t_best
@@ -85,11 +111,9 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
                 node = kEmptyLink;
                 break;
             }
-            const bvh2_node* np = nodes + node;
-            float4 a = ldg4(&np->xy0);
-            float4 b = ldg4(&np->xy1);
-            float4 z = ldg4(&np->z01);
-            int4 link = __ldg(&np->link);
+            float4 a, b, z;
+            int4 link;
+            load_pair(nodes + node, a, b, z, link);
 
             // slab test as (box - origin) * inv_dir, like detail/bvh/intersect.inl:257-276
             float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
@@ -122,7 +146,7 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
             }
             else
             {
-                node = sp > 0 ? stack.get(--sp) : kEmptyLink;
+                node = pop_entry(stack, sp);
             }
         }
         if (node == kEmptyLink) break;
@@ -147,7 +171,7 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
             }
             if (__float_as_uint(t2.w) & kLastInLeaf) break;
         }
-        node = sp > 0 ? stack.get(--sp) : kEmptyLink;
+        node = pop_entry(stack, sp);
     }
     return best;
 }

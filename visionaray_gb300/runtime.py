@@ -34,6 +34,9 @@ SIGNATURES = {
     "gbrt_context_synchronize": (_i32, [_vp]),
     "gbrt_last_error": (ctypes.c_char_p, [_vp]),
     "gbrt_kernel_launch_count": (_u64, [_vp]),
+    "gbrt_context_set_kernel_timing": (_i32, [_vp, _i32]),
+    "gbrt_bvh_rebuild_lbvh": (_i32, [_vp, _vp, _vp, _u32]),
+    "gbrt_context_kernel_times": (_i32, [_vp, _vp, _u32, _vp]),
     "gbrt_context_set_trace_flags": (_i32, [_vp, _u32]),
     "gbrt_context_set_trace_refill": (_i32, [_vp, _u32]),
     "gbrt_context_set_host_chunk": (_i32, [_vp, _u32]),
@@ -70,6 +73,7 @@ SIGNATURES = {
     "gbrt_batch_trace_closest_hit": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "gbrt_batch_set_frames": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32]),
     "gbrt_batch_set_launch": (_i32, [_vp, _vp]),
+    "gbrt_batch_set_lights": (_i32, [_vp, _vp, _vp, _u32, _vp]),
     "gbrt_batch_get_launch": (_i32, [_vp, _vp]),
     "gbrt_batch_height": (_i32, [_vp, _vp, _vp]),
     "gbrt_batch_pathtrace": (_i32, [_vp, _vp, _vp]),
@@ -160,6 +164,19 @@ class Context:
     def launches(self):
         return int(self.lib.gbrt_kernel_launch_count(self.h))
 
+    def set_kernel_timing(self, enable):
+        """Records CUDA events around the traversal kernel of every ray query (see
+        gbrt_context_set_kernel_timing); enabling clears the record."""
+        self.check(self.lib.gbrt_context_set_kernel_timing(self.h, 1 if enable else 0))
+
+    def kernel_times(self, max_queries=256):
+        """Traversal-kernel durations (ms) of the queries recorded since the last call,
+        oldest first (at most the 256 most recent); waits for them."""
+        out = np.zeros(max_queries, np.float32)
+        count = ctypes.c_uint32()
+        self.check(self.lib.gbrt_context_kernel_times(self.h, _hptr(out), max_queries, ctypes.byref(count)))
+        return [float(x) for x in out[:count.value]]
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.gbrt_context_destroy(self.h)
@@ -239,6 +256,14 @@ class IndexBVH:
         n x 44 bytes, the build's input order); topology kept, boxes recomputed."""
         n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
         self.ctx.check(self.ctx.lib.gbrt_bvh_refit(self.ctx.h, self.h, _dptr(tris), n))
+        return self
+
+    def rebuild(self, tris):
+        """lbvh_builder::build into this tree's arrays (gbrt_bvh_rebuild_lbvh): the same
+        number of triangles at any positions (torch uint8 CUDA tensor, n x 44 bytes); no
+        device allocation."""
+        n = tris.numel() * tris.element_size() // TRIANGLE.itemsize
+        self.ctx.check(self.ctx.lib.gbrt_bvh_rebuild_lbvh(self.ctx.h, self.h, _dptr(tris), n))
         return self
 
     def morton_codes(self):
@@ -482,6 +507,16 @@ class Batch:
                                                           _hptr(mats), len(mats)))
         px = pars["width"].astype(np.uint64) * pars["height"].astype(np.uint64)
         self.pixel_offsets = np.concatenate([[0], np.cumsum(px)]).astype(np.uint64)
+
+    def set_lights(self, lights, light_offsets):
+        """Scene s samples lights[light_offsets[s]:light_offsets[s + 1]] (LIGHT records,
+        or AREA_LIGHT records, which are converted)."""
+        from .types import lights_of_area_lights
+        lts = (np.ascontiguousarray(lights, LIGHT) if np.asarray(lights).dtype == LIGHT
+               else lights_of_area_lights(lights))
+        offs = np.ascontiguousarray(light_offsets, np.uint32)
+        self.ctx.check(self.ctx.lib.gbrt_batch_set_lights(self.ctx.h, self.h, _hptr(lts), len(lts),
+                                                          _hptr(offs) if len(lts) else None))
 
     @property
     def launch(self):
