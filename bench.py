@@ -31,8 +31,9 @@ METRIC = "incoherent closest-hit Mrays/s; PT Msamples/s batched vs plain; bwd/fw
 UNIT = "Mrays/s"
 GRID, SCENE_SEED = 2048, 1
 ORIGINS, RAY_SEED, AO_PER_ORIGIN, AO_TMAX, OFFSET = 1 << 22, 7, 8, 0.05, 1e-4
-WORKLOAD = ("heightfield 2048x2048 (8,388,608 tris, 6 sine octaves) LBVH; 4,194,304 closest-hit "
-            "secondary rays + 33,554,432 any-hit AO rays (tmax 0.05) per step")
+WORKLOAD = ("heightfield 2048x2048 (8,388,608 tris, 6 sine octaves) LBVH; one step = closest_hit over 4,194,304 "
+            "incoherent secondary rays (cosine-weighted from surface points); the 33,554,432 any-hit AO rays "
+            "(tmax 0.05) and the LBVH build are timed beside it")
 
 # Algorithmic bytes per ray, B_ray = 32 (ray) + 16 (hit) + N_node*32 + N_tri*48, with
 # N_node / N_tri the mean box / triangle tests per ray of visionaray's CPU traversal on
@@ -43,13 +44,67 @@ N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
-# of the full-size workload with the default ray order; profiles/
-# trace_rays_permuted_heightfield_2048_dram.md).
+# of the full-size workload with the default ray order).
 TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.375e9 + 0.153e9, 2.620e9 + 0.530e9
+
+
+# Algorithmic bytes per path-traced sample, B_sample = sum of B_ray over the sample's
+# path segments and shadow rays, counted on the oracle's FP32 run of each workload at
+# the CUDA path's random numbers (python -m oracle.b_sample): the box frame (every 61st
+# pixel, 64 spp: 6.75 segments per sample), the batch (every 8th scene, 1.77 segments)
+# and the inverse-rendering frame (every 7th pixel, 16 spp: 11.9 segments).
+B_SAMPLE_BOX, B_SAMPLE_BATCH, B_SAMPLE_INVERSE = 24726.4, 6132.6, 31621.4
 
 
 def b_ray(n_node, n_tri):
     return 32 + 16 + n_node * 32 + n_tri * 48
+
+
+def measured_l2_copy_gbs(device):
+    """L2 bandwidth of a device-to-device copy whose source and destination (24 MB
+    each) stay resident in the 129 MB L2: read + write bytes over the CUDA-event time,
+    best of 5 rounds of 50 copies (measured here: no L2 peak is recorded for this GPU)."""
+    import torch
+    n = 6 * 1024 * 1024
+    a = torch.ones(n, dtype=torch.float32, device=device)
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    best = 0.0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(5):
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * 4 * n * 50 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del a, b
+    return round(best, 1)
+
+
+def roofline_of(samples, seconds, b_sample, peak, peak_source, scope, bound="hbm"):
+    achieved = samples * b_sample / seconds / 1e9
+    return {"bound": bound, "scope": scope, "b_sample": b_sample, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_source}
+
+
+def pt_cpu_baseline(tris, mats, lights, cam, params, pixel_step):
+    """visionaray's pathtracing::kernel on the CPU (the oracle's FP32 mode, equal to the
+    reference's kernel bit for bit; its binned-SAH tree, not timed; all host threads) on
+    every pixel_step-th pixel of the frame: Msamples/s."""
+    from oracle import Oracle
+    o = Oracle()
+    tree = o.build_sah(tris)
+    npix = int(params["width"]) * int(params["height"])
+    pix = np.arange(0, npix, pixel_step, dtype=np.uint32)
+    t0 = time.perf_counter()
+    o.pathtrace_pixels(tree, tris, mats, lights, cam, params, pix, mode=Oracle.PT_FLOAT)
+    dt = time.perf_counter() - t0
+    samples = len(pix) * int(params["spp"])
+    return {"value": round(samples / dt / 1e6, 3), "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+            "kind": "port", "sample": f"every {pixel_step}th pixel ({len(pix)} pixels x {int(params['spp'])} spp, "
+                                      f"{dt:.2f} s); binned-SAH tree not timed"}
 
 
 def measured_hbm_peak():
@@ -144,9 +199,10 @@ class ClockSampler:
         return out
 
 
-def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=8, repeats=1):
+def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=4, repeats=1, any_repeats=1):
     """The reference's CPU path (oracle restatement, binned-SAH tree, all host threads)
-    on every `sample_every`-th origin's closest ray and its AO rays."""
+    on every `sample_every`-th origin: its closest-hit ray `repeats` times, then its AO
+    rays `any_repeats` times."""
     from oracle import Oracle, Reference
     kind = "reference" if Reference.available() else "port"
     nthreads = os.cpu_count() or 1
@@ -163,16 +219,27 @@ def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=8, repeats=1)
     sel = np.arange(0, len(closest), sample_every)
     c_s = closest[sel]
     a_s = ao.reshape(len(closest), AO_PER_ORIGIN)[sel].reshape(-1)
-    times = []
+    times_c, times_a = [], []
     for _ in range(repeats):
         t0 = time.perf_counter()
         trace(c_s, False)
+        times_c.append(time.perf_counter() - t0)
+    for _ in range(any_repeats):
+        t0 = time.perf_counter()
         trace(a_s, True)
-        times.append(time.perf_counter() - t0)
-    rays = len(c_s) + len(a_s)
-    return {"kind": kind, "cores": nthreads, "build_s": build_s, "rays": rays, "times": times,
-            "sample": f"every {sample_every}th origin: {len(c_s)} closest + {len(a_s)} AO rays "
-                      f"(1/{sample_every} of a step); binned-SAH tree built in {build_s:.1f} s (not timed)"}
+        times_a.append(time.perf_counter() - t0)
+    return {"kind": kind, "cores": nthreads, "build_s": build_s, "closest_rays": len(c_s), "any_rays": len(a_s),
+            "closest_times": times_c, "any_times": times_a,
+            "sample": f"every {sample_every}th origin: {len(c_s)} closest-hit rays ({len(a_s)} AO rays for the "
+                      f"any-hit figure); binned-SAH tree built in {build_s:.1f} s (not timed)"}
+
+
+# The restatement against visionaray's own CPU code on the same tree and rays (x86-64, 8
+# threads, heightfield 512x512, binned-SAH tree; identical hits): where the reference's
+# CPU code cannot be built (the GPU host has no visionaray sources), the baseline is the
+# restatement and runs at this fraction of the reference's speed.
+PORT_VS_REFERENCE = {"closest": round(1.69 / 2.19, 3), "any": round(5.11 / 5.25, 3),
+                     "measured": "x86-64, 8 threads, heightfield 512x512, binned-SAH tree, identical hits"}
 
 
 def run_reference(args):
@@ -180,17 +247,21 @@ def run_reference(args):
     if rank != 0:
         return 0
     tris, closest, ao = workload(grid=args.grid, origins=args.origins)
-    res = cpu_baseline(tris, closest, ao, sample_every=8, repeats=args.warmup + args.steps)
-    t = res["times"][args.warmup:]
+    res = cpu_baseline(tris, closest, ao, sample_every=4, repeats=args.warmup + args.steps)
+    t = res["closest_times"][args.warmup:]
     ms = 1e3 * statistics.mean(t)
-    value = res["rays"] / statistics.mean(t) / 1e6
+    value = res["closest_rays"] / statistics.mean(t) / 1e6
+    any_value = res["any_rays"] / min(res["any_times"]) / 1e6
+    base = {"value": round(value, 3), "unit": UNIT, "cores": res["cores"], "kind": res["kind"],
+            "sample": res["sample"], "any_hit_mrays_s": round(any_value, 3)}
+    if res["kind"] == "port":
+        base["port_vs_reference"] = PORT_VS_REFERENCE
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD + " (each step a bounded sample, see cpu_baseline.sample)",
                        "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": res["cores"], "kind": res["kind"],
-                             "sample": res["sample"]},
+            "cpu_baseline": base,
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -207,7 +278,7 @@ PT_GLOSSY_WORKLOAD = ("path tracing: the same box, its 256 blobs cycling matte /
                       "64 spp, depth 8, Russian roulette from depth 3")
 
 
-def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc", scene_kind="box"):
+def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc", scene_kind="box", cpu=False):
     """Msamples/s of the path-tracing workload (one frame = 1920x1080 x 64 spp);
     scene_kind "glossy": the materials-and-lights variant of the same box."""
     import torch
@@ -239,10 +310,19 @@ def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc", scene_kind="bo
     ms = ev[0].elapsed_time(ev[1]) / frames
     samples = PT_WIDTH * PT_HEIGHT * PT_SPP
     mean = accum[..., :3].mean().item()
-    return {"workload": PT_GLOSSY_WORKLOAD if scene_kind == "glossy" else PT_WORKLOAD, "flags": flags,
-            "builder": builder, "frames": frames, "ms_per_frame": round(ms, 2),
-            "msamples_s": round(samples / (ms * 1e-3) / 1e6, 2), "image_mean": round(mean, 5),
-            "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
+    res = {"workload": PT_GLOSSY_WORKLOAD if scene_kind == "glossy" else PT_WORKLOAD, "flags": flags,
+           "builder": builder, "frames": frames, "ms_per_frame": round(ms, 2),
+           "msamples_s": round(samples / (ms * 1e-3) / 1e6, 2), "image_mean": round(mean, 5),
+           "gpu_launches_per_frame": (ctx.launches - launches0) // frames}
+    if scene_kind == "box" and flags == 0:
+        peak, kind = measured_hbm_peak()
+        res["roofline"] = roofline_of(samples, ms * 1e-3, B_SAMPLE_BOX, peak, f"{kind} hbm_gbs",
+                                      "frame: every kernel of the wavefront frame (extend, shade, shadow)")
+    if cpu:
+        res["cpu_baseline"] = pt_cpu_baseline(tris, mats, lights, cam,
+                                              scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES,
+                                                               frame_id=1, flags=flags), 61)
+    return res
 
 
 BATCH_WORKLOAD = ("512 random-soup scenes (triangle counts log-uniform in [1k, 1M], vertex offsets 0.5/cbrt(n)), "
@@ -251,11 +331,13 @@ BATCH_WORKLOAD = ("512 random-soup scenes (triangle counts log-uniform in [1k, 1
                   "of every scene")
 
 
-def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_000_000):
+def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_000_000, cpu=False):
     """The batched graph (build + frame of 512 scenes in one CUDA graph, autotuned
-    persistent launch) against the plain per-scene loop (gbrt_bvh_build_lbvh +
-    gbrt_pathtrace_frame per scene) on the same GPU; Msamples/s of both and whether
-    their images are bit-identical."""
+    persistent launch) against two plain per-scene loops on the same GPU -- one that
+    creates a tree and a scene per scene and step (gbrt_bvh_build_lbvh +
+    gbrt_pt_scene_create + gbrt_pathtrace_frame), one that rebuilds trees made once
+    into their own arrays (gbrt_bvh_rebuild_lbvh + gbrt_pathtrace_frame) -- Msamples/s
+    of each and whether their images are bit-identical."""
     import torch
     from visionaray_gb300 import replicas, scenes
     from visionaray_gb300.types import AREA_LIGHT
@@ -272,6 +354,7 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
         cams, params = cams[mine], params[mine]
     ns = len(offsets) - 1
     d_tris = vg.as_device_bytes(tris, ctx.device)
+    tris_host = tris if cpu else None
     del tris
     batch = vg.Batch(offsets, ctx)
     batch.set_frames(cams, params, mats)
@@ -321,14 +404,23 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
             sc.close()
             bvh.close()
 
-    def time_plain():
-        plain_step()   # warm-up (grows the context scratch to the largest scene)
+    kept = []   # (tree, scene) per scene, made once for the preallocated loop
+
+    def preallocated_step():
+        for s in range(ns):
+            bvh, sc = kept[s]
+            bvh.rebuild(d_tris[int(offsets[s]) * 44:int(offsets[s + 1]) * 44])
+            vg.pathtrace_frame(sc, cams[s], params[s], accum=views[s])
+
+    def time_plain(step_fn):
+        plain_images.fill_(-1.0)
+        step_fn()   # warm-up (grows the context scratch to the largest scene)
         ctx.synchronize()
         launches0 = ctx.launches
         torch.cuda.synchronize()
         ev[0].record(ctx.stream)
         for _ in range(plain_steps):
-            plain_step()
+            step_fn()
         ev[1].record(ctx.stream)
         torch.cuda.synchronize()
         ctx.synchronize()
@@ -337,13 +429,24 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
         differ = 0.0 if torch.equal(images.view(torch.int32), plain_images.view(torch.int32)) else 1.0
         identical = replicas.reduce_over_ranks(differ, "sum", f"cuda:{ctx.device}") == 0.0
         return ({"ms_per_step": round(plain_ms, 2), "msamples_s": round(samples / (plain_ms * 1e-3) / 1e6, 2),
-                 "gpu_launches_per_step": int(plain_launches), "steps": plain_steps},
+                 "gpu_launches_per_step": int(plain_launches), "steps": plain_steps,
+                 "images_bit_identical": identical, "speedup_of_batched": round(plain_ms / batch_ms, 2)},
                 round(plain_ms / batch_ms, 2), identical)
 
     if plain_steps <= 0:
-        res_plain, speedup, identical = None, None, None
+        res_plain, speedup, identical, res_pre = None, None, None, None
     else:
-        res_plain, speedup, identical = time_plain()
+        res_plain, speedup, identical = time_plain(plain_step)
+        builder = vg.lbvh_builder(ctx)
+        for s in range(ns):
+            bvh = builder.build(d_tris[int(offsets[s]) * 44:int(offsets[s + 1]) * 44])
+            kept.append((bvh, vg.PTScene(bvh, mats, no_lights)))
+        res_pre, _, identical_pre = time_plain(preallocated_step)
+        identical = identical and identical_pre
+        for bvh, sc in kept:
+            sc.close()
+            bvh.close()
+        kept.clear()
     mean = float(images[:, :3].mean().item())
     workload = BATCH_WORKLOAD if (num_scenes, max_tris) == (512, 1_000_000) else (
         f"REDUCED profiling case: {num_scenes} scenes, triangle counts log-uniform in [1k, {max_tris}]")
@@ -355,25 +458,78 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
                        "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
                        "steps": steps, "launch": {k: int(best[k]) for k in best.dtype.names},
                        "autotune_frame_ms": round(float(tune_ms), 2), "autotune_s": round(tune_s, 1)},
-           "plain": res_plain, "speedup": speedup, "images_bit_identical": identical,
-           "image_mean": round(mean, 5)}
+           "plain": res_plain, "plain_preallocated": res_pre, "speedup": speedup,
+           "images_bit_identical": identical, "image_mean": round(mean, 5)}
+    peak, kind = measured_hbm_peak()
+    res["roofline"] = roofline_of(samples, frame_ms * 1e-3, B_SAMPLE_BATCH, peak, f"{kind} hbm_gbs",
+                                  "the persistent frame kernel (batch_pt) alone")
+    if cpu and world == 1 and (num_scenes, max_tris) == (512, 1_000_000):
+        res["cpu_baseline"] = batch_cpu_baseline(tris_host, offsets, cams, params, mats)
     batch.close()
     del d_tris, images, plain_images, views
     torch.cuda.empty_cache()
     return res
 
 
-def run_adjoint(ctx, steps, rprint, flags=0, builder="ploc"):
+def batch_cpu_baseline(tris, offsets, cams, params, mats, scene_step=32):
+    """The plain per-scene loop on the CPU with visionaray's CPU path (the oracle's
+    restatement: binned-SAH build + pathtracing::kernel in FP32, all host threads) on
+    every scene_step-th scene: Msamples/s over build + render time."""
+    from oracle import Oracle
+
+    from visionaray_gb300.types import AREA_LIGHT
+    o = Oracle()
+    build_s = render_s = 0.0
+    samples = 0
+    chosen = range(0, len(offsets) - 1, scene_step)
+    for s in chosen:
+        t = tris[int(offsets[s]):int(offsets[s + 1])]
+        t0 = time.perf_counter()
+        tree = o.build_sah(t)
+        t1 = time.perf_counter()
+        o.pathtrace(tree, t, mats, np.zeros(0, AREA_LIGHT), cams[s], params[s], mode=Oracle.PT_FLOAT)
+        t2 = time.perf_counter()
+        build_s += t1 - t0
+        render_s += t2 - t1
+        samples += int(params["width"][s]) * int(params["height"][s]) * int(params["spp"][s])
+    return {"value": round(samples / (build_s + render_s) / 1e6, 3), "unit": "Msamples/s",
+            "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"every {scene_step}th scene ({len(chosen)} scenes, {samples} samples): binned-SAH build "
+                      f"{build_s:.2f} s + render {render_s:.2f} s"}
+
+
+def run_adjoint(ctx, steps, rprint, flags=0, builder="ploc", cpu=False):
     """The inverse-albedo workload: `steps` Adam steps of forward frame + L2 loss +
-    path-replay adjoint; median forward / backward times and their ratio."""
+    path-replay adjoint; median forward / backward times and their ratio, the albedo
+    errors at the start and the end on the same sets of slots, and the bias of the
+    gradient estimator (same-seed against decorrelated replay)."""
     from visionaray_gb300 import inverse
     r = inverse.optimize(steps=steps, ctx=ctx, extra_flags=flags, builder=builder)
-    return {"workload": "inverse albedo on the box scene reduced to 4,014 triangles (2 blobs, subdiv 10): "
+    rnd = lambda d: {k: (round(v, 4) if v is not None else None) for k, v in d.items()}  # noqa: E731
+    res = {"workload": "inverse albedo on the box scene reduced to 4,094 triangles (204 blobs of 20 triangles): "
                         "512x512, 16 spp, depth 6 forward + L2 loss + adjoint per step, target 256 spp",
-            "steps": steps, "flags": int(inverse.FLAGS | flags), "builder": builder, "fwd_ms": round(r["fwd_ms"], 3), "bwd_ms": round(r["bwd_ms"], 3),
-            "bwd_over_fwd": round(r["bwd_ms"] / r["fwd_ms"], 3), "loss_start": round(r["losses"][0], 6),
-            "loss_end": round(r["losses"][-1], 6), "albedo_error_start": round(r["albedo_error_start"], 4),
-            "albedo_error_end_seen": round(r["albedo_error_end_seen"], 4)}
+            "steps": steps, "flags": int(inverse.FLAGS | flags), "builder": builder, "fwd_ms": round(r["fwd_ms"], 3),
+            "bwd_ms": round(r["bwd_ms"], 3), "bwd_over_fwd": round(r["bwd_ms"] / r["fwd_ms"], 3),
+            "loss_start": round(r["losses"][0], 6), "loss_end": round(r["losses"][-1], 6),
+            "estimator": r["estimator"], "slots_seen": r["slots_seen"], "slots_ge_64px": r["slots_ge_64px"],
+            "albedo_error_start": rnd(r["errors_start"]), "albedo_error_end": rnd(r["errors_end"]),
+            "gradient_bias": inverse.gradient_bias(ctx=ctx, builder=builder)}
+    # the 4,094-triangle scene (~200 KB of tree and triangles) is L2-resident: its
+    # traversal bytes are served by L2, so the roofline is L2's (measured copy peak)
+    l2 = measured_l2_copy_gbs(f"cuda:{ctx.device}")
+    samples = 512 * 512 * 16
+    res["roofline"] = {
+        "forward": roofline_of(samples, r["fwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 copy measured in this run",
+                               "forward frame (gbrt_pathtrace_forward)", bound="l2"),
+        "backward": roofline_of(samples, r["bwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 copy measured in this run",
+                                "path-replay kernel (replays the forward's segments)", bound="l2")}
+    if cpu:
+        from visionaray_gb300 import scenes
+        tris, mats, lights = scenes.box_scene(n_blobs=204, subdiv=1, seed=1)
+        p = scenes.pt_params(512, 512, 16, num_bounces=6, frame_id=0, flags=inverse.FLAGS | flags)
+        res["cpu_baseline"] = pt_cpu_baseline(tris, mats, lights, scenes.box_camera(), p, 7)
+        res["cpu_baseline"]["note"] = "forward frame only: the reference has no adjoint"
+    return res
 
 
 def run_ours(args):
@@ -429,9 +585,12 @@ def run_ours(args):
         if ev:
             ev[2].record(stream)
 
-    # the clock sampler runs from before the warm-up (nvidia-smi takes a moment to
-    # start); only its samples inside the timed region count
-    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    # The headline step is closest_hit over the 4,194,304 secondary rays (the metric is
+    # closest-hit Mrays/s); the AO any-hit rays and the build-inclusive step (LBVH build
+    # + closest + any hit) are timed beside it.  The clock sampler runs from before the
+    # warm-up (nvidia-smi takes a moment to start); only its samples inside the timed
+    # region count.  Kernel timing records CUDA events around each query's traversal
+    # kernel on the context stream (after the query's ray ordering).
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         # warm-up: at least W steps and at least 1.5 s of them (a GPU fresh out of idle
@@ -439,83 +598,115 @@ def run_ours(args):
         t_warm = time.perf_counter()
         done = 0
         while done < args.warmup or time.perf_counter() - t_warm < 1.5:
-            step()
+            vg.closest_hit(d_closest, bvh, out=h_closest)
+            vg.any_hit(d_ao, bvh, out=h_ao)
             done += 1
             if done % 8 == 0:
                 ctx.synchronize()
         ctx.synchronize()
         launches0 = ctx.launches
+        ctx.set_kernel_timing(True)
         replicas.barrier()
         torch.cuda.synchronize()
         clocks.mark_start()
         start.record(stream)
-        for k in range(args.steps):
-            step(events[k])
+        for _ in range(args.steps):
+            vg.closest_hit(d_closest, bvh, out=h_closest)
         stop.record(stream)
         torch.cuda.synchronize()
         clocks.mark_end()
     replicas.barrier()
     gpu_launches = ctx.launches - launches0
+    closest_kernel_ms = ctx.kernel_times()
     ctx.synchronize()   # raises on a flagged stack overflow / bad index
-    total_ms = start.elapsed_time(stop)
-    t_closest = [e[0].elapsed_time(e[1]) for e in events]
-    t_any = [e[1].elapsed_time(e[2]) for e in events]
-    total_ms = replicas.reduce_over_ranks(total_ms, "max", dev)   # the slowest rank
+    total_ms = replicas.reduce_over_ranks(start.elapsed_time(stop), "max", dev)   # the slowest rank
     ms_per_step = total_ms / args.steps
-    value = world * rays_per_step * args.steps / (total_ms * 1e-3) / 1e6
+    value = world * n_c * args.steps / (total_ms * 1e-3) / 1e6
+
+    # the AO any-hit rays, timed the same way
+    ctx.set_kernel_timing(True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(args.steps):
+        vg.any_hit(d_ao, bvh, out=h_ao)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    any_ms = start.elapsed_time(stop) / args.steps
+    any_kernel_ms = ctx.kernel_times()
+    ctx.set_kernel_timing(False)
+
+    # the whole configuration per step: LBVH build (a new tree each step, through the
+    # public build call) + closest hit + any hit
+    bi_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(bi_steps):
+        step_bvh = builder.build(d_tris)
+        vg.closest_hit(d_closest, step_bvh, out=h_closest)
+        vg.any_hit(d_ao, step_bvh, out=h_ao)
+        del step_bvh
+    stop.record(stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    bi_ms = start.elapsed_time(stop) / bi_steps
 
     # end to end through the host-buffer C ABI: pinned host rays in, hits out, per step
+    # (host wall time, median of up to 10 steps: host-side jitter in the pinned copies
+    # makes single steps vary by ~10 %)
     pin_c = torch.from_numpy(closest.view(np.float32).reshape(-1, 8)).pin_memory()
     pin_a = torch.from_numpy(ao.view(np.float32).reshape(-1, 8)).pin_memory()
     out_c = torch.empty((n_c, 4), dtype=torch.float32).pin_memory()
     out_a = torch.empty((n_a, 4), dtype=torch.float32).pin_memory()
     np_c, np_a = pin_c.numpy().view(closest.dtype).reshape(-1), pin_a.numpy().view(ao.dtype).reshape(-1)
     np_oc, np_oa = out_c.numpy().view(HIT).reshape(-1), out_a.numpy().view(HIT).reshape(-1)
-    # host wall time per step, median of up to 10 steps (host-side jitter in the pinned
-    # copies makes single steps vary by ~10 %)
     e2e_steps = max(3, min(args.steps, 10))
     vg.closest_hit(np_c, bvh, out=np_oc)
     vg.any_hit(np_a, bvh, out=np_oa)
     replicas.barrier()
-    e2e_times = []
+    e2e_c, e2e_both = [], []
     for _ in range(e2e_steps):
         t0 = time.perf_counter()
         vg.closest_hit(np_c, bvh, out=np_oc)
+        t1 = time.perf_counter()
         vg.any_hit(np_a, bvh, out=np_oa)
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = replicas.reduce_over_ranks(statistics.median(e2e_times), "max", dev)
-    e2e_value = world * rays_per_step / e2e_s / 1e6
+        e2e_c.append(t1 - t0)
+        e2e_both.append(time.perf_counter() - t0)
+    e2e_s = replicas.reduce_over_ranks(statistics.median(e2e_c), "max", dev)
+    e2e_value = world * n_c / e2e_s / 1e6
+    e2e_both_s = replicas.reduce_over_ranks(statistics.median(e2e_both), "max", dev)
     # the host path must give the device path's answers
-    same = bool((np_oc.view(np.uint8) == h_closest.cpu().numpy().view(np.uint8).reshape(-1)).all())
+    same = bool((np_oc.view(np.uint8) == h_closest.cpu().numpy().view(np.uint8).reshape(-1)).all() and
+                (np_oa.view(np.uint8) == h_ao.cpu().numpy().view(np.uint8).reshape(-1)).all())
 
-    # roofline of the dominant kernel (per launch)
+    # roofline of the dominant kernel of the step (closest hit's traversal kernel), per
+    # launch: the rays x B_ray over the kernel's own CUDA-event duration
     peak, peak_kind = measured_hbm_peak()
     per = {}
-    for name, ts, n, nn, nt in (("closest", t_closest, n_c, N_NODE_CLOSEST, N_TRI_CLOSEST),
-                                ("any", t_any, n_a, N_NODE_AO, N_TRI_AO)):
-        ms = statistics.mean(ts)
-        rec = {"ms_per_launch": round(ms, 4), "rays": n, "mrays_s": round(n / (ms * 1e-3) / 1e6, 2)}
-        if nn is not None:
-            algo = n * b_ray(nn, nt)
-            rec["algorithmic_bytes"] = int(algo)
-            rec["achieved_gbs"] = round(algo / (ms * 1e-3) / 1e9, 1)
-        per[name] = rec
-    dom = max(per, key=lambda k: per[k]["ms_per_launch"] * 1)
-    d = per[dom]
-    roofline = {"bound": "hbm", "kernel": (f"trace_rays_permuted<{1 if dom == 'any' else 0}, 0>" if args.trace_flags & 1 else
-                           f"trace_rays<{1 if dom == 'any' else 0}, 0>"),
-                "achieved": d.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
-                "frac": round(d["achieved_gbs"] / peak, 4) if d.get("achieved_gbs") else None,
-                "traffic": ((TRAFFIC_ANY if dom == "any" else TRAFFIC_CLOSEST)
-                            if (args.grid, args.origins, args.trace_flags) == (GRID, ORIGINS, 1) else None),
+    for name, kms, qms, n, nn, nt in (("closest", closest_kernel_ms, ms_per_step, n_c, N_NODE_CLOSEST, N_TRI_CLOSEST),
+                                      ("any", any_kernel_ms, any_ms, n_a, N_NODE_AO, N_TRI_AO)):
+        ms = statistics.mean(kms) if kms else qms
+        algo = n * b_ray(nn, nt)
+        per[name] = {"kernel_ms_per_launch": round(ms, 4), "query_ms": round(qms, 4), "rays": n,
+                     "mrays_s": round(n / (qms * 1e-3) / 1e6, 2), "kernel_mrays_s": round(n / (ms * 1e-3) / 1e6, 2),
+                     "algorithmic_bytes": int(algo), "achieved_gbs": round(algo / (ms * 1e-3) / 1e9, 1),
+                     "launches_timed": len(kms)}
+    d = per["closest"]
+    default_cfg = (args.grid, args.origins, args.trace_flags) == (GRID, ORIGINS, 1)
+    roofline = {"bound": "hbm", "kernel": ("trace_rays_permuted<0, 0>" if args.trace_flags & 1 else "trace_rays<0, 0>"),
+                "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": round(d["achieved_gbs"] / peak, 4),
+                "traffic": TRAFFIC_CLOSEST if default_cfg else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, full-size capture",
-                "peak_source": f"{peak_kind} hbm_gbs"}
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "b_ray": round(b_ray(N_NODE_CLOSEST, N_TRI_CLOSEST), 1),
+                "timing": "CUDA events around the traversal kernel on its stream, mean over the timed launches",
+                "limiter": "latency of dependent node fetches under divergence (ncu: DRAM ~10 % of peak)"}
     # the pure-I/O floor (48 B per ray: the ray in, the hit out) and the DRAM bandwidth
     # the launch actually drew (its ncu traffic over its event time)
-    io_gbs = d["rays"] * 48 / (d["ms_per_launch"] * 1e-3) / 1e9
+    io_gbs = d["rays"] * 48 / (d["kernel_ms_per_launch"] * 1e-3) / 1e9
     roofline["io_floor"] = {"bytes_per_ray": 48, "achieved_gbs": round(io_gbs, 1), "frac": round(io_gbs / peak, 4)}
     if roofline["traffic"]:
-        roofline["dram_gbs"] = round(roofline["traffic"] / (d["ms_per_launch"] * 1e-3) / 1e9, 1)
+        roofline["dram_gbs"] = round(roofline["traffic"] / (d["kernel_ms_per_launch"] * 1e-3) / 1e9, 1)
 
     # the same rays through the PLOC tree (a higher-quality GPU build; the workload's
     # builder is the LBVH, so this is reported beside the line's value, not as it)
@@ -526,60 +717,93 @@ def run_ours(args):
         b1.record(stream)
         torch.cuda.synchronize()
         p_build = b0.elapsed_time(b1)
-        pev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
         saved, bvh = bvh, pbvh
         for _ in range(max(3, args.warmup)):
-            step()
+            vg.closest_hit(d_closest, bvh, out=h_closest)
+            vg.any_hit(d_ao, bvh, out=h_ao)
         torch.cuda.synchronize()
-        for k in range(args.steps):
-            step(pev[k])
-        torch.cuda.synchronize()
+        pts = []
+        for fn in (lambda: vg.closest_hit(d_closest, bvh, out=h_closest), lambda: vg.any_hit(d_ao, bvh, out=h_ao)):
+            start.record(stream)
+            for _ in range(args.steps):
+                fn()
+            stop.record(stream)
+            torch.cuda.synchronize()
+            pts.append(start.elapsed_time(stop) / args.steps)
         ctx.synchronize()
-        pc = statistics.mean(e[0].elapsed_time(e[1]) for e in pev)
-        pa = statistics.mean(e[1].elapsed_time(e[2]) for e in pev)
+        pc, pa = pts
         alt = {"builder": "ploc", "build_ms": round(p_build, 3),
-               "value": round(rays_per_step / ((pc + pa) * 1e-3) / 1e6, 2),
                "closest_mrays_s": round(n_c / (pc * 1e-3) / 1e6, 2), "any_mrays_s": round(n_a / (pa * 1e-3) / 1e6, 2),
+               "closest_plus_anyhit_mrays_s": round(rays_per_step / ((pc + pa) * 1e-3) / 1e6, 2),
                "note": "same rays and hits (ties aside) through a PLOC tree; not the workload's LBVH"}
         bvh = saved
         del pbvh
 
+    cpu_legs = rank == 0 and world == 1 and not args.no_cpu_baseline
+    # visionaray's own GPU kernels (oracle/_ref/vsnray_ref_gpu.cubin, device code built
+    # from its headers) on the same GPU, tree and rays, and its path tracer on the box
+    # frame at 16 spp: a baseline beside the line, outside its timed region
+    reference_gpu = None
+    if cpu_legs and not args.no_reference_gpu:
+        from oracle import bench_reference_gpu, ref_gpu
+        if ref_gpu.available():
+            rg = ref_gpu.ReferenceGPU(local)
+            reference_gpu = {"traversal": bench_reference_gpu.traversal(rg, ctx, d_tris, bvh, d_closest, d_ao, 3)}
+            if args.pt_frames > 0:
+                reference_gpu["pathtrace"] = bench_reference_gpu.pathtrace(rg, ctx, 16, 1)
+            del rg
+        else:
+            reference_gpu = {"unavailable": "the reference's GPU kernels were not built (visionaray's headers were "
+                                            "absent where this tree was built)"}
     pt = None
     if args.pt_frames > 0:
-        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint, args.pt_builder, args.pt_scene)
+        pt = run_pathtrace(vg, ctx, args.pt_frames, args.pt_flags, rprint, args.pt_builder, args.pt_scene,
+                           cpu=cpu_legs)
 
     batched = None
     if args.batch_steps > 0:
         batched = run_batch(vg, ctx, args.batch_steps, args.batch_plain_steps, rprint, args.batch_scenes,
-                            args.batch_max_tris)
+                            args.batch_max_tris, cpu=cpu_legs)
 
     adjoint = None
     if args.adjoint_steps > 0:
-        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint, args.pt_flags, args.pt_builder)
+        adjoint = run_adjoint(ctx, args.adjoint_steps, rprint, args.pt_flags, args.pt_builder, cpu=cpu_legs)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        res = cpu_baseline(tris, closest, ao, rank_print=rprint, sample_every=8, repeats=2)
-        tb = min(res["times"])
-        base = {"value": round(res["rays"] / tb / 1e6, 3), "unit": UNIT, "cores": res["cores"],
-                "kind": res["kind"], "sample": res["sample"]}
+        res = cpu_baseline(tris, closest, ao, rank_print=rprint, sample_every=4, repeats=2)
+        base = {"value": round(res["closest_rays"] / min(res["closest_times"]) / 1e6, 3), "unit": UNIT,
+                "cores": res["cores"], "kind": res["kind"], "sample": res["sample"],
+                "any_hit_mrays_s": round(res["any_rays"] / min(res["any_times"]) / 1e6, 3)}
+        if res["kind"] == "port":
+            base["port_vs_reference"] = PORT_VS_REFERENCE
 
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD if (args.grid, args.origins) == (GRID, ORIGINS) else
                        f"REDUCED profiling case: heightfield {args.grid}x{args.grid}, {args.origins} origins",
-                       "rays_per_step": rays_per_step, "closest_rays": n_c, "anyhit_rays": n_a,
+                       "rays_per_step": n_c, "closest_rays": n_c, "anyhit_rays": n_a,
                        "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
                        "trace_flags": args.trace_flags, "trace_refill": args.trace_refill,
                        "warmup_steps_run": done, "builder": args.builder},
             "kernels": per, "roofline": roofline,
-            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(rays_per_step * 32),
-                    "d2h_bytes_per_step": int(rays_per_step * 16), "matches_device_path": same,
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_c * 32),
+                    "d2h_bytes_per_step": int(n_c * 16), "matches_device_path": same,
                     "steps": e2e_steps, "statistic": "median host wall time per step"},
+            "anyhit": {"rays": n_a, "ms_per_step": round(any_ms, 3),
+                       "mrays_s": round(world * n_a / (any_ms * 1e-3) / 1e6, 2)},
+            "closest_plus_anyhit": {
+                "rays_per_step": rays_per_step, "ms_per_step": round(ms_per_step + any_ms, 3),
+                "mrays_s": round(world * rays_per_step / ((ms_per_step + any_ms) * 1e-3) / 1e6, 2),
+                "e2e_mrays_s": round(world * rays_per_step / e2e_both_s / 1e6, 2)},
+            "build_inclusive": {"ms_per_step": round(bi_ms, 3), "steps": bi_steps,
+                                "mrays_s": round(world * rays_per_step / (bi_ms * 1e-3) / 1e6, 2),
+                                "step": "gbrt_bvh_build_lbvh (new tree) + closest hit + any hit"},
             "gpu_launches": int(gpu_launches), "clocks": clocks.summary(), "cpu_baseline": base,
-            "ploc_tree": alt, "pathtrace": pt, "batched_pathtrace": batched, "adjoint": adjoint}
+            "ploc_tree": alt, "reference_gpu": reference_gpu, "pathtrace": pt, "batched_pathtrace": batched,
+            "adjoint": adjoint}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -599,6 +823,8 @@ def main():
     p.add_argument("--pt-scene", choices=("box", "glossy"), default="box",
                    help="path-tracing scene: the matte box of the workload, or its materials-and-lights variant")
     p.add_argument("--no-ploc", action="store_true", help="skip the traversal through the PLOC tree")
+    p.add_argument("--no-reference-gpu", action="store_true",
+                   help="skip the comparison with visionaray's own GPU kernels")
     p.add_argument("--builder", choices=["lbvh", "ploc"], default="lbvh",
                    help="tree of the traversal leg: the LBVH (the workload's builder) or the PLOC build")
     p.add_argument("--pt-builder", choices=["lbvh", "ploc"], default="ploc",
@@ -623,9 +849,14 @@ def main():
         print("# warmup raised to 3 (timing rule)", file=sys.stderr)
         args.warmup = 3
     if args.impl == "reference":
+        from oracle import build as oracle_build
+        oracle_build.build()
         return run_reference(args)
     from visionaray_gb300 import build
     build.build()
+    if not args.no_cpu_baseline:
+        from oracle import build as oracle_build
+        oracle_build.build()   # the CPU-baseline leg's checker build
     return run_ours(args)
 
 

@@ -39,6 +39,75 @@ def timed(fn, reps):
     return statistics.median(out)
 
 
+def traversal(ref, ctx, d_tris, bvh, d_c, d_a, reps):
+    """visionaray's closest_hit / any_hit kernels (best of 64/128/256-thread blocks) and
+    the product's queries on the same tree (the product's LBVH export, byte-identical to
+    the reference GPU builder's) and rays."""
+    import torch
+
+    import visionaray_gb300 as vg
+    from visionaray_gb300.types import NO_HIT
+    n_c, n_a = d_c.shape[0], d_a.shape[0]
+    tree = ref.tree(d_tris, bvh)
+    h_c = torch.empty((n_c, 4), dtype=torch.float32, device=d_c.device)
+    h_a = torch.empty((n_a, 4), dtype=torch.float32, device=d_c.device)
+    r_c, r_a = torch.empty_like(h_c), torch.empty_like(h_a)
+    ours_c = timed(lambda: vg.closest_hit(d_c, bvh, out=h_c), reps)
+    ours_a = timed(lambda: vg.any_hit(d_a, bvh, out=h_a), reps)
+    ref_c, ref_a = {}, {}
+    for block in (64, 128, 256):
+        ref_c[block] = timed(lambda: ref.trace(tree, d_c, r_c, any_hit=False, block=block), reps)
+        ref_a[block] = timed(lambda: ref.trace(tree, d_a, r_a, any_hit=True, block=block), reps)
+    bc, ba = min(ref_c, key=ref_c.get), min(ref_a, key=ref_a.get)
+    ctx.synchronize()
+    hc, rc = vg.hits_to_numpy(h_c), vg.hits_to_numpy(r_c)
+    ha, ra = vg.hits_to_numpy(h_a), vg.hits_to_numpy(r_a)
+    hit_o, hit_r = hc["prim_id"] != NO_HIT, rc["prim_id"] != NO_HIT
+    return {"reps": reps, "tree_height": bvh.counts[2],
+            "ours": {"closest_ms": round(ours_c, 3), "any_ms": round(ours_a, 3),
+                     "closest_mrays_s": round(n_c / (ours_c * 1e-3) / 1e6, 1),
+                     "any_mrays_s": round(n_a / (ours_a * 1e-3) / 1e6, 1)},
+            "reference_gpu": {"closest_ms": round(ref_c[bc], 3), "any_ms": round(ref_a[ba], 3),
+                              "closest_block": bc, "any_block": ba,
+                              "closest_mrays_s": round(n_c / (ref_c[bc] * 1e-3) / 1e6, 1),
+                              "any_mrays_s": round(n_a / (ref_a[ba] * 1e-3) / 1e6, 1)},
+            "closest_speedup": round(ref_c[bc] / ours_c, 2), "any_speedup": round(ref_a[ba] / ours_a, 2),
+            "agreement": {"closest_prim_equal": float((hc["prim_id"] == rc["prim_id"]).mean()),
+                          "closest_hit_flag_equal": float((hit_o == hit_r).mean()),
+                          "ao_occlusion_equal": float(((ha["prim_id"] != NO_HIT) == (ra["prim_id"] != NO_HIT)).mean())}}
+
+
+def pathtrace(ref, ctx, spp, reps, builder="lbvh"):
+    """visionaray's pathtracing::kernel (one thread per pixel, 16x16 blocks) and the
+    product's frame on the box scene at 1920x1080, depth 8, through the same tree."""
+    import torch
+
+    import bench
+    import visionaray_gb300 as vg
+    from visionaray_gb300 import scenes
+    tris, mats, lights = scenes.box_scene()
+    d_tris = vg.as_device_bytes(tris, ctx.device)
+    make = vg.ploc_builder if builder == "ploc" else vg.lbvh_builder
+    bvh = make(ctx).build(d_tris)
+    scene = vg.PTScene(bvh, mats, lights)
+    cam = scenes.box_camera()
+    params = scenes.pt_params(bench.PT_WIDTH, bench.PT_HEIGHT, spp, num_bounces=bench.PT_BOUNCES)
+    img_o = torch.zeros((bench.PT_HEIGHT, bench.PT_WIDTH, 4), dtype=torch.float32, device=d_tris.device)
+    ms_o = timed(lambda: vg.pathtrace_frame(scene, cam, params, accum=img_o), reps)
+    rscene = ref.pt_scene(ref.tree(d_tris, bvh), mats, lights)
+    img_r = torch.zeros_like(img_o)
+    ms_r = timed(lambda: ref.pathtrace(rscene, cam, params, img_r), reps)
+    ctx.synchronize()
+    samples = bench.PT_WIDTH * bench.PT_HEIGHT * spp
+    a, b = img_o[..., :3].double(), img_r[..., :3].double()
+    return {"workload": bench.PT_WORKLOAD.replace("64 spp", f"{spp} spp"), "builder": builder,
+            "ours_ms": round(ms_o, 2), "reference_gpu_ms": round(ms_r, 2),
+            "ours_msamples_s": round(samples / (ms_o * 1e-3) / 1e6, 1),
+            "reference_gpu_msamples_s": round(samples / (ms_r * 1e-3) / 1e6, 1),
+            "speedup": round(ms_r / ms_o, 2),
+            "image_mean": [round(float(a.mean()), 5), round(float(b.mean()), 5)]}
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--reps", type=int, default=5)
@@ -51,80 +120,23 @@ def main():
 
     import bench
     import visionaray_gb300 as vg
+    from oracle import build as oracle_build
     from oracle import ref_gpu
     from visionaray_gb300 import build, scenes
-    from visionaray_gb300.types import NO_HIT
 
     build.build()
+    oracle_build.build()
     ref = ref_gpu.ReferenceGPU(0)
     ctx = vg.default_context(0)
     ctx.set_trace_flags(ctx.TRACE_SORT_RAYS)
-
     tris, closest, ao = bench.workload(print, grid=args.grid, origins=args.origins)
     d_tris = vg.as_device_bytes(tris)
     bvh = vg.lbvh_builder(ctx).build(d_tris)
-    tree = ref.tree(d_tris, bvh)
-    d_c, d_a = vg.device_rays(closest), vg.device_rays(ao)
-    h_c = torch.empty((len(closest), 4), dtype=torch.float32, device="cuda:0")
-    h_a = torch.empty((len(ao), 4), dtype=torch.float32, device="cuda:0")
-    r_c, r_a = torch.empty_like(h_c), torch.empty_like(h_a)
-
-    res = {"workload": bench.WORKLOAD, "reps": args.reps}
-    ours_c = timed(lambda: vg.closest_hit(d_c, bvh, out=h_c), args.reps)
-    ours_a = timed(lambda: vg.any_hit(d_a, bvh, out=h_a), args.reps)
-    ref_c, ref_a = {}, {}
-    for block in (64, 128, 256):
-        ref_c[block] = timed(lambda: ref.trace(tree, d_c, r_c, any_hit=False, block=block), args.reps)
-        ref_a[block] = timed(lambda: ref.trace(tree, d_a, r_a, any_hit=True, block=block), args.reps)
-    bc, ba = min(ref_c, key=ref_c.get), min(ref_a, key=ref_a.get)
-    ctx.synchronize()
-    hc, rc = vg.hits_to_numpy(h_c), vg.hits_to_numpy(r_c)
-    ha, ra = vg.hits_to_numpy(h_a), vg.hits_to_numpy(r_a)
-    n_rays = len(closest) + len(ao)
-    res["ours"] = {"closest_ms": round(ours_c, 3), "any_ms": round(ours_a, 3),
-                   "mrays_s": round(n_rays / ((ours_c + ours_a) * 1e-3) / 1e6, 1),
-                   "closest_mrays_s": round(len(closest) / (ours_c * 1e-3) / 1e6, 1),
-                   "any_mrays_s": round(len(ao) / (ours_a * 1e-3) / 1e6, 1)}
-    res["reference_gpu"] = {"closest_ms": round(ref_c[bc], 3), "any_ms": round(ref_a[ba], 3),
-                            "closest_block": bc, "any_block": ba,
-                            "mrays_s": round(n_rays / ((ref_c[bc] + ref_a[ba]) * 1e-3) / 1e6, 1),
-                            "closest_mrays_s": round(len(closest) / (ref_c[bc] * 1e-3) / 1e6, 1),
-                            "any_mrays_s": round(len(ao) / (ref_a[ba] * 1e-3) / 1e6, 1),
-                            "all_blocks_ms": {"closest": {k: round(v, 3) for k, v in ref_c.items()},
-                                              "any": {k: round(v, 3) for k, v in ref_a.items()}}}
-    res["traversal_speedup"] = round((ref_c[bc] + ref_a[ba]) / (ours_c + ours_a), 2)
-    hit_o, hit_r = hc["prim_id"] != NO_HIT, rc["prim_id"] != NO_HIT
-    res["agreement"] = {"closest_prim_equal": float((hc["prim_id"] == rc["prim_id"]).mean()),
-                        "closest_hit_flag_equal": float((hit_o == hit_r).mean()),
-                        "ao_occlusion_equal": float(((ha["prim_id"] != NO_HIT) == (ra["prim_id"] != NO_HIT)).mean())}
-    res["tree_height"] = bvh.counts[2]
-    del d_c, d_a, h_c, h_a, r_c, r_a, tree, bvh, d_tris
+    res = {"workload": bench.WORKLOAD, "traversal": traversal(ref, ctx, d_tris, bvh, vg.device_rays(closest),
+                                                               vg.device_rays(ao), args.reps)}
+    del bvh, d_tris
     torch.cuda.empty_cache()
-
-    # path tracing: the box scene
-    tris, mats, lights = scenes.box_scene()
-    d_tris = vg.as_device_bytes(tris)
-    bvh = vg.lbvh_builder(ctx).build(d_tris)
-    scene = vg.PTScene(bvh, mats, lights)
-    cam = scenes.box_camera()
-    params = scenes.pt_params(bench.PT_WIDTH, bench.PT_HEIGHT, args.pt_spp, num_bounces=bench.PT_BOUNCES)
-    img_o = torch.zeros((bench.PT_HEIGHT, bench.PT_WIDTH, 4), dtype=torch.float32, device="cuda:0")
-    ms_o = timed(lambda: vg.pathtrace_frame(scene, cam, params, accum=img_o), max(1, args.reps // 2))
-    rscene = ref.pt_scene(ref.tree(d_tris, bvh), mats, lights)
-    img_r = torch.zeros_like(img_o)
-    ms_r = timed(lambda: ref.pathtrace(rscene, cam, params, img_r), max(1, args.reps // 2))
-    ctx.synchronize()
-    samples = bench.PT_WIDTH * bench.PT_HEIGHT * args.pt_spp
-    a, b = img_o[..., :3].double(), img_r[..., :3].double()
-    res["pathtrace"] = {"workload": bench.PT_WORKLOAD.replace("64 spp", f"{args.pt_spp} spp"),
-                        "ours_ms": round(ms_o, 2), "reference_gpu_ms": round(ms_r, 2),
-                        "ours_msamples_s": round(samples / (ms_o * 1e-3) / 1e6, 1),
-                        "reference_gpu_msamples_s": round(samples / (ms_r * 1e-3) / 1e6, 1),
-                        "speedup": round(ms_r / ms_o, 2),
-                        "image_mean": [round(float(a.mean()), 5), round(float(b.mean()), 5)],
-                        "rmse": float(torch.sqrt(((a - b) ** 2).mean()))}
-    del scene, rscene, bvh, d_tris
-    torch.cuda.empty_cache()
+    res["pathtrace"] = pathtrace(ref, ctx, args.pt_spp, max(1, args.reps // 2))
 
     # path tracing with every material kind and generic lights: the box scene's 256
     # blobs cycling matte, plastic, mirror, plastic, glass, plastic walls, lit by
@@ -134,9 +146,10 @@ def main():
     d_tris = vg.as_device_bytes(tris)
     bvh = vg.lbvh_builder(ctx).build(d_tris)
     scene = vg.PTScene(bvh, mats, lights)
+    cam = scenes.box_camera()
     spp = max(1, args.pt_spp // 4)
     params = scenes.pt_params(bench.PT_WIDTH, bench.PT_HEIGHT, spp, num_bounces=bench.PT_BOUNCES)
-    img_o.zero_()
+    img_o = torch.zeros((bench.PT_HEIGHT, bench.PT_WIDTH, 4), dtype=torch.float32, device="cuda:0")
     ms_o = timed(lambda: vg.pathtrace_frame(scene, cam, params, accum=img_o), max(1, args.reps // 2))
     rscene = ref.pt_scene(ref.tree(d_tris, bvh), mats, lights)
     img_r = torch.zeros_like(img_o)

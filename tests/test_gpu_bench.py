@@ -1,7 +1,8 @@
 """bench.py's JSON line on a reduced workload: every key of the benchmark contract is
 present and consistent (value = rays per step / time, e2e on the host path giving the
-device path's hits, a roofline fraction, clock samples taken inside the timed region,
-counted kernel launches)."""
+device path's hits, a roofline fraction from the traversal kernel's own event time,
+clock samples taken inside the timed region, counted kernel launches) and the keys of
+the legs measured beside it."""
 import json
 import os
 import subprocess
@@ -43,4 +44,14 @@ def test_bench_line_has_the_contract_keys():
     assert d["clocks"]["samples"] >= 1
     assert d["pathtrace"]["msamples_s"] > 0 and d["batched_pathtrace"]["images_bit_identical"] is True
     assert d["adjoint"]["bwd_ms"] > 0
+    # the closest-hit kernel's own CUDA-event time: one per timed step, below the query's
+    k = d["kernels"]["closest"]
+    assert k["launches_timed"] == 3 and 0 < k["kernel_ms_per_launch"] <= k["query_ms"] * 1.01
+    assert d["anyhit"]["mrays_s"] > 0 and d["build_inclusive"]["ms_per_step"] > d["ms_per_step"]
+    assert d["closest_plus_anyhit"]["rays_per_step"] == rays + d["config"]["anyhit_rays"]
+    b = d["batched_pathtrace"]
+    assert b["plain_preallocated"]["images_bit_identical"] is True and b["roofline"]["frac"] > 0
+    assert d["pathtrace"]["roofline"]["b_sample"] > 0
+    assert d["adjoint"]["roofline"]["forward"]["bound"] == "l2"
+    assert set(d["adjoint"]["albedo_error_end"]) == set(d["adjoint"]["albedo_error_start"])
 
