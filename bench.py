@@ -60,26 +60,30 @@ def b_ray(n_node, n_tri):
     return 32 + 16 + n_node * 32 + n_tri * 48
 
 
-def measured_l2_copy_gbs(device):
-    """L2 bandwidth of a device-to-device copy whose source and destination (24 MB
-    each) stay resident in the 129 MB L2: read + write bytes over the CUDA-event time,
-    best of 5 rounds of 50 copies (measured here: no L2 peak is recorded for this GPU)."""
+def measured_l2_gbs(device):
+    """L2 bandwidth measured here (no L2 peak is recorded for this GPU): the best of a
+    device-to-device copy (read + write), an in-place add (read + write) and a sum
+    (read) over buffers that stay resident in the 129 MB L2 (16 and 32 MB), in bytes
+    moved over the CUDA-event time, best of 5 rounds of 50 operations each."""
     import torch
-    n = 6 * 1024 * 1024
-    a = torch.ones(n, dtype=torch.float32, device=device)
-    b = torch.empty_like(a)
-    for _ in range(20):
-        b.copy_(a)
     best = 0.0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(5):
-        e0.record()
-        for _ in range(50):
-            b.copy_(a)
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, 2 * 4 * n * 50 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
-    del a, b
+    for mb in (16, 32):
+        n = mb * 1024 * 1024 // 4
+        a = torch.ones(n, dtype=torch.float32, device=device)
+        b = torch.empty_like(a)
+        for name, op, moved in (("copy", lambda: b.copy_(a), 8 * n), ("add", lambda: a.add_(1.0), 8 * n),
+                                ("sum", lambda: a.sum(), 4 * n)):
+            for _ in range(20):
+                op()
+            for _ in range(5):
+                e0.record()
+                for _ in range(50):
+                    op()
+                e1.record()
+                torch.cuda.synchronize()
+                best = max(best, moved * 50 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        del a, b
     return round(best, 1)
 
 
@@ -516,12 +520,12 @@ def run_adjoint(ctx, steps, rprint, flags=0, builder="ploc", cpu=False):
             "gradient_bias": inverse.gradient_bias(ctx=ctx, builder=builder)}
     # the 4,094-triangle scene (~200 KB of tree and triangles) is L2-resident: its
     # traversal bytes are served by L2, so the roofline is L2's (measured copy peak)
-    l2 = measured_l2_copy_gbs(f"cuda:{ctx.device}")
+    l2 = measured_l2_gbs(f"cuda:{ctx.device}")
     samples = 512 * 512 * 16
     res["roofline"] = {
-        "forward": roofline_of(samples, r["fwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 copy measured in this run",
+        "forward": roofline_of(samples, r["fwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 measured in this run (best of copy, in-place add, sum)",
                                "forward frame (gbrt_pathtrace_forward)", bound="l2"),
-        "backward": roofline_of(samples, r["bwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 copy measured in this run",
+        "backward": roofline_of(samples, r["bwd_ms"] * 1e-3, B_SAMPLE_INVERSE, l2, "L2 measured in this run (best of copy, in-place add, sum)",
                                 "path-replay kernel (replays the forward's segments)", bound="l2")}
     if cpu:
         from visionaray_gb300 import scenes
