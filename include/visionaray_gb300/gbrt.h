@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GBRT_ABI_VERSION 2
+#define GBRT_ABI_VERSION 3
 
 typedef enum gbrt_status
 {
@@ -88,6 +88,7 @@ typedef struct gbrt_bvh_node
 
 typedef struct gbrt_context gbrt_context;
 typedef struct gbrt_bvh     gbrt_bvh;
+typedef struct gbrt_tlas    gbrt_tlas;
 
 /* ------------------------------------------------------------------------------ */
 /* Context                                                                         */
@@ -126,6 +127,11 @@ int         gbrt_abi_version(void);
  * context with the flag traverse those.  Implies the 4-wide collapse.  Path tracing
  * keeps the node pairs (or the 4-wide nodes).                                         */
 #define GBRT_TRACE_COMPRESSED_NODES 8u
+/* With this flag set when gbrt_bvh_build_lbvh runs, the tree is also collapsed into
+ * 8-wide nodes (256 bytes, eight children's boxes per fetch; bvh_collapser's BVH8,
+ * detail/bvh/collapse.h:19-169), and ray queries on a context with the flag traverse
+ * those (it takes precedence over the 4-wide flags).                                */
+#define GBRT_TRACE_WIDE8_NODES 16u
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags);
 
 /* Persistent traversal: a warp refills once at least min_idle_lanes (1..32, default 8)
@@ -398,6 +404,21 @@ gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh const* bvh,
                                         gbrt_material const* h_materials, uint32_t num_materials,
                                         gbrt_light const* h_lights, uint32_t num_lights,
                                         gbrt_pt_scene** out);
+
+/* make_kernel_params over an index_bvh<index_bvh_inst_t<P>> (bvh.h:678-782: the
+ * primitives of a two-level tree) for pathtracing::kernel: a scene whose rays are
+ * traced through the instances of a gbrt_tlas (intersect.inl:362-394), each hit shaded
+ * with its instance's triangle in world space (the instance's transform applied to the
+ * triangle's edges) and material slot h_inst_geom[instance] + the triangle's geom_id
+ * (h_inst_geom: one host entry per instance).  Lights as for
+ * gbrt_pt_scene_create_lights, in world space.  gbrt_pathtrace_frame and
+ * gbrt_pathtrace_forward render it (wavefront scheduling only: not with
+ * GBRT_PT_MEGAKERNEL or GBRT_PT_SORT_QUEUES); gbrt_pathtrace_backward takes a scene
+ * over a single tree.  The tlas and its trees must outlive the scene.                */
+gbrt_status gbrt_pt_scene_create_instanced(gbrt_context* ctx, gbrt_tlas const* tlas,
+                                           gbrt_material const* h_materials, uint32_t num_materials,
+                                           gbrt_light const* h_lights, uint32_t num_lights,
+                                           uint32_t const* h_inst_geom, gbrt_pt_scene** out);
 gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene);
 
 /* An environment light in place of the constant ambient light: the kernel's amb_light
@@ -497,7 +518,6 @@ typedef struct gbrt_hit_inst
     uint32_t reserved[2];
 } gbrt_hit_inst;
 
-typedef struct gbrt_tlas gbrt_tlas;
 
 /* Builds the top-level tree over h_instances (host array; the bottom-level trees must
  * outlive the tlas): instance bounds as get_bounds(instance) computes them
@@ -562,11 +582,17 @@ typedef struct gbrt_batch_launch
     uint32_t block;  /* threads per block: 128, 256 or 512                         */
     uint32_t tile;   /* pixels a warp takes from the work queue per grab: 32 or 64  */
     uint32_t stack;  /* traversal stack entries: 16, 24, 32 or 64 (a tree taller
-                        than this sets GBRT_ERR_STACK_OVERFLOW)                     */
+                        than this sets GBRT_ERR_STACK_OVERFLOW); width 2 only       */
     uint32_t order;  /* GBRT_BATCH_ORDER_*                                          */
+    uint32_t width;  /* BVH width: 2 (node pairs), 4 or 8 (each frame first collapses
+                        the last build's trees, bvh_collapser's BVH4/8; hits equal
+                        the pairs' except equal-t ties)                             */
+    uint32_t sort;   /* 1: rays sorted -- each frame first traces every pixel's first
+                        primary ray and takes pixels in the order of (scene, Morton
+                        cell of that hit) instead of `order`; 0: off               */
 } gbrt_batch_launch;
 
-/* Sets / reads the launch shape (default {128, 32, 64, ROWS}).                      */
+/* Sets / reads the launch shape (default {128, 32, 64, ROWS, 2, 0}).                */
 gbrt_status gbrt_batch_set_launch(gbrt_batch* batch, gbrt_batch_launch const* launch);
 gbrt_status gbrt_batch_get_launch(gbrt_batch const* batch, gbrt_batch_launch* out);
 
@@ -579,7 +605,7 @@ gbrt_status gbrt_batch_height(gbrt_context* ctx, gbrt_batch const* batch, uint32
  * gbrt_pathtrace_frame, so scene s's image equals the one gbrt_pathtrace_frame
  * renders with its camera, params and lights).  d_images: RGBA32F, 16-byte aligned,
  * scene s at pixel offset sum_{t<s} width_t * height_t.  Enqueue only.              */
-gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch const* batch, float* d_images);
+gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch* batch, float* d_images);
 
 /* The lights of each scene of a batch (make_kernel_params' light list per scene,
  * pathtracing.inl:42-233 next-event estimation): h_lights (host, area / point / spot
@@ -593,15 +619,19 @@ gbrt_status gbrt_batch_set_lights(gbrt_context* ctx, gbrt_batch* batch, gbrt_lig
 
 /* gbrt_batch_build + gbrt_batch_pathtrace captured once into a CUDA graph and
  * replayed on the context stream on every call (re-captured when d_tris, d_images,
- * the frames or the launch shape change).                                          */
+ * the frames, the lights or the launch shape change); with width 4 or 8 the graph
+ * holds the collapse, with sorting the pixel order, so every replay redoes both.    */
 gbrt_status gbrt_batch_run_graph(gbrt_context* ctx, gbrt_batch* batch, gbrt_triangle const* d_tris,
                                  float* d_images);
 
 /* Autotuner: times gbrt_batch_pathtrace (after gbrt_batch_build and
- * gbrt_batch_set_frames) over every launch shape of the search space whose stack
- * holds the tallest tree, `reps` runs each after one warm-up run, and keeps the
- * fastest (also written to *best, with its time per frame in *best_ms; either may be
- * NULL).  Shapes whose run raised a status are skipped.  d_images is overwritten.   */
+ * gbrt_batch_set_frames) over the search space, `reps` runs each after one warm-up
+ * run, and keeps the fastest (also written to *best, with its time per frame in
+ * *best_ms; either may be NULL): first every block x tile x stack x order on the node
+ * pairs without sorting (stacks that hold the tallest tree), then, at the winner's
+ * block, tile and order, BVH width {2, 4, 8} x ray sorting {off, on} with each frame's
+ * collapse and sort timed in.  Shapes whose run raised a status are skipped.
+ * d_images is overwritten.                                                          */
 gbrt_status gbrt_batch_autotune(gbrt_context* ctx, gbrt_batch* batch, float* d_images, uint32_t reps,
                                 gbrt_batch_launch* best, float* best_ms);
 

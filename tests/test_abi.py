@@ -55,12 +55,12 @@ def test_python_signatures_cover_the_abi():
 
 def test_abi_version_and_struct_sizes():
     lib = runtime.load_library()
-    assert lib.gbrt_abi_version() == 2
+    assert lib.gbrt_abi_version() == 3
     assert types.TRIANGLE.itemsize == 44 and types.RAY.itemsize == 32
     assert types.HIT.itemsize == 16 and types.BVH_NODE.itemsize == 32
     assert types.MATERIAL.itemsize == 64 and types.AREA_LIGHT.itemsize == 60
     assert types.INSTANCE.itemsize == 56 and types.HIT_INST.itemsize == 32
-    assert types.LIGHT.itemsize == 108
+    assert types.LIGHT.itemsize == 108 and types.BATCH_LAUNCH.itemsize == 24
 
 
 def test_null_context_is_rejected_without_touching_the_gpu():

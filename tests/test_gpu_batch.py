@@ -137,6 +137,35 @@ def test_batch_pathtrace_bit_identical(batch_setup, plain, launch):
         assert got.tobytes() == plain[s].tobytes(), f"scene {s}: image differs (launch {launch})"
 
 
+@pytest.mark.parametrize("width,sort", [(2, 1), (4, 0), (4, 1), (8, 0), (8, 1)])
+def test_batch_widths_and_sorted_order(batch_setup, plain, width, sort):
+    """BVH width 4 and 8 (the arena's trees collapsed each frame) and the sorted pixel
+    order (pixels grouped by their first primary hit): every scene's image equals its
+    per-scene frame -- bit for bit through the node pairs; through the wide nodes the
+    triangles of a leaf are visited in another order, so a pixel whose path met an
+    equal-t tie may differ (the soups have none measurable: at most one pixel per scene
+    is allowed).  Directly and replayed from a graph."""
+    tris, offsets, cams, params, mats, d_tris, batch = batch_setup
+    batch.launch = (256, 32, 64, BATCH_ORDER_BLOCKS, width, sort)
+    assert (int(batch.launch["width"]), int(batch.launch["sort"])) == (width, sort)
+    for run in ("direct", "graph"):
+        images = batch.new_images()
+        images.fill_(-1.0)
+        if run == "direct":
+            batch.pathtrace(images)
+        else:
+            batch.run_graph(d_tris, images)
+        batch.ctx.synchronize()
+        for s in range(len(COUNTS)):
+            got = batch.image(images, s, params).cpu().numpy()
+            if width == 2:
+                assert got.tobytes() == plain[s].tobytes(), (run, s)
+            else:
+                differ = int((got != plain[s]).any(axis=2).sum())
+                assert differ <= 1, (run, s, differ)
+    batch.launch = (128, 32, 64, BATCH_ORDER_ROWS)
+
+
 def test_batch_graph_replay_and_recapture(batch_setup, plain):
     tris, offsets, cams, params, mats, d_tris, batch = batch_setup
     batch.launch = (128, 32, 64, BATCH_ORDER_ROWS)
@@ -170,7 +199,9 @@ def test_batch_autotune_picks_a_clean_shape(batch_setup, plain):
     best, ms = batch.autotune(images, reps=1)
     assert ms > 0.0
     assert int(best["stack"]) >= batch.height()
+    assert int(best["width"]) in (2, 4, 8) and int(best["sort"]) in (0, 1)
     assert tuple(int(x) for x in batch.launch) == tuple(int(x) for x in best)
+    batch.launch = tuple(int(x) for x in best)[:4]   # the node pairs, unsorted: bit for bit
     images = batch.pathtrace()
     batch.ctx.synchronize()
     for s in range(len(COUNTS)):

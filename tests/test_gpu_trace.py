@@ -228,6 +228,29 @@ def test_wide_and_binary_nodes_agree(oracle):
     assert ((wide_a["prim_id"] != NO_HIT) == (bin_a["prim_id"] != NO_HIT)).all()
 
 
+@pytest.mark.parametrize("sort", [0, 1])
+def test_eight_wide_nodes_agree(oracle, sort):
+    """The 8-wide collapse (bvh_collapser's BVH8) changes the traversal, not the
+    answers: closest hits as the node pairs' (equal-t ties aside) and every AO ray's
+    occlusion; a soup against the oracle's SAH tree."""
+    tris = scenes.heightfield(grid=256, seed=5)
+    closest, ao = scenes.surface_rays(tris, 1 << 16, seed=11)
+    ctx = vg.Context(0)
+    ctx.set_trace_flags(ctx.TRACE_WIDE8_NODES | sort)
+    bvh = vg.lbvh_builder(ctx).build(vg.as_device_bytes(tris))
+    w_c, w_a = trace(bvh, closest), trace(bvh, ao, any_hit=True)
+    ctx.set_trace_flags(sort)
+    bin_c, bin_a = trace(bvh, closest), trace(bvh, ao, any_hit=True)
+    compare_closest(w_c, bin_c, closest, tris, oracle)
+    assert ((w_a["prim_id"] != NO_HIT) == (bin_a["prim_id"] != NO_HIT)).all()
+    soup = scenes.soup(20000, seed=3)
+    rays = scenes.pinhole_rays(256, 256)
+    ctx.set_trace_flags(ctx.TRACE_WIDE8_NODES)
+    bvh2 = vg.lbvh_builder(ctx).build(vg.as_device_bytes(soup))
+    got = trace(bvh2, rays)
+    compare_closest(got, oracle.trace(oracle.build_sah(soup), soup, rays), rays, soup, oracle)
+
+
 @pytest.mark.parametrize("grid,sort", [(256, 0), (512, 1)])
 def test_compressed_nodes_agree(oracle, grid, sort):
     """The quantised 4-wide nodes (bvh_compressed_node<4> layout, boxes rounded outward)

@@ -21,10 +21,10 @@ LIB = os.path.join(PKG, "_lib")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "batch.cu", "batch_pt.cu", "instances.cu", "lbvh.cu", "noalloc.cu", "pathtrace.cu",
-              "ploc.cu", "radix_sort.cu", "traverse.cu"]
+CU_SOURCES = ["api.cu", "batch.cu", "batch_pt.cu", "batch_pt_wide.cu", "instances.cu", "lbvh.cu", "noalloc.cu",
+              "pathtrace.cu", "ploc.cu", "radix_sort.cu", "traverse.cu"]
 CU_HEADERS = ["device_math.cuh", "bvh_layout.cuh", "api_internal.h", "traverse_core.cuh", "lbvh_device.cuh",
-              "pt_shade.cuh"]
+              "pt_shade.cuh", "collapse.cuh", "batch_pt.cuh"]
 # host code of every unit keeps expressions unfused (-ffp-contract=off) so x86-64 and
 # AArch64 hosts compute the same camera bases and copies
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -32,7 +32,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-I" + os.path.join(ROOT, "include")] + ARCH
 # the path tracer's shading repeats the reference's float expressions operation for
 # operation: no fused multiply-add anywhere in its device code
-PER_FILE_FLAGS = {"pathtrace.cu": ["--fmad=false"], "batch_pt.cu": ["--fmad=false"]}
+PER_FILE_FLAGS = {"pathtrace.cu": ["--fmad=false"], "batch_pt.cu": ["--fmad=false"],
+                  "batch_pt_wide.cu": ["--fmad=false"]}
 
 LIBGBRT = os.path.join(LIB, "libgbrt.so")
 LIBSCENES = os.path.join(LIB, "libgbrt_scenes.so")

@@ -45,10 +45,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 void free_bvh_arrays(gbrt_bvh* b)
 {
-    cudaFree(b->nodes4);
-    b->nodes4 = nullptr;
-    cudaFree(b->nodes4q);
-    b->nodes4q = nullptr;
+    free_wide_nodes(b);
     cudaFree(b->nodes);
     cudaFree(b->tris);
     cudaFree(b->sorted_codes);
@@ -249,7 +246,8 @@ gbrt_status gbrt_context_destroy(gbrt_context* ctx)
 gbrt_status gbrt_context_set_trace_flags(gbrt_context* ctx, uint32_t flags)
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;
-    if (flags & ~(GBRT_TRACE_SORT_RAYS | GBRT_TRACE_WIDE_NODES | GBRT_TRACE_PERSISTENT | GBRT_TRACE_COMPRESSED_NODES))
+    if (flags & ~(GBRT_TRACE_SORT_RAYS | GBRT_TRACE_WIDE_NODES | GBRT_TRACE_PERSISTENT | GBRT_TRACE_COMPRESSED_NODES |
+                  GBRT_TRACE_WIDE8_NODES))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "set_trace_flags: unknown flag");
     ctx->trace_flags = flags;
     return GBRT_OK;

@@ -119,12 +119,47 @@ struct gbrt_bvh
     uint32_t num_nodes4 = 0;
     uint32_t leaf_max4 = 0;
     gbrt::bvh4q_node* nodes4q = nullptr;   // the same nodes quantised (GBRT_TRACE_COMPRESSED_NODES)
+    gbrt::bvh8_node* nodes8 = nullptr;     // 8-wide collapse (GBRT_TRACE_WIDE8_NODES)
+    uint32_t num_nodes8 = 0;
 };
+
+namespace gbrt {
+// Frees a tree's wide collapse (4-wide, quantised and 8-wide nodes).
+inline void free_wide_nodes(gbrt_bvh* b)
+{
+    cudaFree(b->nodes4);
+    b->nodes4 = nullptr;
+    b->num_nodes4 = 0;
+    cudaFree(b->nodes4q);
+    b->nodes4q = nullptr;
+    cudaFree(b->nodes8);
+    b->nodes8 = nullptr;
+    b->num_nodes8 = 0;
+}
+} // namespace gbrt
+
 
 // Many scenes built and traced as one arena (batch.cu, batch_pt.cu).  Scene s owns
 // the sorted primitives [offsets[s], offsets[s + 1]) and the inner node pairs
 // [inner_offsets[s], inner_offsets[s + 1]); its root is roots[s] (an inner index, ~leaf
 // for a one-triangle scene, INT32_MIN for an empty one).
+namespace gbrt {
+struct bvh_view;
+}
+
+struct gbrt_tlas
+{
+    int device = 0;
+    uint32_t num_instances = 0;
+    uint32_t num_inner = 0;
+    int32_t root = INT32_MIN;
+    gbrt::bvh2_node* nodes = nullptr;   // top-level node pairs, leaves ~instance
+    float4* records = nullptr;          // 3 float4 per instance: rows of A^-1 | trans_inv
+    float4* forward = nullptr;          // 3 float4 per instance: rows of A | translation
+    gbrt::bvh_view* views = nullptr;    // the instance's bottom-level tree
+    std::vector<gbrt_bvh const*> blas;  // the same trees, host side
+};
+
 struct gbrt_batch
 {
     int device = 0;
@@ -152,12 +187,29 @@ struct gbrt_batch
     uint32_t num_materials = 0;
     bool extended_materials = false;   // some material is a mirror, glass or plastic
     uint32_t* d_work = nullptr;     // persistent-kernel work counter
+    // per arena inner node: its leaf range (first, last) in triangle-array indices, for
+    // the wide collapse (written by every build)
+    int2* ranges = nullptr;
+    // W-wide collapse of the arena (launch.width 4 or 8; allocated on first use): room
+    // for wide_cap 8-wide nodes (scene s's root at node s), two level queues, the
+    // per-level counts and the node counter; the build generation it was made from
+    void* wide_nodes = nullptr;
+    int2* wide_queue[2] = { nullptr, nullptr };
+    uint32_t* wide_counts = nullptr;
+    uint32_t wide_cap = 0;
+    uint32_t collapsed_width = 0;
+    uint64_t build_gen = 0, collapsed_gen = 0;
+    // sorted pixel order (launch.sort; allocated on first use): keys, values and their
+    // alternates (4 x sort_capacity words) and the radix sort's scratch
+    uint32_t* sort_buf = nullptr;
+    void* sort_scratch = nullptr;
+    uint32_t sort_capacity = 0;
     // lights (gbrt_batch_set_lights): 4 float4 per light, scene s's lights at
     // [light_offsets[s], light_offsets[s + 1])
     float4* d_lights = nullptr;
     uint32_t* d_light_offsets = nullptr;
     uint32_t num_lights = 0;
-    gbrt_batch_launch launch = { 128, 32, 64, GBRT_BATCH_ORDER_ROWS };
+    gbrt_batch_launch launch = { 128, 32, 64, GBRT_BATCH_ORDER_ROWS, 2, 0 };
     // the captured build + frame
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -275,8 +327,18 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
 // batch.cu: the batched build, enqueued on `stream` (allocates nothing, does not
 // synchronise, so it can be captured).
 gbrt_status batch_build(gbrt_context* ctx, gbrt_batch* b, gbrt_triangle const* d_tris, cudaStream_t stream);
-// batch_pt.cu: the batched frame on `stream`.
-gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_images, cudaStream_t stream);
+// Levels of the arena's wide collapse (every tree is at most kStackSize - 1 deep).
+constexpr uint32_t kBatchCollapseLevels = kStackSize;
+// Allocates the wide collapse's nodes and queues (once; not during a capture).
+gbrt_status ensure_batch_wide(gbrt_context* ctx, gbrt_batch* b);
+// Collapses every scene's tree of the last build into width-wide nodes on `stream`
+// (allocates nothing, does not synchronise).
+gbrt_status batch_collapse(gbrt_context* ctx, gbrt_batch* b, uint32_t width, cudaStream_t s);
+// batch_pt.cu: the batched frame on `stream`, with what the launch shape needs before
+// it (the wide collapse, the pixel order); force_collapse re-collapses even when the
+// last build's collapse at this width is current.
+gbrt_status batch_frame_stage(gbrt_context* ctx, gbrt_batch* b, float* d_images, cudaStream_t stream,
+                              bool force_collapse);
 
 } // namespace gbrt
 

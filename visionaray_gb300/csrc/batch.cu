@@ -17,6 +17,7 @@
 // order, same topology and boxes, hence bit-identical hits.  No stage allocates or
 // synchronises: a build can be captured in a CUDA graph.
 
+#include "collapse.cuh"
 #include "lbvh_device.cuh"
 #include "traverse_core.cuh"
 
@@ -132,7 +133,8 @@ __global__ void __launch_bounds__(kBlock) batch_hierarchy(const uint32_t* __rest
                                                           const uint32_t* __restrict__ offsets,
                                                           const uint32_t* __restrict__ inner_offsets,
                                                           uint32_t num_scenes, uint32_t total_inner,
-                                                          bvh2_node* __restrict__ nodes, int* __restrict__ leaf_parent)
+                                                          bvh2_node* __restrict__ nodes, int* __restrict__ leaf_parent,
+                                                          int2* __restrict__ ranges)
 {
     uint32_t g = blockIdx.x * kBlock + threadIdx.x;
     if (g >= total_inner) return;
@@ -169,6 +171,18 @@ __global__ void __launch_bounds__(kBlock) batch_hierarchy(const uint32_t* __rest
     nodes[g].link.x = cl;
     nodes[g].link.y = cr;
     if (i == 0) nodes[g].link.w = -1;
+    ranges[g] = make_int2(base_leaf + first, base_leaf + last);
+}
+
+// Level 0 of the arena's wide collapse: scene s with an inner root gets wide node s.
+__global__ void __launch_bounds__(kBlock) batch_collapse_seed(const int32_t* __restrict__ roots, uint32_t num_scenes,
+                                                              int2* __restrict__ q, uint32_t* __restrict__ count,
+                                                              uint32_t* __restrict__ node_counter)
+{
+    uint32_t s = blockIdx.x * kBlock + threadIdx.x;
+    if (s == 0) *node_counter = num_scenes;
+    if (s >= num_scenes || roots[s] < 0) return;
+    q[atomicAdd(count, 1u)] = make_int2(roots[s], int(s));
 }
 
 // refit_and_emit over all segments: a leaf without a parent (a one-triangle scene) only
@@ -338,6 +352,13 @@ void free_batch(gbrt_batch* b)
     cudaFree(b->d_work);
     cudaFree(b->d_lights);
     cudaFree(b->d_light_offsets);
+    cudaFree(b->ranges);
+    cudaFree(b->wide_nodes);
+    cudaFree(b->wide_queue[0]);
+    cudaFree(b->wide_queue[1]);
+    cudaFree(b->wide_counts);
+    cudaFree(b->sort_buf);
+    cudaFree(b->sort_scratch);
 }
 
 } // namespace
@@ -387,12 +408,65 @@ gbrt_status batch_build(gbrt_context* ctx, gbrt_batch* b, gbrt_triangle const* d
         GBRT_CUDA(ctx, cudaMemsetAsync(b->nodes, 0, size_t(b->total_inner) * sizeof(bvh2_node), s));
         batch_hierarchy<<<blocks_for(b->total_inner), kBlock, 0, s>>>(b->sorted_codes, b->d_offsets, b->d_inner_offsets,
                                                                       b->num_scenes, b->total_inner, b->nodes,
-                                                                      leaf_parent);
+                                                                      leaf_parent, b->ranges);
         GBRT_LAUNCH_CHECK(ctx, "batch_hierarchy");
     }
     batch_refit<<<blocks_for(n), kBlock, 0, s>>>(d_tris, b->sorted_ids, n, b->total_inner, leaf_parent, b->nodes,
                                                  arrivals, b->tris, b->d_height, ctx->d_status);
     GBRT_LAUNCH_CHECK(ctx, "batch_refit");
+    ++b->build_gen;
+    return GBRT_OK;
+}
+
+gbrt_status ensure_batch_wide(gbrt_context* ctx, gbrt_batch* b)
+{
+    if (b->wide_nodes || b->total_inner == 0) return GBRT_OK;
+    // a scene of n triangles has at most 2n / (L + 1) wide nodes above leaves of L
+    uint64_t cap = b->num_scenes;
+    for (uint32_t s = 0; s < b->num_scenes; ++s)
+        cap += 2ull * (b->offsets[s + 1] - b->offsets[s]) / (kLeafMax4 + 1) + 2;
+    if (cap > (1ull << 31)) return fail(ctx, GBRT_ERR_TOO_LARGE, "batch: wide collapse too large");
+    GBRT_CUDA(ctx, cudaMalloc(&b->wide_nodes, size_t(cap) * sizeof(bvh8_node)));
+    GBRT_CUDA(ctx, cudaMalloc(&b->wide_queue[0], size_t(cap) * sizeof(int2)));
+    GBRT_CUDA(ctx, cudaMalloc(&b->wide_queue[1], size_t(cap) * sizeof(int2)));
+    GBRT_CUDA(ctx, cudaMalloc(&b->wide_counts, (kBatchCollapseLevels + 2) * sizeof(uint32_t)));
+    b->wide_cap = uint32_t(cap);
+    return GBRT_OK;
+}
+
+gbrt_status batch_collapse(gbrt_context* ctx, gbrt_batch* b, uint32_t width, cudaStream_t s)
+{
+    if (b->total_inner == 0)
+    {
+        b->collapsed_width = width;
+        b->collapsed_gen = b->build_gen;
+        return GBRT_OK;
+    }
+    if (!b->wide_nodes) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch: wide nodes not allocated");
+    uint32_t* counts = b->wide_counts;                    // [level], node counter last
+    uint32_t* node_counter = counts + kBatchCollapseLevels + 1;
+    GBRT_CUDA(ctx, cudaMemsetAsync(counts, 0, (kBatchCollapseLevels + 2) * sizeof(uint32_t), s));
+    batch_collapse_seed<<<blocks_for(b->num_scenes), kBlock, 0, s>>>(b->d_roots, b->num_scenes, b->wide_queue[0],
+                                                                     counts, node_counter);
+    GBRT_LAUNCH_CHECK(ctx, "batch_collapse_seed");
+    // every level on a fixed grid (the kernel walks its queue): no host synchronisation
+    const uint32_t grid = uint32_t(ctx->num_sms) * 8u;
+    for (uint32_t level = 0; level < kBatchCollapseLevels; ++level)
+    {
+        int2* q_in = b->wide_queue[level & 1];
+        int2* q_out = b->wide_queue[(level + 1) & 1];
+        if (width == 4)
+            collapse_wide<4><<<grid, 256, 0, s>>>(b->nodes, b->ranges, q_in, counts + level, q_out, counts + level + 1,
+                                                  static_cast<bvh4_node*>(b->wide_nodes), node_counter, b->wide_cap,
+                                                  kLeafMax4, int(b->total_inner), ctx->d_status);
+        else
+            collapse_wide<8><<<grid, 256, 0, s>>>(b->nodes, b->ranges, q_in, counts + level, q_out, counts + level + 1,
+                                                  static_cast<bvh8_node*>(b->wide_nodes), node_counter, b->wide_cap,
+                                                  kLeafMax4, int(b->total_inner), ctx->d_status);
+        GBRT_LAUNCH_CHECK(ctx, "collapse_wide");
+    }
+    b->collapsed_width = width;
+    b->collapsed_gen = b->build_gen;
     return GBRT_OK;
 }
 
@@ -449,6 +523,8 @@ extern "C" gbrt_status gbrt_batch_create(gbrt_context* ctx, uint32_t const* h_of
         if ((e = cudaMalloc(&b->sorted_ids, n * 4)) != cudaSuccess) return bail(e, "batch_create");
         if (inner > 0 && (e = cudaMalloc(&b->nodes, size_t(inner) * sizeof(bvh2_node))) != cudaSuccess)
             return bail(e, "batch_create: nodes");
+        if (inner > 0 && (e = cudaMalloc(&b->ranges, size_t(inner) * sizeof(int2))) != cudaSuccess)
+            return bail(e, "batch_create: ranges");
         b->scratch_bytes = scratch_layout(b->total, num_scenes).total;
         if ((e = cudaMalloc(&b->scratch, b->scratch_bytes)) != cudaSuccess) return bail(e, "batch_create: scratch");
     }

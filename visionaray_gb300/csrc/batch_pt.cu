@@ -16,8 +16,9 @@
 // sample's shadow ray is an any-hit query through the scene's tree right after the
 // vertex is shaded.  This unit is compiled with --fmad=false like pathtrace.cu.
 
-#include "pt_shade.cuh"
+#include "batch_pt.cuh"
 
+#include <algorithm>
 #include <new>
 #include <string>
 #include <vector>
@@ -25,157 +26,15 @@
 namespace gbrt {
 namespace {
 
-// Per-scene frame constants (112 bytes).
-struct __align__(16) batch_frame
-{
-    camera_basis cam;
-    float4 bg;          // background with alpha 1 (missed camera rays)
-    float3 ambient;
-    float epsilon;
-    uint32_t width, height, spp, num_bounces;
-    uint32_t frame_id, flags;
-    int32_t root;
-    uint32_t blocks;    // 1: the frame can be walked in 8x4 pixel blocks
-};
-static_assert(sizeof(batch_frame) == 112, "frame record layout");
-
-struct batch_args
-{
-    const batch_frame* frames;
-    const uint32_t* pixel_offsets;
-    uint32_t num_scenes, total_pixels, tile, order;
-    const bvh2_node* nodes;
-    const tri48* tris;
-    int32_t total_inner, total_tris;
-    const gbrt_material* materials;
-    uint32_t num_materials;
-    const float4* lights;            // 4 float4 per light
-    const uint32_t* light_offsets;   // scene s: lights [light_offsets[s], light_offsets[s + 1])
-    const float2* trig;
-    uint32_t* work;
-    float4* images;
-    uint32_t* status;
-};
-
-// Traversal stack entries kept in shared memory (a per-thread column, bank-conflict
-// free); deeper entries in local memory.
-constexpr int kBatchSharedStack = 8;
-// Resident warps per SM the register allocation must allow (launch bounds): the full 64
-// (32 registers, with spills) -- measured on the 512-scene batch, the frame kernel takes
-// 87.7 / 79.8 / 74.9 / 71.8 / 67.4 ms at 24 / 32 / 40 / 48 / 64 warps: latency, not
-// spill traffic, bounds it.
-constexpr int kBatchWarpsPerSM = 64;
-
-// Extended = false: a material table of matte and emissive slots only (the other
-// materials' branches compiled out, as for the adjoint).  Lit = false: no scene has
-// lights (the next-event path compiled out).
-template <int Block, int Stack, bool Extended, bool Lit>
-__global__ void __launch_bounds__(Block, kBatchWarpsPerSM * 32 / Block) batch_pt(batch_args a)
-{
-    const uint32_t full = 0xFFFFFFFFu;
-    const int lane = threadIdx.x & 31;
-    __shared__ int stack_mem[kBatchSharedStack * Block];
-    shared_stack<kBatchSharedStack < Stack ? kBatchSharedStack : Stack - 1, Stack, Block> stack;
-    stack.col = stack_mem + threadIdx.x;
-    shade_params sp;
-    sp.materials = a.materials;
-    sp.num_materials = a.num_materials;
-    sp.lights = nullptr;
-    sp.num_lights = 0;
-    sp.tris = a.tris;
-    sp.num_tris = a.total_tris;
-    sp.albedo = nullptr;
-    sp.emission = nullptr;
-    sp.trig = a.trig;
-    sp.bounce = 0;
-    for (;;)
-    {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(a.work, a.tile);
-        base = __shfl_sync(full, base, 0);
-        if (base >= a.total_pixels) break;
-        for (uint32_t k = uint32_t(lane); k < a.tile; k += 32)
-        {
-            const uint32_t g = base + k;
-            if (g >= a.total_pixels) break;
-            const uint32_t s = upper_segment(a.pixel_offsets, a.num_scenes, g);
-            const batch_frame f = a.frames[s];
-            const uint32_t first = __ldg(&a.pixel_offsets[s]);
-            const uint32_t local = g - first;
-            uint32_t pixel = local;
-            if (a.order == GBRT_BATCH_ORDER_BLOCKS && f.blocks)
-            {
-                uint32_t blk = local >> 5, w = local & 31u, bw = f.width >> 3;
-                pixel = ((blk / bw) * 4u + (w >> 3)) * f.width + (blk % bw) * 8u + (w & 7u);
-            }
-            if constexpr (Lit)
-            {
-                const uint32_t l0 = __ldg(&a.light_offsets[s]);
-                sp.lights = a.lights + 4 * uint64_t(l0);
-                sp.num_lights = __ldg(&a.light_offsets[s + 1]) - l0;
-            }
-            sp.epsilon = f.epsilon;
-            sp.ambient = f.ambient;
-            sp.frame = f.frame_id;
-            sp.flags = f.flags;
-            const v3 eye = { f.cam.eye.x, f.cam.eye.y, f.cam.eye.z };
-            float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            for (uint32_t smp = 0; smp < f.spp; ++smp)
-            {
-                sp.sample = smp;
-                v3 o = eye;
-                v3 d = primary_dir(f.cam, f.width, f.height, f.frame_id, pixel, smp);
-                path_state st{ { 1.0f, 1.0f, 1.0f }, { 0.0f, 0.0f, 0.0f }, 2u, kLastSpecular };
-                for (uint32_t bounce = 0; bounce < f.num_bounces; ++bounce)
-                {
-                    trace_result h = traverse_bvh_with<false>(stack, a.nodes, a.tris, f.root, a.total_inner,
-                                                              a.total_tris, { o.x, o.y, o.z }, { d.x, d.y, d.z }, 0.0f,
-                                                              FLT_MAX, a.status);
-                    vertex_out out;
-                    shade_vertex<Extended>(sp, pixel, bounce, o, d, 0.0f, FLT_MAX, h.tri, h.t, st, out, a.status);
-                    if constexpr (Lit)
-                    {
-                        if (out.shadow)
-                        {
-                            trace_result sh = traverse_bvh_with<true>(
-                                stack, a.nodes, a.tris, f.root, a.total_inner, a.total_tris,
-                                { out.sh_o.x, out.sh_o.y, out.sh_o.z }, { out.sh_d.x, out.sh_d.y, out.sh_d.z },
-                                sp.epsilon, out.sh_tmax, a.status);
-                            if (sh.tri < 0)
-                                st.rad = { st.rad.x + out.contrib.x, st.rad.y + out.contrib.y,
-                                           st.rad.z + out.contrib.z };
-                        }
-                    }
-                    if (!out.cont) break;
-                    o = out.next_o;
-                    d = out.next_d;
-                }
-                // rr.color += result.color (sched_common.h:452-470)
-                float4 c = (st.flags & kFirstHit) ? make_float4(st.rad.x, st.rad.y, st.rad.z, 1.0f) : f.bg;
-                sum = make_float4(sum.x + c.x, sum.y + c.y, sum.z + c.z, sum.w + c.w);
-            }
-            // rr.color /= spp, then the blend with sfactor 1 and dfactor 0 (the
-            // wavefront renderer's pt_blend with those factors)
-            const float spp = float(f.spp);
-            float4 av = make_float4(sum.x / spp, sum.y / spp, sum.z / spp, sum.w / spp);
-            const float sf = 1.0f, df = 0.0f, dz = 0.0f;
-            a.images[uint64_t(first) + pixel] = make_float4(av.x * sf + dz * df, av.y * sf + dz * df,
-                                                            av.z * sf + dz * df, av.w * sf + dz * df);
-        }
-    }
-}
-
-using batch_kernel = void (*)(batch_args);
-
 template <int Block, bool Extended, bool Lit>
 batch_kernel pick_stack(uint32_t stack)
 {
     switch (stack)
     {
-    case 16: return batch_pt<Block, 16, Extended, Lit>;
-    case 24: return batch_pt<Block, 24, Extended, Lit>;
-    case 32: return batch_pt<Block, 32, Extended, Lit>;
-    case 64: return batch_pt<Block, 64, Extended, Lit>;
+    case 16: return batch_pt<Block, 16, Extended, Lit, 2>;
+    case 24: return batch_pt<Block, 24, Extended, Lit, 2>;
+    case 32: return batch_pt<Block, 32, Extended, Lit, 2>;
+    case 64: return batch_pt<Block, 64, Extended, Lit, 2>;
     default: return nullptr;
     }
 }
@@ -194,25 +53,101 @@ batch_kernel pick_block(gbrt_batch_launch const& l)
 
 batch_kernel pick_kernel(gbrt_batch_launch const& l, bool extended, bool lit)
 {
+    if (l.width != 2) return pick_wide_kernel(l, extended, lit);
     if (lit) return extended ? pick_block<true, true>(l) : pick_block<false, true>(l);
     return extended ? pick_block<true, false>(l) : pick_block<false, false>(l);
 }
 
 bool launch_valid(gbrt_batch_launch const& l)
 {
-    return pick_kernel(l, false, false) != nullptr && (l.tile == 32 || l.tile == 64) &&
-           (l.order == GBRT_BATCH_ORDER_ROWS || l.order == GBRT_BATCH_ORDER_BLOCKS);
+    gbrt_batch_launch pairs = l;
+    pairs.width = 2;
+    return pick_kernel(pairs, false, false) != nullptr && pick_kernel(l, false, false) != nullptr &&
+           (l.tile == 32 || l.tile == 64) && (l.order == GBRT_BATCH_ORDER_ROWS || l.order == GBRT_BATCH_ORDER_BLOCKS) &&
+           l.sort <= 1;
+}
+
+// The sorted pixel order's keys: pixel g's first primary ray (sample 0, as the frame
+// draws it) traced to its closest hit; key = scene << (3 b) | the Morton code of the
+// hit point's cell (b bits per axis) in the box of the scene's root, all ones for a
+// miss; value = g.
+__global__ void __launch_bounds__(256) batch_pixel_keys(batch_args a, uint32_t b, uint32_t* __restrict__ keys,
+                                                        uint32_t* __restrict__ values)
+{
+    const uint32_t g = blockIdx.x * 256 + threadIdx.x;
+    if (g >= a.total_pixels) return;
+    const uint32_t s = upper_segment(a.pixel_offsets, a.num_scenes, g);
+    const batch_frame f = a.frames[s];
+    const uint32_t pixel = g - __ldg(&a.pixel_offsets[s]);
+    const uint32_t cells = 1u << b;
+    uint32_t code = (1u << (3 * b)) - 1u;
+    if (f.root >= 0)
+    {
+        const v3 d = primary_dir(f.cam, f.width, f.height, f.frame_id, pixel, 0);
+        trace_result h = traverse_bvh<false>(a.nodes, a.tris, f.root, a.total_inner, a.total_tris,
+                                             { f.cam.eye.x, f.cam.eye.y, f.cam.eye.z }, { d.x, d.y, d.z }, 0.0f,
+                                             FLT_MAX, a.status);
+        if (h.tri >= 0)
+        {
+            const bvh2_node r = a.nodes[f.root];
+            const float lo[3] = { fminf(r.xy0.x, r.xy1.x), fminf(r.xy0.z, r.xy1.z), fminf(r.z01.x, r.z01.z) };
+            const float hi[3] = { fmaxf(r.xy0.y, r.xy1.y), fmaxf(r.xy0.w, r.xy1.w), fmaxf(r.z01.y, r.z01.w) };
+            const float p[3] = { f.cam.eye.x + d.x * h.t, f.cam.eye.y + d.y * h.t, f.cam.eye.z + d.z * h.t };
+            uint32_t c[3];
+            for (int k = 0; k < 3; ++k)
+            {
+                const float ext = hi[k] - lo[k];
+                const float q = ext > 0.0f ? (p[k] - lo[k]) / ext * float(cells) : 0.0f;
+                c[k] = uint32_t(fminf(fmaxf(q, 0.0f), float(cells - 1)));   // NaN lands in cell 0
+            }
+            code = morton3(c[0], c[1], c[2]);
+        }
+    }
+    keys[g] = (s << (3 * b)) | code;
+    values[g] = g;
+}
+
+gbrt_status ensure_batch_sort(gbrt_context* ctx, gbrt_batch* b)
+{
+    if (b->sort_buf && b->sort_capacity >= b->total_pixels) return GBRT_OK;
+    cudaFree(b->sort_buf);
+    cudaFree(b->sort_scratch);
+    b->sort_buf = nullptr;
+    b->sort_scratch = nullptr;
+    b->sort_capacity = 0;
+    const uint32_t n = b->total_pixels > 0 ? b->total_pixels : 1;
+    GBRT_CUDA(ctx, cudaMalloc(&b->sort_buf, 4 * size_t(n) * sizeof(uint32_t)));
+    GBRT_CUDA(ctx, cudaMalloc(&b->sort_scratch, radix_sort_scratch_bytes(n)));
+    b->sort_capacity = n;
+    return GBRT_OK;
+}
+
+// What the current launch shape needs allocated before a frame (never during a capture).
+gbrt_status ensure_batch_extras(gbrt_context* ctx, gbrt_batch* b)
+{
+    if (b->launch.width != 2)
+    {
+        gbrt_status st = ensure_batch_wide(ctx, b);
+        if (st != GBRT_OK) return st;
+    }
+    if (b->launch.sort) return ensure_batch_sort(ctx, b);
+    return GBRT_OK;
 }
 
 } // namespace
 
-gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_images, cudaStream_t stream)
+gbrt_status batch_frame_stage(gbrt_context* ctx, gbrt_batch* b, float* d_images, cudaStream_t stream,
+                              bool force_collapse)
 {
     if (b->frames_set != b->num_scenes) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: frames not set");
     if (!d_images || (reinterpret_cast<uintptr_t>(d_images) & 15u))
         return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: images null or not 16-byte aligned");
     batch_kernel kernel = pick_kernel(b->launch, b->extended_materials, b->num_lights > 0);
     if (!kernel) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: bad launch shape");
+    if (b->launch.width != 2 && !b->wide_nodes && b->total_inner > 0)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: wide nodes not allocated");
+    if (b->launch.sort && (!b->sort_buf || b->sort_capacity < b->total_pixels))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: sort buffers not allocated");
     int per_sm = 0;
     GBRT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, int(b->launch.block), 0));
     if (per_sm < 1) per_sm = 1;
@@ -222,6 +157,12 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     uint64_t blocks = uint64_t(ctx->num_sms) * uint64_t(per_sm);
     if (blocks_needed < blocks) blocks = blocks_needed;
     if (blocks == 0) return GBRT_OK;
+    if (b->launch.width != 2 &&
+        (force_collapse || b->collapsed_width != b->launch.width || b->collapsed_gen != b->build_gen))
+    {
+        gbrt_status st = batch_collapse(ctx, b, b->launch.width, stream);
+        if (st != GBRT_OK) return st;
+    }
     batch_args a;
     a.frames = static_cast<const batch_frame*>(b->d_frames);
     a.pixel_offsets = b->d_pixel_offsets;
@@ -233,6 +174,9 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     a.tris = b->tris;
     a.total_inner = int32_t(b->total_inner);
     a.total_tris = int32_t(b->total);
+    a.nodesw = b->wide_nodes;
+    a.num_nodesw = int32_t(b->wide_cap);
+    a.perm = nullptr;
     a.materials = b->d_materials;
     a.num_materials = b->num_materials;
     a.lights = b->d_lights;
@@ -242,6 +186,24 @@ gbrt_status batch_pathtrace(gbrt_context* ctx, gbrt_batch const* b, float* d_ima
     a.work = b->d_work;
     a.images = reinterpret_cast<float4*>(d_images);
     a.status = ctx->d_status;
+    if (b->launch.sort)
+    {
+        // scene bits + 3 cell bits per axis within 32-bit keys (7 per axis up to 2^11 scenes)
+        uint32_t scene_bits = 0;
+        while ((1u << scene_bits) < b->num_scenes) ++scene_bits;
+        const uint32_t cell_bits = std::min<uint32_t>(7u, (32u - scene_bits) / 3u);
+        const uint32_t n = b->total_pixels;
+        uint32_t* keys = b->sort_buf;
+        uint32_t* values = keys + b->sort_capacity;
+        uint32_t* keys_alt = values + b->sort_capacity;
+        uint32_t* values_alt = keys_alt + b->sort_capacity;
+        batch_pixel_keys<<<(n + 255) / 256, 256, 0, stream>>>(a, cell_bits, keys, values);
+        GBRT_LAUNCH_CHECK(ctx, "batch_pixel_keys");
+        gbrt_status st = radix_sort_pairs(ctx, keys, values, keys_alt, values_alt, n, int(scene_bits + 3 * cell_bits),
+                                          b->sort_scratch, stream);
+        if (st != GBRT_OK) return st;
+        a.perm = values;   // radix_sort_pairs leaves the result in (keys, values)
+    }
     GBRT_CUDA(ctx, cudaMemsetAsync(b->d_work, 0, 4, stream));
     kernel<<<uint32_t(blocks), b->launch.block, 0, stream>>>(a);
     GBRT_LAUNCH_CHECK(ctx, "batch_pt");
@@ -385,12 +347,14 @@ extern "C" gbrt_status gbrt_batch_height(gbrt_context* ctx, gbrt_batch const* ba
     return GBRT_OK;
 }
 
-extern "C" gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch const* batch, float* d_images)
+extern "C" gbrt_status gbrt_batch_pathtrace(gbrt_context* ctx, gbrt_batch* batch, float* d_images)
 {
     if (!ctx) return GBRT_ERR_INVALID_ARG;
     if (!batch) return fail(ctx, GBRT_ERR_INVALID_ARG, "batch_pathtrace: null batch");
     device_guard g(ctx->device);
-    return batch_pathtrace(ctx, batch, d_images, ctx->stream);
+    gbrt_status st = ensure_batch_extras(ctx, batch);
+    if (st != GBRT_OK) return st;
+    return batch_frame_stage(ctx, batch, d_images, ctx->stream, false);
 }
 
 extern "C" gbrt_status gbrt_batch_run_graph(gbrt_context* ctx, gbrt_batch* batch, gbrt_triangle const* d_tris,
@@ -410,10 +374,12 @@ extern "C" gbrt_status gbrt_batch_run_graph(gbrt_context* ctx, gbrt_batch* batch
         }
         if (!batch->capture_stream)
             GBRT_CUDA(ctx, cudaStreamCreateWithFlags(&batch->capture_stream, cudaStreamNonBlocking));
+        gbrt_status est = ensure_batch_extras(ctx, batch);   // nothing allocates inside the capture
+        if (est != GBRT_OK) return est;
         const uint64_t before = ctx->launches;
         GBRT_CUDA(ctx, cudaStreamBeginCapture(batch->capture_stream, cudaStreamCaptureModeThreadLocal));
         gbrt_status st = batch_build(ctx, batch, d_tris, batch->capture_stream);
-        if (st == GBRT_OK) st = batch_pathtrace(ctx, batch, d_images, batch->capture_stream);
+        if (st == GBRT_OK) st = batch_frame_stage(ctx, batch, d_images, batch->capture_stream, true);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(batch->capture_stream, &graph);
         const uint64_t captured = ctx->launches - before;
@@ -463,6 +429,41 @@ extern "C" gbrt_status gbrt_batch_autotune(gbrt_context* ctx, gbrt_batch* batch,
     gbrt_batch_launch winner = saved;
     float winner_ms = -1.0f;
     gbrt_status result = GBRT_OK;
+    // one candidate: a warm-up run, then `reps` timed runs of the frame stage (with the
+    // collapse and the pixel order it needs, as every graph replay does them)
+    auto try_launch = [&](gbrt_batch_launch const& l) {
+        if (result != GBRT_OK) return;
+        batch->launch = l;
+        gbrt_status st = ensure_batch_extras(ctx, batch);
+        if (st == GBRT_OK) st = batch_frame_stage(ctx, batch, d_images, ctx->stream, true);   // warm-up
+        for (uint32_t r = 0; st == GBRT_OK && r < reps; ++r)
+        {
+            if (r == 0 && cudaEventRecord(ev[0], ctx->stream) != cudaSuccess) st = GBRT_ERR_CUDA;
+            if (st == GBRT_OK) st = batch_frame_stage(ctx, batch, d_images, ctx->stream, true);
+        }
+        float ms = 0.0f;
+        if (st == GBRT_OK && (cudaEventRecord(ev[1], ctx->stream) != cudaSuccess ||
+                              cudaEventSynchronize(ev[1]) != cudaSuccess ||
+                              cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess))
+            st = GBRT_ERR_CUDA;
+        uint32_t cs = 0;
+        if (st == GBRT_OK && (cudaMemcpy(&cs, ctx->d_status, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                              (cs != 0 && cudaMemset(ctx->d_status, 0, 4) != cudaSuccess)))
+            st = GBRT_ERR_CUDA;
+        if (st != GBRT_OK)
+        {
+            result = st;
+            return;
+        }
+        if (cs != 0) return;   // this shape raised a status: not a candidate
+        ms /= float(reps);
+        if (winner_ms < 0.0f || ms < winner_ms)
+        {
+            winner_ms = ms;
+            winner = l;
+        }
+    };
+    // phase 1: the launch shape on the node pairs, rays unsorted
     const uint32_t blocks[] = { 128, 256, 512 }, tiles[] = { 32, 64 }, stacks[] = { 16, 24, 32, 64 },
                    orders[] = { GBRT_BATCH_ORDER_ROWS, GBRT_BATCH_ORDER_BLOCKS };
     for (uint32_t stk : stacks)
@@ -471,38 +472,21 @@ extern "C" gbrt_status gbrt_batch_autotune(gbrt_context* ctx, gbrt_batch* batch,
         for (uint32_t blk : blocks)
             for (uint32_t tl : tiles)
                 for (uint32_t ord : orders)
-                {
-                    if (result != GBRT_OK) break;
-                    batch->launch = { blk, tl, stk, ord };
-                    gbrt_status st = batch_pathtrace(ctx, batch, d_images, ctx->stream);   // warm-up
-                    for (uint32_t r = 0; st == GBRT_OK && r < reps; ++r)
-                    {
-                        if (r == 0 && cudaEventRecord(ev[0], ctx->stream) != cudaSuccess) st = GBRT_ERR_CUDA;
-                        if (st == GBRT_OK) st = batch_pathtrace(ctx, batch, d_images, ctx->stream);
-                    }
-                    float ms = 0.0f;
-                    if (st == GBRT_OK && (cudaEventRecord(ev[1], ctx->stream) != cudaSuccess ||
-                                          cudaEventSynchronize(ev[1]) != cudaSuccess ||
-                                          cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess))
-                        st = GBRT_ERR_CUDA;
-                    uint32_t cs = 0;
-                    if (st == GBRT_OK &&
-                        (cudaMemcpy(&cs, ctx->d_status, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
-                         (cs != 0 && cudaMemset(ctx->d_status, 0, 4) != cudaSuccess)))
-                        st = GBRT_ERR_CUDA;
-                    if (st != GBRT_OK)
-                    {
-                        result = st;
-                        break;
-                    }
-                    if (cs != 0) continue;   // this shape raised a status: not a candidate
-                    ms /= float(reps);
-                    if (winner_ms < 0.0f || ms < winner_ms)
-                    {
-                        winner_ms = ms;
-                        winner = batch->launch;
-                    }
-                }
+                    try_launch({ blk, tl, stk, ord, 2, 0 });
+    }
+    // phase 2: BVH width and ray sorting at the winner's block, tile and order
+    if (winner_ms >= 0.0f)
+    {
+        const gbrt_batch_launch base = winner;
+        for (uint32_t width : { 2u, 4u, 8u })
+            for (uint32_t sort : { 0u, 1u })
+            {
+                if (width == 2 && sort == 0) continue;   // timed in phase 1
+                gbrt_batch_launch l = base;
+                l.width = width;
+                l.sort = sort;
+                try_launch(l);
+            }
     }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);

@@ -74,7 +74,22 @@ struct __align__(16) bvh4q_node
 };
 static_assert(sizeof(bvh4q_node) == 64, "quantised 4-wide node is 64 bytes");
 
+// 8-wide node (256 bytes = eight 256-bit loads): the same SoA planes for eight
+// children, each plane two float4; child / count as for bvh4_node.
+struct __align__(32) bvh8_node
+{
+    float4 lox[2], hix[2], loy[2], hiy[2], loz[2], hiz[2];
+    int4 child[2];
+    int4 count[2];
+};
+static_assert(sizeof(bvh8_node) == 256, "8-wide node is 256 bytes");
+
+template <int W> struct wide_node;
+template <> struct wide_node<4> { using type = bvh4_node; };
+template <> struct wide_node<8> { using type = bvh8_node; };
+
 constexpr int kStack4 = 96;        // 4-wide traversal stack entries (up to 3 per level)
-constexpr int kLeafMax4 = 4;       // triangles per 4-wide leaf (default)
+constexpr int kStack8 = 160;       // 8-wide traversal stack entries (up to 7 per level)
+constexpr int kLeafMax4 = 4;       // triangles per wide leaf (default)
 
 } // namespace gbrt

@@ -11,23 +11,13 @@
 // counts, and the reference builds its top-level tree on the host too (the viewer's
 // index_bvh over bvh_inst, viewer.cpp:647-661).
 
-#include "traverse_core.cuh"
+#include "instances.cuh"
 
 #include <algorithm>
 #include <new>
 #include <numeric>
 #include <vector>
 
-struct gbrt_tlas
-{
-    int device = 0;
-    uint32_t num_instances = 0;
-    uint32_t num_inner = 0;
-    int32_t root = INT32_MIN;
-    gbrt::bvh2_node* nodes = nullptr;   // top-level node pairs, leaves ~instance
-    float4* records = nullptr;          // 3 float4 per instance: rows of A | trans_inv
-    gbrt::bvh_view* views = nullptr;    // the instance's bottom-level tree
-};
 
 namespace gbrt {
 namespace {
@@ -168,14 +158,6 @@ int32_t build_top(std::vector<uint32_t>& ids, size_t first, size_t last, std::ve
     return self;
 }
 
-struct tlas_view
-{
-    const bvh2_node* nodes;
-    const float4* records;
-    const bvh_view* views;
-    int32_t root, num_inner, num_instances;
-};
-
 template <bool AnyHit>
 __global__ void __launch_bounds__(kBlock) tlas_trace(tlas_view tv, const gbrt_ray* __restrict__ rays, uint32_t n,
                                                      gbrt_hit_inst* __restrict__ hits, uint32_t* __restrict__ status)
@@ -184,99 +166,14 @@ __global__ void __launch_bounds__(kBlock) tlas_trace(tlas_view tv, const gbrt_ra
     if (i >= n) return;
     float4 r0 = ldg4(&rays[i]);
     float4 r1 = ldg4(reinterpret_cast<const float4*>(&rays[i]) + 1);
-    const f3 o = { r0.x, r0.y, r0.z }, d = { r0.w, r1.x, r1.y };
-    const float tmin = r1.z, tmax = r1.w;
-    const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
-    float best_t = FLT_MAX, best_u = 0.0f, best_v = 0.0f;
-    int best_inst = -1, best_tri = -1;
-    int stack[32];
-    int sp = 0;
-    int node = tv.root;
-    bool done = false;
-    while (node != kEmptyLink && !done)
-    {
-        while (node >= 0)
-        {
-            if (node >= tv.num_inner)
-            {
-                atomicOr(status, kStatusBadIndex);
-                node = kEmptyLink;
-                break;
-            }
-            float4 a, b, z;
-            int4 link;
-            load_pair(tv.nodes + node, a, b, z, link);
-            float lx0 = (a.x - o.x) * ix, hx0 = (a.y - o.x) * ix;
-            float ly0 = (a.z - o.y) * iy, hy0 = (a.w - o.y) * iy;
-            float lz0 = (z.x - o.z) * iz, hz0 = (z.y - o.z) * iz;
-            float lx1 = (b.x - o.x) * ix, hx1 = (b.y - o.x) * ix;
-            float ly1 = (b.z - o.y) * iy, hy1 = (b.w - o.y) * iy;
-            float lz1 = (z.z - o.z) * iz, hz1 = (z.w - o.z) * iz;
-            float tn0 = fmaxf(tmin, fmaxf(fminf(lx0, hx0), fmaxf(fminf(ly0, hy0), fminf(lz0, hz0))));
-            float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
-            float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
-            float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
-            bool h0 = tf0 >= tn0 && tn0 < best_t;
-            bool h1 = tf1 >= tn1 && tn1 < best_t;
-            if (h0 && h1)
-            {
-                bool first0 = tn0 < tn1;
-                if (sp < 32)
-                    stack[sp++] = first0 ? link.y : link.x;
-                else
-                    atomicOr(status, kStatusStackOverflow);
-                node = first0 ? link.x : link.y;
-            }
-            else if (h0 || h1)
-            {
-                node = h0 ? link.x : link.y;
-            }
-            else
-            {
-                node = sp > 0 ? stack[--sp] : kEmptyLink;
-            }
-        }
-        if (node == kEmptyLink) break;
-        const int inst = ~node;
-        if (inst >= tv.num_instances)
-        {
-            atomicOr(status, kStatusBadIndex);
-            break;
-        }
-        // transform_ray (bvh.h:748-755) with the instance's inverse, then its tree
-        const float4 ra = tv.records[3 * inst + 0], rb = tv.records[3 * inst + 1], rc = tv.records[3 * inst + 2];
-        const float px = __fadd_rn(o.x, ra.w), py = __fadd_rn(o.y, rb.w), pz = __fadd_rn(o.z, rc.w);
-        f3 oo = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, px), __fmul_rn(ra.y, py)), __fmul_rn(ra.z, pz)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, px), __fmul_rn(rb.y, py)), __fmul_rn(rb.z, pz)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, px), __fmul_rn(rc.y, py)), __fmul_rn(rc.z, pz)) };
-        f3 dd = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, d.x), __fmul_rn(ra.y, d.y)), __fmul_rn(ra.z, d.z)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, d.x), __fmul_rn(rb.y, d.y)), __fmul_rn(rb.z, d.z)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, d.x), __fmul_rn(rc.y, d.y)), __fmul_rn(rc.z, d.z)) };
-        const bvh_view bv = tv.views[inst];
-        if (bv.num_tris > 0)
-        {
-            local_stack<kStackSize> bstack;
-            trace_result h = traverse_bvh_with<AnyHit>(bstack, bv.nodes, bv.tris, bv.root, bv.num_inner, bv.num_tris,
-                                                       oo, dd, tmin, tmax, status, best_t);
-            if (h.tri >= 0)
-            {
-                best_t = h.t;
-                best_u = h.u;
-                best_v = h.v;
-                best_tri = h.tri;
-                best_inst = inst;
-                if (AnyHit) done = true;
-            }
-        }
-        node = sp > 0 ? stack[--sp] : kEmptyLink;
-    }
+    const tlas_result best = traverse_tlas<AnyHit>(tv, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
     uint4 w0, w1;
-    if (best_inst >= 0)
+    if (best.inst >= 0)
     {
-        const bvh_view bv = tv.views[best_inst];
-        float4 t0 = ldg4(&bv.tris[best_tri].t0), t1 = ldg4(&bv.tris[best_tri].t1);
-        w0 = make_uint4(__float_as_uint(t0.w), uint32_t(best_inst), __float_as_uint(best_t), __float_as_uint(best_u));
-        w1 = make_uint4(__float_as_uint(best_v), __float_as_uint(t1.w), 0u, 0u);
+        const bvh_view bv = tv.views[best.inst];
+        float4 t0 = ldg4(&bv.tris[best.tri].t0), t1 = ldg4(&bv.tris[best.tri].t1);
+        w0 = make_uint4(__float_as_uint(t0.w), uint32_t(best.inst), __float_as_uint(best.t), __float_as_uint(best.u));
+        w1 = make_uint4(__float_as_uint(best.v), __float_as_uint(t1.w), 0u, 0u);
     }
     else
     {
@@ -291,6 +188,7 @@ void free_tlas(gbrt_tlas* t)
 {
     cudaFree(t->nodes);
     cudaFree(t->records);
+    cudaFree(t->forward);
     cudaFree(t->views);
 }
 
@@ -308,7 +206,7 @@ extern "C" gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h
     if (num_instances > (1u << 24)) return fail(ctx, GBRT_ERR_TOO_LARGE, "tlas_build: more than 2^24 instances");
     for (uint32_t k = 0; k < num_instances; ++k)
         if (!h_instances[k].blas) return fail(ctx, GBRT_ERR_INVALID_ARG, "tlas_build: instance without a tree");
-    std::vector<float4> records(size_t(num_instances) * 3);
+    std::vector<float4> records(size_t(num_instances) * 3), forward(size_t(num_instances) * 3);
     std::vector<bvh_view> views(num_instances);
     std::vector<box> boxes(num_instances);
     for (uint32_t k = 0; k < num_instances; ++k)
@@ -322,6 +220,10 @@ extern "C" gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h
         m3 ainv = inverse3(tl);
         float tinv[3] = { -in.transform[9], -in.transform[10], -in.transform[11] };
         for (int r = 0; r < 3; ++r) records[3 * k + r] = make_float4(ainv.m[r][0], ainv.m[r][1], ainv.m[r][2], tinv[r]);
+        // the instance-to-world map as get_bounds forms it (get_bounds.inl:30-56):
+        // affine = inverse(affine_inv), trans = -trans_inv
+        m3 aff = inverse3(ainv);
+        for (int r = 0; r < 3; ++r) forward[3 * k + r] = make_float4(aff.m[r][0], aff.m[r][1], aff.m[r][2], -tinv[r]);
         views[k] = view_of(in.blas);
         boxes[k] = instance_bounds(ainv, tinv, in.blas);
     }
@@ -342,13 +244,18 @@ extern "C" gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h
     t->num_instances = num_instances;
     t->num_inner = uint32_t(nodes.size());
     t->root = root;
+    t->blas.resize(num_instances);
+    for (uint32_t k = 0; k < num_instances; ++k) t->blas[k] = h_instances[k].blas;
     cudaError_t e = cudaSuccess;
     if (num_instances > 0)
     {
         if ((e = cudaMalloc(&t->records, records.size() * sizeof(float4))) == cudaSuccess &&
+            (e = cudaMalloc(&t->forward, forward.size() * sizeof(float4))) == cudaSuccess &&
             (e = cudaMalloc(&t->views, views.size() * sizeof(bvh_view))) == cudaSuccess)
         {
             e = cudaMemcpy(t->records, records.data(), records.size() * sizeof(float4), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(t->forward, forward.data(), forward.size() * sizeof(float4), cudaMemcpyHostToDevice);
             if (e == cudaSuccess)
                 e = cudaMemcpy(t->views, views.data(), views.size() * sizeof(bvh_view), cudaMemcpyHostToDevice);
         }

@@ -19,6 +19,7 @@
 // Topology and boxes equal the reference's for identical Morton codes; the node-pair
 // layout is gbrt::bvh2_node (bvh_layout.cuh).
 
+#include "collapse.cuh"
 #include "lbvh_device.cuh"
 
 #include <algorithm>
@@ -269,141 +270,6 @@ __global__ void __launch_bounds__(kBlock) quantize_nodes4(const bvh4_node* __res
     out[i] = q;
 }
 
-// One level of the collapse into 4-wide nodes: every queued (pair node, 4-wide node)
-// item opens the pair node's two children and keeps opening the inner child of largest
-// surface area until four children are reached; children with at most leaf_max
-// primitives become leaves over their contiguous (Morton-ordered) triangle range, the
-// other inner children get a new 4-wide node and go to the next level's queue.
-__global__ void __launch_bounds__(kBlock) collapse_level(const bvh2_node* __restrict__ nodes2,
-                                                         const int2* __restrict__ ranges,
-                                                         const int2* __restrict__ q_in,
-                                                         const uint32_t* __restrict__ count_in,
-                                                         int2* __restrict__ q_out, uint32_t* __restrict__ count_out,
-                                                         bvh4_node* __restrict__ nodes4,
-                                                         uint32_t* __restrict__ node4_counter, uint32_t cap4,
-                                                         int leaf_max, int num_inner2,
-                                                         uint32_t* __restrict__ status)
-{
-    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= *count_in) return;
-    int2 item = q_in[i];
-    int ref[4], first[4], cnt[4];
-    float bx[4][6];   // lo.x hi.x lo.y hi.y lo.z hi.z
-    int num = 0;
-    auto open = [&](int node) {
-        bvh2_node nd = nodes2[node];
-        for (int side = 0; side < 2; ++side)
-        {
-            int link = side ? nd.link.y : nd.link.x;
-            float4 xy = side ? nd.xy1 : nd.xy0;
-            float zl = side ? nd.z01.z : nd.z01.x, zh = side ? nd.z01.w : nd.z01.y;
-            ref[num] = link;
-            bx[num][0] = xy.x;
-            bx[num][1] = xy.y;
-            bx[num][2] = xy.z;
-            bx[num][3] = xy.w;
-            bx[num][4] = zl;
-            bx[num][5] = zh;
-            if (link < 0)
-            {
-                first[num] = ~link;
-                cnt[num] = 1;
-            }
-            else
-            {
-                int2 r = link < num_inner2 ? ranges[link] : make_int2(0, -1);
-                first[num] = r.x;
-                cnt[num] = r.y - r.x + 1;
-            }
-            ++num;
-        }
-    };
-    if (item.x < 0 || item.x >= num_inner2 || uint32_t(item.y) >= cap4)
-    {
-        atomicOr(status, kStatusBadIndex);
-        return;
-    }
-    open(item.x);
-    while (num < 4)
-    {
-        int best = -1;
-        float best_area = -1.0f;
-        for (int k = 0; k < num; ++k)
-        {
-            if (ref[k] < 0 || cnt[k] <= leaf_max) continue;
-            float dx = bx[k][1] - bx[k][0], dy = bx[k][3] - bx[k][2], dz = bx[k][5] - bx[k][4];
-            float area = dx * dy + dy * dz + dz * dx;
-            if (area > best_area)
-            {
-                best_area = area;
-                best = k;
-            }
-        }
-        if (best < 0) break;
-        int node = ref[best];
-        --num;
-        ref[best] = ref[num];
-        first[best] = first[num];
-        cnt[best] = cnt[num];
-        for (int c = 0; c < 6; ++c) bx[best][c] = bx[num][c];
-        open(node);
-    }
-    float lo[3][4], hi[3][4];
-    int ch[4], ct[4];
-    for (int k = 0; k < 4; ++k)
-    {
-        if (k < num)
-        {
-            lo[0][k] = bx[k][0];
-            hi[0][k] = bx[k][1];
-            lo[1][k] = bx[k][2];
-            hi[1][k] = bx[k][3];
-            lo[2][k] = bx[k][4];
-            hi[2][k] = bx[k][5];
-            if (ref[k] < 0 || cnt[k] <= leaf_max)
-            {
-                ch[k] = first[k];
-                ct[k] = cnt[k];
-            }
-            else
-            {
-                uint32_t idx = atomicAdd(node4_counter, 1u);
-                if (idx >= cap4)
-                {
-                    atomicOr(status, kStatusBadIndex);
-                    ch[k] = -1;
-                    ct[k] = -1;
-                    continue;
-                }
-                ch[k] = int(idx);
-                ct[k] = 0;
-                uint32_t slot = atomicAdd(count_out, 1u);
-                if (slot < cap4)
-                    q_out[slot] = make_int2(ref[k], int(idx));
-                else
-                    atomicOr(status, kStatusBadIndex);
-            }
-        }
-        else
-        {
-            lo[0][k] = lo[1][k] = lo[2][k] = FLT_MAX;
-            hi[0][k] = hi[1][k] = hi[2][k] = -FLT_MAX;
-            ch[k] = -1;
-            ct[k] = -1;
-        }
-    }
-    bvh4_node out;
-    out.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
-    out.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
-    out.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
-    out.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
-    out.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
-    out.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
-    out.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
-    out.count = make_int4(ct[0], ct[1], ct[2], ct[3]);
-    nodes4[item.y] = out;
-}
-
 __global__ void collapse_root(int2* __restrict__ q, uint32_t* __restrict__ counts, uint32_t* __restrict__ node4_counter)
 {
     q[0] = make_int2(0, 0);
@@ -586,15 +452,11 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
     if (!bvh->sorted_ids) GBRT_CUDA(ctx, cudaMalloc(&bvh->sorted_ids, size_t(n) * 4));
     if (bvh->num_inner > 0 && !bvh->nodes)
         GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes, size_t(bvh->num_inner) * sizeof(bvh2_node)));
-    if (bvh->nodes4)
+    if (bvh->nodes4 || bvh->nodes8)
     {
-        // a rebuild with a 4-wide collapse from the previous build: its size may change
+        // a rebuild with a wide collapse from the previous build: its size may change
         GBRT_CUDA(ctx, cudaStreamSynchronize(s));
-        cudaFree(bvh->nodes4);
-        bvh->nodes4 = nullptr;
-        bvh->num_nodes4 = 0;
-        cudaFree(bvh->nodes4q);
-        bvh->nodes4q = nullptr;
+        free_wide_nodes(bvh);
     }
 
     // scratch: centroids | keys_alt | vals_alt | leaf_parent | arrivals | cb(6) | height | sort
@@ -605,17 +467,18 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
     size_t off_arrivals = align_up(off_parent + size_t(n) * 4);
     size_t off_cb = align_up(off_arrivals + size_t(n) * 4);
     size_t off_sort = align_up(off_cb + 8 * 4);
-    // 4-wide collapse: node ranges, two level queues, per-level counts, node counter
-    // and the nodes themselves (a tree with n leaves has at most 2n / (L + 1) nodes above
-    // L leaves, the bound on the 4-wide node count for leaves of at most L triangles)
+    // wide collapse: node ranges, two level queues, per-level counts, node counter and
+    // the nodes themselves (a tree with n leaves has at most 2n / (L + 1) nodes above L
+    // leaves, the bound on the wide node count for leaves of at most L triangles)
     const int leaf_max = kLeafMax4;
     const uint32_t cap4 = uint32_t(2ull * n / (leaf_max + 1) + 2);
+    const size_t wide_bytes = (ctx->trace_flags & GBRT_TRACE_WIDE8_NODES) ? sizeof(bvh8_node) : sizeof(bvh4_node);
     size_t off_ranges = align_up(off_sort + radix_sort_scratch_bytes(n));
     size_t off_q0 = align_up(off_ranges + size_t(n) * 8);
     size_t off_q1 = align_up(off_q0 + size_t(cap4) * 8);
     size_t off_counts = align_up(off_q1 + size_t(cap4) * 8);
     size_t off_nodes4 = align_up(off_counts + 256 * 4);
-    size_t total = off_nodes4 + size_t(cap4) * sizeof(bvh4_node);
+    size_t total = off_nodes4 + size_t(cap4) * wide_bytes;
     gbrt_status st = ensure_scratch(ctx, total);
     if (st != GBRT_OK) return st;
     char* base = static_cast<char*>(ctx->scratch);
@@ -630,7 +493,7 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
     int2* queue[2] = { reinterpret_cast<int2*>(base + off_q0), reinterpret_cast<int2*>(base + off_q1) };
     uint32_t* level_counts = reinterpret_cast<uint32_t*>(base + off_counts);   // [0..254]
     uint32_t* node4_counter = level_counts + 255;
-    bvh4_node* nodes4_tmp = reinterpret_cast<bvh4_node*>(base + off_nodes4);
+    void* wide_tmp = base + off_nodes4;
 
     // cb = (+FLT_MAX x3, -FLT_MAX x3) as ordered ints; root height 1 by default
     int init[8];
@@ -679,42 +542,60 @@ gbrt_status build_lbvh(gbrt_context* ctx, gbrt_triangle const* d_tris, uint32_t 
         // scene bounds: the union of the root's two child boxes
         set_scene_box(bvh, root);
 
-        if (ctx->trace_flags & (GBRT_TRACE_WIDE_NODES | GBRT_TRACE_COMPRESSED_NODES))
-        {
-            // collapse into 4-wide nodes (on request), one level per launch; the pair tree
-            // has h inner levels, so h levels drain every queue
+        // collapse into wide nodes (on request), one level per launch; the pair tree has
+        // h inner levels, so h levels drain every queue
+        auto collapse = [&](auto width_tag, uint32_t* out_count) -> gbrt_status {
+            constexpr int W = decltype(width_tag)::value;
             if (h + 1 > 254) return fail(ctx, GBRT_ERR_STACK_OVERFLOW, "LBVH height exceeds the collapse levels");
             GBRT_CUDA(ctx, cudaMemsetAsync(level_counts, 0, 256 * 4, s));
             collapse_root<<<1, 1, 0, s>>>(queue[0], level_counts, node4_counter);
             GBRT_LAUNCH_CHECK(ctx, "collapse_root");
+            auto* nodes_tmp = static_cast<typename wide_node<W>::type*>(wide_tmp);
             uint64_t width = 1;
             for (uint32_t level = 0; level < h; ++level)
             {
                 uint32_t items = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(width, cap4)));
-                collapse_level<<<blocks_for(items), kBlock, 0, s>>>(
+                collapse_wide<W><<<blocks_for(items), kBlock, 0, s>>>(
                     bvh->nodes, ranges, queue[level & 1], level_counts + level, queue[(level + 1) & 1],
-                    level_counts + level + 1, nodes4_tmp, node4_counter, cap4, leaf_max, int(n - 1), ctx->d_status);
-                GBRT_LAUNCH_CHECK(ctx, "collapse_level");
-                if (width < cap4) width *= 4;   // saturates: 4^level overflows past level 31
+                    level_counts + level + 1, nodes_tmp, node4_counter, cap4, leaf_max, int(n - 1), ctx->d_status);
+                GBRT_LAUNCH_CHECK(ctx, "collapse_wide");
+                if (width < cap4) width *= W;   // saturates: W^level overflows past a few dozen levels
             }
             uint32_t tail[2] = { 0, 0 };
             GBRT_CUDA(ctx, cudaMemcpyAsync(&tail[0], level_counts + h, 4, cudaMemcpyDeviceToHost, s));
             GBRT_CUDA(ctx, cudaMemcpyAsync(&tail[1], node4_counter, 4, cudaMemcpyDeviceToHost, s));
             GBRT_CUDA(ctx, cudaStreamSynchronize(s));
             if (tail[0] != 0 || tail[1] == 0 || tail[1] > cap4)
-                return fail(ctx, GBRT_ERR_CUDA, "4-wide collapse did not complete");
-            bvh->num_nodes4 = tail[1];
+                return fail(ctx, GBRT_ERR_CUDA, "wide collapse did not complete");
+            *out_count = tail[1];
+            return GBRT_OK;
+        };
+        if (ctx->trace_flags & (GBRT_TRACE_WIDE_NODES | GBRT_TRACE_COMPRESSED_NODES))
+        {
+            uint32_t count = 0;
+            st = collapse(std::integral_constant<int, 4>{}, &count);
+            if (st != GBRT_OK) return st;
+            bvh->num_nodes4 = count;
             bvh->leaf_max4 = uint32_t(leaf_max);
-            GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4, size_t(bvh->num_nodes4) * sizeof(bvh4_node)));
-            GBRT_CUDA(ctx, cudaMemcpyAsync(bvh->nodes4, nodes4_tmp, size_t(bvh->num_nodes4) * sizeof(bvh4_node),
+            GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4, size_t(count) * sizeof(bvh4_node)));
+            GBRT_CUDA(ctx, cudaMemcpyAsync(bvh->nodes4, wide_tmp, size_t(count) * sizeof(bvh4_node),
                                            cudaMemcpyDeviceToDevice, s));
             if (ctx->trace_flags & GBRT_TRACE_COMPRESSED_NODES)
             {
-                GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4q, size_t(bvh->num_nodes4) * sizeof(bvh4q_node)));
-                quantize_nodes4<<<blocks_for(bvh->num_nodes4), kBlock, 0, s>>>(bvh->nodes4, bvh->num_nodes4,
-                                                                                bvh->nodes4q);
+                GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes4q, size_t(count) * sizeof(bvh4q_node)));
+                quantize_nodes4<<<blocks_for(count), kBlock, 0, s>>>(bvh->nodes4, count, bvh->nodes4q);
                 GBRT_LAUNCH_CHECK(ctx, "quantize_nodes4");
             }
+        }
+        if (ctx->trace_flags & GBRT_TRACE_WIDE8_NODES)
+        {
+            uint32_t count = 0;
+            st = collapse(std::integral_constant<int, 8>{}, &count);
+            if (st != GBRT_OK) return st;
+            bvh->num_nodes8 = count;
+            GBRT_CUDA(ctx, cudaMalloc(&bvh->nodes8, size_t(count) * sizeof(bvh8_node)));
+            GBRT_CUDA(ctx, cudaMemcpyAsync(bvh->nodes8, wide_tmp, size_t(count) * sizeof(bvh8_node),
+                                           cudaMemcpyDeviceToDevice, s));
         }
     }
     else
@@ -739,14 +620,10 @@ gbrt_status refit_lbvh(gbrt_context* ctx, gbrt_bvh* bvh, gbrt_triangle const* d_
     const uint32_t n = bvh->num_prims;
     if (n == 0) return GBRT_OK;
     cudaStream_t s = ctx->stream;
-    if (bvh->nodes4)
+    if (bvh->nodes4 || bvh->nodes8)
     {
         GBRT_CUDA(ctx, cudaStreamSynchronize(s));
-        cudaFree(bvh->nodes4);
-        bvh->nodes4 = nullptr;
-        bvh->num_nodes4 = 0;
-        cudaFree(bvh->nodes4q);
-        bvh->nodes4q = nullptr;
+        free_wide_nodes(bvh);
     }
     if (n == 1)
     {

@@ -20,6 +20,7 @@
 // deliberate difference is the hemisphere sample's cos/sin, evaluated in double and
 // rounded once (the host's cosf/sinf may differ from that in the last bit).
 
+#include "instances.cuh"
 #include "pt_shade.cuh"
 
 #include <cmath>
@@ -37,6 +38,10 @@ struct gbrt_pt_scene
     uint32_t num_lights = 0;
     bool extended = false;      // some material is a mirror, glass or plastic
     gbrt::env_view* env = nullptr;   // device copy; null: the params' constant ambient light
+    // a scene over a two-level tree (gbrt_pt_scene_create_instanced): the tree and each
+    // instance's first material slot (device); bvh is null then
+    gbrt_tlas const* tlas = nullptr;
+    uint32_t* inst_geom = nullptr;
 };
 
 namespace gbrt {
@@ -192,8 +197,18 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend_sorted(frame_b
 }
 
 // One bounce for every live path of the queue.
+// A scene over a two-level tree: per instance its tree, its instance-to-world rows and
+// its first material slot; views null for a single tree.
+struct inst_shade
+{
+    const bvh_view* views;
+    const float4* forward;
+    const uint32_t* geom_base;
+    int32_t num_instances;
+};
+
 __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) pt_shade(frame_buffers fb, int q, shade_params sp,
-                                                   uint32_t* __restrict__ status)
+                                                   inst_shade is, uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     uint32_t n = fb.counts[q];
@@ -212,6 +227,24 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) pt_shade(frame_buffer
         tmin = r1.z;
         tmax = r1.w;
         uint4 hh = fb.hits[i];
+        if (is.views && int(hh.x) >= 0)
+        {
+            // the hit instance's triangle, carried to world space by shade_vertex
+            const int inst = int(hh.z);
+            if (inst >= 0 && inst < is.num_instances)
+            {
+                const bvh_view bv = is.views[inst];
+                sp.tris = bv.tris;
+                sp.num_tris = bv.num_tris;
+                sp.xform = is.forward + 3 * inst;
+                sp.geom_base = is.geom_base[inst];
+            }
+            else
+            {
+                atomicOr(status, kStatusBadIndex);
+                hh.x = 0xFFFFFFFFu;
+            }
+        }
         uint2 rf = fb.rng_flags[p];
         path_state st{ xyz(fb.throughput[p]), xyz(fb.radiance[p]), rf.x, rf.y };
         shade_vertex(sp, p, sp.bounce, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, int(hh.x),
@@ -279,6 +312,42 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow_sorted(frame_b
     {
         uint32_t p = fb.shadow_path[j];
         float4 c = fb.shadow_contrib[j];
+        float4 r = fb.radiance[p];
+        fb.radiance[p] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+    }
+}
+
+// pt_extend and pt_shadow over a two-level tree: hits carry the instance in z.
+__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend_tlas(frame_buffers fb, int q, tlas_view tv,
+                                                                       uint32_t* __restrict__ status)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i == 0)
+    {
+        fb.counts[q ^ 1] = 0;   // the shade kernel that follows appends to these
+        fb.counts[2] = 0;
+    }
+    uint32_t n = fb.counts[q];
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(&fb.rays[q][i]);
+    float4 r0 = rp[0], r1 = rp[1];
+    tlas_result h = traverse_tlas<false>(tv, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    fb.hits[i] = make_uint4(uint32_t(h.tri), __float_as_uint(h.t), uint32_t(h.inst), 0u);
+}
+
+__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow_tlas(frame_buffers fb, tlas_view tv,
+                                                                       uint32_t* __restrict__ status)
+{
+    uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t n = fb.counts[2];
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(&fb.shadow_rays[i]);
+    float4 r0 = rp[0], r1 = rp[1];
+    tlas_result h = traverse_tlas<true>(tv, { r0.x, r0.y, r0.z }, { r0.w, r1.x, r1.y }, r1.z, r1.w, status);
+    if (h.tri < 0)
+    {
+        uint32_t p = fb.shadow_path[i];
+        float4 c = fb.shadow_contrib[i];
         float4 r = fb.radiance[p];
         fb.radiance[p] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
     }
@@ -820,6 +889,43 @@ gbrt_status gbrt::light_records(gbrt_context* ctx, gbrt_light const* h_lights, u
     return GBRT_OK;
 }
 
+extern "C" gbrt_status gbrt_pt_scene_create_instanced(gbrt_context* ctx, gbrt_tlas const* tlas,
+                                                      gbrt_material const* h_materials, uint32_t num_materials,
+                                                      gbrt_light const* h_lights, uint32_t num_lights,
+                                                      uint32_t const* h_inst_geom, gbrt_pt_scene** out)
+{
+    if (!ctx) return GBRT_ERR_INVALID_ARG;
+    if (!out || !tlas) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_instanced: null tree or output");
+    *out = nullptr;
+    if ((num_materials && !h_materials) || (num_lights && !h_lights) || (tlas->num_instances && !h_inst_geom))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_instanced: null array");
+    for (uint32_t k = 0; k < num_materials; ++k)
+        if (h_materials[k].kind > GBRT_MATERIAL_PLASTIC)
+            return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_instanced: unknown material kind");
+    if (tlas->device != ctx->device) return fail(ctx, GBRT_ERR_INVALID_ARG, "pt_scene_create_instanced: tree on another device");
+    std::vector<float4> rec;
+    gbrt_status st = light_records(ctx, h_lights, num_lights, rec, "pt_scene_create_instanced");
+    if (st != GBRT_OK) return st;
+    gbrt_pt_scene* sc = nullptr;
+    st = create_scene(ctx, nullptr, h_materials, num_materials, rec, &sc);
+    if (st != GBRT_OK) return st;
+    sc->tlas = tlas;
+    if (tlas->num_instances)
+    {
+        device_guard g(ctx->device);
+        cudaError_t e = cudaMalloc(&sc->inst_geom, size_t(tlas->num_instances) * 4);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sc->inst_geom, h_inst_geom, size_t(tlas->num_instances) * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess)
+        {
+            gbrt_pt_scene_destroy(sc);
+            return check_cuda(ctx, e, "pt_scene_create_instanced");
+        }
+    }
+    *out = sc;
+    return GBRT_OK;
+}
+
 extern "C" gbrt_status gbrt_pinhole_camera_basis(gbrt_camera const* camera, uint32_t width, uint32_t height, float* out)
 {
     if (!camera || !out || width == 0 || height == 0) return GBRT_ERR_INVALID_ARG;
@@ -921,6 +1027,7 @@ extern "C" gbrt_status gbrt_pt_scene_destroy(gbrt_pt_scene* scene)
     cudaFree(scene->materials);
     cudaFree(scene->lights);
     cudaFree(scene->env);
+    cudaFree(scene->inst_geom);
     delete scene;
     return GBRT_OK;
 }
@@ -949,8 +1056,8 @@ shade_params shade_params_for(gbrt_context const* ctx, gbrt_pt_scene const* scen
     sp.num_materials = scene->num_materials;
     sp.lights = scene->lights;
     sp.num_lights = scene->num_lights;
-    sp.tris = scene->bvh->tris;
-    sp.num_tris = int32_t(scene->bvh->num_prims);
+    sp.tris = scene->bvh ? scene->bvh->tris : nullptr;   // instanced scenes: set per hit
+    sp.num_tris = scene->bvh ? int32_t(scene->bvh->num_prims) : 0;
     sp.epsilon = p.epsilon;
     sp.ambient = make_float3(p.ambient[0], p.ambient[1], p.ambient[2]);
     sp.frame = p.frame_id;
@@ -961,6 +1068,61 @@ shade_params shade_params_for(gbrt_context const* ctx, gbrt_pt_scene const* scen
     sp.emission = emission;
     sp.env = scene->env;
     return sp;
+}
+
+// The frame's average blended into accum and written to color (cuda_sched's blend).
+gbrt_status finish_frame(gbrt_context* ctx, frame_buffers const& fb, gbrt_pt_params const& p, uint32_t blocks,
+                         float* d_accum, float* d_color)
+{
+    const uint32_t n = p.width * p.height;
+    pt_blend<<<blocks, kBlock, 0, ctx->stream>>>(fb, n, float(p.spp), p.sfactor, p.dfactor,
+                                                 reinterpret_cast<float4*>(d_accum), reinterpret_cast<float4*>(d_color));
+    GBRT_LAUNCH_CHECK(ctx, "pt_blend");
+    return GBRT_OK;
+}
+
+// The wavefront frame of a scene over a two-level tree: each queue traced through the
+// top-level tree and the instances' trees (traverse_tlas), each hit shaded with its
+// instance's triangle carried to world space and its instance's material slots.
+gbrt_status render_frame_instanced(gbrt_context* ctx, gbrt_pt_scene const* scene, camera_basis const& cam,
+                                   gbrt_pt_params const& p, shade_params sp, float4 bg, uint32_t blocks,
+                                   float* d_accum, float* d_color)
+{
+    if (p.flags & (GBRT_PT_MEGAKERNEL | GBRT_PT_SORT_QUEUES))
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace: the megakernel and sorted queues take a single tree");
+    const uint32_t n = p.width * p.height;
+    cudaStream_t s = ctx->stream;
+    gbrt_tlas const* t = scene->tlas;
+    const tlas_view tv{ t->nodes, t->records, t->views, t->num_instances > 0 ? t->root : kEmptyLink,
+                        int32_t(t->num_inner), int32_t(t->num_instances) };
+    const inst_shade is{ t->views, t->forward, scene->inst_geom, int32_t(t->num_instances) };
+    frame_buffers fb;
+    gbrt_status st = frame_buffers_for(ctx, n, fb);
+    if (st != GBRT_OK) return st;
+    for (uint32_t smp = 0; smp < p.spp; ++smp)
+    {
+        sp.sample = smp;
+        pt_raygen<<<blocks, kBlock, 0, s>>>(fb, p.width, p.height, p.frame_id, smp, cam);
+        GBRT_LAUNCH_CHECK(ctx, "pt_raygen");
+        int q = 0;
+        for (uint32_t b = 0; b < p.num_bounces && t->num_instances > 0; ++b)
+        {
+            sp.bounce = b;
+            pt_extend_tlas<<<blocks, kBlock, 0, s>>>(fb, q, tv, ctx->d_status);
+            GBRT_LAUNCH_CHECK(ctx, "pt_extend_tlas");
+            pt_shade<<<blocks, kBlock, 0, s>>>(fb, q, sp, is, ctx->d_status);
+            GBRT_LAUNCH_CHECK(ctx, "pt_shade");
+            if (scene->num_lights > 0)
+            {
+                pt_shadow_tlas<<<blocks, kBlock, 0, s>>>(fb, tv, ctx->d_status);
+                GBRT_LAUNCH_CHECK(ctx, "pt_shadow_tlas");
+            }
+            q ^= 1;
+        }
+        pt_accumulate<<<blocks, kBlock, 0, s>>>(fb, n, smp, bg);
+        GBRT_LAUNCH_CHECK(ctx, "pt_accumulate");
+    }
+    return finish_frame(ctx, fb, p, blocks, d_accum, d_color);
 }
 
 // One frame of the wavefront path tracer into accum (blended) and color.
@@ -982,6 +1144,8 @@ gbrt_status render_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_cam
                             p.background[2] * p.background[3], 1.0f);
     const uint32_t blocks = (n + kBlock - 1) / kBlock;
     cudaStream_t s = ctx->stream;
+    if (scene->tlas)
+        return render_frame_instanced(ctx, scene, cam, p, sp, bg, blocks, d_accum, d_color);
     const bvh_view v = view_of(bvh);
     const bool wide = bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     if (p.flags & GBRT_PT_MEGAKERNEL)
@@ -1040,7 +1204,8 @@ gbrt_status render_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_cam
                     pt_extend<false><<<blocks, kBlock, 0, s>>>(fb, q, v, ctx->d_status);
                 }
                 GBRT_LAUNCH_CHECK(ctx, "pt_extend");
-                pt_shade<<<blocks, kBlock, 0, s>>>(fb, q, sp, ctx->d_status);
+                pt_shade<<<blocks, kBlock, 0, s>>>(fb, q, sp, inst_shade{ nullptr, nullptr, nullptr, 0 },
+                                                   ctx->d_status);
                 GBRT_LAUNCH_CHECK(ctx, "pt_shade");
                 if (scene->num_lights > 0)
                 {
@@ -1073,10 +1238,7 @@ gbrt_status render_frame(gbrt_context* ctx, gbrt_pt_scene const* scene, gbrt_cam
         pt_accumulate<<<blocks, kBlock, 0, s>>>(fb, n, smp, bg);
         GBRT_LAUNCH_CHECK(ctx, "pt_accumulate");
     }
-    pt_blend<<<blocks, kBlock, 0, s>>>(fb, n, float(p.spp), p.sfactor, p.dfactor, reinterpret_cast<float4*>(d_accum),
-                                       reinterpret_cast<float4*>(d_color));
-    GBRT_LAUNCH_CHECK(ctx, "pt_blend");
-    return GBRT_OK;
+    return finish_frame(ctx, fb, p, blocks, d_accum, d_color);
 }
 
 } // namespace
@@ -1122,6 +1284,8 @@ extern "C" gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene 
     gbrt_pt_params const& p = *params;
     if (p.num_bounces > uint32_t(kMaxReplay))
         return fail(ctx, GBRT_ERR_TOO_LARGE, "pathtrace_backward: at most 16 bounces");
+    if (scene->tlas)
+        return fail(ctx, GBRT_ERR_INVALID_ARG, "pathtrace_backward: the replay takes a scene over a single tree");
     gbrt_bvh const* bvh = scene->bvh;
     if (bvh->num_prims == 0 || scene->num_materials == 0) return GBRT_OK;   // nothing to differentiate
     device_guard g(ctx->device);

@@ -148,7 +148,19 @@ struct shade_params
     // (cos, sin) of 2 pi u for the 2^24 values of a draw u (gbrt_context::d_trig)
     const float2* trig;
     const env_view* env = nullptr;   // device record; null: the constant ambient light
+    // a hit inside an instance of a two-level tree: the instance's instance-to-world
+    // rows (3 float4: A | translation) and its first material slot; null / 0 for a hit
+    // in a single tree (tris then is the hit instance's tree's triangles)
+    const float4* xform = nullptr;
+    uint32_t geom_base = 0;
 };
+
+// The 3x3 rows of an instance-to-world map applied to a direction (an edge).
+__device__ __forceinline__ v3 apply_rows(const float4* __restrict__ r, v3 e)
+{
+    const float4 a = r[0], b = r[1], c = r[2];
+    return { a.x * e.x + a.y * e.y + a.z * e.z, b.x * e.x + b.y * e.y + b.z * e.z, c.x * e.x + c.y * e.y + c.z * e.z };
+}
 
 // remap_texture_coordinate (texture/detail/texture_common.h:91-126) for one axis of n
 // texels; clamp(x, a, b) = max(a, min(x, b)) (math/detail/math.h:530-533).
@@ -495,6 +507,14 @@ __device__ __forceinline__ void shade_vertex(shade_params const& sp, uint32_t p,
     float4 t2 = ldg4(&sp.tris[tri].t2);
     v3 e1 = xyz(t1), e2 = xyz(t2);
     uint32_t geom = __float_as_uint(t1.w);
+    if (sp.xform)
+    {
+        // the instance's triangle in world space (its normal and area), its material
+        // slot after the instance's first
+        e1 = apply_rows(sp.xform, e1);
+        e2 = apply_rows(sp.xform, e2);
+        geom += sp.geom_base;
+    }
     v3 view = -dir;
     v3 isect = ori + dir * t;
     v3 gn = normalize3(cross3(e1, e2));

@@ -14,12 +14,14 @@ namespace {
 
 constexpr int kTraceBlock = 128;
 // Entries of the traversal stack held in shared memory (the rest in local memory):
-// 16 x 128 threads x 4 B = 8 KB per block.
-constexpr int kSharedStack = 16;
-// Resident blocks the register allocation must allow (launch bounds): 12 blocks of 128
-// threads = 48 warps per SM at <= 40 registers (the closest-hit variant spills a few
-// words, and still runs faster than at 47 registers and 40 warps).
-constexpr int kMinBlocksAny = 12, kMinBlocksClosest = 12;
+// 8 x 128 threads x 4 B = 4 KB per block.
+constexpr int kSharedStack = 8;
+// Resident blocks the register allocation must allow (launch bounds): any hit 12 blocks
+// of 128 threads = 48 warps per SM at <= 40 registers; closest hit 16 blocks = 64 warps
+// at <= 32 registers.  Measured on the heightfield workload (kernel alone, hits
+// identical): closest 3.412 ms at 16 shared entries and 12 blocks, 3.389 / 3.386 at
+// 14 / 16 blocks, 3.297 at 8 shared entries and 16 blocks; 24 shared entries 3.662.
+constexpr int kMinBlocksAny = 12, kMinBlocksClosest = 16;
 
 // One ray through the node pairs (stack top in shared memory) or the 4-wide nodes.
 // Node layouts of the ray queries: the node pairs, the 4-wide nodes, the quantised
@@ -29,6 +31,7 @@ enum : int
     kNodesPairs = 0,
     kNodesWide = 1,
     kNodesCompressed = 2,
+    kNodesWide8 = 3,
 };
 
 template <bool AnyHit, int Nodes>
@@ -37,6 +40,8 @@ __device__ __forceinline__ trace_result trace_one(bvh_view const& v, f3 o, f3 d,
 {
     if constexpr (Nodes == kNodesCompressed)
         return traverse_bvh4<AnyHit>(v.nodes4q, v.num_nodes4, v.tris, v.num_tris, o, d, tmin, tmax, status);
+    else if constexpr (Nodes == kNodesWide8)
+        return traverse_bvhw<AnyHit, 8>(v.nodes8, v.num_nodes8, v.tris, v.num_tris, o, d, tmin, tmax, status);
     else
         return traverse_view_shared<AnyHit, Nodes == kNodesWide, kTraceBlock, kSharedStack>(v, o, d, tmin, tmax,
                                                                                               status);
@@ -311,10 +316,11 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         return GBRT_OK;
     }
     const bvh_view v = view_of(bvh);
-    const bool compressed = bvh->nodes4q != nullptr && (ctx->trace_flags & GBRT_TRACE_COMPRESSED_NODES);
-    const bool wide = !compressed && bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
+    const bool wide8 = bvh->nodes8 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE8_NODES);
+    const bool compressed = !wide8 && bvh->nodes4q != nullptr && (ctx->trace_flags & GBRT_TRACE_COMPRESSED_NODES);
+    const bool wide = !wide8 && !compressed && bvh->nodes4 != nullptr && (ctx->trace_flags & GBRT_TRACE_WIDE_NODES);
     const bool have_scratch = scratch && scratch_bytes >= trace_scratch_bytes(n);
-    const bool persistent = (ctx->trace_flags & GBRT_TRACE_PERSISTENT) && !wide && !compressed && have_scratch;
+    const bool persistent = (ctx->trace_flags & GBRT_TRACE_PERSISTENT) && !wide && !compressed && !wide8 && have_scratch;
     const uint32_t* perm = nullptr;
     if ((ctx->trace_flags & GBRT_TRACE_SORT_RAYS) && n >= kSortMinRays && have_scratch)
     {
@@ -341,7 +347,9 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
             kernel_timer timer(ctx, stream);
             auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, perm, d_hits,
                                                                                         ctx->d_status); };
-            if (compressed)
+            if (wide8)
+                any_hit ? launch(trace_rays_permuted<true, kNodesWide8>) : launch(trace_rays_permuted<false, kNodesWide8>);
+            else if (compressed)
                 any_hit ? launch(trace_rays_permuted<true, kNodesCompressed>)
                         : launch(trace_rays_permuted<false, kNodesCompressed>);
             else if (wide)
@@ -370,7 +378,9 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
     }
     kernel_timer timer(ctx, stream);
     auto launch = [&](auto kernel) { kernel<<<blocks, kTraceBlock, 0, stream>>>(v, d_rays, n, d_hits, ctx->d_status); };
-    if (compressed)
+    if (wide8)
+        any_hit ? launch(trace_rays<true, kNodesWide8>) : launch(trace_rays<false, kNodesWide8>);
+    else if (compressed)
         any_hit ? launch(trace_rays<true, kNodesCompressed>) : launch(trace_rays<false, kNodesCompressed>);
     else if (wide)
         any_hit ? launch(trace_rays<true, kNodesWide>) : launch(trace_rays<false, kNodesWide>);

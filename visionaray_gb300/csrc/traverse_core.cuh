@@ -16,6 +16,8 @@
 #include "api_internal.h"
 #include "device_math.cuh"
 
+#include <type_traits>
+
 namespace gbrt {
 
 constexpr int kEmptyLink = INT32_MIN;   // stack sentinel: neither an inner node nor a leaf
@@ -58,9 +60,42 @@ struct shared_stack
     __device__ __forceinline__ int get(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
 };
 
+// shared_stack whose top entry stays in a register: a push stores the previous top to
+// its slot, a pop returns the register and loads the entry below it, so the value a
+// pop needs is never waiting on a shared-memory load (the load of the next top has a
+// whole node visit to complete).  The same slots and capacity as shared_stack.
+template <int Shared, int Total, int Stride>
+struct regtop_stack
+{
+    static_assert(Total > Shared, "the local part holds at least one entry");
+    static constexpr int capacity = Total;
+    int* col;
+    int spill[Total - Shared];
+    int top = 0;   // entry sp - 1
+    __device__ __forceinline__ void store(int i, int v)
+    {
+        if (i < Shared)
+            col[i * Stride] = v;
+        else
+            spill[i - Shared] = v;
+    }
+    __device__ __forceinline__ int load(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
+    __device__ __forceinline__ void set(int i, int v)
+    {
+        if (i > 0) store(i - 1, top);
+        top = v;
+    }
+    __device__ __forceinline__ int get(int i)
+    {
+        const int v = top;
+        if (i > 0) top = load(i - 1);
+        return v;
+    }
+};
+
 // The next stack entry to visit, kEmptyLink when the stack is empty.
 template <class StackT>
-__device__ __forceinline__ int pop_entry(StackT const& stack, int& sp)
+__device__ __forceinline__ int pop_entry(StackT& stack, int& sp)
 {
     return sp > 0 ? stack.get(--sp) : kEmptyLink;
 }
@@ -187,8 +222,8 @@ __device__ __forceinline__ trace_result traverse_bvh(const bvh2_node* __restrict
     return traverse_bvh_with<AnyHit>(stack, nodes, tris, root, num_inner, num_tris, o, d, tmin, tmax, status);
 }
 
-// The four child boxes and links of a 4-wide node: eight loads of the plain node ...
-__device__ __forceinline__ void decode4(const bvh4_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
+// The child boxes and links of a wide node: eight loads of the plain 4-wide node ...
+__device__ __forceinline__ void decode_node(const bvh4_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
                                         float hy[4], float lz[4], float hz[4], int ch[4], int ct[4])
 {
     float4 lox = ldg4(&np->lox), hix = ldg4(&np->hix);
@@ -206,9 +241,37 @@ __device__ __forceinline__ void decode4(const bvh4_node* __restrict__ np, float 
     ct[0] = ct4.x, ct[1] = ct4.y, ct[2] = ct4.z, ct[3] = ct4.w;
 }
 
+// ... or eight 256-bit loads of the 8-wide node (one per plane, then the links) ...
+__device__ __forceinline__ void ld8(const void* p, float r[8])
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7])
+        : "l"(p));
+}
+
+__device__ __forceinline__ void decode_node(const bvh8_node* __restrict__ np, float lx[8], float hx[8], float ly[8],
+                                        float hy[8], float lz[8], float hz[8], int ch[8], int ct[8])
+{
+    ld8(np->lox, lx);
+    ld8(np->hix, hx);
+    ld8(np->loy, ly);
+    ld8(np->hiy, hy);
+    ld8(np->loz, lz);
+    ld8(np->hiz, hz);
+    float c[8], n[8];
+    ld8(np->child, c);
+    ld8(np->count, n);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+    {
+        ch[k] = __float_as_int(c[k]);
+        ct[k] = __float_as_int(n[k]);
+    }
+}
+
 // ... or four loads of the quantised node, decoded as origin + q * 2^e rounded down for
 // the low and up for the high planes (q * 2^e is exact), so no box shrinks.
-__device__ __forceinline__ void decode4(const bvh4q_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
+__device__ __forceinline__ void decode_node(const bvh4q_node* __restrict__ np, float lx[4], float hx[4], float ly[4],
                                         float hy[4], float lz[4], float hz[4], int ch[4], int ct[4])
 {
     const uint4* w = reinterpret_cast<const uint4*>(np);
@@ -240,37 +303,39 @@ __device__ __forceinline__ void decode4(const bvh4q_node* __restrict__ np, float
     ct[3] = int(int16_t(w2.w >> 16));
 }
 
-// The same query over 4-wide nodes (bvh_layout.cuh, plain or quantised): one node
-// fetch tests four boxes; hit leaves are tested at once (so best.t shrinks before the
-// inner children are ordered), the hit inner children are visited nearest first and
-// the others pushed with their entry distance, so a popped entry already beyond the
-// best hit is dropped without a fetch.
-template <bool AnyHit, typename Node4>
-__device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ nodes4, int32_t num_nodes4,
+// The same query over W-wide nodes (bvh_layout.cuh: 4-wide plain or quantised,
+// 8-wide), from node `root`: one node fetch tests W boxes; hit leaves are tested at
+// once (so best.t shrinks before the inner children are ordered), the hit inner
+// children are visited nearest first and the others pushed with their entry distance,
+// so a popped entry already beyond the best hit is dropped without a fetch.
+template <bool AnyHit, int W, typename NodeW>
+__device__ __forceinline__ trace_result traverse_bvhw(const NodeW* __restrict__ nodesw, int32_t num_nodesw,
                                                       const tri48* __restrict__ tris, int32_t num_tris, f3 o, f3 d,
-                                                      float tmin, float tmax, uint32_t* __restrict__ status)
+                                                      float tmin, float tmax, uint32_t* __restrict__ status,
+                                                      int32_t root = 0)
 {
+    constexpr int kStackW = W == 4 ? kStack4 : kStack8;
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
     trace_result best{ -1, FLT_MAX, 0.0f, 0.0f };
-    int stack_node[kStack4];
-    float stack_t[kStack4];
+    int stack_node[kStackW];
+    float stack_t[kStackW];
     int sp = 0;
-    int node = 0;
+    int node = root;
 
     while (true)
     {
-        if (node < 0 || node >= num_nodes4)
+        if (node < 0 || node >= num_nodesw)
         {
             atomicOr(status, kStatusBadIndex);
             break;
         }
-        float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
-        int ch[4], ct[4];
-        decode4(nodes4 + node, lx, hx, ly, hy, lz, hz, ch, ct);
-        float tn[4];
-        bool hit[4];
+        float lx[W], hx[W], ly[W], hy[W], lz[W], hz[W];
+        int ch[W], ct[W];
+        decode_node(nodesw + node, lx, hx, ly, hy, lz, hz, ch, ct);
+        float tn[W];
+        bool hit[W];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < W; ++k)
         {
             float x0 = (lx[k] - o.x) * ix, x1 = (hx[k] - o.x) * ix;
             float y0 = (ly[k] - o.y) * iy, y1 = (hy[k] - o.y) * iy;
@@ -281,7 +346,7 @@ __device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ 
         }
         // leaves first
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < W; ++k)
         {
             if (!hit[k] || ct[k] <= 0) continue;
             int end = ch[k] + ct[k];
@@ -305,12 +370,12 @@ __device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ 
                 }
             }
         }
-        // inner children nearest first: a 4-element insertion order by entry distance
-        int order[4];
-        float dist[4];
+        // inner children nearest first: a W-element insertion order by entry distance
+        int order[W];
+        float dist[W];
         int m = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < W; ++k)
         {
             if (!hit[k] || ct[k] != 0 || !(tn[k] < best.t)) continue;
             int pos = m;
@@ -328,7 +393,7 @@ __device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ 
         {
             for (int j = m - 1; j >= 1; --j)
             {
-                if (sp < kStack4)
+                if (sp < kStackW)
                 {
                     stack_node[sp] = order[j];
                     stack_t[sp] = dist[j];
@@ -358,6 +423,15 @@ __device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ 
     return best;
 }
 
+// traverse_bvhw over 4-wide nodes from the root (node 0).
+template <bool AnyHit, typename Node4>
+__device__ __forceinline__ trace_result traverse_bvh4(const Node4* __restrict__ nodes4, int32_t num_nodes4,
+                                                      const tri48* __restrict__ tris, int32_t num_tris, f3 o, f3 d,
+                                                      float tmin, float tmax, uint32_t* __restrict__ status)
+{
+    return traverse_bvhw<AnyHit, 4>(nodes4, num_nodes4, tris, num_tris, o, d, tmin, tmax, status);
+}
+
 // Segment lookup of the batched kernels: the s with offs[s] <= i < offs[s + 1]
 // (offs: count + 1 non-decreasing entries, offs[count] > i).
 __device__ __forceinline__ uint32_t upper_segment(const uint32_t* __restrict__ offs, uint32_t count, uint32_t i)
@@ -380,14 +454,15 @@ struct bvh_view
     const bvh2_node* nodes;
     const bvh4_node* nodes4;
     const bvh4q_node* nodes4q;
+    const bvh8_node* nodes8;
     const tri48* tris;
-    int32_t root, num_inner, num_nodes4, num_tris;
+    int32_t root, num_inner, num_nodes4, num_tris, num_nodes8;
 };
 
 inline bvh_view view_of(gbrt_bvh const* b)
 {
-    return { b->nodes, b->nodes4, b->nodes4q, b->tris, b->root, int32_t(b->num_inner), int32_t(b->num_nodes4),
-             int32_t(b->num_prims) };
+    return { b->nodes, b->nodes4, b->nodes4q, b->nodes8, b->tris, b->root, int32_t(b->num_inner),
+             int32_t(b->num_nodes4), int32_t(b->num_prims), int32_t(b->num_nodes8) };
 }
 
 // Wide: the 4-wide nodes (present for trees with inner nodes built by the LBVH builder).
@@ -401,7 +476,7 @@ __device__ __forceinline__ trace_result traverse_view(bvh_view const& v, f3 o, f
 
 // A query through the node pairs with the stack's first Shared entries in shared
 // memory (a column per thread of a Block-thread block), or through the 4-wide nodes.
-template <bool AnyHit, bool Wide, int Block, int Shared>
+template <bool AnyHit, bool Wide, int Block, int Shared, bool RegTop = false>
 __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
                                                              uint32_t* __restrict__ status)
 {
@@ -412,7 +487,8 @@ __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, 
     else
     {
         __shared__ int stack_mem[Shared * Block];
-        shared_stack<Shared, kStackSize, Block> stack;
+        std::conditional_t<RegTop, regtop_stack<Shared, kStackSize, Block>, shared_stack<Shared, kStackSize, Block>>
+            stack;
         stack.col = stack_mem + threadIdx.x;
         return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
                                          status);

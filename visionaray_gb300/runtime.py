@@ -36,6 +36,7 @@ SIGNATURES = {
     "gbrt_kernel_launch_count": (_u64, [_vp]),
     "gbrt_context_set_kernel_timing": (_i32, [_vp, _i32]),
     "gbrt_bvh_rebuild_lbvh": (_i32, [_vp, _vp, _vp, _u32]),
+    "gbrt_pt_scene_create_instanced": (_i32, [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _pp]),
     "gbrt_context_kernel_times": (_i32, [_vp, _vp, _u32, _vp]),
     "gbrt_context_set_trace_flags": (_i32, [_vp, _u32]),
     "gbrt_context_set_trace_refill": (_i32, [_vp, _u32]),
@@ -147,6 +148,7 @@ class Context:
     TRACE_WIDE_NODES = 2
     TRACE_PERSISTENT = 4
     TRACE_COMPRESSED_NODES = 8
+    TRACE_WIDE8_NODES = 16
 
     def set_trace_flags(self, flags):
         """GBRT_TRACE_* options of the ray queries (TRACE_SORT_RAYS: coherent order)."""
@@ -368,6 +370,25 @@ class PTScene:
         self.h = h
         self._env = None
 
+    @classmethod
+    def over_instances(cls, tlas, materials, lights, inst_geom):
+        """make_kernel_params over a two-level tree (gbrt_pt_scene_create_instanced):
+        rays traced through the TLAS's instances, a hit shaded with its instance's
+        triangle in world space and material slot inst_geom[instance] + geom_id."""
+        from .types import lights_of_area_lights
+        self = cls.__new__(cls)
+        self.bvh, self.tlas, self.ctx = None, tlas, tlas.ctx
+        mats = np.ascontiguousarray(materials, MATERIAL)
+        lts = (np.ascontiguousarray(lights, LIGHT) if np.asarray(lights).dtype == LIGHT
+               else lights_of_area_lights(lights))
+        geom = np.ascontiguousarray(inst_geom, np.uint32)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbrt_pt_scene_create_instanced(self.ctx.h, tlas.h, _hptr(mats), len(mats),
+                                                                   _hptr(lts), len(lts), _hptr(geom), ctypes.byref(h)))
+        self.h = h
+        self._env = None
+        return self
+
     def set_environment(self, texels, filter=FILTER_LINEAR, address=ADDRESS_CLAMP, scale=(1.0, 1.0, 1.0),
                         light_to_world=None):
         """environment_light in place of the ambient light: texels is an (h, w, 4)
@@ -526,7 +547,11 @@ class Batch:
 
     @launch.setter
     def launch(self, value):
-        arr = np.asarray([tuple(int(v) for v in value)], BATCH_LAUNCH)
+        """(block, tile, stack, order[, width[, sort]]): width defaults to 2 (node
+        pairs), sort to 0."""
+        v = [int(x) for x in (tuple(value) if not isinstance(value, np.void) else value.tolist())]
+        v += [2, 0][len(v) - 4:] if len(v) < 6 else []
+        arr = np.asarray([tuple(v)], BATCH_LAUNCH)
         self.ctx.check(self.ctx.lib.gbrt_batch_set_launch(self.h, _hptr(arr)))
 
     def height(self):

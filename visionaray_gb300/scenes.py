@@ -104,6 +104,56 @@ def box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0):
     return tris, mats, lights
 
 
+def instanced_box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0, albedo_seed=9):
+    """box_scene's room with its blobs as instances of ONE noisy icosphere (visionaray's
+    index_bvh_inst_t use): the room (12 wall triangles + the 2-triangle ceiling light)
+    is one tree, the unit blob (20*subdiv^2 triangles, centred at the origin, radius
+    ~1) another; blob k is the unit blob scaled by a radius U[0.03, 0.08] and moved to a
+    centre inside the box (seeded).  Material slots: the room's 14, then one per
+    triangle of every blob instance (Lambertian albedo U[0.2, 0.8]).  Returns a dict:
+    room, blob (triangles), transforms (n_blobs x 12: visionaray's mat4x3, columns),
+    materials, lights, inst_geom (the first material slot of the room and of each
+    blob), flat (the same scene flattened into one triangle array: each blob's
+    triangles carried to world space in float32, geom_id = its material slot)."""
+    room, mats, lights = box_scene(n_blobs=0, subdiv=subdiv, seed=seed, light_y=light_y, emission=emission)
+    one, _, _ = box_scene(n_blobs=1, subdiv=subdiv, seed=seed, light_y=light_y, emission=emission)
+    blob = one[14:].copy()
+    v = np.concatenate([blob["v1"], blob["v1"] + blob["e1"], blob["v1"] + blob["e2"]]).astype(np.float64)
+    c0 = v.mean(axis=0)
+    r0 = float(np.sqrt(((v - c0) ** 2).sum(axis=1)).max())
+    blob["v1"] = ((blob["v1"].astype(np.float64) - c0) / r0).astype(np.float32)
+    blob["e1"] = (blob["e1"].astype(np.float64) / r0).astype(np.float32)
+    blob["e2"] = (blob["e2"].astype(np.float64) / r0).astype(np.float32)
+    nb = len(blob)
+    blob["geom_id"] = np.arange(nb, dtype=np.uint32)
+    blob["prim_id"] = np.arange(nb, dtype=np.uint32)
+    transforms = np.zeros((n_blobs, 12), np.float32)
+    radius = np.array([0.03 + 0.05 * u01(seed, 500, k) for k in range(n_blobs)], np.float32)
+    centre = np.array([[(radius[k] * 1.2) + (1.0 - 2.4 * radius[k]) * u01(seed, 501 + a, k) for a in range(3)]
+                       for k in range(n_blobs)], np.float32)
+    transforms[:, 0] = transforms[:, 4] = transforms[:, 8] = radius
+    transforms[:, 9:12] = centre
+    from .types import MATERIAL, MATTE
+    rng = np.random.default_rng(albedo_seed)
+    blob_mats = np.zeros(n_blobs * nb, MATERIAL)
+    blob_mats["kind"] = MATTE
+    blob_mats["color"] = rng.uniform(0.2, 0.8, size=(n_blobs * nb, 3)).astype(np.float32)
+    blob_mats["scale"] = 1.0
+    materials = np.concatenate([mats, blob_mats])
+    inst_geom = np.concatenate([[0], 14 + nb * np.arange(n_blobs)]).astype(np.uint32)
+    flat = np.empty(14 + n_blobs * nb, TRIANGLE)
+    flat[:14] = room
+    for k in range(n_blobs):
+        t = flat[14 + k * nb:14 + (k + 1) * nb]
+        t["v1"] = blob["v1"] * radius[k] + centre[k]
+        t["e1"] = blob["e1"] * radius[k]
+        t["e2"] = blob["e2"] * radius[k]
+        t["geom_id"] = 14 + k * nb + blob["geom_id"]
+        t["prim_id"] = 14 + k * nb + blob["prim_id"]
+    return {"room": room, "blob": blob, "transforms": transforms, "materials": materials, "lights": lights,
+            "inst_geom": inst_geom, "flat": flat}
+
+
 def specular_box_scene(n_blobs=256, subdiv=22, seed=1, light_y=0.999, emission=15.0, cycle=None):
     """box_scene whose blobs take their material kinds from `cycle` in turn (default
     matte, mirror, glass): a gold-like mirror (conductor Fresnel: ior (0.27, 0.42, 1.35),

@@ -63,7 +63,8 @@ PT_PARAMS = np.dtype([("width", "<u4"), ("height", "<u4"), ("spp", "<u4"), ("num
 INSTANCE = np.dtype([("blas", "<u8"), ("transform", "<f4", (12,))])
 HIT_INST = np.dtype([("prim_id", "<u4"), ("inst_id", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),
                      ("geom_id", "<u4"), ("reserved", "<u4", (2,))])
-BATCH_LAUNCH = np.dtype([("block", "<u4"), ("tile", "<u4"), ("stack", "<u4"), ("order", "<u4")])
+BATCH_LAUNCH = np.dtype([("block", "<u4"), ("tile", "<u4"), ("stack", "<u4"), ("order", "<u4"), ("width", "<u4"),
+                         ("sort", "<u4")])
 MATTE, EMISSIVE, MIRROR, GLASS, PLASTIC = 0, 1, 2, 3, 4
 BATCH_ORDER_ROWS, BATCH_ORDER_BLOCKS = 0, 1
 PT_SHADOW_RANGE_FIX = 1
@@ -77,5 +78,5 @@ FLT_MAX = float(np.finfo(np.float32).max)
 assert TRIANGLE.itemsize == 44 and RAY.itemsize == 32
 assert HIT.itemsize == 16 and BVH_NODE.itemsize == 32
 assert MATERIAL.itemsize == 64 and AREA_LIGHT.itemsize == 60 and CAMERA.itemsize == 40
-assert PT_PARAMS.itemsize == 64 and BATCH_LAUNCH.itemsize == 16
+assert PT_PARAMS.itemsize == 64 and BATCH_LAUNCH.itemsize == 24
 assert INSTANCE.itemsize == 56 and HIT_INST.itemsize == 32
