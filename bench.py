@@ -203,6 +203,15 @@ class ClockSampler:
         return out
 
 
+def workload_config(grid, origins, n_closest, n_any, n_tris, builder="lbvh"):
+    """The line's `config`: the workload alone, identical in both arms (what each run
+    measured beside it goes elsewhere in the line)."""
+    return {"workload": WORKLOAD if (grid, origins) == (GRID, ORIGINS) else
+            f"REDUCED profiling case: heightfield {grid}x{grid}, {origins} origins",
+            "rays_per_step": n_closest, "closest_rays": n_closest, "anyhit_rays": n_any, "triangles": n_tris,
+            "builder": builder, "l2": "inputs larger than L2 (no flush)"}
+
+
 def cpu_baseline(tris, closest, ao, rank_print=print, sample_every=4, repeats=1, any_repeats=1):
     """The reference's CPU path (oracle restatement, binned-SAH tree, all host threads)
     on every `sample_every`-th origin: its closest-hit ray `repeats` times, then its AO
@@ -263,8 +272,9 @@ def run_reference(args):
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD + " (each step a bounded sample, see cpu_baseline.sample)",
-                       "l2": "inputs larger than L2"},
+            "config": workload_config(args.grid, args.origins, len(closest), len(ao), len(tris)),
+            "run": {"sample": "each step a bounded sample of the workload (cpu_baseline.sample)",
+                    "threads": res["cores"]},
             "cpu_baseline": base,
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -322,11 +332,61 @@ def run_pathtrace(vg, ctx, frames, flags, rprint, builder="ploc", scene_kind="bo
         peak, kind = measured_hbm_peak()
         res["roofline"] = roofline_of(samples, ms * 1e-3, B_SAMPLE_BOX, peak, f"{kind} hbm_gbs",
                                       "frame: every kernel of the wavefront frame (extend, shade, shadow)")
+    if scene_kind == "box" and flags == 0:
+        res["instanced"] = run_pathtrace_instanced(vg, ctx, frames, builder)
     if cpu:
         res["cpu_baseline"] = pt_cpu_baseline(tris, mats, lights, cam,
                                               scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES,
                                                                frame_id=1, flags=flags), 61)
     return res
+
+
+def run_pathtrace_instanced(vg, ctx, frames, builder):
+    """The box frame with its 256 blobs as instances of one 9,680-triangle blob
+    (gbrt_pt_scene_create_instanced: a two-level tree, the room and the blob trees),
+    against the same geometry flattened into one tree: Msamples/s and tree bytes."""
+    import torch
+    from visionaray_gb300 import scenes
+    d = scenes.instanced_box_scene(n_blobs=256, subdiv=22, seed=1)
+    make = vg.ploc_builder if builder == "ploc" else vg.lbvh_builder
+    room = make(ctx).build(vg.as_device_bytes(d["room"], ctx.device))
+    blob = make(ctx).build(vg.as_device_bytes(d["blob"], ctx.device))
+    ident = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0]
+    tlas = vg.TLAS([(room, ident)] + [(blob, xf) for xf in d["transforms"]], ctx)
+    scene_i = vg.PTScene.over_instances(tlas, d["materials"], d["lights"], d["inst_geom"])
+    flat = make(ctx).build(vg.as_device_bytes(d["flat"], ctx.device))
+    scene_f = vg.PTScene(flat, d["materials"], d["lights"])
+    cam = scenes.box_camera()
+    dev = f"cuda:{ctx.device}"
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = {"workload": f"{PT_WIDTH}x{PT_HEIGHT}, {PT_SPP} spp, depth {PT_BOUNCES}: the box room + 256 instances of one "
+                       f"{len(d['blob'])}-triangle blob (radii U[0.03, 0.08]), per-instance-triangle albedo",
+           "builder": builder}
+
+    def tree_bytes(n):   # node pairs + leaf triangles
+        return max(n - 1, 0) * 64 + n * 48
+
+    for name, sc in (("instanced", scene_i), ("flattened", scene_f)):
+        accum = torch.zeros((PT_HEIGHT, PT_WIDTH, 4), dtype=torch.float32, device=dev)
+        vg.pathtrace_frame(sc, cam, scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES), accum=accum)
+        ctx.synchronize()
+        ev[0].record(ctx.stream)
+        for f in range(frames):
+            vg.pathtrace_frame(sc, cam, scenes.pt_params(PT_WIDTH, PT_HEIGHT, PT_SPP, num_bounces=PT_BOUNCES,
+                                                         frame_id=f + 1), accum=accum)
+        ev[1].record(ctx.stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / frames
+        out[name] = {"ms_per_frame": round(ms, 2),
+                     "msamples_s": round(PT_WIDTH * PT_HEIGHT * PT_SPP / (ms * 1e-3) / 1e6, 2),
+                     "image_mean": round(float(accum[..., :3].mean().item()), 5)}
+    out["instanced"]["tree_bytes"] = tree_bytes(len(d["room"])) + tree_bytes(len(d["blob"])) + 64 * 256
+    out["flattened"]["tree_bytes"] = tree_bytes(len(d["flat"]))
+    for x in (scene_i, scene_f):
+        x.close()
+    tlas.close()
+    return out
 
 
 BATCH_WORKLOAD = ("512 random-soup scenes (triangle counts log-uniform in [1k, 1M], vertex offsets 0.5/cbrt(n)), "
@@ -391,6 +451,25 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
     ev[1].record(ctx.stream)
     torch.cuda.synchronize()
     frame_ms = ev[0].elapsed_time(ev[1])
+
+    # every BVH width x ray order at the tuner's block, tile, stack and pixel order: one
+    # graph step each (build, the collapse and the pixel sort where the shape has them,
+    # the frame), after a replay that captures it
+    tuned = tuple(int(best[k]) for k in best.dtype.names)
+    width_sort_ms = {}
+    for w, srt in ((2, 0), (2, 1), (4, 0), (4, 1), (8, 0), (8, 1)):
+        batch.launch = tuned[:4] + (w, srt)
+        batch.run_graph(d_tris, images)
+        ctx.synchronize()
+        ev[0].record(ctx.stream)
+        batch.run_graph(d_tris, images)
+        ev[1].record(ctx.stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        width_sort_ms[f"width{w}_sort{srt}"] = round(ev[0].elapsed_time(ev[1]), 2)
+    batch.launch = tuned
+    batch.run_graph(d_tris, images)
+    ctx.synchronize()
 
     plain_images = torch.full_like(images, -1.0)
     no_lights = np.zeros(0, AREA_LIGHT)
@@ -461,7 +540,8 @@ def run_batch(vg, ctx, steps, plain_steps, rprint, num_scenes=512, max_tris=1_00
            "batched": {"ms_per_step": round(batch_ms, 2), "msamples_s": round(samples / (batch_ms * 1e-3) / 1e6, 2),
                        "frame_kernel_ms": round(frame_ms, 2), "gpu_launches_per_step": int(batch_launches),
                        "steps": steps, "launch": {k: int(best[k]) for k in best.dtype.names},
-                       "autotune_frame_ms": round(float(tune_ms), 2), "autotune_s": round(tune_s, 1)},
+                       "autotune_frame_ms": round(float(tune_ms), 2), "autotune_s": round(tune_s, 1),
+                       "graph_step_ms_by_width_and_sort": width_sort_ms},
            "plain": res_plain, "plain_preallocated": res_pre, "speedup": speedup,
            "images_bit_identical": identical, "image_mean": round(mean, 5)}
     peak, kind = measured_hbm_peak()
@@ -785,13 +865,9 @@ def run_ours(args):
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD if (args.grid, args.origins) == (GRID, ORIGINS) else
-                       f"REDUCED profiling case: heightfield {args.grid}x{args.grid}, {args.origins} origins",
-                       "rays_per_step": n_c, "closest_rays": n_c, "anyhit_rays": n_a,
-                       "triangles": int(len(tris)), "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
-                       "trace_flags": args.trace_flags, "trace_refill": args.trace_refill,
-                       "warmup_steps_run": done, "builder": args.builder},
+            "config": workload_config(args.grid, args.origins, n_c, n_a, int(len(tris)), args.builder),
+            "run": {"parallelism": f"replicas x{world}", "build_ms": round(build_ms, 3),
+                    "trace_flags": args.trace_flags, "trace_refill": args.trace_refill, "warmup_steps_run": done},
             "kernels": per, "roofline": roofline,
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_c * 32),
                     "d2h_bytes_per_step": int(n_c * 16), "matches_device_path": same,

@@ -52,6 +52,8 @@ def test_bench_line_has_the_contract_keys():
     b = d["batched_pathtrace"]
     assert b["plain_preallocated"]["images_bit_identical"] is True and b["roofline"]["frac"] > 0
     assert d["pathtrace"]["roofline"]["b_sample"] > 0
+    inst = d["pathtrace"]["instanced"]
+    assert inst["instanced"]["msamples_s"] > 0 and inst["instanced"]["tree_bytes"] < inst["flattened"]["tree_bytes"]
     assert d["adjoint"]["roofline"]["forward"]["bound"] == "l2"
     assert set(d["adjoint"]["albedo_error_end"]) == set(d["adjoint"]["albedo_error_start"])
 

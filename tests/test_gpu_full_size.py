@@ -127,47 +127,56 @@ def inverse_setup():
 
 
 def central_differences(setup, picks, h=1e-3):
-    """[(slot, channel, adjoint, fd, cond)] for each (slot, channel) in picks: fd =
-    (L(a + h) - L(a - h)) / (the float32 step actually applied) of the GPU forward at
-    the forward frame's random numbers; cond = the sum of the gradient's terms' sizes
-    (the replay with |dL/dI| as the image adjoint) over |adjoint|: the gradient's
-    condition as a sum of per-path terms of both signs."""
+    """[(slot, channel, adjoint, fd, spread, cond)] for each (slot, channel) in picks:
+    fd = (L(a + h) - L(a - h)) / (the float32 step actually applied) of the GPU forward
+    at the forward frame's random numbers; spread = the largest difference of fd from
+    the same quotient at 0.73 h and 1.37 h (the image is a polynomial in the albedos, so
+    in exact arithmetic they agree to O(h^2), ~1e-6 relative: the spread measures the
+    FP32 forward's rounding noise in the quotient); cond = the sum of the gradient's
+    per-path terms by size (the replay with |dL/dI| as the image adjoint) over
+    |adjoint|."""
     ctx, scene, tris, mats, lights, cam, target, albedo, emission, params, adj, ga, ge = setup
     ga_np = ga.cpu().numpy()
     gabs, _ = vg.pathtrace_backward(scene, cam, params, albedo, emission, adj.abs())
     gabs_np = gabs.cpu().numpy()
-    rows = []
-    for slot, c in picks:
+
+    def fd_at(slot, c, step):
         ap, am = albedo.clone(), albedo.clone()
-        ap[slot, c] += h
-        am[slot, c] -= h
+        ap[slot, c] += step
+        am[slot, c] -= step
         lp = inverse.l2_adjoint(vg.pathtrace_forward(scene, cam, params, ap, emission), target)[0]
         lm = inverse.l2_adjoint(vg.pathtrace_forward(scene, cam, params, am, emission), target)[0]
-        fd = (lp - lm) / float(ap[slot, c] - am[slot, c])
+        return (lp - lm) / float(ap[slot, c] - am[slot, c])
+
+    rows = []
+    for slot, c in picks:
+        fd = fd_at(slot, c, h)
+        spread = max(abs(fd - fd_at(slot, c, 0.73 * h)), abs(fd - fd_at(slot, c, 1.37 * h)))
         g = float(ga_np[slot, c])
         cond = float(gabs_np[slot, c]) / abs(g) if g != 0.0 else (0.0 if gabs_np[slot, c] == 0 else np.inf)
-        rows.append((slot, c, g, fd, cond, float(gabs_np[slot, c])))
+        rows.append((slot, c, g, fd, spread, cond))
     ctx.synchronize()
     return rows
 
 
-def check_rows(rows, label, min_well_conditioned):
-    """A gradient whose terms cancel to less than 1 % of their summed size (cond > 100)
-    is beyond what FP32 arithmetic resolves to 1e-3 -- in the forward pass the central
-    difference is taken of, and in the adjoint's own sums; every other gradient is held
-    to 1e-3 relative of its central difference with no allowance, the ill-conditioned
-    ones to 1e-3 relative plus 1e-5 of their terms' summed size (~170 FP32 ulps of it).
-    A slot no path reaches has no gradient either way (exact zeros)."""
-    well = [r for r in rows if r[3] != 0.0 and r[4] <= 100.0]
-    worst = max((abs(g - fd) / abs(fd) for _, _, g, fd, _, _ in well), default=0.0)
-    print(f"{label}: {sum(1 for r in rows if r[3] != 0)} nonzero, {len(well)} with cond <= 100, worst relative "
-          f"error of those {worst:.3g}; cond of the others: {sorted(round(r[4]) for r in rows if r[4] > 100.0)}")
-    for slot, c, g, fd, cond, gabs in rows:
-        if cond <= 100.0:
-            assert abs(g - fd) <= 1e-3 * abs(fd), (slot, c, g, fd, cond)
+def check_rows(rows, label, min_resolved):
+    """A gradient the central difference resolves -- its spread over step sizes below
+    1e-4 of it, its terms not cancelling below 1 % of their summed size -- is held to
+    1e-3 relative of that difference with no allowance; at least min_resolved of the
+    64 are.  The others (a parameter that moves the image by less than the FP32
+    forward's rounding in the pixels it touches) are held to 1e-3 plus four times the
+    measured spread.  A slot no path reaches has no gradient either way (exact zeros)."""
+    resolved = [r for r in rows if r[3] != 0.0 and r[4] <= 1e-4 * abs(r[3]) and r[5] <= 100.0]
+    worst = max((abs(g - fd) / abs(fd) for _, _, g, fd, _, _ in resolved), default=0.0)
+    print(f"{label}: {sum(1 for r in rows if r[3] != 0)} nonzero, {len(resolved)} resolved, worst relative error "
+          f"of those {worst:.3g}")
+    for r in rows:
+        slot, c, g, fd, spread, cond = r
+        if r in resolved:
+            assert abs(g - fd) <= 1e-3 * abs(fd), (slot, c, g, fd, spread, cond)
         else:
-            assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-5 * gabs, (slot, c, g, fd, cond)
-    assert len(well) >= min_well_conditioned
+            assert abs(g - fd) <= 1e-3 * abs(fd) + 4.0 * spread, (slot, c, g, fd, spread, cond)
+    assert len(resolved) >= min_resolved
 
 
 def test_inverse_albedo_adjoint_full_size_central_differences_seen_slots(inverse_setup):
@@ -186,7 +195,7 @@ def test_inverse_albedo_adjoint_full_size_central_differences_all_slots(inverse_
     matte = np.flatnonzero(mats["kind"] != EMISSIVE)
     rng = np.random.default_rng(2025)
     picks = [(int(matte[k // 3]), int(k % 3)) for k in rng.choice(len(matte) * 3, 64, replace=False)]
-    check_rows(central_differences(inverse_setup, picks), "all slots", 16)
+    check_rows(central_differences(inverse_setup, picks), "all slots", 12)
 
 
 def test_inverse_albedo_adjoint_full_size_against_fp64_host_adjoint(inverse_setup, oracle):
