@@ -413,8 +413,8 @@ gbrt_status gbrt_pt_scene_create_lights(gbrt_context* ctx, gbrt_bvh const* bvh,
  * (h_inst_geom: one host entry per instance).  Lights as for
  * gbrt_pt_scene_create_lights, in world space.  gbrt_pathtrace_frame and
  * gbrt_pathtrace_forward render it (wavefront scheduling only: not with
- * GBRT_PT_MEGAKERNEL or GBRT_PT_SORT_QUEUES); gbrt_pathtrace_backward takes a scene
- * over a single tree.  The tlas and its trees must outlive the scene.                */
+ * GBRT_PT_MEGAKERNEL or GBRT_PT_SORT_QUEUES) and gbrt_pathtrace_backward replays its
+ * paths (gradients per material slot).  The tlas and its trees must outlive the scene. */
 gbrt_status gbrt_pt_scene_create_instanced(gbrt_context* ctx, gbrt_tlas const* tlas,
                                            gbrt_material const* h_materials, uint32_t num_materials,
                                            gbrt_light const* h_lights, uint32_t num_lights,
@@ -480,7 +480,9 @@ gbrt_status gbrt_pathtrace_forward(gbrt_context* ctx, gbrt_pt_scene const* scene
  * numbers -- the same shading code as the forward frame, so the same path -- and its
  * vertices swept backwards; nothing of the forward frame is stored (memory O(pixels)).
  * Gradients are accumulated with warp-reduced FP32 atomics.  Geometry, visibility and
- * roulette decisions are not differentiated.  num_bounces <= 16.                  */
+ * roulette decisions are not differentiated.  num_bounces <= 16.  A scene over
+ * instances (gbrt_pt_scene_create_instanced) replays through the same two-level tree;
+ * a slot's gradient sums the vertices of every instance that uses the slot.      */
 gbrt_status gbrt_pathtrace_backward(gbrt_context* ctx, gbrt_pt_scene const* scene,
                                     gbrt_camera const* camera, gbrt_pt_params const* params,
                                     const float* d_albedo, const float* d_emission,

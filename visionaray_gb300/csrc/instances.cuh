@@ -27,9 +27,11 @@ struct tlas_result
     float t, u, v;
 };
 
-template <bool AnyHit>
-__device__ __forceinline__ tlas_result traverse_tlas(tlas_view const& tv, f3 o, f3 d, float tmin, float tmax,
-                                                     uint32_t* __restrict__ status)
+// bstack: the bottom-level traversals' stack (a local_stack, or a shared_stack whose
+// top entries sit in shared memory); the top level keeps its own 32 entries.
+template <bool AnyHit, class BlasStack>
+__device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tlas_view const& tv, f3 o, f3 d,
+                                                          float tmin, float tmax, uint32_t* __restrict__ status)
 {
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
     tlas_result best{ -1, -1, FLT_MAX, 0.0f, 0.0f };
@@ -98,7 +100,6 @@ __device__ __forceinline__ tlas_result traverse_tlas(tlas_view const& tv, f3 o, 
         const bvh_view bv = tv.views[inst];
         if (bv.num_tris > 0)
         {
-            local_stack<kStackSize> bstack;
             trace_result h = traverse_bvh_with<AnyHit>(bstack, bv.nodes, bv.tris, bv.root, bv.num_inner, bv.num_tris,
                                                        oo, dd, tmin, tmax, status, best.t);
             if (h.tri >= 0)
@@ -110,6 +111,26 @@ __device__ __forceinline__ tlas_result traverse_tlas(tlas_view const& tv, f3 o, 
         node = sp > 0 ? stack[--sp] : kEmptyLink;
     }
     return best;
+}
+
+template <bool AnyHit>
+__device__ __forceinline__ tlas_result traverse_tlas(tlas_view const& tv, f3 o, f3 d, float tmin, float tmax,
+                                                     uint32_t* __restrict__ status)
+{
+    local_stack<kStackSize> bstack;
+    return traverse_tlas_with<AnyHit>(bstack, tv, o, d, tmin, tmax, status);
+}
+
+// traverse_tlas with the bottom-level stack's first Shared entries in shared memory (a
+// column per thread of a Block-thread block).
+template <bool AnyHit, int Block, int Shared>
+__device__ __forceinline__ tlas_result traverse_tlas_shared(tlas_view const& tv, f3 o, f3 d, float tmin, float tmax,
+                                                            uint32_t* __restrict__ status)
+{
+    __shared__ int stack_mem[Shared * Block];
+    shared_stack<Shared, kStackSize, Block> bstack;
+    bstack.col = stack_mem + threadIdx.x;
+    return traverse_tlas_with<AnyHit>(bstack, tv, o, d, tmin, tmax, status);
 }
 
 } // namespace gbrt
