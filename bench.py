@@ -43,9 +43,10 @@ N_NODE_CLOSEST, N_TRI_CLOSEST = 76.92786217, 7.44575715   # B_ray = 2867.1 bytes
 N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
-# of the full-size workload with the default ray order).
-TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.375e9 + 0.153e9, 2.620e9 + 0.530e9
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, mean of two
+# launches each in one ncu capture of the full-size workload with the default ray
+# order and the shipped kernel build).
+TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.800e9 + 0.240e9, 2.641e9 + 0.542e9
 
 
 # Algorithmic bytes per path-traced sample, B_sample = sum of B_ray over the sample's
@@ -784,7 +785,7 @@ def run_ours(args):
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "b_ray": round(b_ray(N_NODE_CLOSEST, N_TRI_CLOSEST), 1),
                 "timing": "CUDA events around the traversal kernel on its stream, mean over the timed launches",
-                "limiter": "latency of dependent node fetches under divergence (ncu: DRAM ~10 % of peak)"}
+                "limiter": "latency of dependent node fetches under divergence (ncu: DRAM ~14 % of peak)"}
     # the pure-I/O floor (48 B per ray: the ray in, the hit out) and the DRAM bandwidth
     # the launch actually drew (its ncu traffic over its event time)
     io_gbs = d["rays"] * 48 / (d["kernel_ms_per_launch"] * 1e-3) / 1e9
@@ -832,7 +833,8 @@ def run_ours(args):
         from oracle import bench_reference_gpu, ref_gpu
         if ref_gpu.available():
             rg = ref_gpu.ReferenceGPU(local)
-            reference_gpu = {"traversal": bench_reference_gpu.traversal(rg, ctx, d_tris, bvh, d_closest, d_ao, 3)}
+            reference_gpu = {"traversal": bench_reference_gpu.traversal(rg, ctx, d_tris, bvh, d_closest, d_ao, 3),
+                             "lbvh_build": bench_reference_gpu.lbvh_build(rg, ctx, d_tris, 3)}
             if args.pt_frames > 0:
                 reference_gpu["pathtrace"] = bench_reference_gpu.pathtrace(rg, ctx, 16, 1)
             del rg

@@ -9,7 +9,8 @@ Workloads are bench.py's: the 2048x2048 heightfield (8,388,608 triangles) with
 4,194,304 closest-hit and 33,554,432 any-hit AO rays, traced by visionaray's
 closest_hit / any_hit over the cuda_index_bvh that its GPU lbvh_builder produces for
 these triangles (the product's export, byte-identical to it), one thread per ray, best
-of 64/128/256-thread blocks; and the closed-box path-tracing scene at 1920x1080,
+of 64/128/256-thread blocks; visionaray's GPU LBVH build of those triangles (its
+kernels, CUB's merge sort), compared with the product's tree byte for byte; and the closed-box path-tracing scene at 1920x1080,
 depth 8, through pathtracing::kernel one thread per pixel in cuda_sched's 16x16 blocks.
 The product runs its default configuration on the same inputs.  Times are CUDA events
 on the launching stream, median of `reps` after a warm-up; prints one JSON line.
@@ -19,6 +20,8 @@ import json
 import os
 import statistics
 import sys
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
@@ -77,6 +80,36 @@ def traversal(ref, ctx, d_tris, bvh, d_c, d_a, reps):
                           "ao_occlusion_equal": float(((ha["prim_id"] != NO_HIT) == (ra["prim_id"] != NO_HIT)).mean())}}
 
 
+def lbvh_build(ref, ctx, d_tris, reps):
+    """visionaray's GPU LBVH build (lbvh_builder::build, detail/bvh/lbvh.h:681-844: its
+    own kernels, CUB's stable merge sort, the primitive copy) against the product's
+    build of the same triangles: the trees compared byte for byte (nodes and indices of
+    the reference's cuda_index_bvh layout; the product's through gbrt_bvh_export_bvh2),
+    then both timed.  The reference's device arrays are allocated once, outside its
+    timed builds (its own build allocates them on every call); the product is timed
+    both ways: the public build (allocates the tree) and the in-place rebuild (none)."""
+    import torch
+
+    import visionaray_gb300 as vg
+    n = d_tris.numel() // 44
+    b = ref.lbvh_buffers(n)
+    nodes_r, idx_r = ref.lbvh_build(d_tris, b)
+    bvh = vg.lbvh_builder(ctx).build(d_tris)
+    nodes_o, idx_o = bvh.export_bvh2()
+    torch.cuda.synchronize()
+    same_nodes = bool(np.array_equal(nodes_r.cpu().numpy(), np.ascontiguousarray(nodes_o).view(np.uint8)))
+    same_idx = bool(np.array_equal(idx_r.cpu().numpy(), np.ascontiguousarray(idx_o).view(np.uint8)))
+    ms_r = timed(lambda: ref.lbvh_build(d_tris, b), reps)
+    ms_o = timed(lambda: vg.lbvh_builder(ctx).build(d_tris), reps)
+    ms_rebuild = timed(lambda: bvh.rebuild(d_tris), reps)
+    ctx.synchronize()
+    return {"triangles": int(n), "tree_nodes_identical": same_nodes, "tree_indices_identical": same_idx,
+            "reference_gpu_ms": round(ms_r, 3), "ours_build_ms": round(ms_o, 3), "ours_rebuild_ms": round(ms_rebuild, 3),
+            "speedup": round(ms_r / ms_o, 2), "speedup_rebuild": round(ms_r / ms_rebuild, 2),
+            "note": "reference timed without its per-build allocations; sort = CUB DeviceMergeSort::StableSortKeys "
+                    "as the reference calls it"}
+
+
 def pathtrace(ref, ctx, spp, reps, builder="lbvh"):
     """visionaray's pathtracing::kernel (one thread per pixel, 16x16 blocks) and the
     product's frame on the box scene at 1920x1080, depth 8, through the same tree."""
@@ -133,7 +166,8 @@ def main():
     d_tris = vg.as_device_bytes(tris)
     bvh = vg.lbvh_builder(ctx).build(d_tris)
     res = {"workload": bench.WORKLOAD, "traversal": traversal(ref, ctx, d_tris, bvh, vg.device_rays(closest),
-                                                               vg.device_rays(ao), args.reps)}
+                                                               vg.device_rays(ao), args.reps),
+           "lbvh_build": lbvh_build(ref, ctx, d_tris, args.reps)}
     del bvh, d_tris
     torch.cuda.empty_cache()
     res["pathtrace"] = pathtrace(ref, ctx, args.pt_spp, max(1, args.reps // 2))

@@ -2,6 +2,8 @@
 
 Products, all git-ignored and rebuilt on every machine:
   oracle/_build/liboracle.so             the CPU restatement (oracle.cpp, pathtrace.cpp)
+  oracle/_build/libref_sort.so           CUB's stable merge sort of the reference GPU LBVH
+                                         build's prim refs (ref_sort.cu; CUDA toolkit only)
   oracle/_ref/libvsnray_ref.so           visionaray's own CPU code, compiled from its
                                          unmodified headers (ref_driver.cpp)
   oracle/_ref/vsnray_ref_gpu.cubin       visionaray's own GPU traversal and path tracer
@@ -27,6 +29,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 LIBORACLE = os.path.join(HERE, "_build", "liboracle.so")
+LIBSORT = os.path.join(HERE, "_build", "libref_sort.so")
 LIBREF = os.path.join(HERE, "_ref", "libvsnray_ref.so")
 REFCUBIN = os.path.join(HERE, "_ref", "vsnray_ref_gpu.cubin")
 REFCUBIN_EXACT = os.path.join(HERE, "_ref", "vsnray_ref_gpu_exact.cubin")
@@ -67,6 +70,11 @@ def build(verbose=False, with_reference=True):
     if _stale(LIBORACLE, deps):
         os.makedirs(os.path.dirname(LIBORACLE), exist_ok=True)
         jobs.append(("oracle", CXX_FLAGS + ["-o", LIBORACLE] + srcs + ["-lpthread"]))
+    sort_src = os.path.join(HERE, "ref_sort.cu")
+    if _stale(LIBSORT, [sort_src]):
+        os.makedirs(os.path.dirname(LIBSORT), exist_ok=True)
+        jobs.append(("ref-sort", [NVCC, "-shared", "-Xcompiler", "-fPIC", "-O3", "-std=c++17"] + ARCH +
+                     [sort_src, "-o", LIBSORT]))
     have_ref = with_reference and reference_available()
     ref_src = os.path.join(HERE, "ref_driver.cpp")
     if have_ref and _stale(LIBREF, deps + [ref_src]):

@@ -322,7 +322,7 @@ extern "C" __global__ void vsnray_ref_pathtrace_ext(const tree_ref_t* refs, cons
 }
 
 // sizeof of the visionaray objects the host allocates arrays of: tree ref, material,
-// light.
+// light, and the GPU LBVH build's construction node, prim ref and box.
 extern "C" __global__ void vsnray_ref_sizes(unsigned* out)
 {
     out[0] = unsigned(sizeof(tree_ref_t));
@@ -330,4 +330,22 @@ extern "C" __global__ void vsnray_ref_sizes(unsigned* out)
     out[2] = unsigned(sizeof(light_t));
     out[3] = unsigned(sizeof(mat_ext_t));
     out[4] = unsigned(sizeof(light_ext_t));
+    out[5] = unsigned(sizeof(detail::lbvh::node));
+    out[6] = unsigned(sizeof(detail::lbvh::prim_ref));
+    out[7] = unsigned(sizeof(aabb));
 }
+
+// visionaray's GPU LBVH build kernels (detail/bvh/lbvh.h:215-466), kept in this cubin
+// so that oracle/ref_gpu.py can launch them in lbvh_builder::build's order
+// (lbvh.h:681-844) and time the reference's GPU build beside the product's.  Taking
+// their addresses instantiates them (the bounds kernel for the triangle type); they
+// keep the reference's names, which the loader finds by enumerating the module.
+void* vsnray_ref_lbvh_kernels[] = {
+    reinterpret_cast<void*>(&detail::lbvh::compute_bounds_and_centroids<triangle_t>),
+    reinterpret_cast<void*>(&detail::lbvh::assign_morton_codes),
+    reinterpret_cast<void*>(&detail::lbvh::init_nodes),
+    reinterpret_cast<void*>(&detail::lbvh::build_hierarchy),
+    reinterpret_cast<void*>(&detail::lbvh::assign_node_bounds),
+    reinterpret_cast<void*>(&detail::lbvh::collapse),
+    reinterpret_cast<void*>(&detail::lbvh::sequence),
+};

@@ -12,6 +12,7 @@ the product imports it.
 """
 import ctypes
 import os
+import re
 
 import numpy as np
 
@@ -20,6 +21,10 @@ CUBIN = os.path.join(HERE, "_ref", "vsnray_ref_gpu.cubin")               # nvcc 
 CUBIN_EXACT = os.path.join(HERE, "_ref", "vsnray_ref_gpu_exact.cubin")   # --fmad=false
 KERNELS = ("vsnray_ref_closest_hit", "vsnray_ref_any_hit", "vsnray_ref_pt_setup", "vsnray_ref_pathtrace",
            "vsnray_ref_pt_setup_ext", "vsnray_ref_pathtrace_ext", "vsnray_ref_sizes")
+# visionaray's GPU LBVH build kernels (detail/bvh/lbvh.h:215-466), by their own names
+LBVH_KERNELS = ("compute_bounds_and_centroids", "assign_morton_codes", "init_nodes", "build_hierarchy",
+                "assign_node_bounds", "collapse", "sequence")
+LIBSORT = os.path.join(HERE, "_build", "libref_sort.so")
 
 
 def available(exact=False):
@@ -82,8 +87,9 @@ class ReferenceGPU:
         sizes = torch.zeros(8, dtype=torch.int32, device=self.dev)
         self._launch("vsnray_ref_sizes", (1, 1, 1), (1, 1, 1), [vp(sizes.data_ptr())])
         torch.cuda.synchronize()
-        self.size_ref, self.size_mat, self.size_light, self.size_mat_ext, self.size_light_ext = (
-            int(x) for x in sizes.tolist()[:5])
+        (self.size_ref, self.size_mat, self.size_light, self.size_mat_ext, self.size_light_ext, self.size_node,
+         self.size_prim_ref, self.size_aabb) = (int(x) for x in sizes.tolist())
+        self.lbvh = None
 
     def _check(self, err, what):
         if err != 0:
@@ -165,3 +171,107 @@ class ReferenceGPU:
                      [vp(scene["refs"].data_ptr()), vp(scene["mats"].data_ptr()), vp(scene["lights"].data_ptr()),
                       ctypes.c_uint(scene["nl"]), cam, par, vp(accum.data_ptr())])
         return accum
+
+    # -- visionaray's GPU LBVH build (lbvh_builder::build, detail/bvh/lbvh.h:681-844) --
+
+    def _lbvh_kernels(self):
+        """The build's kernels of the cubin, found by enumerating the module (they keep
+        the reference's internal-linkage names)."""
+        if self.lbvh is not None:
+            return self.lbvh
+        cu, vp = self.cu, ctypes.c_void_p
+        cu.cuModuleGetFunctionCount.argtypes = [ctypes.POINTER(ctypes.c_uint), vp]
+        cu.cuModuleEnumerateFunctions.argtypes = [ctypes.POINTER(vp), ctypes.c_uint, vp]
+        cu.cuFuncGetName.argtypes = [ctypes.POINTER(ctypes.c_char_p), vp]
+        count = ctypes.c_uint()
+        self._check(cu.cuModuleGetFunctionCount(ctypes.byref(count), self.mod), "cuModuleGetFunctionCount")
+        funcs = (vp * count.value)()
+        self._check(cu.cuModuleEnumerateFunctions(funcs, count, self.mod), "cuModuleEnumerateFunctions")
+        names = {}
+        for f in funcs:
+            nm = ctypes.c_char_p()
+            self._check(cu.cuFuncGetName(ctypes.byref(nm), f), "cuFuncGetName")
+            names[nm.value.decode()] = vp(f)
+        found = {}
+        for k in LBVH_KERNELS:
+            pat = re.compile(r"4lbvhL?%d%s[EI]" % (len(k), k))
+            hits = [n for n in names if pat.search(n)]
+            if len(hits) != 1:
+                raise RuntimeError(f"LBVH kernel {k}: {len(hits)} matches in the cubin")
+            found[k] = names[hits[0]]
+        sort = ctypes.CDLL(LIBSORT)
+        sort.vsnray_ref_sort_bytes.argtypes = [ctypes.c_uint32]
+        sort.vsnray_ref_sort_bytes.restype = ctypes.c_size_t
+        sort.vsnray_ref_sort.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_uint32, vp]
+        sort.vsnray_ref_sort.restype = ctypes.c_int
+        self.lbvh = (found, sort)
+        return self.lbvh
+
+    def _launch_fn(self, fn, count, args, what):
+        block = 1024   # the build's num_threads
+        ptrs = (ctypes.c_void_p * len(args))(*[ctypes.addressof(a) for a in args])
+        stream = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        self._check(self.cu.cuLaunchKernel(fn, (count + block - 1) // block, 1, 1, block, 1, 1, 0, stream, ptrs, None),
+                    what)
+
+    def lbvh_buffers(self, n):
+        """Device buffers of one build of n >= 2 triangles: the build's own arrays
+        (bounds, centroids, prim refs, construction nodes), the output tree (2n - 1
+        nodes, n triangles, n indices) and the sort's temporary storage.  Allocated once,
+        outside the timed build (the reference allocates them on every build)."""
+        if n < 2:
+            raise ValueError("the timed build takes at least two triangles")
+        torch = self.torch
+        _, sort = self._lbvh_kernels()
+        temp_bytes = int(sort.vsnray_ref_sort_bytes(n))
+        if temp_bytes == 0:
+            raise RuntimeError("cub::DeviceMergeSort::StableSortKeys: no temporary storage size")
+
+        def buf(nbytes):
+            return torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=self.dev)
+
+        flt = np.finfo(np.float32).max
+        invalid = np.tile(np.array([flt, flt, flt, -flt, -flt, -flt], np.float32), 2)   # aabb::invalidate
+        assert self.size_aabb == 24 and self.size_prim_ref == 8
+        return {"n": n, "invalid": torch.from_numpy(invalid.view(np.uint8)).to(self.dev),
+                "bounds": buf(2 * self.size_aabb), "prim_bounds": buf(n * self.size_aabb),
+                "centroids": buf(n * 12), "prim_refs": buf(n * self.size_prim_ref),
+                "inner": buf((n - 1) * self.size_node), "leaves": buf(n * self.size_node),
+                "nodes": buf((2 * n - 1) * 32), "prims": buf(n * 44), "indices": buf(n * 4),
+                "temp": buf(temp_bytes), "temp_bytes": temp_bytes}
+
+    def lbvh_build(self, tris, b):
+        """lbvh_builder::build(cuda_index_bvh<basic_triangle<3, float>>{}, tris, n) on the
+        current stream: the reference's kernels in its order with its launch shape
+        (1024-thread blocks), CUB's stable merge sort of the prim refs, the device copy of
+        the primitives and the index sequence; into the buffers of lbvh_buffers(n)."""
+        fns, sort = self._lbvh_kernels()
+        vp, n = ctypes.c_void_p, b["n"]
+
+        def p(name):
+            return vp(b[name].data_ptr())
+
+        bounds = b["bounds"]
+        bounds.copy_(b["invalid"])
+        scene_b, centroid_b = vp(bounds.data_ptr()), vp(bounds.data_ptr() + self.size_aabb)
+        self._launch_fn(fns["compute_bounds_and_centroids"], n,
+                        [p("prim_bounds"), p("centroids"), scene_b, centroid_b, vp(tris.data_ptr()), ctypes.c_int(n)],
+                        "compute_bounds_and_centroids")
+        self._launch_fn(fns["assign_morton_codes"], n, [p("prim_refs"), p("centroids"), centroid_b, ctypes.c_int(n)],
+                        "assign_morton_codes")
+        stream = vp(self.torch.cuda.current_stream().cuda_stream)
+        err = sort.vsnray_ref_sort(p("temp"), b["temp_bytes"], p("prim_refs"), n, stream)
+        if err != 0:
+            raise RuntimeError(f"cub::DeviceMergeSort::StableSortKeys: cudaError {err}")
+        self._launch_fn(fns["init_nodes"], n - 1, [p("inner"), ctypes.c_size_t(n - 1)], "init_nodes")
+        self._launch_fn(fns["init_nodes"], n, [p("leaves"), ctypes.c_size_t(n)], "init_nodes")
+        self._launch_fn(fns["build_hierarchy"], n, [p("inner"), p("leaves"), p("prim_refs"), ctypes.c_int(n)],
+                        "build_hierarchy")
+        self._launch_fn(fns["assign_node_bounds"], n,
+                        [p("inner"), p("leaves"), p("prim_bounds"), p("prim_refs"), ctypes.c_int(n)],
+                        "assign_node_bounds")
+        self._launch_fn(fns["collapse"], n, [p("nodes"), p("inner"), p("leaves"), p("prim_refs"), ctypes.c_int(n)],
+                        "collapse")
+        b["prims"][:n * 44].copy_(tris.reshape(-1)[:n * 44])
+        self._launch_fn(fns["sequence"], n, [p("indices"), ctypes.c_uint(n)], "sequence")
+        return b["nodes"][:(2 * n - 1) * 32], b["indices"][:n * 4]

@@ -48,6 +48,31 @@ def test_reference_gpu_traversal_agrees(ref):
             assert np.percentile(ulp_diff(ours["t"][same], theirs["t"][same]), 99.9) <= 64
 
 
+@pytest.mark.parametrize("exact", [False, True])
+@pytest.mark.parametrize("kind", ["soup", "heightfield"])
+def test_reference_gpu_lbvh_build_equals_ours(kind, exact):
+    """visionaray's own GPU LBVH build (its kernels in lbvh_builder::build's order, CUB's
+    stable merge sort) gives the product's tree byte for byte: nodes in the reference's
+    cuda_index_bvh layout and the index array, on a random soup (many equal Morton
+    codes) and a heightfield, from both reference builds (the bounds and Morton
+    arithmetic has no multiply-add to contract)."""
+    tris = scenes.soup(65536, seed=3) if kind == "soup" else scenes.heightfield(grid=256, seed=2)
+    d_tris = vg.as_device_bytes(tris)
+    ref = ref_gpu.ReferenceGPU(0, exact=exact)
+    b = ref.lbvh_buffers(len(tris))
+    nodes_r, idx_r = ref.lbvh_build(d_tris, b)
+    bvh = vg.lbvh_builder().build(d_tris)
+    nodes_o, idx_o = bvh.export_bvh2()
+    torch.cuda.synchronize()
+    first = nodes_r.cpu().numpy()   # a copy: the next build reuses the buffers
+    assert np.array_equal(first, np.ascontiguousarray(nodes_o).view(np.uint8))
+    assert np.array_equal(idx_r.cpu().numpy(), np.ascontiguousarray(idx_o).view(np.uint8))
+    # a second build into the same buffers gives the same tree
+    nodes_2, _ = ref.lbvh_build(d_tris, b)
+    torch.cuda.synchronize()
+    assert np.array_equal(nodes_2.cpu().numpy(), first)
+
+
 def render_pair(exact, tris, mats, lights, cam, params):
     d_tris = vg.as_device_bytes(tris)
     bvh = vg.lbvh_builder().build(d_tris)
