@@ -243,8 +243,9 @@ class ReferenceGPU:
     def lbvh_build(self, tris, b):
         """lbvh_builder::build(cuda_index_bvh<basic_triangle<3, float>>{}, tris, n) on the
         current stream: the reference's kernels in its order with its launch shape
-        (1024-thread blocks), CUB's stable merge sort of the prim refs, the device copy of
-        the primitives and the index sequence; into the buffers of lbvh_buffers(n)."""
+        (1024-thread blocks), CUB's stable merge sort of the prim refs, the zero fill of
+        the node array its resize does, the device copy of the primitives and the index
+        sequence; into the buffers of lbvh_buffers(n)."""
         fns, sort = self._lbvh_kernels()
         vp, n = ctypes.c_void_p, b["n"]
 
@@ -267,6 +268,9 @@ class ReferenceGPU:
         self._launch_fn(fns["init_nodes"], n, [p("leaves"), ctypes.c_size_t(n)], "init_nodes")
         self._launch_fn(fns["build_hierarchy"], n, [p("inner"), p("leaves"), p("prim_refs"), ctypes.c_int(n)],
                         "build_hierarchy")
+        # tree.nodes().resize(2n - 1) value-initialises the nodes (zeros); set_leaf leaves
+        # a leaf's two ordered-traversal bytes as they were, so they stay zero
+        b["nodes"].zero_()
         self._launch_fn(fns["assign_node_bounds"], n,
                         [p("inner"), p("leaves"), p("prim_bounds"), p("prim_refs"), ctypes.c_int(n)],
                         "assign_node_bounds")

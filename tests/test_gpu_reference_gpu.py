@@ -60,6 +60,8 @@ def test_reference_gpu_lbvh_build_equals_ours(kind, exact):
     d_tris = vg.as_device_bytes(tris)
     ref = ref_gpu.ReferenceGPU(0, exact=exact)
     b = ref.lbvh_buffers(len(tris))
+    for name in ("prim_bounds", "centroids", "prim_refs", "inner", "leaves", "nodes", "prims", "indices"):
+        b[name].fill_(0xA5)   # the build must not depend on what the buffers held
     nodes_r, idx_r = ref.lbvh_build(d_tris, b)
     bvh = vg.lbvh_builder().build(d_tris)
     nodes_o, idx_o = bvh.export_bvh2()
