@@ -305,11 +305,13 @@ gbrt_status build_lbvh_in_scratch(gbrt_context* ctx, gbrt_triangle const* d_tris
                                   size_t scratch_bytes, gbrt_bvh_node* d_nodes, uint32_t* d_indices);
 
 // radix_sort.cu: stable LSD sort of (key, value) pairs by the low `key_bits` bits.
-// Result lands in (keys, values); keys_alt/values_alt are same-sized scratch.
+// Result lands in (keys, values); keys_alt/values_alt are same-sized scratch.  With
+// sorted_values non-null nothing is copied back: *sorted_values is values or
+// values_alt, whichever the last pass wrote.
 size_t radix_sort_scratch_bytes(uint32_t n);
 gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values,
                              uint32_t* keys_alt, uint32_t* values_alt, uint32_t n, int key_bits,
-                             void* scratch, cudaStream_t stream);
+                             void* scratch, cudaStream_t stream, uint32_t** sorted_values = nullptr);
 inline gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values,
                                     uint32_t* keys_alt, uint32_t* values_alt, uint32_t n, int key_bits,
                                     void* scratch)

@@ -11,6 +11,8 @@
 //   3. scatter: each warp ranks its 512 keys in input order with __match_any_sync, the
 //      tile is reordered by digit in shared memory, and every digit's run is written
 //      out contiguously (coalesced) at its scanned offset.
+// An odd number of passes ends in the alternate buffers: the result is copied back
+// unless the caller asks where the sorted values are (sorted_values).
 
 #include "api_internal.h"
 
@@ -35,15 +37,35 @@ __global__ void __launch_bounds__(kThreads) count_digits(const uint32_t* __restr
     __shared__ uint32_t hist[kRadix];
     for (int d = threadIdx.x; d < kRadix; d += kThreads) hist[d] = 0;
     __syncthreads();
-    uint64_t base = uint64_t(blockIdx.x) * kTile;
-#pragma unroll 4
-    for (int k = 0; k < kItems; ++k)
+    const uint64_t base = uint64_t(blockIdx.x) * kTile;
+    if (base + kTile <= n)
     {
-        uint64_t i = base + uint64_t(k) * kThreads + threadIdx.x;
-        if (i < n)
+        // a full tile: four 128-bit loads per thread, all issued before the first use
+        // (tiles start at multiples of 4096 keys of a 256-byte aligned array)
+        const uint4* k4 = reinterpret_cast<const uint4*>(keys + base);
+        uint4 v[kItems / 4];
+#pragma unroll
+        for (int j = 0; j < kItems / 4; ++j) v[j] = __ldg(&k4[j * kThreads + threadIdx.x]);
+#pragma unroll
+        for (int j = 0; j < kItems / 4; ++j)
         {
-            uint32_t d = (__ldg(&keys[i]) >> shift) & (kRadix - 1);
-            atomicAdd(&hist[d], 1u);
+            atomicAdd(&hist[(v[j].x >> shift) & (kRadix - 1)], 1u);
+            atomicAdd(&hist[(v[j].y >> shift) & (kRadix - 1)], 1u);
+            atomicAdd(&hist[(v[j].z >> shift) & (kRadix - 1)], 1u);
+            atomicAdd(&hist[(v[j].w >> shift) & (kRadix - 1)], 1u);
+        }
+    }
+    else
+    {
+#pragma unroll 4
+        for (int k = 0; k < kItems; ++k)
+        {
+            uint64_t i = base + uint64_t(k) * kThreads + threadIdx.x;
+            if (i < n)
+            {
+                uint32_t d = (__ldg(&keys[i]) >> shift) & (kRadix - 1);
+                atomicAdd(&hist[d], 1u);
+            }
         }
     }
     __syncthreads();
@@ -139,10 +161,17 @@ __global__ void __launch_bounds__(kScanBlock) scan_apply(uint32_t* __restrict__ 
     }
 }
 
-__global__ void __launch_bounds__(kThreads) scatter_digits(
+// Resident blocks of the scatter kernel the register allocation must allow: 5 x 256
+// threads at <= 48 registers (no spills; 5 x 43 KB of shared memory also fit).  The ranking keeps one packed word per item (rank within
+// the warp's 512 keys in the low half, digit in the high half); keys and values are
+// read again, from L1, when the tile is reordered.  Holding keys, values and ranks in
+// registers through the block prefix took 111 registers (2 blocks per SM).
+constexpr int kScatterMinBlocks = 5;
+
+__global__ void __launch_bounds__(kThreads, kScatterMinBlocks) scatter_digits(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
-    const uint32_t* __restrict__ offsets, uint32_t tiles, int identity_values)
+    const uint32_t* __restrict__ offsets, uint32_t tiles)
 {
     __shared__ uint32_t warp_hist[kWarps][kRadix];
     __shared__ uint32_t digit_start[kRadix];   // exclusive start of each digit in the tile
@@ -160,22 +189,20 @@ __global__ void __launch_bounds__(kThreads) scatter_digits(
     for (int d = lane; d < kRadix; d += 32) warp_hist[warp][d] = 0;
     __syncwarp();
 
-    uint32_t key[kItems], val[kItems], rank[kItems];
+    uint32_t packed[kItems];   // rank within the warp's keys | digit << 16
 #pragma unroll
     for (int k = 0; k < kItems; ++k)
     {
         uint64_t i = warp_base + uint64_t(k) * 32 + lane;
         bool valid = i < n;
-        key[k] = valid ? keys_in[i] : 0u;
-        val[k] = valid ? (identity_values ? uint32_t(i) : vals_in[i]) : 0u;
         // invalid items get a digit outside [0, kRadix) so they never match a real one
-        uint32_t d = valid ? (key[k] >> shift) & (kRadix - 1) : uint32_t(kRadix);
+        uint32_t d = valid ? (__ldg(&keys_in[i]) >> shift) & (kRadix - 1) : uint32_t(kRadix);
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
         uint32_t before = valid ? warp_hist[warp][d] : 0u;
         __syncwarp();
         if (valid && (peers & lanemask_lt) == 0) warp_hist[warp][d] = before + __popc(peers);
         __syncwarp();
-        rank[k] = before + __popc(peers & lanemask_lt);
+        packed[k] = (before + __popc(peers & lanemask_lt)) | (d << 16);
     }
     __syncthreads();
 
@@ -232,10 +259,10 @@ __global__ void __launch_bounds__(kThreads) scatter_digits(
         uint64_t i = warp_base + uint64_t(k) * 32 + lane;
         if (i < n)
         {
-            uint32_t d = (key[k] >> shift) & (kRadix - 1);
-            uint32_t pos = digit_start[d] + warp_hist[warp][d] + rank[k];
-            skeys[pos] = key[k];
-            svals[pos] = val[k];
+            uint32_t d = packed[k] >> 16;
+            uint32_t pos = digit_start[d] + warp_hist[warp][d] + (packed[k] & 0xFFFFu);
+            skeys[pos] = __ldg(&keys_in[i]);
+            svals[pos] = __ldg(&vals_in[i]);
         }
     }
     __syncthreads();
@@ -262,7 +289,8 @@ size_t radix_sort_scratch_bytes(uint32_t n)
 }
 
 gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values, uint32_t* keys_alt,
-                             uint32_t* values_alt, uint32_t n, int key_bits, void* scratch, cudaStream_t stream)
+                             uint32_t* values_alt, uint32_t n, int key_bits, void* scratch, cudaStream_t stream,
+                             uint32_t** sorted_values)
 {
     if (n == 0) return GBRT_OK;
     const uint32_t tiles = num_tiles(n);
@@ -287,11 +315,15 @@ gbrt_status radix_sort_pairs(gbrt_context* ctx, uint32_t* keys, uint32_t* values
         GBRT_LAUNCH_CHECK(ctx, "scan_sums");
         scan_apply<<<chunks, kScanBlock, 0, stream>>>(counts, len, sums);
         GBRT_LAUNCH_CHECK(ctx, "scan_apply");
-        scatter_digits<<<tiles, kThreads, 0, stream>>>(kin, vin, kout, vout, n, shift, counts,
-                                                            tiles, 0);
+        scatter_digits<<<tiles, kThreads, 0, stream>>>(kin, vin, kout, vout, n, shift, counts, tiles);
         GBRT_LAUNCH_CHECK(ctx, "scatter_digits");
         std::swap(kin, kout);
         std::swap(vin, vout);
+    }
+    if (sorted_values)
+    {
+        *sorted_values = vin;   // the caller takes the values where the last pass left them
+        return GBRT_OK;
     }
     if (kin != keys)
     {

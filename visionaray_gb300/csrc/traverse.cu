@@ -339,9 +339,11 @@ gbrt_status trace(gbrt_context* ctx, gbrt_bvh const* bvh, gbrt_ray const* d_rays
         ray_origin_keys<<<blocks, kTraceBlock, 0, stream>>>(d_rays, n, lo, scale, cell_bits, any_hit, keys, vals);
         GBRT_LAUNCH_CHECK(ctx, "ray_origin_keys");
         const int key_bits = 3 * cell_bits + (any_hit ? 3 : 0);
-        gbrt_status st = radix_sort_pairs(ctx, keys, vals, keys_alt, vals_alt, n, key_bits, base + 4 * w, stream);
+        uint32_t* sorted = nullptr;
+        gbrt_status st = radix_sort_pairs(ctx, keys, vals, keys_alt, vals_alt, n, key_bits, base + 4 * w, stream,
+                                          &sorted);
         if (st != GBRT_OK) return st;
-        perm = vals;   // radix_sort_pairs leaves the result in (keys, values)
+        perm = sorted;   // vals or vals_alt, wherever the last pass left the order
         if (!persistent)
         {
             kernel_timer timer(ctx, stream);
