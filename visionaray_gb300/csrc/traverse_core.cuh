@@ -131,7 +131,11 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
                                                           float t_best = FLT_MAX)
 {
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
-    trace_result best{ -1, t_best, 0.0f, 0.0f };
+    // the loop carries the best triangle and its t only; u and v are recomputed from
+    // that triangle at the end (the same test on the same inputs: the same values),
+    // which keeps two registers free in the node loop
+    int best_tri = -1;
+    float best_t = t_best;
 
     int sp = 0;
     int node = root;
@@ -161,8 +165,8 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
             float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
             float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
             float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
-            bool h0 = tf0 >= tn0 && tn0 < best.t;
-            bool h1 = tf1 >= tn1 && tn1 < best.t;
+            bool h0 = tf0 >= tn0 && tn0 < best_t;
+            bool h1 = tf1 >= tn1 && tn1 < best_t;
 
             if (h0 && h1)
             {
@@ -199,14 +203,26 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
             float4 t1 = ldg4(&tp->t1);
             float4 t2 = ldg4(&tp->t2);
             tri_hit h = intersect_triangle(o, d, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z }, { t2.x, t2.y, t2.z });
-            if (h.hit && h.t < best.t && h.t >= tmin && h.t <= tmax)
+            if (h.hit && h.t < best_t && h.t >= tmin && h.t <= tmax)
             {
-                best = { t, h.t, h.u, h.v };
-                if (AnyHit) return best;
+                if (AnyHit) return trace_result{ t, h.t, h.u, h.v };
+                best_tri = t;
+                best_t = h.t;
             }
             if (__float_as_uint(t2.w) & kLastInLeaf) break;
         }
         node = pop_entry(stack, sp);
+    }
+    trace_result best{ best_tri, best_t, 0.0f, 0.0f };
+    if (!AnyHit && best_tri >= 0)
+    {
+        const tri48* tp = tris + best_tri;
+        float4 t0 = ldg4(&tp->t0);
+        float4 t1 = ldg4(&tp->t1);
+        float4 t2 = ldg4(&tp->t2);
+        tri_hit h = intersect_triangle(o, d, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z }, { t2.x, t2.y, t2.z });
+        best.u = h.u;
+        best.v = h.v;
     }
     return best;
 }
