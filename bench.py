@@ -46,7 +46,7 @@ N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, mean of two
 # launches each in one ncu capture of the full-size workload with the default ray
 # order and the shipped kernel build).
-TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.800e9 + 0.240e9, 2.641e9 + 0.542e9
+TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.705e9 + 0.201e9, 2.642e9 + 0.542e9
 
 
 # Algorithmic bytes per path-traced sample, B_sample = sum of B_ray over the sample's
@@ -785,7 +785,7 @@ def run_ours(args):
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "b_ray": round(b_ray(N_NODE_CLOSEST, N_TRI_CLOSEST), 1),
                 "timing": "CUDA events around the traversal kernel on its stream, mean over the timed launches",
-                "limiter": "latency of dependent node fetches under divergence (ncu: DRAM ~14 % of peak)"}
+                "limiter": "latency of dependent node fetches under divergence (ncu: DRAM ~14 % of peak at full size)"}
     # the pure-I/O floor (48 B per ray: the ray in, the hit out) and the DRAM bandwidth
     # the launch actually drew (its ncu traffic over its event time)
     io_gbs = d["rays"] * 48 / (d["kernel_ms_per_launch"] * 1e-3) / 1e9
