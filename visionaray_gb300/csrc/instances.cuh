@@ -27,6 +27,20 @@ struct tlas_result
     float t, u, v;
 };
 
+// transform_ray (bvh.h:748-755): the world ray carried into instance `inst`'s space
+// with the instance's inverse 3x3 rows and negated translation.
+__device__ __forceinline__ void instance_ray(tlas_view const& tv, int inst, f3 o, f3 d, f3& oo, f3& dd)
+{
+    const float4 ra = tv.records[3 * inst + 0], rb = tv.records[3 * inst + 1], rc = tv.records[3 * inst + 2];
+    const float px = __fadd_rn(o.x, ra.w), py = __fadd_rn(o.y, rb.w), pz = __fadd_rn(o.z, rc.w);
+    oo = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, px), __fmul_rn(ra.y, py)), __fmul_rn(ra.z, pz)),
+           __fadd_rn(__fadd_rn(__fmul_rn(rb.x, px), __fmul_rn(rb.y, py)), __fmul_rn(rb.z, pz)),
+           __fadd_rn(__fadd_rn(__fmul_rn(rc.x, px), __fmul_rn(rc.y, py)), __fmul_rn(rc.z, pz)) };
+    dd = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, d.x), __fmul_rn(ra.y, d.y)), __fmul_rn(ra.z, d.z)),
+           __fadd_rn(__fadd_rn(__fmul_rn(rb.x, d.x), __fmul_rn(rb.y, d.y)), __fmul_rn(rb.z, d.z)),
+           __fadd_rn(__fadd_rn(__fmul_rn(rc.x, d.x), __fmul_rn(rc.y, d.y)), __fmul_rn(rc.z, d.z)) };
+}
+
 // bstack: the bottom-level traversals' stack (a local_stack, or a shared_stack whose
 // top entries sit in shared memory); the top level keeps its own 32 entries.
 template <bool AnyHit, class BlasStack>
@@ -34,6 +48,9 @@ __device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tla
                                                           float tmin, float tmax, uint32_t* __restrict__ status)
 {
     const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
+    // the loop carries the best instance, triangle and t; u and v are recomputed at the
+    // end from that instance's carried ray and triangle (the same operations on the
+    // same inputs, so the same values)
     tlas_result best{ -1, -1, FLT_MAX, 0.0f, 0.0f };
     int stack[32];
     int sp = 0;
@@ -88,15 +105,8 @@ __device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tla
             atomicOr(status, kStatusBadIndex);
             break;
         }
-        // transform_ray (bvh.h:748-755) with the instance's inverse, then its tree
-        const float4 ra = tv.records[3 * inst + 0], rb = tv.records[3 * inst + 1], rc = tv.records[3 * inst + 2];
-        const float px = __fadd_rn(o.x, ra.w), py = __fadd_rn(o.y, rb.w), pz = __fadd_rn(o.z, rc.w);
-        f3 oo = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, px), __fmul_rn(ra.y, py)), __fmul_rn(ra.z, pz)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, px), __fmul_rn(rb.y, py)), __fmul_rn(rb.z, pz)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, px), __fmul_rn(rc.y, py)), __fmul_rn(rc.z, pz)) };
-        f3 dd = { __fadd_rn(__fadd_rn(__fmul_rn(ra.x, d.x), __fmul_rn(ra.y, d.y)), __fmul_rn(ra.z, d.z)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rb.x, d.x), __fmul_rn(rb.y, d.y)), __fmul_rn(rb.z, d.z)),
-                  __fadd_rn(__fadd_rn(__fmul_rn(rc.x, d.x), __fmul_rn(rc.y, d.y)), __fmul_rn(rc.z, d.z)) };
+        f3 oo, dd;
+        instance_ray(tv, inst, o, d, oo, dd);
         const bvh_view bv = tv.views[inst];
         if (bv.num_tris > 0)
         {
@@ -104,11 +114,23 @@ __device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tla
                                                        oo, dd, tmin, tmax, status, best.t);
             if (h.tri >= 0)
             {
-                best = { inst, h.tri, h.t, h.u, h.v };
-                if (AnyHit) break;
+                if (AnyHit) return tlas_result{ inst, h.tri, h.t, h.u, h.v };
+                best.inst = inst;
+                best.tri = h.tri;
+                best.t = h.t;
             }
         }
         node = sp > 0 ? stack[--sp] : kEmptyLink;
+    }
+    if (!AnyHit && best.inst >= 0)
+    {
+        f3 oo, dd;
+        instance_ray(tv, best.inst, o, d, oo, dd);
+        const tri48* tp = tv.views[best.inst].tris + best.tri;
+        const float4 t0 = ldg4(&tp->t0), t1 = ldg4(&tp->t1), t2 = ldg4(&tp->t2);
+        const tri_hit h = intersect_triangle(oo, dd, { t0.x, t0.y, t0.z }, { t1.x, t1.y, t1.z }, { t2.x, t2.y, t2.z });
+        best.u = h.u;
+        best.v = h.v;
     }
     return best;
 }

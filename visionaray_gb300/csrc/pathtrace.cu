@@ -322,6 +322,11 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow_sorted(frame_b
 // instances): 984.5 ms per frame with the local stack, 1057.0 / 1061.1 ms with 8 / 16
 // entries in shared memory.
 constexpr int kPtTlasSharedStack = 0;
+// Resident blocks the two-level extend and shadow kernels' registers must allow: 8
+// (64 registers, no spills; the top-level loop around the bottom-level one holds more
+// state than one tree's traversal).  Measured on the instanced box: 980.6 ms per frame
+// at 12 blocks (40 registers, spilling), 896.4 at 10, 874.1 at 8.
+constexpr int kPtTlasMinBlocks = 8;
 
 template <bool AnyHit>
 __device__ __forceinline__ tlas_result trace_tlas(tlas_view const& tv, f3 o, f3 d, float tmin, float tmax,
@@ -334,7 +339,7 @@ __device__ __forceinline__ tlas_result trace_tlas(tlas_view const& tv, f3 o, f3 
 }
 
 // pt_extend and pt_shadow over a two-level tree: hits carry the instance in z.
-__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend_tlas(frame_buffers fb, int q, tlas_view tv,
+__global__ void __launch_bounds__(kBlock, kPtTlasMinBlocks) pt_extend_tlas(frame_buffers fb, int q, tlas_view tv,
                                                                        uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
@@ -351,7 +356,7 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_extend_tlas(frame_buf
     fb.hits[i] = make_uint4(uint32_t(h.tri), __float_as_uint(h.t), uint32_t(h.inst), 0u);
 }
 
-__global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow_tlas(frame_buffers fb, tlas_view tv,
+__global__ void __launch_bounds__(kBlock, kPtTlasMinBlocks) pt_shadow_tlas(frame_buffers fb, tlas_view tv,
                                                                        uint32_t* __restrict__ status)
 {
     uint32_t i = blockIdx.x * kBlock + threadIdx.x;
