@@ -118,37 +118,118 @@ box merge(box const& a, box const& b)
     return r;
 }
 
-// Median split on the longest axis of the centroid bounds, one instance per leaf;
-// returns the link of the subtree (inner index, or ~instance).
+float half_area(box const& b)
+{
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Binned SAH split (16 bins per axis over the instance centroids; cost = half area x
+// instances on each side), one instance per leaf; the median of the longest centroid
+// axis when every centroid falls in one bin, and below `sah_levels` levels, so that the
+// tree is at most 31 levels deep (the traversal's top-level stack holds 32 entries).
+// An instance box as large as the scene (a room around its furniture) is split off near
+// the root instead of widening half of the tree.  Returns the link of the subtree
+// (inner index, or ~instance).
 int32_t build_top(std::vector<uint32_t>& ids, size_t first, size_t last, std::vector<box> const& boxes,
-                  std::vector<bvh2_node>& nodes, box& out_box)
+                  std::vector<bvh2_node>& nodes, box& out_box, int sah_levels)
 {
     if (last - first == 1)
     {
         out_box = boxes[ids[first]];
         return ~int32_t(ids[first]);
     }
+    auto centroid = [&](uint32_t i, int a) { return 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]); };
     float clo[3] = { FLT_MAX, FLT_MAX, FLT_MAX }, chi[3] = { -FLT_MAX, -FLT_MAX, -FLT_MAX };
     for (size_t i = first; i < last; ++i)
         for (int a = 0; a < 3; ++a)
         {
-            float c = 0.5f * (boxes[ids[i]].lo[a] + boxes[ids[i]].hi[a]);
+            float c = centroid(ids[i], a);
             clo[a] = vmin(clo[a], c);
             chi[a] = vmax(chi[a], c);
         }
-    int axis = 0;
-    for (int a = 1; a < 3; ++a)
-        if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
-    size_t mid = first + (last - first) / 2;
-    std::nth_element(ids.begin() + first, ids.begin() + mid, ids.begin() + last, [&](uint32_t a, uint32_t b) {
-        float ca = boxes[a].lo[axis] + boxes[a].hi[axis], cb = boxes[b].lo[axis] + boxes[b].hi[axis];
-        return ca < cb || (ca == cb && a < b);
-    });
+    constexpr int kBins = 16;
+    // the bin of a centroid; a non-finite one goes to bin 0
+    auto bin_of = [&](uint32_t i, int a, float extent) {
+        const float f = float(kBins) * (centroid(i, a) - clo[a]) / extent;
+        return f >= 0.0f ? (f < float(kBins) ? int(f) : kBins - 1) : 0;
+    };
+    int best_axis = -1, best_split = 0;
+    float best_cost = FLT_MAX;
+    for (int a = 0; a < 3 && sah_levels > 0; ++a)
+    {
+        const float extent = chi[a] - clo[a];
+        if (!(extent > 0.0f)) continue;
+        box bb[kBins];
+        size_t cnt[kBins] = {};
+        for (int k = 0; k < kBins; ++k)
+            for (int c = 0; c < 3; ++c)
+            {
+                bb[k].lo[c] = FLT_MAX;
+                bb[k].hi[c] = -FLT_MAX;
+            }
+        for (size_t i = first; i < last; ++i)
+        {
+            const int k = bin_of(ids[i], a, extent);
+            bb[k] = merge(bb[k], boxes[ids[i]]);
+            ++cnt[k];
+        }
+        // cost of splitting after bin k: left bins [0, k], right bins (k, kBins)
+        float right_area[kBins];
+        size_t right_cnt[kBins];
+        box acc = bb[kBins - 1];
+        size_t n_acc = cnt[kBins - 1];
+        for (int k = kBins - 2; k >= 0; --k)
+        {
+            right_area[k] = n_acc ? half_area(acc) : 0.0f;
+            right_cnt[k] = n_acc;
+            acc = merge(acc, bb[k]);
+            n_acc += cnt[k];
+        }
+        box left = bb[0];
+        size_t n_left = cnt[0];
+        for (int k = 0; k < kBins - 1; ++k)
+        {
+            if (k > 0)
+            {
+                left = merge(left, bb[k]);
+                n_left += cnt[k];
+            }
+            if (n_left == 0 || right_cnt[k] == 0) continue;
+            const float cost = half_area(left) * float(n_left) + right_area[k] * float(right_cnt[k]);
+            if (cost < best_cost)
+            {
+                best_cost = cost;
+                best_axis = a;
+                best_split = k;
+            }
+        }
+    }
+    size_t mid;
+    if (best_axis >= 0)
+    {
+        const int a = best_axis;
+        const float extent = chi[a] - clo[a];
+        auto goes_left = [&](uint32_t i) { return bin_of(i, a, extent) <= best_split; };
+        // stable partition: instances keep their relative order on each side
+        mid = size_t(std::stable_partition(ids.begin() + first, ids.begin() + last, goes_left) - ids.begin());
+    }
+    else
+    {
+        int axis = 0;
+        for (int a = 1; a < 3; ++a)
+            if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+        mid = first + (last - first) / 2;
+        std::nth_element(ids.begin() + first, ids.begin() + mid, ids.begin() + last, [&](uint32_t x, uint32_t y) {
+            float cx = boxes[x].lo[axis] + boxes[x].hi[axis], cy = boxes[y].lo[axis] + boxes[y].hi[axis];
+            return cx < cy || (cx == cy && x < y);
+        });
+    }
     int32_t self = int32_t(nodes.size());
     nodes.emplace_back();
     box lb, rb;
-    int32_t l = build_top(ids, first, mid, boxes, nodes, lb);
-    int32_t r = build_top(ids, mid, last, boxes, nodes, rb);
+    int32_t l = build_top(ids, first, mid, boxes, nodes, lb, sah_levels - 1);
+    int32_t r = build_top(ids, mid, last, boxes, nodes, rb, sah_levels - 1);
     bvh2_node& nd = nodes[size_t(self)];
     nd.xy0 = make_float4(lb.lo[0], lb.hi[0], lb.lo[1], lb.hi[1]);
     nd.xy1 = make_float4(rb.lo[0], rb.hi[0], rb.lo[1], rb.hi[1]);
@@ -235,7 +316,10 @@ extern "C" gbrt_status gbrt_tlas_build(gbrt_context* ctx, gbrt_instance const* h
         std::iota(ids.begin(), ids.end(), 0u);
         nodes.reserve(num_instances);
         box all;
-        root = build_top(ids, 0, num_instances, boxes, nodes, all);
+        // SAH levels such that SAH levels + the median split's ceil(log2 n) <= 31
+        int log2n = 0;
+        while ((uint64_t(1) << log2n) < uint64_t(num_instances)) ++log2n;
+        root = build_top(ids, 0, num_instances, boxes, nodes, all, 31 - log2n);
     }
     device_guard g(ctx->device);
     auto* t = new (std::nothrow) gbrt_tlas;
