@@ -322,7 +322,8 @@ __global__ void __launch_bounds__(kBlock, kPtMinBlocks) pt_shadow_sorted(frame_b
 // Bottom-level stack entries of the two-level queries held in shared memory (0: the
 // whole stack in local memory).  Measured on the instanced box (1920x1080x64, 256 blob
 // instances): 984.5 ms per frame with the local stack, 1057.0 / 1061.1 ms with 8 / 16
-// entries in shared memory.
+// entries in shared memory at 12 blocks per SM; at 8 blocks with the SAH top level
+// 780.4 ms local, 795.2 / 807.2 ms with 8 / 16 shared entries.
 constexpr int kPtTlasSharedStack = 0;
 // Resident blocks the two-level extend and shadow kernels' registers must allow: 8
 // (64 registers, no spills; the top-level loop around the bottom-level one holds more
