@@ -36,7 +36,7 @@ static_assert(sizeof(batch_frame) == 112, "frame record layout");
 
 struct batch_args
 {
-    const batch_frame* frames;
+    const batch_frame* __restrict__ frames;
     const uint32_t* pixel_offsets;
     uint32_t num_scenes, total_pixels, tile, order;
     const bvh2_node* nodes;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(Block, (Width == 2 ? kBatchWarpsPerSM : kBatch
             if (g0 >= a.total_pixels) break;
             const uint32_t g = a.perm ? __ldg(&a.perm[g0]) : g0;
             const uint32_t s = upper_segment(a.pixel_offsets, a.num_scenes, g);
-            const batch_frame f = a.frames[s];
+            const batch_frame& f = a.frames[s];   // fields read where they are used
             const uint32_t first = __ldg(&a.pixel_offsets[s]);
             const uint32_t local = g - first;
             uint32_t pixel = local;
