@@ -16,8 +16,6 @@
 #include "api_internal.h"
 #include "device_math.cuh"
 
-#include <type_traits>
-
 namespace gbrt {
 
 constexpr int kEmptyLink = INT32_MIN;   // stack sentinel: neither an inner node nor a leaf
@@ -58,39 +56,6 @@ struct shared_stack
             spill[i - Shared] = v;
     }
     __device__ __forceinline__ int get(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
-};
-
-// shared_stack whose top entry stays in a register: a push stores the previous top to
-// its slot, a pop returns the register and loads the entry below it, so the value a
-// pop needs is never waiting on a shared-memory load (the load of the next top has a
-// whole node visit to complete).  The same slots and capacity as shared_stack.
-template <int Shared, int Total, int Stride>
-struct regtop_stack
-{
-    static_assert(Total > Shared, "the local part holds at least one entry");
-    static constexpr int capacity = Total;
-    int* col;
-    int spill[Total - Shared];
-    int top = 0;   // entry sp - 1
-    __device__ __forceinline__ void store(int i, int v)
-    {
-        if (i < Shared)
-            col[i * Stride] = v;
-        else
-            spill[i - Shared] = v;
-    }
-    __device__ __forceinline__ int load(int i) const { return i < Shared ? col[i * Stride] : spill[i - Shared]; }
-    __device__ __forceinline__ void set(int i, int v)
-    {
-        if (i > 0) store(i - 1, top);
-        top = v;
-    }
-    __device__ __forceinline__ int get(int i)
-    {
-        const int v = top;
-        if (i > 0) top = load(i - 1);
-        return v;
-    }
 };
 
 // The next stack entry to visit, kEmptyLink when the stack is empty.
@@ -492,7 +457,7 @@ __device__ __forceinline__ trace_result traverse_view(bvh_view const& v, f3 o, f
 
 // A query through the node pairs with the stack's first Shared entries in shared
 // memory (a column per thread of a Block-thread block), or through the 4-wide nodes.
-template <bool AnyHit, bool Wide, int Block, int Shared, bool RegTop = false>
+template <bool AnyHit, bool Wide, int Block, int Shared>
 __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
                                                              uint32_t* __restrict__ status)
 {
@@ -503,8 +468,7 @@ __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, 
     else
     {
         __shared__ int stack_mem[Shared * Block];
-        std::conditional_t<RegTop, regtop_stack<Shared, kStackSize, Block>, shared_stack<Shared, kStackSize, Block>>
-            stack;
+        shared_stack<Shared, kStackSize, Block> stack;
         stack.col = stack_mem + threadIdx.x;
         return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
                                          status);
