@@ -47,6 +47,10 @@ N_NODE_AO, N_TRI_AO = 65.19375747, 6.29761556             # B_ray = 2436.5 bytes
 # launches each in one ncu capture of the full-size workload with the default ray
 # order and the shipped kernel build).
 TRAFFIC_CLOSEST, TRAFFIC_ANY = 2.705e9 + 0.201e9, 2.642e9 + 0.542e9
+# L1 <-> L2 bytes per launch of the same kernels (lts__t_sectors_srcunit_tex_op_read.sum
+# + lts__t_sectors_srcunit_tex_op_write.sum, 32-byte sectors; one single-pass ncu
+# capture of the full-size workload).
+L2_TRAFFIC_CLOSEST, L2_TRAFFIC_ANY = (336.27e6 + 45.39e6) * 32, (878.37e6 + 37.64e6) * 32
 
 
 # Algorithmic bytes per path-traced sample, B_sample = sum of B_ray over the sample's
@@ -792,6 +796,15 @@ def run_ours(args):
     roofline["io_floor"] = {"bytes_per_ray": 48, "achieved_gbs": round(io_gbs, 1), "frac": round(io_gbs / peak, 4)}
     if roofline["traffic"]:
         roofline["dram_gbs"] = round(roofline["traffic"] / (d["kernel_ms_per_launch"] * 1e-3) / 1e9, 1)
+        # the L2 side of the same launch: its L1 <-> L2 bytes over its time, against the
+        # L2 bandwidth measured in this run
+        l2_peak = measured_l2_gbs(dev)
+        l2_gbs = L2_TRAFFIC_CLOSEST / (d["kernel_ms_per_launch"] * 1e-3) / 1e9
+        roofline["l2"] = {"traffic": L2_TRAFFIC_CLOSEST, "achieved_gbs": round(l2_gbs, 1), "peak": l2_peak,
+                          "frac": round(l2_gbs / l2_peak, 4),
+                          "traffic_source": "ncu lts__t_sectors_srcunit_tex_op_read.sum + _write.sum x 32 B "
+                                            "per launch, full-size capture",
+                          "peak_source": "L2 measured in this run (best of copy, in-place add, sum)"}
 
     # the same rays through the PLOC tree (a higher-quality GPU build; the workload's
     # builder is the LBVH, so this is reported beside the line's value, not as it)
