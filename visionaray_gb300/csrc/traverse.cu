@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_dynamic(bvh_view v, co
             bool h1 = tf1 >= tn1 && tn1 < best.t;
             if (h0 && h1)
             {
-                bool first0 = tn0 < tn1;
+                bool first0 = AnyHit || tn0 < tn1;   // traverse_bvh_with's order
                 int near_child = first0 ? link.x : link.y;
                 int far_child = first0 ? link.y : link.x;
                 if (sp < kStackSize)
