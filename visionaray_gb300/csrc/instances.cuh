@@ -78,8 +78,8 @@ __device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tla
             float tf0 = fminf(tmax, fminf(fmaxf(lx0, hx0), fminf(fmaxf(ly0, hy0), fmaxf(lz0, hz0))));
             float tn1 = fmaxf(tmin, fmaxf(fminf(lx1, hx1), fmaxf(fminf(ly1, hy1), fminf(lz1, hz1))));
             float tf1 = fminf(tmax, fminf(fmaxf(lx1, hx1), fminf(fmaxf(ly1, hy1), fmaxf(lz1, hz1))));
-            bool h0 = tf0 >= tn0 && tn0 < best.t;
-            bool h1 = tf1 >= tn1 && tn1 < best.t;
+            bool h0 = tf0 >= tn0 && (AnyHit || tn0 < best.t);   // as traverse_bvh_with
+            bool h1 = tf1 >= tn1 && (AnyHit || tn1 < best.t);
             if (h0 && h1)
             {
                 bool first0 = AnyHit || tn0 < tn1;   // any hit: no order needed (traverse_bvh_with)
