@@ -82,7 +82,7 @@ __device__ __forceinline__ tlas_result traverse_tlas_with(BlasStack& bstack, tla
             bool h1 = tf1 >= tn1 && (AnyHit || tn1 < best.t);
             if (h0 && h1)
             {
-                bool first0 = AnyHit || tn0 < tn1;   // any hit: no order needed (traverse_bvh_with)
+                bool first0 = tn0 < tn1;   // near first, any hit too (traverse_bvh_with)
                 if (sp < 32)
                     stack[sp++] = first0 ? link.y : link.x;
                 else

@@ -43,8 +43,9 @@ __device__ __forceinline__ trace_result trace_one(bvh_view const& v, f3 o, f3 d,
     else if constexpr (Nodes == kNodesWide8)
         return traverse_bvhw<AnyHit, 8>(v.nodes8, v.num_nodes8, v.tris, v.num_tris, o, d, tmin, tmax, status);
     else
-        return traverse_view_shared<AnyHit, Nodes == kNodesWide, kTraceBlock, kSharedStack>(v, o, d, tmin, tmax,
-                                                                                              status);
+        // any-hit ray queries unordered (traverse_bvh_with)
+        return traverse_view_shared<AnyHit, Nodes == kNodesWide, kTraceBlock, kSharedStack, !AnyHit>(v, o, d, tmin,
+                                                                                                       tmax, status);
 }
 
 template <bool AnyHit, int Nodes>
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_rays_dynamic(bvh_view v, co
             bool h1 = tf1 >= tn1 && (AnyHit || tn1 < best.t);
             if (h0 && h1)
             {
-                bool first0 = AnyHit || tn0 < tn1;   // traverse_bvh_with's order
+                bool first0 = AnyHit || tn0 < tn1;   // the ray queries' order (trace_one)
                 int near_child = first0 ? link.x : link.y;
                 int far_child = first0 ? link.y : link.x;
                 if (sp < kStackSize)

@@ -87,8 +87,14 @@ __device__ __forceinline__ void load_pair(const bvh2_node* np, float4& a, float4
 // A tree taller than the stack's capacity sets kStatusStackOverflow and skips the
 // subtrees that did not fit.  t_best: a hit must be strictly closer than this (a
 // closer hit found elsewhere, e.g. in another instance); the result's t is t_best
-// when nothing closer was found.
-template <bool AnyHit, class StackT>
+// when nothing closer was found.  NearFirst: of two hit children the nearer is visited
+// first (ties to child 1, intersect.inl:283); without it child 0 goes first and the
+// entry distances are not compared.  A closest-hit query needs the order.  An any-hit
+// query's answer does not depend on it (which occluder it reports does): the ray
+// queries' AO rays, short and issue-bound, run unordered (14.52 -> 14.00 ms per
+// launch), while path-tracing shadow rays, long and towards a light, meet their
+// occluders sooner in order (instanced box frame 781 vs 878 ms).
+template <bool AnyHit, class StackT, bool NearFirst = true>
 __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const bvh2_node* __restrict__ nodes,
                                                           const tri48* __restrict__ tris, int32_t root,
                                                           int32_t num_inner, int32_t num_tris, f3 o, f3 d,
@@ -137,11 +143,7 @@ __device__ __forceinline__ trace_result traverse_bvh_with(StackT& stack, const b
 
             if (h0 && h1)
             {
-                // closest hit: the nearer child first, ties to child 1 (intersect.inl:283);
-                // any hit: child 0 first without the comparison -- an occlusion query's
-                // answer does not depend on the order (which occluder it reports does),
-                // and the loop is issue-bound (AO rays 14.52 -> 14.00 ms per launch)
-                bool first0 = AnyHit || tn0 < tn1;
+                bool first0 = !NearFirst || tn0 < tn1;
                 int near_child = first0 ? link.x : link.y;
                 int far_child = first0 ? link.y : link.x;
                 if (sp < StackT::capacity)
@@ -463,7 +465,7 @@ __device__ __forceinline__ trace_result traverse_view(bvh_view const& v, f3 o, f
 
 // A query through the node pairs with the stack's first Shared entries in shared
 // memory (a column per thread of a Block-thread block), or through the 4-wide nodes.
-template <bool AnyHit, bool Wide, int Block, int Shared>
+template <bool AnyHit, bool Wide, int Block, int Shared, bool NearFirst = true>
 __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, f3 o, f3 d, float tmin, float tmax,
                                                              uint32_t* __restrict__ status)
 {
@@ -476,8 +478,8 @@ __device__ __forceinline__ trace_result traverse_view_shared(bvh_view const& v, 
         __shared__ int stack_mem[Shared * Block];
         shared_stack<Shared, kStackSize, Block> stack;
         stack.col = stack_mem + threadIdx.x;
-        return traverse_bvh_with<AnyHit>(stack, v.nodes, v.tris, v.root, v.num_inner, v.num_tris, o, d, tmin, tmax,
-                                         status);
+        return traverse_bvh_with<AnyHit, decltype(stack), NearFirst>(stack, v.nodes, v.tris, v.root, v.num_inner,
+                                                                     v.num_tris, o, d, tmin, tmax, status);
     }
 }
 
