@@ -244,7 +244,9 @@ gbrt_status gbrt_trace_closest_hit(gbrt_context* ctx, gbrt_bvh const* bvh,
 
 /* any_hit(ray, refs, refs + 1) (detail/traverse_linear.inl:156-189): stops at the
  * first accepted hit (detail/exit_traversal.h:49-56).  Which triangle is reported
- * depends on traversal order; whether a hit exists does not.                       */
+ * depends on traversal order; whether a hit exists does not.  These queries visit the
+ * two hit children of a node in index order rather than nearest first (fewer
+ * instructions per node), so the reported triangle can differ from the reference's. */
 gbrt_status gbrt_trace_any_hit(gbrt_context* ctx, gbrt_bvh const* bvh,
                                gbrt_ray const* d_rays, uint32_t n, gbrt_hit* d_hits);
 
