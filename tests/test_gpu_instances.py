@@ -54,3 +54,26 @@ def test_empty_and_single_instance(oracle):
     t.ctx.synchronize()
     want = oracle.trace_instances([(oracle.build_sah(tri), tri, ident)], rays)
     assert compare_inst(got, want) == 0
+
+
+def test_many_and_coincident_instances(oracle):
+    """The binned-SAH top level over 300 instances, 40 of them at one transform (their
+    centroids in one bin: the median split takes over) and the rest spread out: hits
+    equal the oracle's except equal-t ties (the coincident instances tie with each
+    other on every ray that meets them)."""
+    meshes, inst_mesh, transforms = make_instances(n_inst=260, seed=21)
+    same = transforms[0].copy()
+    inst_mesh = np.concatenate([inst_mesh, np.zeros(40, np.uint32)])
+    transforms = np.concatenate([transforms, np.repeat(same[None, :], 40, axis=0)])
+    blas = [vg.lbvh_builder().build(vg.as_device_bytes(m)) for m in meshes]
+    tlas = vg.TLAS([(blas[m], transforms[k]) for k, m in enumerate(inst_mesh)])
+    rays = make_rays(2048, seed=22)
+    d_rays = vg.device_rays(rays)
+    got = vg.hits_inst_to_numpy(tlas.closest_hit(d_rays), len(rays))
+    got_any = vg.hits_inst_to_numpy(tlas.any_hit(d_rays), len(rays))
+    tlas.ctx.synchronize()
+    trees = [oracle.build_sah(m) for m in meshes]
+    want = oracle.trace_instances([(trees[m], meshes[m], transforms[k]) for k, m in enumerate(inst_mesh)], rays)
+    assert (want["prim_id"] != NO_HIT).sum() > len(rays) // 4
+    compare_inst(got, want)
+    assert ((got_any["prim_id"] != NO_HIT) == (got["prim_id"] != NO_HIT)).all()
