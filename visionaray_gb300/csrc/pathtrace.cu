@@ -56,7 +56,10 @@ constexpr int kPtSharedStack = 16;
 constexpr int kPtMinBlocks = 12;
 // The adjoint's replay kernel: resident blocks its registers must allow -- 16 blocks
 // (64 warps, 32 registers; the vertex records live in local memory anyway): backward
-// 15.4 -> 13.0 ms per inverse-rendering step (8 blocks 13.4, 12 blocks 14.3).
+// 15.4 -> 13.0 ms per inverse-rendering step (8 blocks 13.4, 12 blocks 14.3).  Its
+// traversal keeps the whole stack in local memory: a shared-memory top of 8 / 16
+// entries took the 512x512x16 replay from 46.2 to 55.1 / 65.6 ms (the shared carve-out
+// takes the L1 that the local vertex records use).
 constexpr int kAdjointMinBlocks = 16;
 // The shading kernel: 8 resident blocks (32 warps, at most 64 registers), the occupancy
 // it has without the out-of-line material samplers' call overhead.
