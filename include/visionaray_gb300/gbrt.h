@@ -101,7 +101,7 @@ gbrt_status gbrt_context_create(int device, void* stream, gbrt_context** out);
 gbrt_status gbrt_context_destroy(gbrt_context* ctx);
 gbrt_status gbrt_context_set_stream(gbrt_context* ctx, void* stream);
 /* Blocks until all work queued on the context's stream is done and reports any
- * deferred device-side error (watchdog, stack overflow).                          */
+ * deferred device-side error (a traversal stack overflow, an out-of-range index).  */
 gbrt_status gbrt_context_synchronize(gbrt_context* ctx);
 const char* gbrt_last_error(gbrt_context const* ctx);
 int         gbrt_abi_version(void);
